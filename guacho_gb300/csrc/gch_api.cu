@@ -1,0 +1,420 @@
+// gch_api.cu -- the C ABI declared in include/guacho_gb300.h: parameter
+// validation, device allocation, host<->device transfers, and the host-side
+// sequencing of the per-precision engines.
+#include <cuda_runtime.h>
+#include <string.h>
+
+#include <algorithm>
+#include <cmath>
+#include <new>
+
+#include "gch_domain.h"
+
+using gch::EngineOps;
+using gch::KParams;
+using gch::StepScalars;
+
+namespace {
+
+const EngineOps& engine(const gch_domain* d) {
+  return d->mode == GCH_FP64 ? gch::kEngineFP64 : gch::kEngineMixed;
+}
+
+int cuda_ok(cudaError_t e) { return e == cudaSuccess ? GCH_OK : GCH_ERR_CUDA; }
+
+bool valid_bc(int b) {
+  return b == GCH_BC_OUTFLOW || b == GCH_BC_CLOSED || b == GCH_BC_PERIODIC || b == GCH_BC_OTHER;
+}
+
+// Device-side control writes: launched with by-value arguments so no host
+// buffer must outlive the call.
+__global__ void k_set_ctrl(StepScalars* sc, int iter, int n_iter, double time, double tprint,
+                           double dtprint, double tmax, int active) {
+  sc->iter = iter;
+  sc->n_iter = n_iter;
+  sc->time = time;
+  sc->tprint = tprint;
+  sc->dtprint = dtprint;
+  sc->tmax = tmax;
+  sc->active = active;
+  sc->dump = 0;
+}
+__global__ void k_set_dt(StepScalars* sc, double dt) {
+  sc->dt = dt;
+  sc->active = 1;
+}
+__global__ void k_set_active(StepScalars* sc) { sc->active = 1; }
+__global__ void k_clear_info(StepScalars* sc) {
+  sc->err = 0;
+  sc->pfloor = 0;
+}
+
+int fetch_scalars(gch_domain* d) {
+  int st = cuda_ok(cudaMemcpyAsync(d->sc_host, d->sc, sizeof(StepScalars), cudaMemcpyDeviceToHost,
+                                   d->stream));
+  st |= cuda_ok(cudaStreamSynchronize(d->stream));
+  return st;
+}
+
+}  // namespace
+
+extern "C" {
+
+void gch_params_default(gch_params_t* p, int nx, int ny, int nz) {
+  memset(p, 0, sizeof(*p));
+  p->abi_version = GCH_ABI_VERSION;
+  p->precision = GCH_FP64;
+  p->nx = nx;
+  p->ny = ny;
+  p->nz = nz;
+  p->neq = 8;
+  p->mhd = 1;
+  p->pmhd = 0;
+  p->riemann_solver = GCH_SOLVER_HLLD;
+  p->slope_limiter = GCH_LIMITER_MINMOD;
+  p->eq_of_state = GCH_EOS_ADIABATIC;
+  p->cooling = GCH_COOL_NONE;
+  p->enable_flux_cd = 1;
+  p->eight_wave = 0;
+  p->user_source_terms = 0;
+  p->bc_left = p->bc_right = p->bc_bottom = p->bc_top = p->bc_out = p->bc_in = GCH_BC_PERIODIC;
+  p->bc_user = 0;
+  p->dx = 1.0 / nx;
+  p->dy = 1.0 / ny;
+  p->dz = 1.0 / nz;
+  p->cv = 1.5;
+  p->gamma = (p->cv + 1.0) / p->cv;
+  p->cfl = 0.2;
+  p->eta = 0.0;
+  p->Tempsc = 1.0;
+  p->Psc = 1.0;
+  p->tsc = 1.0;
+  p->tab_Tmin = 1e4;
+}
+
+int gch_params_check(const gch_params_t* p) {
+  if (!p || p->abi_version != GCH_ABI_VERSION) return GCH_ERR_PARAM;
+  if (p->precision != GCH_FP64 && p->precision != GCH_FP32_MIXED) return GCH_ERR_PARAM;
+  if (p->nx < 1 || p->ny < 1 || p->nz < 1) return GCH_ERR_PARAM;
+  if (p->neq != 5 && p->neq != 8) return GCH_ERR_PARAM;
+  const bool bfield = p->neq == 8;
+  if (p->mhd && !bfield) return GCH_ERR_PARAM;
+  if (bfield && !(p->mhd || p->pmhd)) return GCH_ERR_PARAM;
+  if (p->mhd && p->pmhd) return GCH_ERR_PARAM;
+  switch (p->riemann_solver) {
+    case GCH_SOLVER_HLLD:
+    case GCH_SOLVER_HLLE:
+      if (!p->mhd) return GCH_ERR_PARAM;  // both need the full MHD flux
+      break;
+    case GCH_SOLVER_HLLC:
+    case GCH_SOLVER_HLL:
+      if (p->mhd) return GCH_ERR_PARAM;   // hydro (or passive B) solvers
+      break;
+    default:
+      return GCH_ERR_PARAM;
+  }
+  if (p->slope_limiter < GCH_LIMITER_NO_AVERAGE || p->slope_limiter > GCH_LIMITER_SUPERBEE)
+    return GCH_ERR_PARAM;
+  if (p->eq_of_state != GCH_EOS_ADIABATIC && p->eq_of_state != GCH_EOS_SINGLE_SPECIE)
+    return GCH_ERR_PARAM;
+  if (p->cooling != GCH_COOL_NONE && p->cooling != GCH_COOL_DMC && p->cooling != GCH_COOL_CHI)
+    return GCH_ERR_PARAM;
+  if (p->cooling != GCH_COOL_NONE &&
+      (p->ntab < 2 || p->ntab > GCH_MAX_TABLE || !(p->tab_inv_dlog > 0.0)))
+    return GCH_ERR_PARAM;
+  // flux-CD needs B (the reference's hydro build leaves up untouched then)
+  if (p->enable_flux_cd && !bfield) return GCH_ERR_PARAM;
+  if (p->eight_wave && !p->mhd) return GCH_ERR_PARAM;
+  const int bcs[6] = {p->bc_left, p->bc_right, p->bc_bottom, p->bc_top, p->bc_out, p->bc_in};
+  for (int i = 0; i < 6; ++i)
+    if (!valid_bc(bcs[i])) return GCH_ERR_PARAM;
+  for (int a = 0; a < 3; ++a)  // periodic walls come in pairs (src/boundaries.f90:111)
+    if ((bcs[2 * a] == GCH_BC_PERIODIC) != (bcs[2 * a + 1] == GCH_BC_PERIODIC)) return GCH_ERR_PARAM;
+  if (p->nsph < 0 || p->nsph > GCH_MAX_SPHERES || p->ngrav < 0 || p->ngrav > GCH_MAX_GRAV)
+    return GCH_ERR_PARAM;
+  if (p->bc_user && p->nsph == 0) return GCH_ERR_PARAM;
+  if (p->user_source_terms && p->ngrav == 0) return GCH_ERR_PARAM;
+  if (!(p->dx > 0 && p->dy > 0 && p->dz > 0 && p->cv > 0 && p->gamma > 0 && p->cfl > 0))
+    return GCH_ERR_PARAM;
+  if (!(p->eta >= 0.0)) return GCH_ERR_PARAM;
+  return GCH_OK;
+}
+
+int gch_destroy(gch_domain_t* d) {
+  if (!d) return GCH_OK;
+  if (d->graph) cudaGraphExecDestroy(d->graph);
+  cudaFree(d->u);
+  cudaFree(d->up);
+  cudaFree(d->w);
+  cudaFree(d->E);
+  cudaFree(d->s678);
+  cudaFree(d->primit);
+  cudaFree(d->tab);
+  cudaFree(d->sph);
+  cudaFree(d->grav);
+  cudaFree(d->sc);
+  cudaFree(d->stage);
+  if (d->sc_host) cudaFreeHost(d->sc_host);
+  if (d->stream && d->own_stream) cudaStreamDestroy(d->stream);
+  delete d;
+  return GCH_OK;
+}
+
+int gch_create(const gch_params_t* p, void* stream, gch_domain_t** out) {
+  if (!out) return GCH_ERR_PARAM;
+  *out = nullptr;
+  int st = gch_params_check(p);
+  if (st) return st;
+  int dev = 0, ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return GCH_ERR_NO_DEVICE;
+  if (cudaGetDevice(&dev) != cudaSuccess) return GCH_ERR_NO_DEVICE;
+  cudaDeviceProp prop;
+  if (cudaGetDeviceProperties(&prop, dev) != cudaSuccess) return GCH_ERR_NO_DEVICE;
+  if (prop.major != 10) return GCH_ERR_NO_DEVICE;  // built for sm_103a only
+
+  gch_domain* d = new (std::nothrow) gch_domain();
+  if (!d) return GCH_ERR_CUDA;
+  d->hp = *p;
+  d->mode = p->precision;
+  d->prim_in = p->cooling == GCH_COOL_DMC || p->cooling == GCH_COOL_CHI;
+  d->tu_size = 8;
+  d->ts_size = d->mode == GCH_FP64 ? 8 : 4;
+
+  KParams& k = d->kp;
+  memset(&k, 0, sizeof(k));
+  k.nx = p->nx; k.ny = p->ny; k.nz = p->nz;
+  k.NX = p->nx + 2 * gch::NG; k.NY = p->ny + 2 * gch::NG; k.NZ = p->nz + 2 * gch::NG;
+  k.pitch = (k.NX + 3) & ~3;
+  k.fs = (long long)k.pitch * k.NY * k.NZ;
+  k.neq = p->neq;
+  k.mhd = p->mhd; k.pmhd = p->pmhd;
+  k.solver = p->riemann_solver; k.limiter = p->slope_limiter;
+  k.eos = p->eq_of_state; k.cooling = p->cooling;
+  k.flux_cd = p->enable_flux_cd; k.eight_wave = p->eight_wave; k.user_src = p->user_source_terms;
+  k.bc[0] = p->bc_left; k.bc[1] = p->bc_right; k.bc[2] = p->bc_bottom;
+  k.bc[3] = p->bc_top; k.bc[4] = p->bc_out; k.bc[5] = p->bc_in;
+  k.bc_user = p->bc_user;
+  k.dx = p->dx; k.dy = p->dy; k.dz = p->dz;
+  k.cv = p->cv; k.gamma = p->gamma; k.cfl = p->cfl; k.eta = p->eta;
+  k.Tempsc = p->Tempsc; k.Psc = p->Psc; k.tsc = p->tsc;
+  k.ntab = p->ntab; k.tab_i0 = p->tab_i0;
+  k.tab_inv_dlog = p->tab_inv_dlog; k.tab_tail = p->tab_tail; k.tab_Tmin = p->tab_Tmin;
+  k.nsph = p->bc_user ? p->nsph : 0;
+  k.ngrav = p->user_source_terms ? p->ngrav : 0;
+
+  // z planes per block: enough blocks to fill the 152 SMs several times
+  {
+    const long long tiles = (long long)((k.nx + gch::TX - 1) / gch::TX) * ((k.ny + gch::TY - 1) / gch::TY);
+    int kz = 16;
+    while (kz > 2 && tiles * ((k.nz + kz - 1) / kz) < 8 * 152) kz /= 2;
+    d->kz = std::min(kz, k.nz);
+  }
+
+  cudaStream_t s = (cudaStream_t)stream;
+  if (!s) {
+    // graph capture needs a stream other than the legacy default stream
+    if (cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking) != cudaSuccess) {
+      delete d;
+      return GCH_ERR_CUDA;
+    }
+    d->own_stream = true;
+  }
+  d->stream = s;
+
+  const size_t fs = (size_t)k.fs;
+  cudaError_t e = cudaSuccess;
+  auto alloc = [&](void** ptr, size_t bytes) {
+    if (e == cudaSuccess) e = cudaMalloc(ptr, bytes);
+    if (e == cudaSuccess) e = cudaMemsetAsync(*ptr, 0, bytes, s);
+  };
+  alloc(&d->u, fs * k.neq * d->tu_size);
+  alloc(&d->up, fs * k.neq * d->ts_size);
+  if (p->eta != 0.0) alloc(&d->w, fs * k.neq * d->tu_size);
+  if (k.neq == 8 && p->enable_flux_cd) alloc(&d->E, fs * 3 * d->ts_size);
+  if (p->eight_wave) alloc(&d->s678, fs * 3 * d->ts_size);
+  if (d->prim_in) alloc(&d->primit, fs * k.neq * d->ts_size);
+  d->ncell_host = (size_t)k.NX * k.NY * k.NZ;
+  alloc((void**)&d->stage, d->ncell_host * k.neq * sizeof(double));
+  alloc((void**)&d->sc, sizeof(StepScalars));
+  if (e == cudaSuccess && p->cooling != GCH_COOL_NONE) {
+    e = cudaMalloc((void**)&d->tab, 2 * p->ntab * sizeof(double));
+    if (e == cudaSuccess) e = cudaMemcpy(d->tab, p->tab_T, p->ntab * sizeof(double), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess)
+      e = cudaMemcpy(d->tab + p->ntab, p->tab_L, p->ntab * sizeof(double), cudaMemcpyHostToDevice);
+    k.tabT = d->tab;
+    k.tabL = d->tab + p->ntab;
+  }
+  if (e == cudaSuccess && k.nsph > 0) {
+    e = cudaMalloc((void**)&d->sph, k.nsph * sizeof(gch_sphere_t));
+    if (e == cudaSuccess) e = cudaMemcpy(d->sph, p->sph, k.nsph * sizeof(gch_sphere_t), cudaMemcpyHostToDevice);
+    k.sph = d->sph;
+  }
+  if (e == cudaSuccess && k.ngrav > 0) {
+    double g[4 * GCH_MAX_GRAV];
+    for (int l = 0; l < k.ngrav; ++l) {
+      g[l] = p->grav_GM[l];
+      g[k.ngrav + l] = p->grav_x[l];
+      g[2 * k.ngrav + l] = p->grav_y[l];
+      g[3 * k.ngrav + l] = p->grav_z[l];
+    }
+    e = cudaMalloc((void**)&d->grav, 4 * k.ngrav * sizeof(double));
+    if (e == cudaSuccess) e = cudaMemcpy(d->grav, g, 4 * k.ngrav * sizeof(double), cudaMemcpyHostToDevice);
+    k.grav = d->grav;
+  }
+  if (e == cudaSuccess) e = cudaMallocHost((void**)&d->sc_host, sizeof(StepScalars));
+  if (e == cudaSuccess) {
+    StepScalars init;
+    memset(&init, 0, sizeof(init));
+    init.dtmin_bits = 0x7FF0000000000000ull;
+    init.active = 1;
+    init.n_iter = 10;
+    init.iter = 1;
+    *d->sc_host = init;
+    e = cudaMemcpyAsync(d->sc, d->sc_host, sizeof(StepScalars), cudaMemcpyHostToDevice, s);
+  }
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  if (e != cudaSuccess) {
+    gch_destroy(d);
+    return GCH_ERR_CUDA;
+  }
+  *out = d;
+  return GCH_OK;
+}
+
+int gch_upload(gch_domain_t* d, const double* u) {
+  if (!d || !u) return GCH_ERR_PARAM;
+  int st = cuda_ok(cudaMemcpyAsync(d->stage, u, d->ncell_host * d->kp.neq * sizeof(double),
+                                   cudaMemcpyHostToDevice, d->stream));
+  st |= engine(d).upload(d);
+  st |= cuda_ok(cudaStreamSynchronize(d->stream));
+  return st;
+}
+
+int gch_download(gch_domain_t* d, double* u, double* primit) {
+  if (!d) return GCH_ERR_PARAM;
+  const size_t bytes = d->ncell_host * d->kp.neq * sizeof(double);
+  int st = GCH_OK;
+  if (u) {
+    st |= engine(d).download_u(d);
+    st |= cuda_ok(cudaMemcpyAsync(u, d->stage, bytes, cudaMemcpyDeviceToHost, d->stream));
+  }
+  if (primit) {
+    st |= engine(d).download_prim(d);
+    st |= cuda_ok(cudaMemcpyAsync(primit, d->stage, bytes, cudaMemcpyDeviceToHost, d->stream));
+  }
+  st |= cuda_ok(cudaStreamSynchronize(d->stream));
+  return st;
+}
+
+int gch_boundaryI(gch_domain_t* d) {
+  if (!d) return GCH_ERR_PARAM;
+  k_set_active<<<1, 1, 0, d->stream>>>(d->sc);
+  return engine(d).boundaryI(d);
+}
+
+int gch_calcprim(gch_domain_t* d) {
+  if (!d) return GCH_ERR_PARAM;
+  k_set_active<<<1, 1, 0, d->stream>>>(d->sc);
+  return engine(d).calcprim(d);
+}
+
+int gch_get_timestep(gch_domain_t* d, int current_iter, int n_iter, double current_time,
+                     double tprint, double* dt, int* dump_flag) {
+  if (!d || !dt || !dump_flag) return GCH_ERR_PARAM;
+  k_set_ctrl<<<1, 1, 0, d->stream>>>(d->sc, current_iter, n_iter, current_time, tprint, 0.0, 0.0, 1);
+  int st = engine(d).get_dt(d);
+  st |= fetch_scalars(d);
+  *dt = d->sc_host->dt;
+  if (d->sc_host->dump) *dump_flag = 1;
+  st |= d->sc_host->err;
+  return st;
+}
+
+int gch_tstep(gch_domain_t* d, double dt) {
+  if (!d) return GCH_ERR_PARAM;
+  if (!(dt > 0.0) || !std::isfinite(dt)) return GCH_ERR_DT;
+  k_set_dt<<<1, 1, 0, d->stream>>>(d->sc, dt);
+  return engine(d).tstep(d);
+}
+
+int gch_step_host(gch_domain_t* d, double* u, int current_iter, int n_iter, double current_time,
+                  double tprint, double* dt, int* dump_flag) {
+  if (!d || !u || !dt || !dump_flag) return GCH_ERR_PARAM;
+  const size_t bytes = d->ncell_host * d->kp.neq * sizeof(double);
+  int st = cuda_ok(cudaMemcpyAsync(d->stage, u, bytes, cudaMemcpyHostToDevice, d->stream));
+  st |= engine(d).upload(d);
+  if (d->prim_in) st |= engine(d).calcprim(d);
+  k_set_ctrl<<<1, 1, 0, d->stream>>>(d->sc, current_iter, n_iter, current_time, tprint, 0.0, 0.0, 1);
+  st |= engine(d).get_dt(d);
+  st |= engine(d).tstep(d);
+  st |= engine(d).download_u(d);
+  st |= cuda_ok(cudaMemcpyAsync(u, d->stage, bytes, cudaMemcpyDeviceToHost, d->stream));
+  st |= fetch_scalars(d);
+  *dt = d->sc_host->dt;
+  if (d->sc_host->dump) *dump_flag = 1;
+  st |= d->sc_host->err;
+  return st;
+}
+
+}  // extern "C"
+
+// Enqueue up to max_steps device-resident iterations (no host sync).
+int gch_advance_enqueue(gch_domain* d, int max_steps, double tmax, double dtprint, int n_iter,
+                        double time, int iter, double tprint) {
+  k_set_ctrl<<<1, 1, 0, d->stream>>>(d->sc, iter, n_iter, time, tprint, dtprint, tmax,
+                                     time <= tmax ? 1 : 0);
+  int st = cuda_ok(cudaGetLastError());
+  if (!d->graph) {
+    // capture one device-resident iteration of src/main.f90:94-125
+    cudaGraph_t g = nullptr;
+    st |= cuda_ok(cudaStreamBeginCapture(d->stream, cudaStreamCaptureModeThreadLocal));
+    st |= engine(d).get_dt(d);
+    st |= engine(d).tstep(d);
+    st |= engine(d).loopfin(d);
+    st |= cuda_ok(cudaStreamEndCapture(d->stream, &g));
+    if (st == GCH_OK) st |= cuda_ok(cudaGraphInstantiate(&d->graph, g, 0));
+    if (g) cudaGraphDestroy(g);
+    if (st) return st;
+  }
+  for (int n = 0; n < max_steps; ++n) st |= cuda_ok(cudaGraphLaunch(d->graph, d->stream));
+  return st;
+}
+
+// Wait for the enqueued iterations and read the loop state back.
+int gch_advance_finish(gch_domain* d, double* time, int* iter, double* tprint) {
+  int st = fetch_scalars(d);
+  if (time) *time = d->sc_host->time;
+  if (iter) *iter = d->sc_host->iter;
+  if (tprint) *tprint = d->sc_host->tprint;
+  st |= d->sc_host->err;
+  return st;
+}
+
+extern "C" {
+
+int gch_advance(gch_domain_t* d, int max_steps, double tmax, double dtprint, int n_iter,
+                double* time, int* iter, double* tprint, int* steps_done) {
+  if (!d || !time || !iter || !tprint) return GCH_ERR_PARAM;
+  const int iter0 = *iter;
+  int st = gch_advance_enqueue(d, max_steps, tmax, dtprint, n_iter, *time, *iter, *tprint);
+  if (st) return st;
+  st |= gch_advance_finish(d, time, iter, tprint);
+  if (steps_done) *steps_done = *iter - iter0;
+  return st;
+}
+
+int gch_last_step_info(gch_domain_t* d, long long* pfloor_hits, int* err_bits) {
+  if (!d) return GCH_ERR_PARAM;
+  int st = fetch_scalars(d);
+  if (pfloor_hits) *pfloor_hits = (long long)d->sc_host->pfloor;
+  if (err_bits) *err_bits = d->sc_host->err;
+  k_clear_info<<<1, 1, 0, d->stream>>>(d->sc);
+  return st;
+}
+
+int gch_launches_per_step(gch_domain_t* d) {
+  if (!d) return -1;
+  return d->launches + 2;  // + k_cfl and k_dtfin of get_timestep
+}
+
+}  // extern "C"

@@ -1,0 +1,522 @@
+// gch_device.cuh -- device-side building blocks of the GB300 timestep:
+// precision policies, the kernel parameter block, array indexing, and the
+// per-cell / per-interface physics of Guacho-3D restated for CUDA.
+//
+// Expression order follows the reference routine cited at each function
+// (left to right, parentheses kept): compiled without FMA contraction
+// (-fmad=false) the FP64 instantiation reproduces the reference's FP64 bits.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "guacho_gb300.h"
+
+namespace gch {
+
+constexpr int NG = 2;            // ghost cells per side (OT/parameters.f90:193)
+constexpr int kMaxNeq = 8;
+constexpr int TX = 32;           // stage-kernel tile width (one warp along x)
+constexpr int TY = 8;            // stage-kernel tile height
+constexpr int NT = TX * TY;
+
+// ---------------------------------------------------------------------------
+// Precision policies.
+//   TU: storage of u (the conserved state carried between steps)
+//   TS: storage of up / primit (stage state), E
+//   TC: arithmetic of reconstruction, Riemann fluxes and E
+struct PolFP64 {
+  using TU = double;
+  using TS = double;
+  using TC = double;
+  static constexpr int kMode = GCH_FP64;
+};
+struct PolMixed {
+  using TU = double;
+  using TS = float;
+  using TC = float;
+  static constexpr int kMode = GCH_FP32_MIXED;
+};
+
+// ---------------------------------------------------------------------------
+// Kernel parameter block (by value; tables live in device memory).
+struct KParams {
+  int nx, ny, nz;             // interior cells
+  int NX, NY, NZ;             // with ghosts
+  int pitch;                  // elements per x row (>= NX, multiple of 4)
+  long long fs;               // elements per field (pitch*NY*NZ)
+  int neq;
+  int mhd, pmhd;
+  int solver, limiter, eos, cooling;
+  int flux_cd, eight_wave, user_src;
+  int bc[6];                  // left,right,bottom,top,out,in
+  int bc_user;
+  double dx, dy, dz;
+  double cv, gamma, cfl, eta;
+  double Tempsc, Psc, tsc;
+  // cooling table (device pointers)
+  int ntab, tab_i0;
+  double tab_inv_dlog, tab_tail, tab_Tmin;
+  const double* tabT;
+  const double* tabL;
+  // user spheres and point masses (device pointers)
+  int nsph, ngrav;
+  const gch_sphere_t* sph;
+  const double* grav;         // [4][ngrav]: GM, x, y, z
+};
+
+// Scalars shared by the kernels of one step, resident in device memory so a
+// step can be captured in a CUDA graph without host round trips.
+struct StepScalars {
+  double dt;                  // dt_CFL of the step
+  double time;                // simulated time
+  double tprint;              // next output time
+  double dtprint;
+  double tmax;
+  unsigned long long dtmin_bits;  // running min of the CFL reduction
+  int iter;                   // currentIteration
+  int n_iter;
+  int dump;                   // dump flag of the last get_timestep
+  int err;                    // GCH_ERR_* bits raised on the device
+  int active;                 // loop condition of the device time loop
+  int pad;
+  unsigned long long pfloor;  // pressure-floor hits (u2prim)
+};
+
+__host__ __device__ inline long long cell_index(const KParams& p, int ax, int ay, int az) {
+  return ((long long)az * p.NY + ay) * p.pitch + ax;
+}
+
+// ---------------------------------------------------------------------------
+// Small helpers with the reference's semantics.
+template <class T>
+__device__ __forceinline__ T tmax_(T a, T b) { return a > b ? a : b; }
+template <class T>
+__device__ __forceinline__ T tmin_(T a, T b) { return a < b ? a : b; }
+__device__ __forceinline__ double tcopysign(double a, double b) { return copysign(a, b); }
+__device__ __forceinline__ float tcopysign(float a, float b) { return copysignf(a, b); }
+__device__ __forceinline__ double tsqrt(double a) { return sqrt(a); }
+__device__ __forceinline__ float tsqrt(float a) { return sqrtf(a); }
+__device__ __forceinline__ double tabs(double a) { return fabs(a); }
+__device__ __forceinline__ float tabs(float a) { return fabsf(a); }
+
+template <class T>
+__device__ __forceinline__ bool has_b(const KParams& p) { return p.neq >= 8; }
+
+// src/hydro_core.f90:395-476  prim2f (x direction)
+template <class T, int NEQ>
+__device__ __forceinline__ void prim2f(const KParams& p, const T* prim, T* ff) {
+  const T cv = (T)p.cv;
+  if (NEQ >= 8 && p.mhd) {
+    T etot = T(0.5) * (prim[0] * (prim[1] * prim[1] + prim[2] * prim[2] + prim[3] * prim[3])
+                       + prim[5] * prim[5] + prim[6] * prim[6] + prim[7] * prim[7])
+             + cv * prim[4];
+    ff[0] = prim[0] * prim[1];
+    ff[1] = prim[0] * prim[1] * prim[1] + prim[4]
+            + T(0.5) * (prim[6] * prim[6] + prim[7] * prim[7] - prim[5] * prim[5]);
+    ff[2] = prim[0] * prim[1] * prim[2] - prim[5] * prim[6];
+    ff[3] = prim[0] * prim[1] * prim[3] - prim[5] * prim[7];
+    ff[4] = prim[1] * (etot + prim[4]
+                       + T(0.5) * (prim[5] * prim[5] + prim[6] * prim[6] + prim[7] * prim[7]))
+            - prim[5] * (prim[1] * prim[5] + prim[2] * prim[6] + prim[3] * prim[7]);
+  } else {
+    T etot = T(0.5) * prim[0] * (prim[1] * prim[1] + prim[2] * prim[2] + prim[3] * prim[3])
+             + cv * prim[4];
+    ff[0] = prim[0] * prim[1];
+    ff[1] = prim[0] * prim[1] * prim[1] + prim[4];
+    ff[2] = prim[0] * prim[1] * prim[2];
+    ff[3] = prim[0] * prim[1] * prim[3];
+    ff[4] = prim[1] * (etot + prim[4]);
+  }
+  if (NEQ >= 8) {
+    ff[5] = T(0);
+    ff[6] = prim[1] * prim[6] - prim[5] * prim[2];
+    ff[7] = prim[1] * prim[7] - prim[5] * prim[3];
+  }
+}
+
+// src/hydro_core.f90:331-383  prim2u
+template <class T, int NEQ>
+__device__ __forceinline__ void prim2u(const KParams& p, const T* prim, T* uu) {
+  uu[0] = prim[0];
+  uu[1] = prim[0] * prim[1];
+  uu[2] = prim[0] * prim[2];
+  uu[3] = prim[0] * prim[3];
+  uu[4] = T(0.5) * prim[0] * (prim[1] * prim[1] + prim[2] * prim[2] + prim[3] * prim[3])
+          + (T)p.cv * prim[4];
+  if (NEQ >= 8) {
+    if (p.mhd) uu[4] = uu[4] + T(0.5) * (prim[5] * prim[5] + prim[6] * prim[6] + prim[7] * prim[7]);
+    uu[5] = prim[5];
+    uu[6] = prim[6];
+    uu[7] = prim[7];
+  }
+}
+
+// src/hydro_core.f90:591-604  cfastX
+template <class T>
+__device__ __forceinline__ T cfastX(const KParams& p, const T* prim) {
+  const T g = (T)p.gamma;
+  T b2 = prim[5] * prim[5] + prim[6] * prim[6] + prim[7] * prim[7];
+  T cs2va2 = (g * prim[4] + b2) / prim[0];
+  return tsqrt(T(0.5) * (cs2va2 + tsqrt(cs2va2 * cs2va2
+                                        - T(4.0) * g * prim[4] * (prim[5] * prim[5]) / prim[0]
+                                              / prim[0])));
+}
+
+// src/hydro_core.f90:544-553  csound
+template <class T>
+__device__ __forceinline__ T csound(const KParams& p, T pr, T d) {
+  return tsqrt((T)p.gamma * pr / d);
+}
+
+// src/hydro_core.f90:735-796  average (slope limiter)
+template <class T>
+__device__ __forceinline__ T average(int lim, T a, T b) {
+  T s, c, d, av, av1, av2;
+  const T delta = T(1e-7);
+  switch (lim) {
+    case GCH_LIMITER_NO_AVERAGE: return T(0);
+    case GCH_LIMITER_NO_LIMIT: return T(0.5) * (a + b);
+    case GCH_LIMITER_MINMOD:
+      s = tcopysign(T(1), a);
+      return s * tmax_(T(0), tmin_(tabs(a), s * b));
+    case GCH_LIMITER_VAN_LEER:
+      if (a * b <= T(0)) return T(0);
+      return a * b * (a + b) / (a * a + b * b);
+    case GCH_LIMITER_VAN_ALBADA:
+      return (a * (b * b + delta) + b * (a * a + delta)) / (a * a + b * b + delta);
+    case GCH_LIMITER_UMIST:
+      s = tcopysign(T(1), a);
+      c = T(0.25) * a + T(0.75) * b;
+      d = T(0.75) * a + T(0.25) * b;
+      av = tmin_(tmin_(tmin_(T(2) * tabs(a), T(2) * s * b), s * c), s * d);
+      return s * tmax_(T(0), av);
+    case GCH_LIMITER_WOODWARD:
+      s = tcopysign(T(1), a);
+      c = T(0.5) * (a + b);
+      av = tmin_(tmin_(T(2) * tabs(a), T(2) * s * b), s * c);
+      return s * tmax_(T(0), av);
+    case GCH_LIMITER_SUPERBEE:
+      s = tcopysign(T(1), b);
+      av1 = tmin_(T(2) * tabs(b), s * a);
+      av2 = tmin_(tabs(b), T(2) * s * a);
+      return s * tmax_(tmax_(T(0), av1), av2);
+  }
+  return T(0);
+}
+
+// ---------------------------------------------------------------------------
+// Riemann solvers, x direction.  `err` collects GCH_ERR_* bits.
+
+// src/hlld.f90:48-319  prim2fhlld
+template <class T>
+__device__ __forceinline__ void hlld(const KParams& p, const T* pl, const T* pr, T* ff, int& err) {
+  const T cv = (T)p.cv;
+  T csl = cfastX(p, pl);
+  T csr = cfastX(p, pr);
+  T sr = tmax_(pl[1] + csl, pr[1] + csr);
+  T sl = tmin_(pl[1] - csl, pr[1] - csr);
+  if (sl > T(0)) { prim2f<T, 8>(p, pl, ff); return; }
+  if (sr < T(0)) { prim2f<T, 8>(p, pr, ff); return; }
+
+  T bx = T(0.5) * (pl[5] + pr[5]);
+  T signBx = tcopysign(T(1), bx);
+  T pTL = pl[4] + T(0.5) * (bx * bx + pl[6] * pl[6] + pl[7] * pl[7]);
+  T pTR = pr[4] + T(0.5) * (bx * bx + pr[6] * pr[6] + pr[7] * pr[7]);
+  T slmul = sl - pl[1];
+  T srmur = sr - pr[1];
+  T rholul = pl[0] * pl[1];
+  T rhorur = pr[0] * pr[1];
+  T sM = (srmur * rhorur - slmul * rholul - pTR + pTL) / (srmur * pr[0] - slmul * pl[0]);
+  T srmsM = sr - sM;
+  T slmsM = sl - sM;
+  T rhostl = pl[0] * slmul / slmsM;
+  T rhostr = pr[0] * srmur / srmsM;
+  T sstl = sM - tabs(bx) / tsqrt(rhostl);
+  T sstr = sM + tabs(bx) / tsqrt(rhostr);
+  T pst = (srmur * pr[0] * pTL - slmul * pl[0] * pTR
+           + pl[0] * pr[0] * srmur * slmul * (pr[1] - pl[1]))
+          / (srmur * pr[0] - slmul * pl[0]);
+  T vstl, wstl, bystl, bzstl, vstr, wstr, bystr, bzstr;
+
+  if (sstl >= T(0)) {  // UL* region
+    T el = T(0.5) * pl[0] * (pl[1] * pl[1] + pl[2] * pl[2] + pl[3] * pl[3]) + cv * pl[4]
+           + T(0.5) * (bx * bx + pl[6] * pl[6] + pl[7] * pl[7]);
+    T sMmul = sM - pl[1];
+    T denl = pl[0] * slmul * slmsM - bx * bx;
+    if (denl == T(0)) {
+      vstl = pl[2]; wstl = pl[3]; bystl = T(0); bzstl = T(0);
+    } else {
+      vstl = pl[2] - bx * pl[6] * sMmul / denl;
+      wstl = pl[3] - bx * pl[7] * sMmul / denl;
+      bystl = pl[6] * (pl[0] * (slmul * slmul) - bx * bx) / denl;
+      bzstl = pl[7] * (pl[0] * (slmul * slmul) - bx * bx) / denl;
+    }
+    T vdotbl = pl[1] * bx + pl[2] * pl[6] + pl[3] * pl[7];
+    T vstdotbstl = sM * bx + vstl * bystl + wstl * bzstl;
+    T estl = (slmul * el - pTL * pl[1] + pst * sM + bx * (vdotbl - vstdotbstl)) / slmsM;
+    ff[0] = rhostl * sM;
+    ff[1] = rhostl * (sM * sM) + pst - bx * bx;
+    ff[2] = rhostl * sM * vstl - bx * bystl;
+    ff[3] = rhostl * sM * wstl - bx * bzstl;
+    ff[4] = sM * (estl + pst) - bx * (vstdotbstl);
+    ff[5] = T(0);
+    ff[6] = bystl * sM - bx * vstl;
+    ff[7] = bzstl * sM - bx * wstl;
+    return;
+  }
+  if (sstr <= T(0)) {  // UR* region
+    T er = T(0.5) * pr[0] * (pr[1] * pr[1] + pr[2] * pr[2] + pr[3] * pr[3]) + cv * pr[4]
+           + T(0.5) * (bx * bx + pr[6] * pr[6] + pr[7] * pr[7]);
+    T sMmur = sM - pr[1];
+    T denr = pr[0] * srmur * srmsM - bx * bx;
+    if (denr == T(0)) {
+      // the reference leaves the R star state uninitialised here
+      // (src/hlld.f90:167-171); mirror the L fallback
+      vstr = pr[2]; wstr = pr[3]; bystr = T(0); bzstr = T(0);
+    } else {
+      vstr = pr[2] - bx * pr[6] * sMmur / denr;
+      wstr = pr[3] - bx * pr[7] * sMmur / denr;
+      bystr = pr[6] * (pr[0] * (srmur * srmur) - bx * bx) / denr;
+      bzstr = pr[7] * (pr[0] * (srmur * srmur) - bx * bx) / denr;
+    }
+    T vdotbr = pr[1] * bx + pr[2] * pr[6] + pr[3] * pr[7];
+    T vstdotbstr = sM * bx + vstr * bystr + wstr * bzstr;
+    T estr = (srmur * er - pTR * pr[1] + pst * sM + bx * (vdotbr - vstdotbstr)) / srmsM;
+    ff[0] = rhostr * sM;
+    ff[1] = rhostr * (sM * sM) + pst - bx * bx;
+    ff[2] = rhostr * sM * vstr - bx * bystr;
+    ff[3] = rhostr * sM * wstr - bx * bzstr;
+    ff[4] = sM * (estr + pst) - bx * (vstdotbstr);
+    ff[5] = T(0);
+    ff[6] = bystr * sM - bx * vstr;
+    ff[7] = bzstr * sM - bx * wstr;
+    return;
+  }
+  T sMmul = sM - pl[1];
+  T sMmur = sM - pr[1];
+  T denl = pl[0] * slmul * slmsM - bx * bx;
+  T denr = pr[0] * srmur * srmsM - bx * bx;
+  if (denl == T(0)) {
+    vstl = pl[2]; wstl = pl[3]; bystl = T(0); bzstl = T(0);
+  } else {
+    vstl = pl[2] - bx * pl[6] * sMmul / denl;
+    wstl = pl[3] - bx * pl[7] * sMmul / denl;
+    bystl = pl[6] * (pl[0] * (slmul * slmul) - bx * bx) / denl;
+    bzstl = pl[7] * (pl[0] * (slmul * slmul) - bx * bx) / denl;
+  }
+  if (denr == T(0)) {
+    vstr = pr[2]; wstr = pr[3]; bystr = T(0); bzstr = T(0);
+  } else {
+    vstr = pr[2] - bx * pr[6] * sMmur / denr;
+    wstr = pr[3] - bx * pr[7] * sMmur / denr;
+    bystr = pr[6] * (pr[0] * (srmur * srmur) - bx * bx) / denr;
+    bzstr = pr[7] * (pr[0] * (srmur * srmur) - bx * bx) / denr;
+  }
+  T sql = tsqrt(rhostl), sqr = tsqrt(rhostr);
+  T dd = sql + sqr;
+  T vstst = (sql * vstl + sqr * vstr + (bystr - bystl) * signBx) / dd;
+  T wstst = (sql * wstl + sqr * wstr + (bzstr - bzstl) * signBx) / dd;
+  T sqlr = tsqrt(rhostl * rhostr);
+  T bystst = (sql * bystr + sqr * bystl + sqlr * (vstr - vstl) * signBx) / dd;
+  T bzstst = (sql * bzstr + sqr * bzstl + sqlr * (wstr - wstl) * signBx) / dd;
+  T vststdotbstst = sM * bx + vstst * bystst + wstst * bzstst;
+  if (sM >= T(0)) {  // UL** region
+    T el = T(0.5) * pl[0] * (pl[1] * pl[1] + pl[2] * pl[2] + pl[3] * pl[3]) + cv * pl[4]
+           + T(0.5) * (bx * bx + pl[6] * pl[6] + pl[7] * pl[7]);
+    T vdotbl = pl[1] * bx + pl[2] * pl[6] + pl[3] * pl[7];
+    T vstdotbstl = sM * bx + vstl * bystl + wstl * bzstl;
+    T estl = (slmul * el - pTL * pl[1] + pst * sM + bx * (vdotbl - vstdotbstl)) / slmsM;
+    T eststl = estl - sql * (vstdotbstl - vststdotbstst) * signBx;
+    ff[0] = rhostl * sM;
+    ff[1] = rhostl * (sM * sM) + pst - bx * bx;
+    ff[2] = rhostl * sM * vstst - bx * bystst;
+    ff[3] = rhostl * sM * wstst - bx * bzstst;
+    ff[4] = sM * (eststl + pst) - bx * (vststdotbstst);
+    ff[5] = T(0);
+    ff[6] = bystst * sM - bx * vstst;
+    ff[7] = bzstst * sM - bx * wstst;
+    return;
+  }
+  if (sM <= T(0)) {  // UR** region
+    T er = T(0.5) * pr[0] * (pr[1] * pr[1] + pr[2] * pr[2] + pr[3] * pr[3]) + cv * pr[4]
+           + T(0.5) * (bx * bx + pr[6] * pr[6] + pr[7] * pr[7]);
+    T vdotbr = pr[1] * bx + pr[2] * pr[6] + pr[3] * pr[7];
+    T vstdotbstr = sM * bx + vstr * bystr + wstr * bzstr;
+    T estr = (srmur * er - pTR * pr[1] + pst * sM + bx * (vdotbr - vstdotbstr)) / srmsM;
+    T eststr = estr + sqr * (vstdotbstr - vststdotbstst) * signBx;
+    ff[0] = rhostr * sM;
+    ff[1] = rhostr * (sM * sM) + pst - bx * bx;
+    ff[2] = rhostr * sM * vstst - bx * bystst;
+    ff[3] = rhostr * sM * wstst - bx * bzstst;
+    ff[4] = sM * (eststr + pst) - bx * (vststdotbstst);
+    ff[5] = T(0);
+    ff[6] = bystst * sM - bx * vstst;
+    ff[7] = bzstst * sM - bx * wstst;
+    return;
+  }
+  // src/hlld.f90:316-317 prints and stops here (sM not finite)
+  for (int q = 0; q < 8; ++q) ff[q] = sM;
+  err |= GCH_ERR_HLLD;
+}
+
+// src/hllc.f90:44-140  prim2fhllc (hydro, or passive B when NEQ == 8)
+template <class T, int NEQ>
+__device__ __forceinline__ void hllc(const KParams& p, const T* pl, const T* pr, T* ff, int& err) {
+  const T cv = (T)p.cv;
+  T csl = csound(p, pl[4], pl[0]);
+  T csr = csound(p, pr[4], pr[0]);
+  T sr = tmax_(pl[1] + csl, pr[1] + csr);
+  T sl = tmin_(pl[1] - csl, pr[1] - csr);
+  if (sl > T(0)) { prim2f<T, NEQ>(p, pl, ff); return; }
+  if (sr < T(0)) { prim2f<T, NEQ>(p, pr, ff); return; }
+  T slmul = sl - pl[1];
+  T srmur = sr - pr[1];
+  T rholul = pl[0] * pl[1];
+  T rhorur = pr[0] * pr[1];
+  T sst = (srmur * rhorur - slmul * rholul - pr[4] + pl[4]) / (srmur * pr[0] - slmul * pl[0]);
+  T uu[NEQ], uuk[NEQ];
+  if (sst >= T(0)) {
+    T rhost = pl[0] * (slmul) / (sl - sst);
+    T ek = T(0.5) * pl[0] * (pl[1] * pl[1] + pl[2] * pl[2] + pl[3] * pl[3]) + cv * pl[4];
+    uuk[0] = rhost;
+    uuk[1] = rhost * sst;
+    uuk[2] = rhost * pl[2];
+    uuk[3] = rhost * pl[3];
+    uuk[4] = rhost * (ek / pl[0] + (sst - pl[1]) * (sst + pl[4] / (pl[0] * slmul)));
+    if (NEQ >= 8) {
+      uuk[5] = rhost * pl[5] / pl[0];
+      uuk[6] = rhost * pl[6] / pl[0];
+      uuk[7] = rhost * pl[7] / pl[0];
+    }
+    prim2f<T, NEQ>(p, pl, ff);
+    prim2u<T, NEQ>(p, pl, uu);
+#pragma unroll
+    for (int q = 0; q < NEQ; ++q) ff[q] = ff[q] + sl * (uuk[q] - uu[q]);
+    return;
+  }
+  if (sst <= T(0)) {
+    T rhost = pr[0] * (srmur) / (sr - sst);
+    T ek = T(0.5) * pr[0] * (pr[1] * pr[1] + pr[2] * pr[2] + pr[3] * pr[3]) + cv * pr[4];
+    uuk[0] = rhost;
+    uuk[1] = rhost * sst;
+    uuk[2] = rhost * pr[2];
+    uuk[3] = rhost * pr[3];
+    uuk[4] = rhost * (ek / pr[0] + (sst - pr[1]) * (sst + pr[4] / (pr[0] * srmur)));
+    if (NEQ >= 8) {
+      uuk[5] = rhost * pr[5] / pr[0];
+      uuk[6] = rhost * pr[6] / pr[0];
+      uuk[7] = rhost * pr[7] / pr[0];
+    }
+    prim2f<T, NEQ>(p, pr, ff);
+    prim2u<T, NEQ>(p, pr, uu);
+#pragma unroll
+    for (int q = 0; q < NEQ; ++q) ff[q] = ff[q] + sr * (uuk[q] - uu[q]);
+    return;
+  }
+  // src/hllc.f90:135-138 prints and stops here
+#pragma unroll
+  for (int q = 0; q < NEQ; ++q) ff[q] = sst;
+  err |= GCH_ERR_HLLC;
+}
+
+// src/hlle.f90:48-83 (FAST=true, MHD) and src/hll.f90:47-82 (FAST=false)
+template <class T, int NEQ, bool FAST>
+__device__ __forceinline__ void hll2(const KParams& p, const T* pl, const T* pr, T* ff) {
+  T csl, csr;
+  if (FAST) {
+    csl = cfastX(p, pl);
+    csr = cfastX(p, pr);
+  } else {
+    csl = csound(p, pl[4], pl[0]);
+    csr = csound(p, pr[4], pr[0]);
+  }
+  T sr = tmax_(pl[1] + csl, pr[1] + csr);
+  T sl = tmin_(pl[1] - csl, pr[1] - csr);
+  if (sl > T(0)) { prim2f<T, NEQ>(p, pl, ff); return; }
+  if (sr < T(0)) { prim2f<T, NEQ>(p, pr, ff); return; }
+  T fL[NEQ], fR[NEQ], uL[NEQ], uR[NEQ];
+  prim2f<T, NEQ>(p, pl, fL);
+  prim2f<T, NEQ>(p, pr, fR);
+  prim2u<T, NEQ>(p, pl, uL);
+  prim2u<T, NEQ>(p, pr, uR);
+#pragma unroll
+  for (int q = 0; q < NEQ; ++q)
+    ff[q] = (sr * fL[q] - sl * fR[q] + sl * sr * (uR[q] - uL[q])) / (sr - sl);
+}
+
+template <int SOLVER, int NEQ>
+struct Riemann;
+template <>
+struct Riemann<GCH_SOLVER_HLLD, 8> {
+  template <class T>
+  __device__ __forceinline__ static void solve(const KParams& p, const T* l, const T* r, T* f,
+                                               int& e) {
+    hlld<T>(p, l, r, f, e);
+  }
+};
+template <int NEQ>
+struct Riemann<GCH_SOLVER_HLLC, NEQ> {
+  template <class T>
+  __device__ __forceinline__ static void solve(const KParams& p, const T* l, const T* r, T* f,
+                                               int& e) {
+    hllc<T, NEQ>(p, l, r, f, e);
+  }
+};
+template <>
+struct Riemann<GCH_SOLVER_HLLE, 8> {
+  template <class T>
+  __device__ __forceinline__ static void solve(const KParams& p, const T* l, const T* r, T* f,
+                                               int&) {
+    hll2<T, 8, true>(p, l, r, f);
+  }
+};
+template <int NEQ>
+struct Riemann<GCH_SOLVER_HLL, NEQ> {
+  template <class T>
+  __device__ __forceinline__ static void solve(const KParams& p, const T* l, const T* r, T* f,
+                                               int&) {
+    hll2<T, NEQ, false>(p, l, r, f);
+  }
+};
+
+// ---------------------------------------------------------------------------
+// Field permutations of swapy / swapz (src/hydro_core.f90:485-534):
+// component q of the rotated state is component perm(q) of the original.
+template <int DIR>
+__device__ __forceinline__ int perm(int q) {
+  if (DIR == 1) return q == 1 ? 2 : q == 2 ? 1 : q == 5 ? 6 : q == 6 ? 5 : q;
+  if (DIR == 2) return q == 1 ? 3 : q == 3 ? 1 : q == 5 ? 7 : q == 7 ? 5 : q;
+  return q;
+}
+
+// ---------------------------------------------------------------------------
+// Ghost mapping.  For an array coordinate c (0..N-1, interior NG..NG+n-1)
+// return the coordinate whose value a ghost cell holds after the boundary
+// fill, and whether the normal component flips sign (closed walls).
+// `layers` = 1 follows boundaryI (src/boundaries.f90:44-247), 2 boundaryII
+// (:256-512), both equal for layer 1.
+__device__ __forceinline__ int ghost_src(int c, int n, int bclo, int bchi, bool& flip) {
+  flip = false;
+  if (c < NG) {
+    int l = NG - 1 - c;  // 0 for the first ghost layer
+    if (bclo == GCH_BC_PERIODIC) return NG + n - 1 - l;
+    if (bclo == GCH_BC_CLOSED) flip = true;
+    return NG + l;
+  }
+  if (c >= NG + n) {
+    int l = c - (NG + n);
+    if (bchi == GCH_BC_PERIODIC) return NG + l;
+    if (bchi == GCH_BC_CLOSED) flip = true;
+    return NG + n - 1 - l;
+  }
+  return c;
+}
+
+// EXO/exoplanet.f90:156-158 cell position measured from the grid centre
+__device__ __forceinline__ double cell_pos(int a, int n, double d) {
+  int i = a - NG + 1;  // Fortran index
+  return ((double)(i - n / 2) + 0.5) * d;
+}
+
+}  // namespace gch

@@ -1,0 +1,61 @@
+// gch_domain.h -- host-side state of one domain and the per-precision engine
+// table.  Shared by the C-ABI layer (gch_api.cu) and the kernel instantiation
+// units (gch_fp64.cu, gch_fp32.cu).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "gch_device.cuh"
+#include "guacho_gb300.h"
+
+struct gch_domain {
+  gch_params_t hp;              // parameters as given
+  gch::KParams kp;              // kernel parameter block
+  cudaStream_t stream = nullptr;
+  bool own_stream = false;      // created here (destroyed with the domain)
+  int mode = GCH_FP64;
+  bool prim_in = false;         // tabulated cooling keeps a primit array
+  size_t tu_size = 8, ts_size = 8;
+  // device arrays
+  void* u = nullptr;            // neq fields, TU
+  void* up = nullptr;           // neq fields, TS
+  void* w = nullptr;            // neq fields, TU (stage-2 result when eta != 0)
+  void* E = nullptr;            // 3 fields, TS
+  void* s678 = nullptr;         // 3 fields, TS (eight-wave sources)
+  void* primit = nullptr;       // neq fields, TS (tabulated cooling)
+  double* tab = nullptr;        // [2][ntab]
+  gch_sphere_t* sph = nullptr;
+  double* grav = nullptr;       // [4][ngrav]
+  gch::StepScalars* sc = nullptr;       // device
+  gch::StepScalars* sc_host = nullptr;  // pinned mirror
+  double* stage = nullptr;      // device staging buffer, host layout (FP64 AoS)
+  size_t ncell_host = 0;        // NX*NY*NZ
+  int kz = 8;                   // z planes per block of the stage kernels
+  int launches = 0;             // kernel launches of the last tstep
+  // CUDA graph of one device-resident step (get_timestep + tstep + loop tail)
+  cudaGraphExec_t graph = nullptr;
+};
+
+namespace gch {
+
+struct EngineOps {
+  int (*get_dt)(gch_domain*);         // k_cfl + k_dtfin
+  int (*tstep)(gch_domain*);          // both stages + boundaries
+  int (*boundaryI)(gch_domain*);      // ghost layer of u + user spheres
+  int (*calcprim)(gch_domain*);       // primit from u (tabulated cooling)
+  int (*upload)(gch_domain*);         // stage (host layout) -> u
+  int (*download_u)(gch_domain*);     // u -> stage
+  int (*download_prim)(gch_domain*);  // primit -> stage
+  int (*loopfin)(gch_domain*);        // device time-loop tail
+};
+
+extern const EngineOps kEngineFP64;
+extern const EngineOps kEngineMixed;
+
+}  // namespace gch
+
+// Device-resident time loop split in its asynchronous and waiting halves
+// (used by the batched driver to overlap boxes on their own streams).
+int gch_advance_enqueue(gch_domain* d, int max_steps, double tmax, double dtprint, int n_iter,
+                        double time, int iter, double tprint);
+int gch_advance_finish(gch_domain* d, double* time, int* iter, double* tprint);

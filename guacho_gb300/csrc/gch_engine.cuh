@@ -1,0 +1,173 @@
+// gch_engine.cuh -- launch orchestration of one timestep for a precision
+// policy.  Included by exactly one translation unit per policy, which also
+// defines that policy's EngineOps table.
+#pragma once
+
+#include "gch_domain.h"
+#include "gch_kernels.cuh"
+
+namespace gch {
+
+inline int cuda_status(cudaError_t e) { return e == cudaSuccess ? GCH_OK : GCH_ERR_CUDA; }
+
+template <class Pol>
+struct Engine {
+  using TU = typename Pol::TU;
+  using TS = typename Pol::TS;
+
+  static dim3 cell_grid(const KParams& p) {
+    return dim3((p.nx + 31) / 32, (p.ny + 7) / 8, p.nz);
+  }
+
+  // ---- stage kernels, dispatched on solver and neq ----------------------
+  template <int SOLVER, int NEQ, int STAGE, bool PRIM_IN>
+  static void flux_launch(gch_domain* d, const void* src, void* dst) {
+    const KParams& p = d->kp;
+    dim3 grid((p.nx + TX - 1) / TX, (p.ny + TY - 1) / TY, (p.nz + d->kz - 1) / d->kz);
+    dim3 block(TX, TY);
+    using TIn = typename Src<Pol, NEQ, STAGE, PRIM_IN>::TIn;
+    using TD = typename std::conditional<STAGE == 1, TS, TU>::type;
+    k_flux<Pol, SOLVER, NEQ, STAGE, PRIM_IN><<<grid, block, 0, d->stream>>>(
+        p, (const TIn*)src, (const TU*)d->u, (TD*)dst, (TS*)d->E, (TS*)d->s678, d->sc, d->kz);
+  }
+
+  template <int STAGE, bool PRIM_IN>
+  static int flux(gch_domain* d, const void* src, void* dst) {
+    const int s = d->kp.solver, neq = d->kp.neq;
+    if (s == GCH_SOLVER_HLLD && neq == 8) flux_launch<GCH_SOLVER_HLLD, 8, STAGE, PRIM_IN>(d, src, dst);
+    else if (s == GCH_SOLVER_HLLC && neq == 5) flux_launch<GCH_SOLVER_HLLC, 5, STAGE, PRIM_IN>(d, src, dst);
+    else if (s == GCH_SOLVER_HLLC && neq == 8) flux_launch<GCH_SOLVER_HLLC, 8, STAGE, PRIM_IN>(d, src, dst);
+    else if (s == GCH_SOLVER_HLLE && neq == 8) flux_launch<GCH_SOLVER_HLLE, 8, STAGE, PRIM_IN>(d, src, dst);
+    else if (s == GCH_SOLVER_HLL && neq == 5) flux_launch<GCH_SOLVER_HLL, 5, STAGE, PRIM_IN>(d, src, dst);
+    else if (s == GCH_SOLVER_HLL && neq == 8) flux_launch<GCH_SOLVER_HLL, 8, STAGE, PRIM_IN>(d, src, dst);
+    else return GCH_ERR_PARAM;
+    return GCH_OK;
+  }
+
+  template <class T>
+  static void ghost(gch_domain* d, T* a, int layers) {
+    const KParams& p = d->kp;
+    for (int axis = 0; axis < 3; ++axis) {
+      int N0, N1;
+      if (axis == 0) { N0 = p.NY; N1 = p.NZ; }
+      else if (axis == 1) { N0 = p.NX; N1 = p.NZ; }
+      else { N0 = p.NX; N1 = p.NY; }
+      dim3 grid((N0 + 127) / 128, N1, 2 * layers);
+      k_ghost<T><<<grid, 128, 0, d->stream>>>(p, a, p.neq, axis, layers, d->sc);
+      ++d->launches;
+    }
+    if (p.bc_user && p.nsph > 0) {
+      k_user_bc<T><<<dim3(64, p.nsph), 256, 0, d->stream>>>(p, a, p.neq, d->sc);
+      ++d->launches;
+    }
+  }
+
+  // ---- get_timestep --------------------------------------------------------
+  static int get_dt(gch_domain* d) {
+    const KParams& p = d->kp;
+    dim3 grid = cell_grid(p), block(32, 8);
+    if (d->prim_in) {
+      if (p.neq == 8) k_cfl<Pol, 8, true><<<grid, block, 0, d->stream>>>(p, (const TS*)d->primit, d->sc);
+      else k_cfl<Pol, 5, true><<<grid, block, 0, d->stream>>>(p, (const TS*)d->primit, d->sc);
+    } else {
+      if (p.neq == 8) k_cfl<Pol, 8, false><<<grid, block, 0, d->stream>>>(p, (const TU*)d->u, d->sc);
+      else k_cfl<Pol, 5, false><<<grid, block, 0, d->stream>>>(p, (const TU*)d->u, d->sc);
+    }
+    k_dtfin<<<1, 1, 0, d->stream>>>(d->sc, p.cfl);
+    return cuda_status(cudaGetLastError());
+  }
+
+  // ---- tstep (src/hydro_solver.f90:134-229) ---------------------------------
+  static int tstep(gch_domain* d) {
+    const KParams& p = d->kp;
+    int st = GCH_OK;
+    d->launches = 0;
+    const bool ct = p.neq >= 8 && p.flux_cd;
+    const dim3 cgrid = cell_grid(p), cblock(32, 8);
+    // 1st half step: first-order fluxes, up = u - dtm*divF
+    if (d->prim_in) st |= flux<1, true>(d, d->primit, d->up);
+    else st |= flux<1, false>(d, d->u, d->up);
+    ++d->launches;
+    if (ct) {
+      k_ct<Pol, 1><<<cgrid, cblock, 0, d->stream>>>(p, (const TU*)d->u, (TS*)d->up,
+                                                     (const TS*)d->E, (const TS*)d->s678, d->sc);
+      ++d->launches;
+    }
+    // boundaryII on up (+ user spheres)
+    ghost<TS>(d, (TS*)d->up, 2);
+    // 2nd half step: limited reconstruction, u(+w) = u - dt*divF
+    void* dst2 = p.eta != 0.0 ? d->w : d->u;
+    st |= flux<2, false>(d, d->up, dst2);
+    ++d->launches;
+    if (ct) {
+      k_ct<Pol, 2><<<cgrid, cblock, 0, d->stream>>>(p, (const TU*)d->u, (TU*)dst2,
+                                                     (const TS*)d->E, (const TS*)d->s678, d->sc);
+      ++d->launches;
+    }
+    if (p.eta != 0.0) {
+      if (p.neq == 8) k_visc<Pol, 8><<<cgrid, cblock, 0, d->stream>>>(p, (TU*)d->u, (const TU*)d->w, (const TS*)d->up, d->sc);
+      else k_visc<Pol, 5><<<cgrid, cblock, 0, d->stream>>>(p, (TU*)d->u, (const TU*)d->w, (const TS*)d->up, d->sc);
+      ++d->launches;
+    }
+    if (d->prim_in) {  // tabulated cooling (updates primit and u(5))
+      if (p.neq == 8) k_cool<Pol, 8><<<cgrid, cblock, 0, d->stream>>>(p, (TU*)d->u, (TS*)d->primit, d->sc);
+      else k_cool<Pol, 5><<<cgrid, cblock, 0, d->stream>>>(p, (TU*)d->u, (TS*)d->primit, d->sc);
+      ++d->launches;
+    }
+    // boundaryI on u (+ user spheres), then primitives of the ghost shell
+    ghost<TU>(d, (TU*)d->u, 1);
+    if (d->prim_in) {
+      dim3 g((p.NX + 31) / 32, (p.NY + 7) / 8, p.NZ);
+      if (p.neq == 8) k_calcprim<Pol, 8><<<g, cblock, 0, d->stream>>>(p, (const TU*)d->u, (TS*)d->primit, 1, d->sc);
+      else k_calcprim<Pol, 5><<<g, cblock, 0, d->stream>>>(p, (const TU*)d->u, (TS*)d->primit, 1, d->sc);
+      ++d->launches;
+    }
+    st |= cuda_status(cudaGetLastError());
+    return st;
+  }
+
+  static int boundaryI(gch_domain* d) {
+    ghost<TU>(d, (TU*)d->u, 1);
+    return cuda_status(cudaGetLastError());
+  }
+
+  static int calcprim(gch_domain* d) {
+    if (!d->prim_in) return GCH_OK;  // primitives are formed on the fly
+    const KParams& p = d->kp;
+    dim3 g((p.NX + 31) / 32, (p.NY + 7) / 8, p.NZ), b(32, 8);
+    if (p.neq == 8) k_calcprim<Pol, 8><<<g, b, 0, d->stream>>>(p, (const TU*)d->u, (TS*)d->primit, 0, d->sc);
+    else k_calcprim<Pol, 5><<<g, b, 0, d->stream>>>(p, (const TU*)d->u, (TS*)d->primit, 0, d->sc);
+    return cuda_status(cudaGetLastError());
+  }
+
+  static int upload(gch_domain* d) {
+    k_aos_to_soa<TU><<<1024, 256, 0, d->stream>>>(d->kp, d->stage, (TU*)d->u, d->kp.neq);
+    return cuda_status(cudaGetLastError());
+  }
+  static int download_u(gch_domain* d) {
+    k_soa_to_aos<TU><<<1024, 256, 0, d->stream>>>(d->kp, (const TU*)d->u, d->stage, d->kp.neq);
+    return cuda_status(cudaGetLastError());
+  }
+  static int download_prim(gch_domain* d) {
+    const KParams& p = d->kp;
+    if (d->prim_in) {
+      k_soa_to_aos<TS><<<1024, 256, 0, d->stream>>>(p, (const TS*)d->primit, d->stage, p.neq);
+    } else if (p.neq == 8) {
+      k_prim_to_aos<Pol, 8><<<1024, 256, 0, d->stream>>>(p, (const TU*)d->u, d->stage);
+    } else {
+      k_prim_to_aos<Pol, 5><<<1024, 256, 0, d->stream>>>(p, (const TU*)d->u, d->stage);
+    }
+    return cuda_status(cudaGetLastError());
+  }
+  static int loopfin(gch_domain* d) {
+    k_loopfin<<<1, 1, 0, d->stream>>>(d->sc);
+    return cuda_status(cudaGetLastError());
+  }
+
+  static constexpr EngineOps ops() {
+    return EngineOps{&get_dt, &tstep, &boundaryI, &calcprim,
+                     &upload, &download_u, &download_prim, &loopfin};
+  }
+};
+
+}  // namespace gch

@@ -1,0 +1,731 @@
+// gch_kernels.cuh -- kernels of one Guacho timestep on sm_103a.
+//
+// A step is (src/hydro_solver.f90:134-229):
+//   k_flux<STAGE 1>   u (or primit) -> first-order HLL*-family fluxes on the
+//                     faces of an x-y tile marching along z; hydro update of
+//                     up(1:5) and the cell-centred E of flux-CD, fused
+//   k_ct<1>           up(6:8) from E (src/flux_cd_module.f90:311-321)
+//   k_ghost x3        boundaryII on up (2 layers) [+ k_user_bc]
+//   k_flux<STAGE 2>   up -> limited linear reconstruction + fluxes; u(1:5)
+//   k_ct<2>           u(6:8)
+//   [k_visc] [k_cool] k_ghost x3 (boundaryI, 1 layer) [+ k_user_bc]
+//   [k_prim_ghost]
+// and get_timestep is k_cfl (block min -> one atomic per block) + k_dtfin.
+//
+// Memory layout: structure of arrays, one 3-D array per field with the
+// reference's two ghost cells per side, x fastest, rows padded to a multiple
+// of 4 elements (16-byte aligned rows in FP32 and FP64).
+#pragma once
+
+#include <type_traits>
+
+#include "gch_policy.cuh"
+
+namespace gch {
+
+
+__device__ __forceinline__ void raise_err(int* errp, int bits) {
+  if (bits) atomicOr(errp, bits);
+}
+
+// ---------------------------------------------------------------------------
+// Per-cell prim load from the stage source.
+template <class Pol, int NEQ, int STAGE, bool PRIM_IN>
+struct Src {
+  using TC = typename Ops<Pol>::TC;
+  // STAGE 1: u (TU) or primit (TS, PRIM_IN); STAGE 2: up (TS)
+  using TIn = typename std::conditional<(STAGE == 1 && !PRIM_IN), typename Pol::TU,
+                                        typename Pol::TS>::type;
+  __device__ __forceinline__ static void load(const KParams& p, const TIn* src, long long idx,
+                                              TC* prim, unsigned& pfl) {
+    if (PRIM_IN)
+      Ops<Pol>::template load_stored_prim<NEQ>(p, src, idx, prim);
+    else
+      Ops<Pol>::template load_prim<NEQ>(p, src, idx, prim, pfl);
+  }
+};
+
+// ---------------------------------------------------------------------------
+// Stage kernel.  Block = TX x TY cells of one x-y tile; the block marches
+// over planes [kb, ke) of z.  Per plane:
+//   1. the prim plane with an H-cell halo (H = 1 first order, 2 limited)
+//      goes to shared memory (centre cells carried from the previous plane
+//      in registers, halo ring recomputed from global memory);
+//   2. x and y face fluxes of the tile -> shared memory; the z face k+1/2
+//      of each column in registers (face k-1/2 carried);
+//   3. each cell: hydro update (+ sources) and E from its six faces.
+// Fluxes are never written to global memory.
+template <class Pol, int SOLVER, int NEQ, int STAGE, bool PRIM_IN>
+__global__ void __launch_bounds__(NT)
+k_flux(KParams p, const typename Src<Pol, NEQ, STAGE, PRIM_IN>::TIn* __restrict__ src,
+       const typename Pol::TU* u,
+       typename std::conditional<STAGE == 1, typename Pol::TS, typename Pol::TU>::type* dst,
+       typename Pol::TS* __restrict__ E, typename Pol::TS* __restrict__ s678,
+       StepScalars* sc, int kz) {
+  using TC = typename Ops<Pol>::TC;
+  using TD = typename std::conditional<STAGE == 1, typename Pol::TS, typename Pol::TU>::type;
+  using S = Src<Pol, NEQ, STAGE, PRIM_IN>;
+  if (!sc->active) return;
+  constexpr int H = STAGE == 1 ? 1 : 2;
+  constexpr int PW = TX + 2 * H;
+  constexpr int PH = TY + 2 * H;
+  constexpr int NRING = 2 * H * (TX + TY);
+
+  __shared__ TC sP[NEQ][PH][PW];
+  __shared__ TC sF[NEQ][TY][TX + 1];
+  __shared__ TC sG[NEQ][TY + 1][TX];
+
+  const int tx = threadIdx.x, ty = threadIdx.y;
+  const int tid = ty * TX + tx;
+  const int i0 = blockIdx.x * TX, j0 = blockIdx.y * TY;
+  const int kb = blockIdx.z * kz;
+  const int ke = min(p.nz, kb + kz);
+  const int ci = i0 + tx, cj = j0 + ty;
+  const bool active = ci < p.nx && cj < p.ny;
+  const bool ct = NEQ >= 8 && p.flux_cd;
+  const int lim = p.limiter;
+
+  const double dt = STAGE == 1 ? sc->dt / 2.0 : sc->dt;  // dtm = dt_CFL/2.
+  const TC dtdx = (TC)(dt / p.dx), dtdy = (TC)(dt / p.dy), dtdz = (TC)(dt / p.dz);
+
+  int err = 0;
+  unsigned pfl = 0;
+
+  // clamp a global coordinate into the array (inactive lanes of partial
+  // tiles read valid memory; their values are never used)
+  auto gidx = [&](int ax, int ay, int az) -> long long {
+    ax = min(max(ax, 0), p.NX - 1);
+    ay = min(max(ay, 0), p.NY - 1);
+    az = min(max(az, 0), p.NZ - 1);
+    return cell_index(p, ax, ay, az);
+  };
+  const int axc = ci + NG, ayc = cj + NG;
+
+  // column state
+  TC pcen[NEQ];   // prim at (ci, cj, k)
+  TC pn[NEQ];     // prim at k+1 (STAGE 2)
+  TC slc[NEQ];    // z slope at k (STAGE 2)
+  TC hprev[NEQ];  // z flux at k-1/2
+  TC bzm = 0;     // Bz at k-1 (eight-wave div B)
+
+  // ---- prologue: z face kb-1/2 -------------------------------------------
+  {
+    if (STAGE == 1) {
+      TC pm[NEQ];
+      S::load(p, src, gidx(axc, ayc, kb - 1 + NG), pm, pfl);
+      S::load(p, src, gidx(axc, ayc, kb + NG), pcen, pfl);
+      if (NEQ >= 8) bzm = pm[7];
+      if (active) {
+        TC l[NEQ], r[NEQ], f[NEQ];
+#pragma unroll
+        for (int q = 0; q < NEQ; ++q) { l[q] = pm[perm<2>(q)]; r[q] = pcen[perm<2>(q)]; }
+        Riemann<SOLVER, NEQ>::solve(p, l, r, f, err);
+#pragma unroll
+        for (int q = 0; q < NEQ; ++q) hprev[perm<2>(q)] = f[q];
+      }
+    } else {
+      TC pm2[NEQ], pm1[NEQ];
+      S::load(p, src, gidx(axc, ayc, kb - 2 + NG), pm2, pfl);
+      S::load(p, src, gidx(axc, ayc, kb - 1 + NG), pm1, pfl);
+      S::load(p, src, gidx(axc, ayc, kb + NG), pcen, pfl);
+      S::load(p, src, gidx(axc, ayc, kb + 1 + NG), pn, pfl);
+      if (NEQ >= 8) bzm = pm1[7];
+      if (active) {
+        TC l[NEQ], r[NEQ], f[NEQ];
+#pragma unroll
+        for (int q = 0; q < NEQ; ++q) {
+          const int s = perm<2>(q);
+          TC sm1 = average(lim, pm1[s] - pm2[s], pcen[s] - pm1[s]);
+          slc[s] = average(lim, pcen[s] - pm1[s], pn[s] - pcen[s]);
+          l[q] = pm1[s] + sm1 * TC(0.5);
+          r[q] = pcen[s] - slc[s] * TC(0.5);
+        }
+        Riemann<SOLVER, NEQ>::solve(p, l, r, f, err);
+#pragma unroll
+        for (int q = 0; q < NEQ; ++q) hprev[perm<2>(q)] = f[q];
+      }
+    }
+  }
+
+  for (int k = kb; k < ke; ++k) {
+    const int az = k + NG;
+    // next column value(s)
+    TC pnext[NEQ];  // STAGE 1: prim at k+1; STAGE 2: prim at k+2
+    S::load(p, src, gidx(axc, ayc, az + (STAGE == 1 ? 1 : 2)), pnext, pfl);
+
+    __syncthreads();  // previous plane's readers are done with sP/sF/sG
+    // 1. prim plane k: centre from registers, halo ring from global memory
+#pragma unroll
+    for (int q = 0; q < NEQ; ++q) sP[q][ty + H][tx + H] = pcen[q];
+    for (int r = tid; r < NRING; r += NT) {
+      int hx, hy;
+      if (r < 2 * H * TX) {  // rows below / above the tile
+        const int row = r / TX;
+        hx = r % TX;
+        hy = row < H ? row - H : TY + (row - H);
+      } else {  // columns left / right
+        const int rr = r - 2 * H * TX;
+        const int col = rr / TY;
+        hy = rr % TY;
+        hx = col < H ? col - H : TX + (col - H);
+      }
+      TC pr[NEQ];
+      S::load(p, src, gidx(i0 + hx + NG, j0 + hy + NG, az), pr, pfl);
+#pragma unroll
+      for (int q = 0; q < NEQ; ++q) sP[q][hy + H][hx + H] = pr[q];
+    }
+    __syncthreads();
+
+    // 2a. x faces: face fx (0..TX) between tile cells fx-1 and fx
+    const int nfx = (TX + 1) * TY;
+    const int nfy = TX * (TY + 1);
+    for (int w = tid; w < nfx + nfy; w += NT) {
+      const bool isx = w < nfx;
+      int fx, fy;
+      if (isx) { fx = w % (TX + 1); fy = w / (TX + 1); }
+      else { fx = (w - nfx) % TX; fy = (w - nfx) / TX; }
+      // needed only if an adjacent cell is inside the domain
+      const bool need = isx ? (j0 + fy < p.ny && i0 + fx - 1 < p.nx)
+                            : (i0 + fx < p.nx && j0 + fy - 1 < p.ny);
+      if (!need) continue;
+      TC l[NEQ], r[NEQ], f[NEQ];
+      if (isx) {
+        const int cy = fy + H, cl = fx - 1 + H;
+#pragma unroll
+        for (int q = 0; q < NEQ; ++q) {
+          l[q] = sP[q][cy][cl];
+          r[q] = sP[q][cy][cl + 1];
+          if (STAGE == 2) {
+            const TC ll = sP[q][cy][cl - 1], rr = sP[q][cy][cl + 2];
+            const TC dl = l[q] - ll, dm = r[q] - l[q], dr = rr - r[q];
+            const TC al = average(lim, dl, dm), ar = average(lim, dm, dr);
+            l[q] = l[q] + al * TC(0.5);
+            r[q] = r[q] - ar * TC(0.5);
+          }
+        }
+        Riemann<SOLVER, NEQ>::solve(p, l, r, f, err);
+#pragma unroll
+        for (int q = 0; q < NEQ; ++q) sF[q][fy][fx] = f[q];
+      } else {
+        const int cx = fx + H, cl = fy - 1 + H;
+#pragma unroll
+        for (int q = 0; q < NEQ; ++q) {
+          const int s = perm<1>(q);
+          l[q] = sP[s][cl][cx];
+          r[q] = sP[s][cl + 1][cx];
+          if (STAGE == 2) {
+            const TC ll = sP[s][cl - 1][cx], rr = sP[s][cl + 2][cx];
+            const TC dl = l[q] - ll, dm = r[q] - l[q], dr = rr - r[q];
+            const TC al = average(lim, dl, dm), ar = average(lim, dm, dr);
+            l[q] = l[q] + al * TC(0.5);
+            r[q] = r[q] - ar * TC(0.5);
+          }
+        }
+        Riemann<SOLVER, NEQ>::solve(p, l, r, f, err);
+#pragma unroll
+        for (int q = 0; q < NEQ; ++q) sG[perm<1>(q)][fy][fx] = f[q];
+      }
+    }
+
+    // 2b. z face k+1/2 of this column
+    TC hnext[NEQ];
+    TC slnext[NEQ];
+    if (active) {
+      TC l[NEQ], r[NEQ], f[NEQ];
+      if (STAGE == 1) {
+#pragma unroll
+        for (int q = 0; q < NEQ; ++q) { l[q] = pcen[perm<2>(q)]; r[q] = pnext[perm<2>(q)]; }
+      } else {
+#pragma unroll
+        for (int q = 0; q < NEQ; ++q) {
+          const int s = perm<2>(q);
+          slnext[s] = average(lim, pn[s] - pcen[s], pnext[s] - pn[s]);
+          l[q] = pcen[s] + slc[s] * TC(0.5);
+          r[q] = pn[s] - slnext[s] * TC(0.5);
+        }
+      }
+      Riemann<SOLVER, NEQ>::solve(p, l, r, f, err);
+#pragma unroll
+      for (int q = 0; q < NEQ; ++q) hnext[perm<2>(q)] = f[q];
+    }
+    __syncthreads();
+
+    // 3. cell update and E
+    if (active) {
+      const long long c = cell_index(p, axc, ayc, az);
+      const int nupd = ct ? 5 : NEQ;
+      TC sv[NEQ];
+#pragma unroll
+      for (int q = 0; q < NEQ; ++q) sv[q] = TC(0);
+      const bool src_terms = p.user_src || (NEQ >= 8 && p.eight_wave);
+      if (src_terms) {
+        // src/sources.f90:190-220 with the cell's stage primitives
+        if (p.user_src) {
+          // EXO/user_mod.f90:158-206 point masses
+          const double xc = ((double)(ci + 1 - p.nx / 2) - 0.5) * p.dx;
+          const double yc = ((double)(cj + 1 - p.ny / 2) - 0.5) * p.dy;
+          const double zc = ((double)(k + 1 - p.nz / 2) - 0.5) * p.dz;
+          for (int l = 0; l < p.ngrav; ++l) {
+            const TC x = (TC)(xc - p.grav[p.ngrav + l]);
+            const TC y = (TC)(yc - p.grav[2 * p.ngrav + l]);
+            const TC z = (TC)(zc - p.grav[3 * p.ngrav + l]);
+            const TC GM = (TC)p.grav[l];
+            const TC rad2 = x * x + y * y + z * z;
+            const TC r15 = (TC)pow((double)rad2, 1.5);
+            sv[1] = sv[1] - pcen[0] * GM * x / r15;
+            sv[2] = sv[2] - pcen[0] * GM * y / r15;
+            sv[3] = sv[3] - pcen[0] * GM * z / r15;
+            sv[4] = sv[4] - pcen[0] * GM * (pcen[1] * x + pcen[2] * y + pcen[3] * z) / r15;
+          }
+        }
+        if (NEQ >= 8 && p.eight_wave) {
+          // src/sources.f90:124-175
+          const TC bzp = STAGE == 1 ? pnext[7] : pn[7];
+          const TC divB = (sP[5][ty + H][tx + H + 1] - sP[5][ty + H][tx + H - 1]) / (TC)(2.0 * p.dx)
+                          + (sP[6][ty + H + 1][tx + H] - sP[6][ty + H - 1][tx + H]) / (TC)(2.0 * p.dy)
+                          + (bzp - bzm) / (TC)(2.0 * p.dz);
+          sv[1] = sv[1] - divB * pcen[5];
+          sv[2] = sv[2] - divB * pcen[6];
+          sv[3] = sv[3] - divB * pcen[7];
+          sv[4] = sv[4] - divB * (pcen[1] * pcen[5] + pcen[2] * pcen[6] + pcen[3] * pcen[7]);
+          sv[5] = sv[5] - divB * pcen[1];
+          sv[6] = sv[6] - divB * pcen[2];
+          sv[7] = sv[7] - divB * pcen[3];
+        }
+      }
+#pragma unroll
+      for (int q = 0; q < NEQ; ++q) {
+        if (q < nupd) {
+          double unew = Ops<Pol>::update((double)u[q * p.fs + c], dtdx, dtdy, dtdz,
+                                         sF[q][ty][tx], sF[q][ty][tx + 1], sG[q][ty][tx],
+                                         sG[q][ty + 1][tx], hprev[q], hnext[q]);
+          if (src_terms) unew = unew + dt * (double)sv[q];
+          dst[q * p.fs + c] = (TD)unew;
+        }
+      }
+      if (ct) {
+        // src/flux_cd_module.f90:258-265
+        const TC e1 = TC(0.25) * (-sG[7][ty][tx] - sG[7][ty + 1][tx] + hprev[6] + hnext[6]);
+        const TC e2 = TC(0.25) * (+sF[7][ty][tx] + sF[7][ty][tx + 1] - hprev[5] - hnext[5]);
+        const TC e3 = TC(0.25) * (-sF[6][ty][tx] - sF[6][ty][tx + 1] + sG[5][ty][tx] + sG[5][ty + 1][tx]);
+        E[c] = e1;
+        E[p.fs + c] = e2;
+        E[2 * p.fs + c] = e3;
+        if (p.eight_wave) {
+          s678[c] = sv[5];
+          s678[p.fs + c] = sv[6];
+          s678[2 * p.fs + c] = sv[7];
+        }
+      }
+    }
+
+    // carry the column state to plane k+1
+    if (NEQ >= 8) bzm = pcen[7];
+#pragma unroll
+    for (int q = 0; q < NEQ; ++q) {
+      hprev[q] = hnext[q];
+      if (STAGE == 1) {
+        pcen[q] = pnext[q];
+      } else {
+        pcen[q] = pn[q];
+        pn[q] = pnext[q];
+        slc[q] = slnext[q];
+      }
+    }
+  }
+  raise_err(&sc->err, err);
+}
+
+// ---------------------------------------------------------------------------
+// Constrained transport of B (src/flux_cd_module.f90:311-321) with the E
+// ghost layer of boundaryI_ef (:45-237) applied as an index map.
+template <class Pol, int STAGE>
+__global__ void __launch_bounds__(256)
+k_ct(KParams p, const typename Pol::TU* u,
+     typename std::conditional<STAGE == 1, typename Pol::TS, typename Pol::TU>::type* dst,
+     const typename Pol::TS* __restrict__ E, const typename Pol::TS* __restrict__ s678,
+     StepScalars* sc) {
+  using TC = typename Ops<Pol>::TC;
+  using TD = typename std::conditional<STAGE == 1, typename Pol::TS, typename Pol::TU>::type;
+  const int ci = blockIdx.x * blockDim.x + threadIdx.x;
+  const int cj = blockIdx.y * blockDim.y + threadIdx.y;
+  const int ck = blockIdx.z;
+  if (ci >= p.nx || cj >= p.ny || !sc->active) return;
+  const int ax = ci + NG, ay = cj + NG, az = ck + NG;
+  const double dt = STAGE == 1 ? sc->dt / 2.0 : sc->dt;
+  const double dtdx = dt / p.dx, dtdy = dt / p.dy, dtdz = dt / p.dz;
+  const TC hx = (TC)(0.5 * dtdx), hy = (TC)(0.5 * dtdy), hz = (TC)(0.5 * dtdz);
+
+  // E component q at a face neighbour (the ghost layer follows boundaryI_ef:
+  // periodic copy, outflow copy, closed copy with the normal component of the
+  // x/y walls negated and nothing negated on z walls)
+  auto e_at = [&](int q, int bx, int by, int bz) -> TC {
+    bool fx = false, fy = false, fz = false;
+    const int sx = ghost_src(bx, p.nx, p.bc[0], p.bc[1], fx);
+    const int sy = ghost_src(by, p.ny, p.bc[2], p.bc[3], fy);
+    const int sz = ghost_src(bz, p.nz, p.bc[4], p.bc[5], fz);
+    TC v = (TC)E[q * p.fs + cell_index(p, sx, sy, sz)];
+    if ((fx && q == 0) || (fy && q == 1)) v = -v;
+    return v;
+  };
+  const long long c = cell_index(p, ax, ay, az);
+  const double u6 = (double)u[5 * p.fs + c];
+  const double u7 = (double)u[6 * p.fs + c];
+  const double u8 = (double)u[7 * p.fs + c];
+  double b6 = Ops<Pol>::ct(u6, hy, e_at(2, ax, ay - 1, az), e_at(2, ax, ay + 1, az), hz,
+                           e_at(1, ax, ay, az - 1), e_at(1, ax, ay, az + 1), true);
+  double b7 = Ops<Pol>::ct(u7, hx, e_at(2, ax - 1, ay, az), e_at(2, ax + 1, ay, az), hz,
+                           e_at(0, ax, ay, az - 1), e_at(0, ax, ay, az + 1), false);
+  double b8 = Ops<Pol>::ct(u8, hx, e_at(1, ax - 1, ay, az), e_at(1, ax + 1, ay, az), hy,
+                           e_at(0, ax, ay - 1, az), e_at(0, ax, ay + 1, az), true);
+  if (p.eight_wave) {
+    b6 = b6 + dt * (double)s678[c];
+    b7 = b7 + dt * (double)s678[p.fs + c];
+    b8 = b8 + dt * (double)s678[2 * p.fs + c];
+  }
+  dst[5 * p.fs + c] = (TD)b6;
+  dst[6 * p.fs + c] = (TD)b7;
+  dst[7 * p.fs + c] = (TD)b8;
+}
+
+// ---------------------------------------------------------------------------
+// Ghost fill of one axis (src/boundaries.f90:44-512): `layers` ghost layers
+// on both sides of `axis`, over the whole transverse extent.
+template <class T>
+__global__ void k_ghost(KParams p, T* a, int neq, int axis, int layers, const StepScalars* sc) {
+  if (!sc->active) return;
+  const int t0 = blockIdx.x * blockDim.x + threadIdx.x;  // transverse fast index
+  const int t1 = blockIdx.y;                              // transverse slow index
+  const int side_layer = blockIdx.z;                      // 2*layers entries
+  const int side = side_layer & 1;
+  const int l = side_layer >> 1;
+  int n, N0, N1, blo, bhi;
+  if (axis == 0) { n = p.nx; N0 = p.NY; N1 = p.NZ; blo = p.bc[0]; bhi = p.bc[1]; }
+  else if (axis == 1) { n = p.ny; N0 = p.NX; N1 = p.NZ; blo = p.bc[2]; bhi = p.bc[3]; }
+  else { n = p.nz; N0 = p.NX; N1 = p.NY; blo = p.bc[4]; bhi = p.bc[5]; }
+  if (t0 >= N0 || t1 >= N1 || l >= layers) return;
+  const int bc = side ? bhi : blo;
+  if (bc == GCH_BC_OTHER) return;
+  const int g = side ? NG + n + l : NG - 1 - l;
+  bool flip;
+  const int s = ghost_src(g, n, blo, bhi, flip);
+  int dx, dy, dz, sx, sy, sz;
+  if (axis == 0) { dx = g; sx = s; dy = sy = t0; dz = sz = t1; }
+  else if (axis == 1) { dy = g; sy = s; dx = sx = t0; dz = sz = t1; }
+  else { dz = g; sz = s; dx = sx = t0; dy = sy = t1; }
+  const long long di = cell_index(p, dx, dy, dz), si = cell_index(p, sx, sy, sz);
+  for (int q = 0; q < neq; ++q) {
+    T v = a[q * p.fs + si];
+    if (flip && q == axis + 1) v = -v;
+    a[q * p.fs + di] = v;
+  }
+}
+
+// User boundary spheres (EXO/exoplanet.f90:125-266 pattern) over the box
+// [lo, hi) of array coordinates of sphere `m`; the first sphere containing a
+// cell wins.
+template <class T>
+__global__ void k_user_bc(KParams p, T* a, int neq, const StepScalars* sc) {
+  if (!sc->active) return;
+  const int m = blockIdx.y;
+  const gch_sphere_t sp = p.sph[m];
+  // bounding box of the sphere in array coordinates, clipped to the array
+  auto lo_hi = [&](double c, double r, double d, int n, int N, int& lo, int& hi) {
+    // cell centre of array coordinate a: ((a-NG+1 - n/2) + 0.5)*d
+    double amin = (c - r) / d - 0.5 + n / 2 + NG - 1;
+    double amax = (c + r) / d - 0.5 + n / 2 + NG - 1;
+    lo = max(0, (int)floor(amin) - 1);
+    hi = min(N, (int)ceil(amax) + 2);
+  };
+  int xl, xh, yl, yh, zl, zh;
+  lo_hi(sp.xc, sp.radius, p.dx, p.nx, p.NX, xl, xh);
+  lo_hi(sp.yc, sp.radius, p.dy, p.ny, p.NY, yl, yh);
+  lo_hi(sp.zc, sp.radius, p.dz, p.nz, p.NZ, zl, zh);
+  const long long wx = xh - xl, wy = yh - yl, wz = zh - zl;
+  if (wx <= 0 || wy <= 0 || wz <= 0) return;
+  const long long total = wx * wy * wz;
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < total;
+       t += (long long)gridDim.x * blockDim.x) {
+    const int ax = xl + (int)(t % wx);
+    const int ay = yl + (int)((t / wx) % wy);
+    const int az = zl + (int)(t / (wx * wy));
+    const double x = cell_pos(ax, p.nx, p.dx);
+    const double y = cell_pos(ay, p.ny, p.dy);
+    const double z = cell_pos(az, p.nz, p.dz);
+    bool earlier = false;
+    for (int e = 0; e < m; ++e) {
+      const gch_sphere_t& q = p.sph[e];
+      const double xs = x - q.xc, ys = y - q.yc, zs = z - q.zc;
+      if (sqrt(xs * xs + ys * ys + zs * zs) <= q.radius) { earlier = true; break; }
+    }
+    if (earlier) continue;
+    const double xs = x - sp.xc, ys = y - sp.yc, zs = z - sp.zc;
+    double rads = sqrt(xs * xs + ys * ys + zs * zs);
+    if (!(rads <= sp.radius)) continue;
+    if (rads == 0.0) rads = p.dx * 0.10;
+    const double velx = sp.vorb[0] + sp.vwind * xs / rads;
+    const double vely = sp.vorb[1] + sp.vwind * ys / rads;
+    const double velz = sp.vorb[2] + sp.vwind * zs / rads;
+    const double dens = sp.dens;
+    const long long c = cell_index(p, ax, ay, az);
+    a[c] = (T)dens;
+    a[p.fs + c] = (T)(dens * velx);
+    a[2 * p.fs + c] = (T)(dens * vely);
+    a[3 * p.fs + c] = (T)(dens * velz);
+    double b2 = 0.0;
+    if (neq >= 8) {
+      const double rr = sp.radius / rads;
+      const double cpi = sp.bdip * (rr * rr * rr) / (2.0 * (rads * rads));
+      const double b5 = 3.0 * ys * xs * cpi;
+      const double b6 = (3.0 * (ys * ys) - rads * rads) * cpi;
+      const double b7 = 3.0 * ys * zs * cpi;
+      a[5 * p.fs + c] = (T)b5;
+      a[6 * p.fs + c] = (T)b6;
+      a[7 * p.fs + c] = (T)b7;
+      b2 = b5 * b5 + b6 * b6 + b7 * b7;
+    }
+    double e = 0.5 * dens * (velx * velx + vely * vely + velz * velz) + p.cv * dens * sp.tfac;
+    if (p.mhd) e = e + 0.5 * b2;
+    a[4 * p.fs + c] = (T)e;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// CFL reduction (src/hydro_core.f90:644-675): per-cell candidate, warp
+// shuffle min, one atomicMin per block on the bits of the positive double.
+template <class Pol, int NEQ, bool PRIM_IN>
+__global__ void __launch_bounds__(256)
+k_cfl(KParams p, const typename std::conditional<PRIM_IN, typename Pol::TS, typename Pol::TU>::type* src,
+      StepScalars* sc) {
+  using TC = typename Ops<Pol>::TC;
+  if (!sc->active) return;
+  const int ci = blockIdx.x * blockDim.x + threadIdx.x;
+  const int cj = blockIdx.y * blockDim.y + threadIdx.y;
+  const int ck = blockIdx.z;
+  double dtp = 1e30;
+  int bad = 0;
+  if (ci < p.nx && cj < p.ny) {
+    const long long c = cell_index(p, ci + NG, cj + NG, ck + NG);
+    TC pr[NEQ];
+    TC cand[3];
+    unsigned pfl = 0;
+    if (PRIM_IN)
+      Ops<Pol>::template load_stored_prim<NEQ>(p, src, c, pr);
+    else
+      Ops<Pol>::template load_prim<NEQ>(p, src, c, pr, pfl);
+    if (NEQ >= 8 && p.mhd) {
+      // src/hydro_core.f90:568-581 cfast
+      const TC g = (TC)p.gamma;
+      const TC bx = pr[5], by = pr[6], bz = pr[7];
+      const TC b2 = bx * bx + by * by + bz * bz;
+      const TC a = g * pr[4] + b2;
+      const TC cx = tsqrt(TC(0.5) * (a + tsqrt(a * a - TC(4.0) * g * pr[4] * bx * bx)) / pr[0]);
+      const TC cy = tsqrt(TC(0.5) * (a + tsqrt(a * a - TC(4.0) * g * pr[4] * by * by)) / pr[0]);
+      const TC cz = tsqrt(TC(0.5) * (a + tsqrt(a * a - TC(4.0) * g * pr[4] * bz * bz)) / pr[0]);
+      cand[0] = (TC)p.dx / (tabs(pr[1]) + cx);
+      cand[1] = (TC)p.dy / (tabs(pr[2]) + cy);
+      cand[2] = (TC)p.dz / (tabs(pr[3]) + cz);
+    } else {
+      const TC c0 = csound(p, pr[4], pr[0]);
+      cand[0] = (TC)p.dx / (tabs(pr[1]) + c0);
+      cand[1] = (TC)p.dy / (tabs(pr[2]) + c0);
+      cand[2] = (TC)p.dz / (tabs(pr[3]) + c0);
+    }
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+      if (cand[d] == cand[d]) dtp = tmin_(dtp, (double)cand[d]);
+      else bad = 1;
+    }
+    if (pfl) atomicAdd(&sc->pfloor, (unsigned long long)pfl);
+  }
+  if (__any_sync(0xffffffffu, bad) && (threadIdx.x & 31) == 0) atomicOr(&sc->err, GCH_ERR_DT);
+  for (int o = 16; o > 0; o >>= 1) dtp = tmin_(dtp, __shfl_xor_sync(0xffffffffu, dtp, o));
+  __shared__ double sm[8];
+  const int lane = (threadIdx.y * blockDim.x + threadIdx.x) & 31;
+  const int wid = (threadIdx.y * blockDim.x + threadIdx.x) >> 5;
+  if (lane == 0) sm[wid] = dtp;
+  __syncthreads();
+  if (wid == 0) {
+    const int nw = (blockDim.x * blockDim.y) >> 5;
+    double v = lane < nw ? sm[lane] : 1e30;
+    for (int o = 16; o > 0; o >>= 1) v = tmin_(v, __shfl_xor_sync(0xffffffffu, v, o));
+    if (lane == 0) {
+      // positive doubles order like their bit patterns
+      atomicMin(&sc->dtmin_bits, (unsigned long long)__double_as_longlong(v));
+    }
+  }
+}
+
+// get_timestep's scalar tail (src/hydro_core.f90:677-694) and the bookkeeping
+// of the device time loop (src/main.f90:94-125).
+static __global__ void k_dtfin(StepScalars* sc, double cfl) {
+  if (!sc->active) return;
+  double dtp = __longlong_as_double((long long)sc->dtmin_bits);
+  sc->dtmin_bits = 0x7FF0000000000000ull;  // +inf for the next reduction
+  if (sc->iter <= sc->n_iter)
+    dtp = cfl * ldexp(1.0, -(sc->n_iter + 1 - sc->iter)) * dtp;
+  else
+    dtp = cfl * dtp;
+  double dt = dtp;
+  int dump = 0;
+  if ((sc->time + dt) >= sc->tprint) {
+    dt = sc->tprint - sc->time;
+    dump = 1;
+  }
+  if (!(dt > 0.0) || !(dt < 1e300)) sc->err |= GCH_ERR_DT;
+  sc->dt = dt;
+  sc->dump = dump;
+}
+
+// Time-loop tail after a tstep (src/main.f90:108-123): device-resident loop.
+static __global__ void k_loopfin(StepScalars* sc) {
+  if (!sc->active) return;
+  sc->time = sc->time + sc->dt;
+  if (sc->dump) {
+    sc->tprint = sc->tprint + sc->dtprint;
+    sc->dump = 0;
+  }
+  sc->iter = sc->iter + 1;
+  sc->active = (sc->time <= sc->tmax) && sc->err == 0;
+}
+
+// ---------------------------------------------------------------------------
+// Tabulated cooling (src/cooling_dmc.f90:115-156, src/cooling_chi.f90:114-154),
+// FP64 throughout (the reference keeps Lambda in real(8)).  Writes primit of
+// every interior cell and u(5) of the cooled ones.
+template <class Pol, int NEQ>
+__global__ void k_cool(KParams p, typename Pol::TU* u, typename Pol::TS* primit,
+                       StepScalars* sc) {
+  const int ci = blockIdx.x * blockDim.x + threadIdx.x;
+  const int cj = blockIdx.y * blockDim.y + threadIdx.y;
+  const int ck = blockIdx.z;
+  if (ci >= p.nx || cj >= p.ny || !sc->active) return;
+  const long long c = cell_index(p, ci + NG, cj + NG, ck + NG);
+  double uu[NEQ], pp[NEQ];
+#pragma unroll
+  for (int q = 0; q < NEQ; ++q) uu[q] = (double)u[q * p.fs + c];
+  unsigned pfl = 0;
+  double T;
+  Ops<PolFP64>::u2prim<NEQ>(p, uu, pp, pfl, &T);
+  if (T > p.tab_Tmin) {
+    const double Eth0 = p.cv * pp[4];
+    double aloss;
+    if (T > 1e8) {
+      aloss = p.tab_tail * sqrt(T);
+    } else {
+      int if1 = (int)(log10(T) * p.tab_inv_dlog) - p.tab_i0;
+      if1 = max(0, min(if1, p.ntab - 2));
+      const double T0 = p.tabT[if1], c0 = p.tabL[if1];
+      const double T1 = p.tabT[if1 + 1], c1 = p.tabL[if1 + 1];
+      aloss = (c1 - c0) * (T - T0) / (T1 - T0) + c0;
+    }
+    const double dens = pp[0];
+    const double ce = (aloss * (dens * dens)) / (Eth0 * p.Psc);
+    pp[4] = pp[4] * exp(-ce * (sc->dt * p.tsc));
+    u[4 * p.fs + c] = (typename Pol::TU)(uu[4] - Eth0 + p.cv * pp[4]);
+  }
+#pragma unroll
+  for (int q = 0; q < NEQ; ++q) primit[q * p.fs + c] = (typename Pol::TS)pp[q];
+}
+
+// src/hydro_solver.f90:47-65 viscous_copy: u = w + eta*(sum of the six
+// neighbours - 6 w); w holds the stage-2 interior, its ghosts are up's.
+template <class Pol, int NEQ>
+__global__ void k_visc(KParams p, typename Pol::TU* u, const typename Pol::TU* w,
+                       const typename Pol::TS* up, const StepScalars* sc) {
+  const int ci = blockIdx.x * blockDim.x + threadIdx.x;
+  const int cj = blockIdx.y * blockDim.y + threadIdx.y;
+  const int ck = blockIdx.z;
+  if (ci >= p.nx || cj >= p.ny || !sc->active) return;
+  const int ax = ci + NG, ay = cj + NG, az = ck + NG;
+  auto val = [&](int q, int x, int y, int z) -> double {
+    const bool inside = x >= NG && x < NG + p.nx && y >= NG && y < NG + p.ny && z >= NG &&
+                        z < NG + p.nz;
+    const long long c = cell_index(p, x, y, z);
+    return inside ? (double)w[q * p.fs + c] : (double)up[q * p.fs + c];
+  };
+  const long long c = cell_index(p, ax, ay, az);
+  for (int q = 0; q < NEQ; ++q) {
+    const double v = val(q, ax, ay, az);
+    u[q * p.fs + c] = (typename Pol::TU)(
+        v + p.eta * (val(q, ax + 1, ay, az) + val(q, ax - 1, ay, az) + val(q, ax, ay + 1, az) +
+                     val(q, ax, ay - 1, az) + val(q, ax, ay, az + 1) + val(q, ax, ay, az - 1) -
+                     6.0 * v));
+  }
+}
+
+// calcprim over the one-cell ghost shell (src/hydro_core.f90:258-300) or over
+// the whole array; writes primit in the stored type.
+template <class Pol, int NEQ>
+__global__ void k_calcprim(KParams p, const typename Pol::TU* u, typename Pol::TS* primit,
+                           int only_ghost, const StepScalars* sc) {
+  const int ax = blockIdx.x * blockDim.x + threadIdx.x;
+  const int ay = blockIdx.y * blockDim.y + threadIdx.y;
+  const int az = blockIdx.z;
+  if (ax >= p.NX || ay >= p.NY || !sc->active) return;
+  if (only_ghost) {
+    // the shell of the box [NG-1, NG+n] in each direction
+    const bool inx = ax >= NG - 1 && ax <= NG + p.nx, iny = ay >= NG - 1 && ay <= NG + p.ny,
+               inz = az >= NG - 1 && az <= NG + p.nz;
+    if (!(inx && iny && inz)) return;
+    const bool shell = ax == NG - 1 || ax == NG + p.nx || ay == NG - 1 || ay == NG + p.ny ||
+                       az == NG - 1 || az == NG + p.nz;
+    if (!shell) return;
+  }
+  const long long c = cell_index(p, ax, ay, az);
+  double uu[NEQ], pp[NEQ];
+#pragma unroll
+  for (int q = 0; q < NEQ; ++q) uu[q] = (double)u[q * p.fs + c];
+  unsigned pfl = 0;
+  Ops<PolFP64>::u2prim<NEQ>(p, uu, pp, pfl);
+#pragma unroll
+  for (int q = 0; q < NEQ; ++q) primit[q * p.fs + c] = (typename Pol::TS)pp[q];
+}
+
+// Host layout (Fortran u(neq, x, y, z), FP64, no pitch) <-> device SoA.
+template <class T>
+__global__ void k_aos_to_soa(KParams p, const double* __restrict__ aos, T* __restrict__ soa,
+                             int neq) {
+  const long long n = (long long)p.NX * p.NY * p.NZ;
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n;
+       t += (long long)gridDim.x * blockDim.x) {
+    const int ax = (int)(t % p.NX);
+    const int ay = (int)((t / p.NX) % p.NY);
+    const int az = (int)(t / ((long long)p.NX * p.NY));
+    const long long c = cell_index(p, ax, ay, az);
+    for (int q = 0; q < neq; ++q) soa[q * p.fs + c] = (T)aos[t * neq + q];
+  }
+}
+template <class T>
+__global__ void k_soa_to_aos(KParams p, const T* __restrict__ soa, double* __restrict__ aos,
+                             int neq) {
+  const long long n = (long long)p.NX * p.NY * p.NZ;
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n;
+       t += (long long)gridDim.x * blockDim.x) {
+    const int ax = (int)(t % p.NX);
+    const int ay = (int)((t / p.NX) % p.NY);
+    const int az = (int)(t / ((long long)p.NX * p.NY));
+    const long long c = cell_index(p, ax, ay, az);
+    for (int q = 0; q < neq; ++q) aos[t * neq + q] = (double)soa[q * p.fs + c];
+  }
+}
+// primit (full array, from u) straight into the host layout
+template <class Pol, int NEQ>
+__global__ void k_prim_to_aos(KParams p, const typename Pol::TU* __restrict__ u,
+                              double* __restrict__ aos) {
+  const long long n = (long long)p.NX * p.NY * p.NZ;
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n;
+       t += (long long)gridDim.x * blockDim.x) {
+    const int ax = (int)(t % p.NX);
+    const int ay = (int)((t / p.NX) % p.NY);
+    const int az = (int)(t / ((long long)p.NX * p.NY));
+    const long long c = cell_index(p, ax, ay, az);
+    double uu[NEQ], pp[NEQ];
+    for (int q = 0; q < NEQ; ++q) uu[q] = (double)u[q * p.fs + c];
+    unsigned pfl = 0;
+    Ops<PolFP64>::u2prim<NEQ>(p, uu, pp, pfl);
+    for (int q = 0; q < NEQ; ++q) aos[t * NEQ + q] = pp[q];
+  }
+}
+
+}  // namespace gch

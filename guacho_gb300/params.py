@@ -1,0 +1,124 @@
+"""The parameter surface of Guacho's parameters.f90 as a Python object.
+
+Field names follow OT/parameters.f90:48-177 (riemann_solver, slope_limiter,
+bc_left, cfl, eta, ...).  `Params` is converted to the C-ABI struct
+`gch_params_t` (include/guacho_gb300.h) by `guacho_gb300._abi`.
+"""
+from __future__ import annotations
+
+import dataclasses
+import math
+from dataclasses import dataclass, field
+
+# src/constants.f90:56-98
+SOLVER_HLL, SOLVER_HLLC, SOLVER_HLLE, SOLVER_HLLD = 1, 2, 3, 4
+EOS_ADIABATIC, EOS_SINGLE_SPECIE = 1, 2
+COOL_NONE, COOL_DMC, COOL_CHI = 0, 3, 4
+BC_OUTFLOW, BC_CLOSED, BC_PERIODIC, BC_OTHER = 1, 2, 3, 4
+(LIMITER_NO_AVERAGE, LIMITER_NO_LIMIT, LIMITER_MINMOD, LIMITER_VAN_LEER,
+ LIMITER_VAN_ALBADA, LIMITER_UMIST, LIMITER_WOODWARD, LIMITER_SUPERBEE) = range(-1, 7)
+
+# precision modes (include/guacho_gb300.h)
+FP64, FP32_MIXED, FP32_KAHAN = 0, 1, 2
+NGHOST = 2
+
+
+@dataclass
+class Sphere:
+    """A wind sphere re-imposed by the user boundary hook (EXO pattern)."""
+    xc: float = 0.0
+    yc: float = 0.0
+    zc: float = 0.0
+    radius: float = 0.1
+    dens: float = 1.0
+    vwind: float = 0.0
+    vorb: tuple = (0.0, 0.0, 0.0)
+    tfac: float = 1.0
+    bdip: float = 0.0
+
+
+@dataclass
+class Params:
+    nx: int = 128
+    ny: int = 128
+    nz: int = 4
+    precision: int = FP64
+    mhd: bool = True
+    pmhd: bool = False
+    riemann_solver: int = SOLVER_HLLD
+    slope_limiter: int = LIMITER_MINMOD
+    eq_of_state: int = EOS_ADIABATIC
+    cooling: int = COOL_NONE
+    enable_flux_cd: bool = True
+    eight_wave: bool = False
+    user_source_terms: bool = False
+    bc_left: int = BC_PERIODIC
+    bc_right: int = BC_PERIODIC
+    bc_bottom: int = BC_PERIODIC
+    bc_top: int = BC_PERIODIC
+    bc_out: int = BC_PERIODIC
+    bc_in: int = BC_PERIODIC
+    bc_user: bool = False
+    xmax: float = 1.0
+    ymax: float = 1.0
+    zmax: float = 1.0
+    cv: float = 1.5
+    cfl: float = 0.2
+    eta: float = 0.0
+    Tempsc: float = 1.0
+    Psc: float = 1.0
+    tsc: float = 1.0
+    # tabulated cooling
+    tab_T: list = field(default_factory=list)
+    tab_L: list = field(default_factory=list)
+    tab_inv_dlog: float = 10.0
+    tab_i0: int = 40
+    tab_tail: float = 0.27e-26
+    tab_Tmin: float = 1e4
+    spheres: list = field(default_factory=list)
+    # point masses: (GM, x, y, z)
+    grav: list = field(default_factory=list)
+
+    @property
+    def bfield(self) -> bool:
+        return self.mhd or self.pmhd
+
+    @property
+    def neq(self) -> int:
+        return 8 if self.bfield else 5
+
+    @property
+    def gamma(self) -> float:
+        return (self.cv + 1.0) / self.cv  # OT/parameters.f90:158
+
+    # dx = xmax/nxtot (src/init.f90:120-122)
+    @property
+    def dx(self) -> float:
+        return self.xmax / self.nx if self.nx else float("nan")
+
+    @property
+    def dy(self) -> float:
+        return self.ymax / self.ny if self.ny else float("nan")
+
+    @property
+    def dz(self) -> float:
+        return self.zmax / self.nz if self.nz else float("nan")
+
+    @property
+    def shape(self) -> tuple:
+        """Host array shape in C order (z, y, x, neq) of the Fortran
+        u(neq, nxmin:nxmax, nymin:nymax, nzmin:nzmax)."""
+        g = NGHOST
+        return (self.nz + 2 * g, self.ny + 2 * g, self.nx + 2 * g, self.neq)
+
+    def replace(self, **kw) -> "Params":
+        return dataclasses.replace(self, **kw)
+
+
+def table_from_log(logT: list, logL: list, tail: float) -> dict:
+    """Cooling-table fields from rows equally spaced in log10 T."""
+    n = len(logT)
+    dlog = (logT[-1] - logT[0]) / (n - 1)
+    inv = 1.0 / dlog
+    return dict(tab_T=[10.0 ** a for a in logT], tab_L=[10.0 ** b for b in logL],
+                tab_inv_dlog=round(inv, 9), tab_i0=int(round(logT[0] * inv)), tab_tail=tail)

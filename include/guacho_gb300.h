@@ -1,0 +1,243 @@
+/*
+ * guacho_gb300.h -- C ABI of the GB300 (sm_103a) per-timestep update for
+ * Guacho-3D.
+ *
+ * The entry points replace, one for one, the Fortran routines that
+ * src/main.f90 calls on the hot path:
+ *
+ *   gch_boundaryI     <- boundaryI()               src/boundaries.f90:44
+ *                                                   (called at src/main.f90:76)
+ *   gch_calcprim      <- calcprim(u, primit)       src/hydro_core.f90:245
+ *                                                   (called at src/main.f90:79)
+ *   gch_get_timestep  <- get_timestep(...)         src/hydro_core.f90:623
+ *                                                   (called at src/main.f90:97)
+ *   gch_tstep         <- tstep()                   src/hydro_solver.f90:134
+ *                                                   (called at src/main.f90:106)
+ *
+ * plus the state transfers a GPU drop-in needs around them (the reference
+ * keeps u/primit as host globals, src/globals.f90:33-38):
+ *
+ *   gch_create / gch_destroy   <- allocate/deallocate in initmain
+ *                                 (src/init.f90:145-158)
+ *   gch_upload / gch_download  <- u/primit host arrays, Fortran layout
+ *                                 u(neq, 1-nghost:nx+nghost, ..., ...)
+ *
+ * and two device-resident drivers with no host round trip per step:
+ *
+ *   gch_advance        <- the time loop of src/main.f90:94-125, with dt kept
+ *                         on the device, steps captured as a CUDA graph
+ *   gch_batch_*        <- many independent boxes of uneven size advanced in
+ *                         one persistent launch, each with its own dt
+ *
+ * Every call returns 0 (GCH_OK) or a bitmask of GCH_ERR_* bits.  The Fortran
+ * shim prints and stops on a non-zero status, as the reference does
+ * (src/hlld.f90:316-317, src/hllc.f90:135-138, src/init.f90:79-84).
+ *
+ * Threading: one host thread drives a domain; calls on one domain are not
+ * reentrant.  All work of a domain runs on the CUDA stream given at creation
+ * (0 = the legacy default stream).
+ *
+ * Plain C types only: no torch or CUDA types cross this boundary.
+ */
+#ifndef GUACHO_GB300_H
+#define GUACHO_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define GCH_ABI_VERSION 1
+
+/* ---- switch ids: identical values to src/constants.f90:56-98 ----------- */
+#define GCH_SOLVER_HLL 1
+#define GCH_SOLVER_HLLC 2
+#define GCH_SOLVER_HLLE 3
+#define GCH_SOLVER_HLLD 4
+
+#define GCH_EOS_ADIABATIC 1
+#define GCH_EOS_SINGLE_SPECIE 2
+
+#define GCH_COOL_NONE 0
+#define GCH_COOL_DMC 3
+#define GCH_COOL_CHI 4
+
+#define GCH_BC_OUTFLOW 1
+#define GCH_BC_CLOSED 2
+#define GCH_BC_PERIODIC 3
+#define GCH_BC_OTHER 4
+
+#define GCH_LIMITER_NO_AVERAGE (-1)
+#define GCH_LIMITER_NO_LIMIT 0
+#define GCH_LIMITER_MINMOD 1
+#define GCH_LIMITER_VAN_LEER 2
+#define GCH_LIMITER_VAN_ALBADA 3
+#define GCH_LIMITER_UMIST 4
+#define GCH_LIMITER_WOODWARD 5
+#define GCH_LIMITER_SUPERBEE 6
+
+/* ---- precision modes (no counterpart in the reference) ------------------ */
+/* Plain FP64 drop-in: every value and operation in FP64, no FMA contraction,
+ * bitwise equal to the reference's x86-64 FP64 build where all operations
+ * are IEEE-exact (everything but cooling's exp/log10). */
+#define GCH_FP64 0
+/* FP32 state, reconstruction and fluxes; u stored in FP64; FP64 for the
+ * pressure recovery in u2prim, the u += dt*divF accumulation, dt and time. */
+#define GCH_FP32_MIXED 1
+/* As GCH_FP32_MIXED but u stored as a compensated (hi, lo) FP32 pair and
+ * accumulated with Kahan-style error-free sums instead of FP64. */
+#define GCH_FP32_KAHAN 2
+
+/* ---- status bits --------------------------------------------------------- */
+#define GCH_OK 0
+#define GCH_ERR_PARAM 0x1            /* rejected parameter set            */
+#define GCH_ERR_CUDA 0x2             /* a CUDA runtime call failed        */
+#define GCH_ERR_HLLD 0x4             /* HLLD fell through (hlld.f90:316)  */
+#define GCH_ERR_HLLC 0x8             /* HLLC fell through (hllc.f90:135)  */
+#define GCH_ERR_DT 0x10              /* dt <= 0 or not finite             */
+#define GCH_ERR_TIMEOUT 0x20         /* a bounded device wait ran out     */
+#define GCH_ERR_NO_DEVICE 0x40       /* no CUDA device / not sm_103       */
+#define GCH_ERR_STATE 0x80           /* call out of order                 */
+
+#define GCH_MAX_SPHERES 8
+#define GCH_MAX_GRAV 4
+#define GCH_MAX_TABLE 512
+
+/* A wind sphere re-imposed by the user boundary hook on every boundary
+ * call, the pattern of impose_exo (EXO/exoplanet.f90:125-266) and
+ * impose_user_bc (EXO/user_mod.f90:131-144).  Cells whose centre lies within
+ * `radius` of (xc, yc, zc) (measured from the grid centre) are set to
+ * rho = dens, v = vorb + vwind * r_hat, E = 1/2 rho v^2 + cv*dens*tfac
+ * (+ the dipole field of strength bdip and its energy when MHD). */
+typedef struct {
+  double xc, yc, zc;
+  double radius;
+  double dens;
+  double vwind;
+  double vorb[3];
+  double tfac;
+  double bdip;
+} gch_sphere_t;
+
+/* The parameter surface of parameters.f90 (OT/parameters.f90:48-177), as
+ * runtime values.  Field names follow the Fortran names. */
+typedef struct {
+  int32_t abi_version;      /* = GCH_ABI_VERSION */
+  int32_t precision;        /* GCH_FP64 | GCH_FP32_MIXED | GCH_FP32_KAHAN */
+  /* grid: interior cells of the (single) domain, nghost = 2 fixed */
+  int32_t nx, ny, nz;
+  int32_t neq;              /* 8 with BFIELD, 5 without */
+  /* physics switches */
+  int32_t mhd, pmhd;
+  int32_t riemann_solver;
+  int32_t slope_limiter;
+  int32_t eq_of_state;
+  int32_t cooling;
+  int32_t enable_flux_cd;
+  int32_t eight_wave;
+  int32_t user_source_terms;
+  int32_t bc_left, bc_right, bc_bottom, bc_top, bc_out, bc_in;
+  int32_t bc_user;
+  /* spacing (dx = xmax/nxtot, src/init.f90:120-122) and EOS */
+  double dx, dy, dz;
+  double cv, gamma;         /* gamma = (cv+1)/cv (OT/parameters.f90:158) */
+  double cfl, eta;
+  double Tempsc, Psc, tsc;  /* scalings (OT/parameters.f90:163-170) */
+  /* tabulated cooling (COOL_DMC / COOL_CHI): rows equally spaced in log10 T
+   * (reference tables: 41 rows of 0.1 dex from 1e4 K) */
+  int32_t ntab;
+  int32_t tab_i0;           /* round(log10(T_first) * tab_inv_dlog) */
+  double tab_inv_dlog;      /* 1 / row spacing in dex */
+  double tab_tail;          /* Lambda = tab_tail*sqrt(T) above 1e8 K */
+  double tab_Tmin;          /* cooling acts only above this T (1e4 K) */
+  double tab_T[GCH_MAX_TABLE];
+  double tab_L[GCH_MAX_TABLE];
+  /* user boundary spheres (bc_user) */
+  int32_t nsph;
+  int32_t ngrav;
+  gch_sphere_t sph[GCH_MAX_SPHERES];
+  /* user source terms: point masses (EXO/user_mod.f90:158-206) */
+  double grav_GM[GCH_MAX_GRAV];
+  double grav_x[GCH_MAX_GRAV], grav_y[GCH_MAX_GRAV], grav_z[GCH_MAX_GRAV];
+} gch_params_t;
+
+typedef struct gch_domain gch_domain_t;
+
+/* Fill *p with the OT/parameters.f90 defaults (HLLD, minmod, flux-CD,
+ * periodic, cv = 1.5, cfl = 0.2, eta = 0) for an nx x ny x nz box. */
+void gch_params_default(gch_params_t* p, int nx, int ny, int nz);
+
+/* Validate a parameter set without allocating; returns GCH_OK or
+ * GCH_ERR_PARAM. */
+int gch_params_check(const gch_params_t* p);
+
+/* Allocate the device state of one domain (src/init.f90:145-158).  `stream`
+ * is a cudaStream_t passed as an opaque pointer (NULL: default stream). */
+int gch_create(const gch_params_t* p, void* stream, gch_domain_t** out);
+int gch_destroy(gch_domain_t* d);
+
+/* Host <-> device transfer of the conserved variables in the reference's
+ * layout: u(neq, 1-2:nx+2, 1-2:ny+2, 1-2:nz+2), column major, FP64.
+ * gch_download also writes primit (same layout) when primit != NULL. */
+int gch_upload(gch_domain_t* d, const double* u);
+int gch_download(gch_domain_t* d, double* u, double* primit);
+
+/* src/boundaries.f90:44 boundaryI: one ghost layer of u, then the user
+ * boundary spheres. */
+int gch_boundaryI(gch_domain_t* d);
+
+/* src/hydro_core.f90:245 calcprim(u, primit) over the whole array. */
+int gch_calcprim(gch_domain_t* d);
+
+/* src/hydro_core.f90:623 get_timestep: CFL dt from the interior primitives,
+ * ramped over the first n_iter iterations, clipped to land on tprint (sets
+ * *dump_flag = 1 then). */
+int gch_get_timestep(gch_domain_t* d, int current_iter, int n_iter, double current_time,
+                     double tprint, double* dt, int* dump_flag);
+
+/* src/hydro_solver.f90:134 tstep: advance u by dt (both stages, flux-CD,
+ * sources, viscosity, cooling, boundaries, primitives). */
+int gch_tstep(gch_domain_t* d, double dt);
+
+/* gch_get_timestep + gch_tstep with the state in HOST memory: uploads u,
+ * steps once and downloads u, for callers whose hooks need the host arrays
+ * current after every step.  *dt and *dump_flag as gch_get_timestep. */
+int gch_step_host(gch_domain_t* d, double* u, int current_iter, int n_iter,
+                  double current_time, double tprint, double* dt, int* dump_flag);
+
+/* The time loop of src/main.f90:94-125 on the device: up to max_steps
+ * iterations while time <= tmax, dt never leaves the device.  *time, *iter
+ * and *tprint are the loop state (in/out).  Returns after a host sync. */
+int gch_advance(gch_domain_t* d, int max_steps, double tmax, double dtprint, int n_iter,
+                double* time, int* iter, double* tprint, int* steps_done);
+
+/* Device-side counters of the last step: number of cells whose pressure hit
+ * the 1e-16 floor in u2prim (src/hydro_core.f90:78) during the step, and the
+ * accumulated error bits. */
+int gch_last_step_info(gch_domain_t* d, long long* pfloor_hits, int* err_bits);
+
+/* Number of kernel launches one gch_tstep issues (for launch accounting). */
+int gch_launches_per_step(gch_domain_t* d);
+
+/* ---- batched boxes ------------------------------------------------------ */
+typedef struct gch_batch gch_batch_t;
+
+/* n independent domains (each its own params, size and dt) advanced
+ * together.  All boxes must share precision, neq and the physics switches;
+ * sizes, spacings, boundary kinds and problem data may differ. */
+int gch_batch_create(int n, const gch_params_t* params, void* stream, gch_batch_t** out);
+int gch_batch_destroy(gch_batch_t* b);
+int gch_batch_upload(gch_batch_t* b, int box, const double* u);
+int gch_batch_download(gch_batch_t* b, int box, double* u);
+/* Advance every box by `steps` steps, each with its own CFL dt (ramp over
+ * the first n_iter iterations of each box), no output clipping. */
+int gch_batch_advance(gch_batch_t* b, int steps, int n_iter);
+/* Per-box simulated time and iteration count. */
+int gch_batch_time(gch_batch_t* b, double* times, int* iters);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,1099 @@
+/*
+ * guacho_oracle.c -- CPU (FP64) restatement of Guacho-3D's per-timestep update.
+ *
+ * TEST INFRASTRUCTURE ONLY: the parity checker for the CUDA path.  Only the
+ * tests, the smoke check and the CPU-baseline leg of the benchmark load it.
+ *
+ * Every routine restates the reference routine cited beside it, in the same
+ * loop order and with the same floating-point expression order (left to right,
+ * parentheses kept), so that a build with -O2 -ffp-contract=off reproduces the
+ * bits of gfortran -O3 -fdefault-real-8 on x86-64 (which has no FMA in its
+ * baseline ISA).  Citations are file:line within the reference project.
+ *
+ * Deliberate deviations, each also recorded in the design notes:
+ *  - HLLD, UR* region with denr == 0 (src/hlld.f90:167-171) assigns the L
+ *    star variables and then reads the uninitialised R ones.  Here the R
+ *    fallback mirrors the L one: vstr=primr(3), wstr=primr(4), bystr=bzstr=0.
+ *  - The table lookup of the cooling curve (src/cooling_dmc.f90:98-102) reads
+ *    one row past the table end when log10(T) rounds to exactly 8; the row
+ *    index is clamped to the last interval here.
+ *  - Ghost filling uses the serial (non-MPI) semantics of src/boundaries.f90
+ *    (x, then y, then z faces).  The MPI build fills edge/corner ghosts in a
+ *    different order; no interior result reads an edge or corner ghost.
+ *  - The serial build of the E-field periodic branch does not compile in the
+ *    reference (src/flux_cd_module.f90:120-128, unclosed if); the intended
+ *    periodic copy is restated.
+ */
+#include "guacho_oracle.h"
+
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+#define NG 2
+
+struct gor_state {
+  gor_params_t p;
+  int NX, NY, NZ;     /* with ghosts */
+  size_t ncell;
+  double *u, *up, *primit, *f, *g, *h, *e;
+  double time;
+  int err;
+};
+
+/* cell index for 1-based interior coordinates i in [1-NG, n+NG] */
+#define CID(s, i, j, k) \
+  ((size_t)((k) + NG - 1) * (size_t)(s)->NY * (size_t)(s)->NX + \
+   (size_t)((j) + NG - 1) * (size_t)(s)->NX + (size_t)((i) + NG - 1))
+#define AT(s, arr, q, i, j, k) ((arr)[CID(s, i, j, k) * (size_t)(s)->p.neq + (q) - 1])
+#define EAT(s, q, i, j, k) ((s)->e[CID(s, i, j, k) * 3 + (q) - 1])
+
+static inline double dmax(double a, double b) { return a > b ? a : b; }
+static inline double dmin(double a, double b) { return a < b ? a : b; }
+static inline int bfield(const gor_params_t* p) { return p->neq >= 8; }
+
+/* ---------------------------------------------------------------------- */
+/* src/hydro_core.f90:46-129  u2prim                                        */
+static void u2prim(const gor_params_t* p, const double* uu, double* prim, double* T) {
+  double r = dmax(uu[0], 1e-15);
+  prim[0] = r;
+  prim[1] = uu[1] / r;
+  prim[2] = uu[2] / r;
+  prim[3] = uu[3] / r;
+  if (p->mhd) {
+    prim[4] = (uu[4] - 0.5 * r * (prim[1] * prim[1] + prim[2] * prim[2] + prim[3] * prim[3])
+               - 0.5 * (uu[5] * uu[5] + uu[6] * uu[6] + uu[7] * uu[7])) / p->cv;
+  } else {
+    prim[4] = (uu[4] - 0.5 * r * (prim[1] * prim[1] + prim[2] * prim[2] + prim[3] * prim[3]))
+              / p->cv;
+  }
+  prim[4] = dmax(prim[4], 1e-16);
+  if (bfield(p) && (p->mhd || p->pmhd)) {
+    prim[5] = uu[5];
+    prim[6] = uu[6];
+    prim[7] = uu[7];
+  }
+  double t = 0.0;
+  if (p->eq_of_state == GOR_EOS_ADIABATIC) t = (prim[4] / r) * p->Tempsc;
+  if (p->eq_of_state == GOR_EOS_SINGLE_SPECIE) {
+    r = dmax(r, 1e-15);
+    t = dmax(1.0, (prim[4] / r) * p->Tempsc);
+    prim[4] = r * t / p->Tempsc;
+  }
+  if (T) *T = t;
+}
+
+/* src/hydro_core.f90:331-383  prim2u (non-split branch) */
+static void prim2u(const gor_params_t* p, const double* prim, double* uu) {
+  uu[0] = prim[0];
+  uu[1] = prim[0] * prim[1];
+  uu[2] = prim[0] * prim[2];
+  uu[3] = prim[0] * prim[3];
+  uu[4] = 0.5 * prim[0] * (prim[1] * prim[1] + prim[2] * prim[2] + prim[3] * prim[3])
+          + p->cv * prim[4];
+  if (bfield(p) && p->mhd)
+    uu[4] = uu[4] + 0.5 * (prim[5] * prim[5] + prim[6] * prim[6] + prim[7] * prim[7]);
+  if (bfield(p) && (p->mhd || p->pmhd)) {
+    uu[5] = prim[5];
+    uu[6] = prim[6];
+    uu[7] = prim[7];
+  }
+}
+
+/* src/hydro_core.f90:395-476  prim2f (non-split branch) */
+static void prim2f(const gor_params_t* p, const double* prim, double* ff) {
+  if (p->mhd) {
+    double etot = 0.5 * (prim[0] * (prim[1] * prim[1] + prim[2] * prim[2] + prim[3] * prim[3])
+                         + prim[5] * prim[5] + prim[6] * prim[6] + prim[7] * prim[7])
+                  + p->cv * prim[4];
+    ff[0] = prim[0] * prim[1];
+    ff[1] = prim[0] * prim[1] * prim[1] + prim[4]
+            + 0.5 * (prim[6] * prim[6] + prim[7] * prim[7] - prim[5] * prim[5]);
+    ff[2] = prim[0] * prim[1] * prim[2] - prim[5] * prim[6];
+    ff[3] = prim[0] * prim[1] * prim[3] - prim[5] * prim[7];
+    ff[4] = prim[1] * (etot + prim[4] + 0.5 * (prim[5] * prim[5] + prim[6] * prim[6]
+                                               + prim[7] * prim[7]))
+            - prim[5] * (prim[1] * prim[5] + prim[2] * prim[6] + prim[3] * prim[7]);
+  } else {
+    double etot = 0.5 * prim[0] * (prim[1] * prim[1] + prim[2] * prim[2] + prim[3] * prim[3])
+                  + p->cv * prim[4];
+    ff[0] = prim[0] * prim[1];
+    ff[1] = prim[0] * prim[1] * prim[1] + prim[4];
+    ff[2] = prim[0] * prim[1] * prim[2];
+    ff[3] = prim[0] * prim[1] * prim[3];
+    ff[4] = prim[1] * (etot + prim[4]);
+  }
+  if (bfield(p) && (p->mhd || p->pmhd)) {
+    ff[5] = 0.0;
+    ff[6] = prim[1] * prim[6] - prim[5] * prim[2];
+    ff[7] = prim[1] * prim[7] - prim[5] * prim[3];
+  }
+}
+
+/* src/hydro_core.f90:485-534  swapy / swapz */
+static void swapy(const gor_params_t* p, double* v) {
+  double a = v[1]; v[1] = v[2]; v[2] = a;
+  if (bfield(p) && (p->mhd || p->pmhd)) { a = v[5]; v[5] = v[6]; v[6] = a; }
+}
+static void swapz(const gor_params_t* p, double* v) {
+  double a = v[1]; v[1] = v[3]; v[3] = a;
+  if (bfield(p) && (p->mhd || p->pmhd)) { a = v[5]; v[5] = v[7]; v[7] = a; }
+}
+
+/* src/hydro_core.f90:544-553  csound */
+static inline double csound(const gor_params_t* p, double pr, double d) {
+  return sqrt(p->gamma * pr / d);
+}
+
+/* src/hydro_core.f90:568-581  cfast */
+static void cfast(const gor_params_t* p, double pr, double d, double bx, double by, double bz,
+                  double* cfx, double* cfy, double* cfz) {
+  double g = p->gamma;
+  double b2 = bx * bx + by * by + bz * bz;
+  double a = g * pr + b2;
+  *cfx = sqrt(0.5 * (a + sqrt(a * a - 4.0 * g * pr * bx * bx)) / d);
+  *cfy = sqrt(0.5 * (a + sqrt(a * a - 4.0 * g * pr * by * by)) / d);
+  *cfz = sqrt(0.5 * (a + sqrt(a * a - 4.0 * g * pr * bz * bz)) / d);
+}
+
+/* src/hydro_core.f90:591-604  cfastX */
+static inline double cfastX(const gor_params_t* p, const double* prim) {
+  double g = p->gamma;
+  double b2 = prim[5] * prim[5] + prim[6] * prim[6] + prim[7] * prim[7];
+  double cs2va2 = (g * prim[4] + b2) / prim[0];
+  return sqrt(0.5 * (cs2va2 + sqrt(cs2va2 * cs2va2
+                                   - 4.0 * g * prim[4] * (prim[5] * prim[5]) / prim[0] / prim[0])));
+}
+
+/* src/hydro_core.f90:735-796  average (the slope limiter switch) */
+static inline double average(int lim, double a, double b) {
+  double s, c, d, av, av1, av2;
+  const double delta = 1e-7;
+  switch (lim) {
+    case GOR_LIMITER_NO_AVERAGE: return 0.0;
+    case GOR_LIMITER_NO_LIMIT: return 0.5 * (a + b);
+    case GOR_LIMITER_MINMOD:
+      s = copysign(1.0, a);
+      return s * dmax(0.0, dmin(fabs(a), s * b));
+    case GOR_LIMITER_VAN_LEER:
+      if (a * b <= 0.0) return 0.0;
+      return a * b * (a + b) / (a * a + b * b);
+    case GOR_LIMITER_VAN_ALBADA:
+      return (a * (b * b + delta) + b * (a * a + delta)) / (a * a + b * b + delta);
+    case GOR_LIMITER_UMIST:
+      s = copysign(1.0, a);
+      c = 0.25 * a + 0.75 * b;
+      d = 0.75 * a + 0.25 * b;
+      av = dmin(dmin(dmin(2.0 * fabs(a), 2.0 * s * b), s * c), s * d);
+      return s * dmax(0.0, av);
+    case GOR_LIMITER_WOODWARD:
+      s = copysign(1.0, a);
+      c = 0.5 * (a + b);
+      av = dmin(dmin(2.0 * fabs(a), 2.0 * s * b), s * c);
+      return s * dmax(0.0, av);
+    case GOR_LIMITER_SUPERBEE:
+      s = copysign(1.0, b);
+      av1 = dmin(2.0 * fabs(b), s * a);
+      av2 = dmin(fabs(b), 2.0 * s * a);
+      return s * dmax(dmax(0.0, av1), av2);
+  }
+  return 0.0;
+}
+
+/* src/hydro_core.f90:712-731  limiter */
+static void limiter(const gor_params_t* p, const double* pll, double* pl, double* pr,
+                    const double* prr) {
+  for (int q = 0; q < p->neq; ++q) {
+    double dl = pl[q] - pll[q];
+    double dm = pr[q] - pl[q];
+    double dr = prr[q] - pr[q];
+    double al = average(p->slope_limiter, dl, dm);
+    double ar = average(p->slope_limiter, dm, dr);
+    pl[q] = pl[q] + al * 0.5;
+    pr[q] = pr[q] - ar * 0.5;
+  }
+}
+
+/* ---------------------------------------------------------------------- */
+/* src/hlld.f90:48-319  prim2fhlld */
+static void prim2fhlld(const gor_params_t* p, const double* pl, const double* pr, double* ff,
+                       int* err) {
+  const double cv = p->cv;
+  double csl = cfastX(p, pl);
+  double csr = cfastX(p, pr);
+  double sr = dmax(pl[1] + csl, pr[1] + csr);
+  double sl = dmin(pl[1] - csl, pr[1] - csr);
+  if (sl > 0) { prim2f(p, pl, ff); return; }
+  if (sr < 0) { prim2f(p, pr, ff); return; }
+
+  double bx = 0.5 * (pl[5] + pr[5]);
+  double signBx = copysign(1.0, bx);
+  double pTL = pl[4] + 0.5 * (bx * bx + pl[6] * pl[6] + pl[7] * pl[7]);
+  double pTR = pr[4] + 0.5 * (bx * bx + pr[6] * pr[6] + pr[7] * pr[7]);
+  double slmul = sl - pl[1];
+  double srmur = sr - pr[1];
+  double rholul = pl[0] * pl[1];
+  double rhorur = pr[0] * pr[1];
+  double sM = (srmur * rhorur - slmul * rholul - pTR + pTL) / (srmur * pr[0] - slmul * pl[0]);
+  double srmsM = sr - sM;
+  double slmsM = sl - sM;
+  double rhostl = pl[0] * slmul / slmsM;
+  double rhostr = pr[0] * srmur / srmsM;
+  double sstl = sM - fabs(bx) / sqrt(rhostl);
+  double sstr = sM + fabs(bx) / sqrt(rhostr);
+  double pst = (srmur * pr[0] * pTL - slmul * pl[0] * pTR
+                + pl[0] * pr[0] * srmur * slmul * (pr[1] - pl[1]))
+               / (srmur * pr[0] - slmul * pl[0]);
+  double vstl, wstl, bystl, bzstl, vstr, wstr, bystr, bzstr;
+  double el, er, denl, denr, sMmul, sMmur, vdotbl, vdotbr, vstdotbstl, vstdotbstr, estl, estr;
+
+  /* UL* region */
+  if (sstl >= 0) {
+    el = 0.5 * pl[0] * (pl[1] * pl[1] + pl[2] * pl[2] + pl[3] * pl[3]) + cv * pl[4]
+         + 0.5 * (bx * bx + pl[6] * pl[6] + pl[7] * pl[7]);
+    sMmul = sM - pl[1];
+    denl = pl[0] * slmul * slmsM - bx * bx;
+    if (denl == 0) {
+      vstl = pl[2]; wstl = pl[3]; bystl = 0.0; bzstl = 0.0;
+    } else {
+      vstl = pl[2] - bx * pl[6] * sMmul / denl;
+      wstl = pl[3] - bx * pl[7] * sMmul / denl;
+      bystl = pl[6] * (pl[0] * (slmul * slmul) - bx * bx) / denl;
+      bzstl = pl[7] * (pl[0] * (slmul * slmul) - bx * bx) / denl;
+    }
+    vdotbl = pl[1] * bx + pl[2] * pl[6] + pl[3] * pl[7];
+    vstdotbstl = sM * bx + vstl * bystl + wstl * bzstl;
+    estl = (slmul * el - pTL * pl[1] + pst * sM + bx * (vdotbl - vstdotbstl)) / slmsM;
+    ff[0] = rhostl * sM;
+    ff[1] = rhostl * (sM * sM) + pst - bx * bx;
+    ff[2] = rhostl * sM * vstl - bx * bystl;
+    ff[3] = rhostl * sM * wstl - bx * bzstl;
+    ff[4] = sM * (estl + pst) - bx * (vstdotbstl);
+    ff[5] = 0.0;
+    ff[6] = bystl * sM - bx * vstl;
+    ff[7] = bzstl * sM - bx * wstl;
+    return;
+  }
+
+  /* UR* region */
+  if (sstr <= 0) {
+    er = 0.5 * pr[0] * (pr[1] * pr[1] + pr[2] * pr[2] + pr[3] * pr[3]) + cv * pr[4]
+         + 0.5 * (bx * bx + pr[6] * pr[6] + pr[7] * pr[7]);
+    sMmur = sM - pr[1];
+    denr = pr[0] * srmur * srmsM - bx * bx;
+    if (denr == 0) {
+      /* deviation: the reference leaves these uninitialised (hlld.f90:167-171) */
+      vstr = pr[2]; wstr = pr[3]; bystr = 0.0; bzstr = 0.0;
+    } else {
+      vstr = pr[2] - bx * pr[6] * sMmur / denr;
+      wstr = pr[3] - bx * pr[7] * sMmur / denr;
+      bystr = pr[6] * (pr[0] * (srmur * srmur) - bx * bx) / denr;
+      bzstr = pr[7] * (pr[0] * (srmur * srmur) - bx * bx) / denr;
+    }
+    vdotbr = pr[1] * bx + pr[2] * pr[6] + pr[3] * pr[7];
+    vstdotbstr = sM * bx + vstr * bystr + wstr * bzstr;
+    estr = (srmur * er - pTR * pr[1] + pst * sM + bx * (vdotbr - vstdotbstr)) / srmsM;
+    ff[0] = rhostr * sM;
+    ff[1] = rhostr * (sM * sM) + pst - bx * bx;
+    ff[2] = rhostr * sM * vstr - bx * bystr;
+    ff[3] = rhostr * sM * wstr - bx * bzstr;
+    ff[4] = sM * (estr + pst) - bx * (vstdotbstr);
+    ff[5] = 0.0;
+    ff[6] = bystr * sM - bx * vstr;
+    ff[7] = bzstr * sM - bx * wstr;
+    return;
+  }
+
+  sMmul = sM - pl[1];
+  sMmur = sM - pr[1];
+  denl = pl[0] * slmul * slmsM - bx * bx;
+  denr = pr[0] * srmur * srmsM - bx * bx;
+  if (denl == 0) {
+    vstl = pl[2]; wstl = pl[3]; bystl = 0.0; bzstl = 0.0;
+  } else {
+    vstl = pl[2] - bx * pl[6] * sMmul / denl;
+    wstl = pl[3] - bx * pl[7] * sMmul / denl;
+    bystl = pl[6] * (pl[0] * (slmul * slmul) - bx * bx) / denl;
+    bzstl = pl[7] * (pl[0] * (slmul * slmul) - bx * bx) / denl;
+  }
+  if (denr == 0) {
+    vstr = pr[2]; wstr = pr[3]; bystr = 0.0; bzstr = 0.0;
+  } else {
+    vstr = pr[2] - bx * pr[6] * sMmur / denr;
+    wstr = pr[3] - bx * pr[7] * sMmur / denr;
+    bystr = pr[6] * (pr[0] * (srmur * srmur) - bx * bx) / denr;
+    bzstr = pr[7] * (pr[0] * (srmur * srmur) - bx * bx) / denr;
+  }
+  double dd = sqrt(rhostl) + sqrt(rhostr);
+  double vstst = (sqrt(rhostl) * vstl + sqrt(rhostr) * vstr + (bystr - bystl) * signBx) / dd;
+  double wstst = (sqrt(rhostl) * wstl + sqrt(rhostr) * wstr + (bzstr - bzstl) * signBx) / dd;
+  double bystst = (sqrt(rhostl) * bystr + sqrt(rhostr) * bystl
+                   + sqrt(rhostl * rhostr) * (vstr - vstl) * signBx) / dd;
+  double bzstst = (sqrt(rhostl) * bzstr + sqrt(rhostr) * bzstl
+                   + sqrt(rhostl * rhostr) * (wstr - wstl) * signBx) / dd;
+  double vststdotbstst = sM * bx + vstst * bystst + wstst * bzstst;
+
+  /* UL** region */
+  if (sM >= 0) {
+    el = 0.5 * pl[0] * (pl[1] * pl[1] + pl[2] * pl[2] + pl[3] * pl[3]) + cv * pl[4]
+         + 0.5 * (bx * bx + pl[6] * pl[6] + pl[7] * pl[7]);
+    vdotbl = pl[1] * bx + pl[2] * pl[6] + pl[3] * pl[7];
+    vstdotbstl = sM * bx + vstl * bystl + wstl * bzstl;
+    estl = (slmul * el - pTL * pl[1] + pst * sM + bx * (vdotbl - vstdotbstl)) / slmsM;
+    double eststl = estl - sqrt(rhostl) * (vstdotbstl - vststdotbstst) * signBx;
+    ff[0] = rhostl * sM;
+    ff[1] = rhostl * (sM * sM) + pst - bx * bx;
+    ff[2] = rhostl * sM * vstst - bx * bystst;
+    ff[3] = rhostl * sM * wstst - bx * bzstst;
+    ff[4] = sM * (eststl + pst) - bx * (vststdotbstst);
+    ff[5] = 0.0;
+    ff[6] = bystst * sM - bx * vstst;
+    ff[7] = bzstst * sM - bx * wstst;
+    return;
+  }
+  /* UR** region */
+  if (sM <= 0) {
+    er = 0.5 * pr[0] * (pr[1] * pr[1] + pr[2] * pr[2] + pr[3] * pr[3]) + cv * pr[4]
+         + 0.5 * (bx * bx + pr[6] * pr[6] + pr[7] * pr[7]);
+    vdotbr = pr[1] * bx + pr[2] * pr[6] + pr[3] * pr[7];
+    vstdotbstr = sM * bx + vstr * bystr + wstr * bzstr;
+    estr = (srmur * er - pTR * pr[1] + pst * sM + bx * (vdotbr - vstdotbstr)) / srmsM;
+    double eststr = estr + sqrt(rhostr) * (vstdotbstr - vststdotbstst) * signBx;
+    ff[0] = rhostr * sM;
+    ff[1] = rhostr * (sM * sM) + pst - bx * bx;
+    ff[2] = rhostr * sM * vstst - bx * bystst;
+    ff[3] = rhostr * sM * wstst - bx * bzstst;
+    ff[4] = sM * (eststr + pst) - bx * (vststdotbstst);
+    ff[5] = 0.0;
+    ff[6] = bystst * sM - bx * vstst;
+    ff[7] = bzstst * sM - bx * wstst;
+    return;
+  }
+  /* src/hlld.f90:316-317: print and stop */
+  for (int q = 0; q < 8; ++q) ff[q] = NAN;
+  *err |= GOR_ERR_HLLD_FALLTHROUGH;
+}
+
+/* src/hllc.f90:44-140  prim2fhllc */
+static void prim2fhllc(const gor_params_t* p, const double* pl, const double* pr, double* ff,
+                       int* err) {
+  const int neq = p->neq;
+  double uu[8], uuk[8];
+  double csl = csound(p, pl[4], pl[0]);
+  double csr = csound(p, pr[4], pr[0]);
+  double sr = dmax(pl[1] + csl, pr[1] + csr);
+  double sl = dmin(pl[1] - csl, pr[1] - csr);
+  if (sl > 0) { prim2f(p, pl, ff); return; }
+  if (sr < 0) { prim2f(p, pr, ff); return; }
+  double slmul = sl - pl[1];
+  double srmur = sr - pr[1];
+  double rholul = pl[0] * pl[1];
+  double rhorur = pr[0] * pr[1];
+  double sst = (srmur * rhorur - slmul * rholul - pr[4] + pl[4]) / (srmur * pr[0] - slmul * pl[0]);
+  if (sst >= 0.0) {
+    double rhost = pl[0] * (slmul) / (sl - sst);
+    double ek = 0.5 * pl[0] * (pl[1] * pl[1] + pl[2] * pl[2] + pl[3] * pl[3]) + p->cv * pl[4];
+    uuk[0] = rhost;
+    uuk[1] = rhost * sst;
+    uuk[2] = rhost * pl[2];
+    uuk[3] = rhost * pl[3];
+    uuk[4] = rhost * (ek / pl[0] + (sst - pl[1]) * (sst + pl[4] / (pl[0] * slmul)));
+    if (p->pmhd && bfield(p)) {
+      uuk[5] = rhost * pl[5] / pl[0];
+      uuk[6] = rhost * pl[6] / pl[0];
+      uuk[7] = rhost * pl[7] / pl[0];
+    } else if (bfield(p)) {
+      /* uninitialised in the reference when neither pmhd nor passives;
+       * HLLC is not used with full MHD */
+      uuk[5] = uuk[6] = uuk[7] = 0.0;
+    }
+    prim2f(p, pl, ff);
+    prim2u(p, pl, uu);
+    for (int q = 0; q < neq; ++q) ff[q] = ff[q] + sl * (uuk[q] - uu[q]);
+    return;
+  }
+  if (sst <= 0.0) {
+    double rhost = pr[0] * (srmur) / (sr - sst);
+    double ek = 0.5 * pr[0] * (pr[1] * pr[1] + pr[2] * pr[2] + pr[3] * pr[3]) + p->cv * pr[4];
+    uuk[0] = rhost;
+    uuk[1] = rhost * sst;
+    uuk[2] = rhost * pr[2];
+    uuk[3] = rhost * pr[3];
+    uuk[4] = rhost * (ek / pr[0] + (sst - pr[1]) * (sst + pr[4] / (pr[0] * srmur)));
+    if (p->pmhd && bfield(p)) {
+      uuk[5] = rhost * pr[5] / pr[0];
+      uuk[6] = rhost * pr[6] / pr[0];
+      uuk[7] = rhost * pr[7] / pr[0];
+    } else if (bfield(p)) {
+      uuk[5] = uuk[6] = uuk[7] = 0.0;
+    }
+    prim2f(p, pr, ff);
+    prim2u(p, pr, uu);
+    for (int q = 0; q < neq; ++q) ff[q] = ff[q] + sr * (uuk[q] - uu[q]);
+    return;
+  }
+  for (int q = 0; q < neq; ++q) ff[q] = NAN;
+  *err |= GOR_ERR_HLLC_FALLTHROUGH;
+}
+
+/* src/hlle.f90:48-83 (prim2fhlle) and src/hll.f90:47-82 (prim2fhll):
+ * the same two-wave formula with fast (HLLE) or sound (HLL) speeds. */
+static void prim2fhll_common(const gor_params_t* p, const double* pl, const double* pr,
+                             double* ff, int fast) {
+  double fL[8], fR[8], uL[8], uR[8];
+  double csl, csr;
+  if (fast) {
+    csl = cfastX(p, pl);
+    csr = cfastX(p, pr);
+  } else {
+    csl = csound(p, pl[4], pl[0]);
+    csr = csound(p, pr[4], pr[0]);
+  }
+  double sr = dmax(pl[1] + csl, pr[1] + csr);
+  double sl = dmin(pl[1] - csl, pr[1] - csr);
+  if (sl > 0) { prim2f(p, pl, ff); return; }
+  if (sr < 0) { prim2f(p, pr, ff); return; }
+  prim2f(p, pl, fL);
+  prim2f(p, pr, fR);
+  prim2u(p, pl, uL);
+  prim2u(p, pr, uR);
+  for (int q = 0; q < p->neq; ++q)
+    ff[q] = (sr * fL[q] - sl * fR[q] + sl * sr * (uR[q] - uL[q])) / (sr - sl);
+}
+
+static void riemann(const gor_params_t* p, const double* pl, const double* pr, double* ff,
+                    int* err) {
+  switch (p->riemann_solver) {
+    case GOR_SOLVER_HLLD: prim2fhlld(p, pl, pr, ff, err); break;
+    case GOR_SOLVER_HLLC: prim2fhllc(p, pl, pr, ff, err); break;
+    case GOR_SOLVER_HLLE: prim2fhll_common(p, pl, pr, ff, 1); break;
+    case GOR_SOLVER_HLL: prim2fhll_common(p, pl, pr, ff, 0); break;
+    default: *err |= GOR_ERR_BAD_PARAM;
+  }
+}
+
+/* src/hlld.f90:331-432 (hlldfluxes) and its twins hllc.f90:152-253,
+ * hlle.f90:95-196, hll.f90:93-194: fluxes at i+1/2, j+1/2, k+1/2 for
+ * i,j,k in [0,n]. */
+static void fluxes(gor_state_t* s, int choice) {
+  const gor_params_t* p = &s->p;
+  const int neq = p->neq, nx = p->nx, ny = p->ny, nz = p->nz;
+  int err = 0;
+#pragma omp parallel for schedule(static) reduction(| : err)
+  for (int k = 0; k <= nz; ++k) {
+    double pl[8], pr[8], pll[8], prr[8], ff[8];
+    for (int j = 0; j <= ny; ++j) {
+      for (int i = 0; i <= nx; ++i) {
+        /* x direction */
+        for (int q = 1; q <= neq; ++q) {
+          pl[q - 1] = AT(s, s->primit, q, i, j, k);
+          pr[q - 1] = AT(s, s->primit, q, i + 1, j, k);
+        }
+        if (choice == 2) {
+          for (int q = 1; q <= neq; ++q) {
+            pll[q - 1] = AT(s, s->primit, q, i - 1, j, k);
+            prr[q - 1] = AT(s, s->primit, q, i + 2, j, k);
+          }
+          limiter(p, pll, pl, pr, prr);
+        }
+        riemann(p, pl, pr, ff, &err);
+        for (int q = 1; q <= neq; ++q) AT(s, s->f, q, i, j, k) = ff[q - 1];
+
+        /* y direction */
+        for (int q = 1; q <= neq; ++q) {
+          pl[q - 1] = AT(s, s->primit, q, i, j, k);
+          pr[q - 1] = AT(s, s->primit, q, i, j + 1, k);
+        }
+        swapy(p, pl);
+        swapy(p, pr);
+        if (choice == 2) {
+          for (int q = 1; q <= neq; ++q) {
+            pll[q - 1] = AT(s, s->primit, q, i, j - 1, k);
+            prr[q - 1] = AT(s, s->primit, q, i, j + 2, k);
+          }
+          swapy(p, pll);
+          swapy(p, prr);
+          limiter(p, pll, pl, pr, prr);
+        }
+        riemann(p, pl, pr, ff, &err);
+        swapy(p, ff);
+        for (int q = 1; q <= neq; ++q) AT(s, s->g, q, i, j, k) = ff[q - 1];
+
+        /* z direction */
+        for (int q = 1; q <= neq; ++q) {
+          pl[q - 1] = AT(s, s->primit, q, i, j, k);
+          pr[q - 1] = AT(s, s->primit, q, i, j, k + 1);
+        }
+        swapz(p, pl);
+        swapz(p, pr);
+        if (choice == 2) {
+          for (int q = 1; q <= neq; ++q) {
+            pll[q - 1] = AT(s, s->primit, q, i, j, k - 1);
+            prr[q - 1] = AT(s, s->primit, q, i, j, k + 2);
+          }
+          swapz(p, pll);
+          swapz(p, prr);
+          limiter(p, pll, pl, pr, prr);
+        }
+        riemann(p, pl, pr, ff, &err);
+        swapz(p, ff);
+        for (int q = 1; q <= neq; ++q) AT(s, s->h, q, i, j, k) = ff[q - 1];
+      }
+    }
+  }
+  s->err |= err;
+}
+
+/* ---------------------------------------------------------------------- */
+/* src/flux_cd_module.f90:45-237  boundaryI_ef (serial semantics) */
+static void boundaryI_ef(gor_state_t* s) {
+  const gor_params_t* p = &s->p;
+  const int nx = p->nx, ny = p->ny, nz = p->nz;
+  /* periodic */
+  if (p->bc_left == GOR_BC_PERIODIC && p->bc_right == GOR_BC_PERIODIC)
+    for (int k = 1 - NG; k <= nz + NG; ++k)
+      for (int j = 1 - NG; j <= ny + NG; ++j)
+        for (int q = 1; q <= 3; ++q) {
+          EAT(s, q, 0, j, k) = EAT(s, q, nx, j, k);
+          EAT(s, q, nx + 1, j, k) = EAT(s, q, 1, j, k);
+        }
+  if (p->bc_bottom == GOR_BC_PERIODIC && p->bc_top == GOR_BC_PERIODIC)
+    for (int k = 1 - NG; k <= nz + NG; ++k)
+      for (int i = 1 - NG; i <= nx + NG; ++i)
+        for (int q = 1; q <= 3; ++q) {
+          EAT(s, q, i, 0, k) = EAT(s, q, i, ny, k);
+          EAT(s, q, i, ny + 1, k) = EAT(s, q, i, 1, k);
+        }
+  if (p->bc_out == GOR_BC_PERIODIC && p->bc_in == GOR_BC_PERIODIC)
+    for (int j = 1 - NG; j <= ny + NG; ++j)
+      for (int i = 1 - NG; i <= nx + NG; ++i)
+        for (int q = 1; q <= 3; ++q) {
+          EAT(s, q, i, j, 0) = EAT(s, q, i, j, nz);
+          EAT(s, q, i, j, nz + 1) = EAT(s, q, i, j, 1);
+        }
+  /* closed (reflecting) */
+  for (int k = 0; k <= nz + 1; ++k)
+    for (int j = 0; j <= ny + 1; ++j) {
+      if (p->bc_left == GOR_BC_CLOSED) {
+        EAT(s, 1, 0, j, k) = -EAT(s, 1, 1, j, k);
+        EAT(s, 2, 0, j, k) = EAT(s, 2, 1, j, k);
+        EAT(s, 3, 0, j, k) = EAT(s, 3, 1, j, k);
+      }
+      if (p->bc_right == GOR_BC_CLOSED) {
+        EAT(s, 1, nx + 1, j, k) = -EAT(s, 1, nx, j, k);
+        EAT(s, 2, nx + 1, j, k) = EAT(s, 2, nx, j, k);
+        EAT(s, 3, nx + 1, j, k) = EAT(s, 3, nx, j, k);
+      }
+    }
+  for (int k = 0; k <= nz + 1; ++k)
+    for (int i = 0; i <= nx + 1; ++i) {
+      if (p->bc_bottom == GOR_BC_CLOSED) {
+        EAT(s, 1, i, 0, k) = EAT(s, 1, i, 1, k);
+        EAT(s, 2, i, 0, k) = -EAT(s, 2, i, 1, k);
+        EAT(s, 3, i, 0, k) = EAT(s, 3, i, 1, k);
+      }
+      if (p->bc_top == GOR_BC_CLOSED) {
+        EAT(s, 1, i, ny + 1, k) = EAT(s, 1, i, ny, k);
+        EAT(s, 2, i, ny + 1, k) = -EAT(s, 2, i, ny, k);
+        EAT(s, 3, i, ny + 1, k) = EAT(s, 3, i, ny, k);
+      }
+    }
+  /* the z faces of the closed case copy all three components unchanged
+   * (src/flux_cd_module.f90:179-192) */
+  for (int j = 0; j <= ny + 1; ++j)
+    for (int i = 0; i <= nx + 1; ++i)
+      for (int q = 1; q <= 3; ++q) {
+        if (p->bc_out == GOR_BC_CLOSED) EAT(s, q, i, j, 0) = EAT(s, q, i, j, 1);
+        if (p->bc_in == GOR_BC_CLOSED) EAT(s, q, i, j, nz + 1) = EAT(s, q, i, j, nz);
+      }
+  /* outflow */
+  for (int k = 0; k <= nz + 1; ++k)
+    for (int j = 0; j <= ny + 1; ++j)
+      for (int q = 1; q <= 3; ++q) {
+        if (p->bc_left == GOR_BC_OUTFLOW) EAT(s, q, 0, j, k) = EAT(s, q, 1, j, k);
+        if (p->bc_right == GOR_BC_OUTFLOW) EAT(s, q, nx + 1, j, k) = EAT(s, q, nx, j, k);
+      }
+  for (int k = 0; k <= nz + 1; ++k)
+    for (int i = 0; i <= nx + 1; ++i)
+      for (int q = 1; q <= 3; ++q) {
+        if (p->bc_bottom == GOR_BC_OUTFLOW) EAT(s, q, i, 0, k) = EAT(s, q, i, 1, k);
+        if (p->bc_top == GOR_BC_OUTFLOW) EAT(s, q, i, ny + 1, k) = EAT(s, q, i, ny, k);
+      }
+  for (int j = 0; j <= ny + 1; ++j)
+    for (int i = 0; i <= nx + 1; ++i)
+      for (int q = 1; q <= 3; ++q) {
+        if (p->bc_out == GOR_BC_OUTFLOW) EAT(s, q, i, j, 0) = EAT(s, q, i, j, 1);
+        if (p->bc_in == GOR_BC_OUTFLOW) EAT(s, q, i, j, nz + 1) = EAT(s, q, i, j, nz);
+      }
+}
+
+/* src/flux_cd_module.f90:245-273  get_efield */
+static void get_efield(gor_state_t* s) {
+  const int nx = s->p.nx, ny = s->p.ny, nz = s->p.nz;
+#pragma omp parallel for schedule(static)
+  for (int k = 1; k <= nz; ++k)
+    for (int j = 1; j <= ny; ++j)
+      for (int i = 1; i <= nx; ++i) {
+        EAT(s, 1, i, j, k) = 0.25 * (-AT(s, s->g, 8, i, j - 1, k) - AT(s, s->g, 8, i, j, k)
+                                     + AT(s, s->h, 7, i, j, k - 1) + AT(s, s->h, 7, i, j, k));
+        EAT(s, 2, i, j, k) = 0.25 * (+AT(s, s->f, 8, i - 1, j, k) + AT(s, s->f, 8, i, j, k)
+                                     - AT(s, s->h, 6, i, j, k - 1) - AT(s, s->h, 6, i, j, k));
+        EAT(s, 3, i, j, k) = 0.25 * (-AT(s, s->f, 7, i - 1, j, k) - AT(s, s->f, 7, i, j, k)
+                                     + AT(s, s->g, 6, i, j - 1, k) + AT(s, s->g, 6, i, j, k));
+      }
+  boundaryI_ef(s);
+}
+
+/* ---------------------------------------------------------------------- */
+/* src/sources.f90:57-69 getpos is not needed: the user hook below computes
+ * its own position (EXO/user_mod.f90:179-181). */
+
+/* EXO/user_mod.f90:158-206  get_user_source_terms (point masses) */
+static void user_source(const gor_params_t* p, const double* pp, double* sv, int i, int j,
+                        int k) {
+  double xc = ((double)(i - p->nx / 2) - 0.5) * p->dx;
+  double yc = ((double)(j - p->ny / 2) - 0.5) * p->dy;
+  double zc = ((double)(k - p->nz / 2) - 0.5) * p->dz;
+  for (int l = 0; l < p->ngrav; ++l) {
+    double x = xc - p->grav_x[l], y = yc - p->grav_y[l], z = zc - p->grav_z[l];
+    double rad2 = x * x + y * y + z * z;
+    double r15 = pow(rad2, 1.5);
+    double GM = p->grav_GM[l];
+    sv[1] = sv[1] - pp[0] * GM * x / r15;
+    sv[2] = sv[2] - pp[0] * GM * y / r15;
+    sv[3] = sv[3] - pp[0] * GM * z / r15;
+    sv[4] = sv[4] - pp[0] * GM * (pp[1] * x + pp[2] * y + pp[3] * z) / r15;
+  }
+}
+
+/* src/sources.f90:190-220 source, with divbcorr_8w_source :151-175 and
+ * divergence_B :124-134 */
+static void source(const gor_state_t* s, int i, int j, int k, const double* prim, double* sv) {
+  const gor_params_t* p = &s->p;
+  for (int q = 0; q < p->neq; ++q) sv[q] = 0.0;
+  if (p->user_source_terms) user_source(p, prim, sv, i, j, k);
+  if (p->eight_wave && bfield(p)) {
+    double divB = (AT(s, s->primit, 6, i + 1, j, k) - AT(s, s->primit, 6, i - 1, j, k))
+                      / (2.0 * p->dx)
+                  + (AT(s, s->primit, 7, i, j + 1, k) - AT(s, s->primit, 7, i, j - 1, k))
+                        / (2.0 * p->dy)
+                  + (AT(s, s->primit, 8, i, j, k + 1) - AT(s, s->primit, 8, i, j, k - 1))
+                        / (2.0 * p->dz);
+    sv[1] = sv[1] - divB * prim[5];
+    sv[2] = sv[2] - divB * prim[6];
+    sv[3] = sv[3] - divB * prim[7];
+    sv[4] = sv[4] - divB * (prim[1] * prim[5] + prim[2] * prim[6] + prim[3] * prim[7]);
+    sv[5] = sv[5] - divB * prim[1];
+    sv[6] = sv[6] - divB * prim[2];
+    sv[7] = sv[7] - divB * prim[3];
+  }
+}
+
+/* src/hydro_solver.f90:77-127  step (with flux_cd_update,
+ * src/flux_cd_module.f90:285-323) */
+static void step(gor_state_t* s, double dt) {
+  const gor_params_t* p = &s->p;
+  const int neq = p->neq, nx = p->nx, ny = p->ny, nz = p->nz;
+  double dtdx = dt / p->dx, dtdy = dt / p->dy, dtdz = dt / p->dz;
+  int ct = p->enable_flux_cd && bfield(p);
+  if (ct) get_efield(s);
+  int src = p->user_source_terms || p->eight_wave;
+#pragma omp parallel for schedule(static)
+  for (int k = 1; k <= nz; ++k) {
+    double sv[8], prim[8];
+    for (int j = 1; j <= ny; ++j)
+      for (int i = 1; i <= nx; ++i) {
+        if (!ct) {
+          for (int q = 1; q <= neq; ++q)
+            AT(s, s->up, q, i, j, k) =
+                AT(s, s->u, q, i, j, k)
+                - dtdx * (AT(s, s->f, q, i, j, k) - AT(s, s->f, q, i - 1, j, k))
+                - dtdy * (AT(s, s->g, q, i, j, k) - AT(s, s->g, q, i, j - 1, k))
+                - dtdz * (AT(s, s->h, q, i, j, k) - AT(s, s->h, q, i, j, k - 1));
+        } else {
+          for (int q = 1; q <= 5; ++q)
+            AT(s, s->up, q, i, j, k) =
+                AT(s, s->u, q, i, j, k)
+                - dtdx * (AT(s, s->f, q, i, j, k) - AT(s, s->f, q, i - 1, j, k))
+                - dtdy * (AT(s, s->g, q, i, j, k) - AT(s, s->g, q, i, j - 1, k))
+                - dtdz * (AT(s, s->h, q, i, j, k) - AT(s, s->h, q, i, j, k - 1));
+          AT(s, s->up, 6, i, j, k) = AT(s, s->u, 6, i, j, k)
+                                     - 0.5 * dtdy * (EAT(s, 3, i, j + 1, k) - EAT(s, 3, i, j - 1, k))
+                                     + 0.5 * dtdz * (EAT(s, 2, i, j, k + 1) - EAT(s, 2, i, j, k - 1));
+          AT(s, s->up, 7, i, j, k) = AT(s, s->u, 7, i, j, k)
+                                     + 0.5 * dtdx * (EAT(s, 3, i + 1, j, k) - EAT(s, 3, i - 1, j, k))
+                                     - 0.5 * dtdz * (EAT(s, 1, i, j, k + 1) - EAT(s, 1, i, j, k - 1));
+          AT(s, s->up, 8, i, j, k) = AT(s, s->u, 8, i, j, k)
+                                     - 0.5 * dtdx * (EAT(s, 2, i + 1, j, k) - EAT(s, 2, i - 1, j, k))
+                                     + 0.5 * dtdy * (EAT(s, 1, i, j + 1, k) - EAT(s, 1, i, j - 1, k));
+        }
+        if (src) {
+          for (int q = 1; q <= neq; ++q) prim[q - 1] = AT(s, s->primit, q, i, j, k);
+          source(s, i, j, k, prim, sv);
+          for (int q = 1; q <= neq; ++q)
+            AT(s, s->up, q, i, j, k) = AT(s, s->up, q, i, j, k) + dt * sv[q - 1];
+        }
+      }
+  }
+}
+
+/* src/hydro_solver.f90:47-65  viscous_copy */
+static void viscous_copy(gor_state_t* s) {
+  const gor_params_t* p = &s->p;
+  const int neq = p->neq, nx = p->nx, ny = p->ny, nz = p->nz;
+  const double eta = p->eta;
+#pragma omp parallel for schedule(static)
+  for (int k = 1; k <= nz; ++k)
+    for (int j = 1; j <= ny; ++j)
+      for (int i = 1; i <= nx; ++i)
+        for (int q = 1; q <= neq; ++q)
+          AT(s, s->u, q, i, j, k) =
+              AT(s, s->up, q, i, j, k)
+              + eta * (AT(s, s->up, q, i + 1, j, k) + AT(s, s->up, q, i - 1, j, k)
+                       + AT(s, s->up, q, i, j + 1, k) + AT(s, s->up, q, i, j - 1, k)
+                       + AT(s, s->up, q, i, j, k + 1) + AT(s, s->up, q, i, j, k - 1)
+                       - 6.0 * AT(s, s->up, q, i, j, k));
+}
+
+/* ---------------------------------------------------------------------- */
+/* Boundaries: src/boundaries.f90:44-247 (boundaryI, one ghost layer) and
+ * :256-512 (boundaryII, two layers), serial semantics. */
+static void copy_cell(const gor_state_t* s, double* a, int i, int j, int k, int si, int sj,
+                      int sk, int flipq) {
+  const int neq = s->p.neq;
+  double* dst = &a[CID(s, i, j, k) * (size_t)neq];
+  const double* src = &a[CID(s, si, sj, sk) * (size_t)neq];
+  for (int q = 0; q < neq; ++q) dst[q] = (q + 1 == flipq) ? -src[q] : src[q];
+}
+
+static void impose_user_bc(gor_state_t* s, double* a);
+
+static void boundary_fill(gor_state_t* s, double* a, int layers) {
+  const gor_params_t* p = &s->p;
+  const int nx = p->nx, ny = p->ny, nz = p->nz;
+  /* range of the transverse indices: boundaryI covers 0..n+1, boundaryII the
+   * whole array */
+  const int lo = layers == 1 ? 0 : 1 - NG;
+  const int hix = layers == 1 ? nx + 1 : nx + NG;
+  const int hiy = layers == 1 ? ny + 1 : ny + NG;
+  const int hiz = layers == 1 ? nz + 1 : nz + NG;
+  /* periodic (full transverse planes in both cases) */
+  if (p->bc_left == GOR_BC_PERIODIC && p->bc_right == GOR_BC_PERIODIC)
+    for (int k = 1 - NG; k <= nz + NG; ++k)
+      for (int j = 1 - NG; j <= ny + NG; ++j)
+        for (int l = 0; l < layers; ++l) {
+          copy_cell(s, a, -l, j, k, nx - l, j, k, 0);
+          copy_cell(s, a, nx + 1 + l, j, k, 1 + l, j, k, 0);
+        }
+  if (p->bc_bottom == GOR_BC_PERIODIC && p->bc_top == GOR_BC_PERIODIC)
+    for (int k = 1 - NG; k <= nz + NG; ++k)
+      for (int i = 1 - NG; i <= nx + NG; ++i)
+        for (int l = 0; l < layers; ++l) {
+          copy_cell(s, a, i, -l, k, i, ny - l, k, 0);
+          copy_cell(s, a, i, ny + 1 + l, k, i, 1 + l, k, 0);
+        }
+  if (p->bc_out == GOR_BC_PERIODIC && p->bc_in == GOR_BC_PERIODIC)
+    for (int j = 1 - NG; j <= ny + NG; ++j)
+      for (int i = 1 - NG; i <= nx + NG; ++i)
+        for (int l = 0; l < layers; ++l) {
+          copy_cell(s, a, i, j, -l, i, j, nz - l, 0);
+          copy_cell(s, a, i, j, nz + 1 + l, i, j, 1 + l, 0);
+        }
+  /* closed, then outflow: the mirror source of ghost layer l is interior
+   * layer l+1 counted from the face (j=nghost..1 in boundaryII; layer 1 only
+   * in boundaryI) */
+  for (int pass = 0; pass < 2; ++pass) {
+    int bc = pass == 0 ? GOR_BC_CLOSED : GOR_BC_OUTFLOW;
+    int fx = pass == 0 ? 2 : 0, fy = pass == 0 ? 3 : 0, fz = pass == 0 ? 4 : 0;
+    for (int k = lo; k <= hiz; ++k)
+      for (int j = lo; j <= hiy; ++j)
+        for (int l = 0; l < layers; ++l) {
+          if (p->bc_left == bc) copy_cell(s, a, -l, j, k, 1 + l, j, k, fx);
+          if (p->bc_right == bc) copy_cell(s, a, nx + 1 + l, j, k, nx - l, j, k, fx);
+        }
+    for (int k = lo; k <= hiz; ++k)
+      for (int i = lo; i <= hix; ++i)
+        for (int l = 0; l < layers; ++l) {
+          if (p->bc_bottom == bc) copy_cell(s, a, i, -l, k, i, 1 + l, k, fy);
+          if (p->bc_top == bc) copy_cell(s, a, i, ny + 1 + l, k, i, ny - l, k, fy);
+        }
+    for (int j = lo; j <= hiy; ++j)
+      for (int i = lo; i <= hix; ++i)
+        for (int l = 0; l < layers; ++l) {
+          if (p->bc_out == bc) copy_cell(s, a, i, j, -l, i, j, 1 + l, fz);
+          if (p->bc_in == bc) copy_cell(s, a, i, j, nz + 1 + l, i, j, nz - l, fz);
+        }
+  }
+  if (p->bc_user) impose_user_bc(s, a);
+}
+
+/* EXO/exoplanet.f90:125-266  impose_exo, generalised to a list of spheres
+ * (the first sphere that contains a cell wins, as the if/else-if chain). */
+static void impose_user_bc(gor_state_t* s, double* a) {
+  const gor_params_t* p = &s->p;
+  const int neq = p->neq, nx = p->nx, ny = p->ny, nz = p->nz;
+  for (int k = 1 - NG; k <= nz + NG; ++k)
+    for (int j = 1 - NG; j <= ny + NG; ++j)
+      for (int i = 1 - NG; i <= nx + NG; ++i) {
+        double x = ((double)(i - nx / 2) + 0.5) * p->dx;
+        double y = ((double)(j - ny / 2) + 0.5) * p->dy;
+        double z = ((double)(k - nz / 2) + 0.5) * p->dz;
+        for (int m = 0; m < p->nsph; ++m) {
+          const gor_sphere_t* sp = &p->sph[m];
+          double xs = x - sp->xc, ys = y - sp->yc, zs = z - sp->zc;
+          double rads = sqrt(xs * xs + ys * ys + zs * zs);
+          if (rads <= sp->radius) {
+            if (rads == 0.0) rads = p->dx * 0.10;
+            double velx = sp->vorb[0] + sp->vwind * xs / rads;
+            double vely = sp->vorb[1] + sp->vwind * ys / rads;
+            double velz = sp->vorb[2] + sp->vwind * zs / rads;
+            double dens = sp->dens;
+            double* c = &a[CID(s, i, j, k) * (size_t)neq];
+            c[0] = dens;
+            c[1] = dens * velx;
+            c[2] = dens * vely;
+            c[3] = dens * velz;
+            double b2 = 0.0;
+            if (bfield(p) && (p->mhd || p->pmhd)) {
+              double rr = sp->radius / rads;
+              double cpi = sp->bdip * (rr * rr * rr) / (2.0 * (rads * rads));
+              c[5] = 3.0 * ys * xs * cpi;
+              c[6] = (3.0 * (ys * ys) - rads * rads) * cpi;
+              c[7] = 3.0 * ys * zs * cpi;
+              b2 = c[5] * c[5] + c[6] * c[6] + c[7] * c[7];
+            }
+            c[4] = 0.5 * dens * (velx * velx + vely * vely + velz * velz) + p->cv * dens * sp->tfac;
+            if (p->mhd) c[4] = c[4] + 0.5 * b2;
+            break;
+          }
+        }
+      }
+}
+
+void gor_boundaryI(gor_state_t* s) { boundary_fill(s, s->u, 1); }
+static void boundaryII(gor_state_t* s) { boundary_fill(s, s->up, 2); }
+
+/* ---------------------------------------------------------------------- */
+/* src/hydro_core.f90:245-320  calcprim */
+static void calcprim_arr(gor_state_t* s, const double* uarr, int only_ghost) {
+  const gor_params_t* p = &s->p;
+  const int neq = p->neq, nx = p->nx, ny = p->ny, nz = p->nz;
+  if (only_ghost) {
+    for (int j = 0; j <= ny + 1; ++j)
+      for (int i = 0; i <= nx + 1; ++i) {
+        u2prim(p, &uarr[CID(s, i, j, 0) * neq], &s->primit[CID(s, i, j, 0) * neq], NULL);
+        u2prim(p, &uarr[CID(s, i, j, nz + 1) * neq], &s->primit[CID(s, i, j, nz + 1) * neq], NULL);
+      }
+    for (int k = 0; k <= nz + 1; ++k)
+      for (int i = 0; i <= nx + 1; ++i) {
+        u2prim(p, &uarr[CID(s, i, 0, k) * neq], &s->primit[CID(s, i, 0, k) * neq], NULL);
+        u2prim(p, &uarr[CID(s, i, ny + 1, k) * neq], &s->primit[CID(s, i, ny + 1, k) * neq], NULL);
+      }
+    for (int k = 0; k <= nz + 1; ++k)
+      for (int j = 0; j <= ny + 1; ++j) {
+        u2prim(p, &uarr[CID(s, 0, j, k) * neq], &s->primit[CID(s, 0, j, k) * neq], NULL);
+        u2prim(p, &uarr[CID(s, nx + 1, j, k) * neq], &s->primit[CID(s, nx + 1, j, k) * neq], NULL);
+      }
+    return;
+  }
+  const size_t n = s->ncell;
+#pragma omp parallel for schedule(static)
+  for (size_t c = 0; c < n; ++c) u2prim(p, &uarr[c * neq], &s->primit[c * neq], NULL);
+}
+
+void gor_calcprim(gor_state_t* s, int only_ghost) { calcprim_arr(s, s->u, only_ghost); }
+
+/* src/cooling_dmc.f90:89-106 cooldmc / src/cooling_chi.f90:87-105 coolchi,
+ * with the row index int(log10(T)*10)-39 written for a table of any 1/dlog. */
+static double cooltab(const gor_params_t* p, double T) {
+  if (T > 1e8) return p->tab_tail * sqrt(T);
+  int if1 = (int)(log10(T) * p->tab_inv_dlog) - p->tab_i0; /* 0-based row */
+  if (if1 < 0) if1 = 0;
+  if (if1 > p->ntab - 2) if1 = p->ntab - 2;
+  double T0 = p->tab_T[if1], c0 = p->tab_L[if1];
+  double T1 = p->tab_T[if1 + 1], c1 = p->tab_L[if1 + 1];
+  return (c1 - c0) * (T - T0) / (T1 - T0) + c0;
+}
+
+/* src/cooling_dmc.f90:115-156 coolingdmc (coolingchi is identical) */
+static void cooling_table(gor_state_t* s, double dt) {
+  const gor_params_t* p = &s->p;
+  const int neq = p->neq, nx = p->nx, ny = p->ny, nz = p->nz;
+  const double dt_seconds = dt * p->tsc;
+  const double Tmin = p->tab_Tmin;
+#pragma omp parallel for schedule(static)
+  for (int k = 1; k <= nz; ++k)
+    for (int j = 1; j <= ny; ++j)
+      for (int i = 1; i <= nx; ++i) {
+        double* uu = &s->u[CID(s, i, j, k) * neq];
+        double* pp = &s->primit[CID(s, i, j, k) * neq];
+        double T;
+        u2prim(p, uu, pp, &T);
+        if (T > Tmin) {
+          double Eth0 = p->cv * pp[4];
+          double aloss = cooltab(p, T);
+          double dens = pp[0];
+          double ce = (aloss * (dens * dens)) / (Eth0 * p->Psc);
+          pp[4] = pp[4] * exp(-ce * dt_seconds);
+          uu[4] = uu[4] - Eth0 + p->cv * pp[4];
+        }
+      }
+}
+
+/* src/hydro_core.f90:623-697  get_timestep */
+void gor_get_timestep(gor_state_t* s, int iter, int n_iter, double t, double tprint,
+                      double* dt, int* dump) {
+  const gor_params_t* p = &s->p;
+  const int neq = p->neq, nx = p->nx, ny = p->ny, nz = p->nz;
+  double dtp = 1e30;
+#pragma omp parallel for schedule(static) reduction(min : dtp)
+  for (int k = 1; k <= nz; ++k)
+    for (int j = 1; j <= ny; ++j)
+      for (int i = 1; i <= nx; ++i) {
+        const double* pr = &s->primit[CID(s, i, j, k) * neq];
+        if (p->mhd) {
+          double cx, cy, cz;
+          cfast(p, pr[4], pr[0], pr[5], pr[6], pr[7], &cx, &cy, &cz);
+          dtp = dmin(dtp, p->dx / (fabs(pr[1]) + cx));
+          dtp = dmin(dtp, p->dy / (fabs(pr[2]) + cy));
+          dtp = dmin(dtp, p->dz / (fabs(pr[3]) + cz));
+        } else {
+          double c = csound(p, pr[4], pr[0]);
+          dtp = dmin(dtp, p->dx / (fabs(pr[1]) + c));
+          dtp = dmin(dtp, p->dy / (fabs(pr[2]) + c));
+          dtp = dmin(dtp, p->dz / (fabs(pr[3]) + c));
+        }
+      }
+  if (iter <= n_iter)
+    dtp = p->cfl * ldexp(1.0, -(n_iter + 1 - iter)) * dtp;
+  else
+    dtp = p->cfl * dtp;
+  *dt = dtp;
+  if ((t + *dt) >= tprint) {
+    *dt = tprint - t;
+    *dump = 1;
+  }
+}
+
+/* src/hydro_solver.f90:134-229  tstep */
+void gor_tstep(gor_state_t* s, double dt_CFL) {
+  const gor_params_t* p = &s->p;
+  double dtm = dt_CFL / 2.0;
+  fluxes(s, 1);
+  step(s, dtm);
+  boundaryII(s);
+  calcprim_arr(s, s->up, 0);
+  fluxes(s, 2);
+  step(s, dt_CFL);
+  viscous_copy(s);
+  int table = p->cooling == GOR_COOL_DMC || p->cooling == GOR_COOL_CHI;
+  if (table) cooling_table(s, dt_CFL);
+  gor_boundaryI(s);
+  calcprim_arr(s, s->u, table);
+}
+
+/* ---------------------------------------------------------------------- */
+gor_state_t* gor_create(const gor_params_t* p) {
+  if (p->nx < 1 || p->ny < 1 || p->nz < 1) return NULL;
+  if (p->neq != 5 && p->neq != 8) return NULL;
+  gor_state_t* s = (gor_state_t*)calloc(1, sizeof(gor_state_t));
+  s->p = *p;
+  s->NX = p->nx + 2 * NG;
+  s->NY = p->ny + 2 * NG;
+  s->NZ = p->nz + 2 * NG;
+  s->ncell = (size_t)s->NX * s->NY * s->NZ;
+  size_t nv = s->ncell * (size_t)p->neq;
+  s->u = (double*)calloc(nv, sizeof(double));
+  s->up = (double*)calloc(nv, sizeof(double));
+  s->primit = (double*)calloc(nv, sizeof(double));
+  s->f = (double*)calloc(nv, sizeof(double));
+  s->g = (double*)calloc(nv, sizeof(double));
+  s->h = (double*)calloc(nv, sizeof(double));
+  s->e = (double*)calloc(s->ncell * 3, sizeof(double));
+  if (!s->u || !s->up || !s->primit || !s->f || !s->g || !s->h || !s->e) {
+    gor_destroy(s);
+    return NULL;
+  }
+  return s;
+}
+
+void gor_destroy(gor_state_t* s) {
+  if (!s) return;
+  free(s->u); free(s->up); free(s->primit);
+  free(s->f); free(s->g); free(s->h); free(s->e);
+  free(s);
+}
+
+int gor_nthreads(int n) {
+#ifdef _OPENMP
+  if (n > 0) omp_set_num_threads(n);
+  return omp_get_max_threads();
+#else
+  (void)n;
+  return 1;
+#endif
+}
+
+void gor_set_u(gor_state_t* s, const double* u) {
+  memcpy(s->u, u, s->ncell * s->p.neq * sizeof(double));
+}
+void gor_get_u(const gor_state_t* s, double* u) {
+  memcpy(u, s->u, s->ncell * s->p.neq * sizeof(double));
+}
+void gor_get_primit(const gor_state_t* s, double* pr) {
+  memcpy(pr, s->primit, s->ncell * s->p.neq * sizeof(double));
+}
+void gor_set_primit(gor_state_t* s, const double* pr) {
+  memcpy(s->primit, pr, s->ncell * s->p.neq * sizeof(double));
+}
+double gor_time(const gor_state_t* s) { return s->time; }
+void gor_set_time(gor_state_t* s, double t) { s->time = t; }
+int gor_error(const gor_state_t* s) { return s->err; }
+
+void gor_riemann(const gor_params_t* p, const double* pl, const double* pr, double* ff,
+                 int* err) {
+  riemann(p, pl, pr, ff, err);
+}
+void gor_prim2f(const gor_params_t* p, const double* prim, double* ff) { prim2f(p, prim, ff); }
+void gor_u2prim(const gor_params_t* p, const double* uu, double* prim, double* T) {
+  u2prim(p, uu, prim, T);
+}
+void gor_prim2u(const gor_params_t* p, const double* prim, double* uu) { prim2u(p, prim, uu); }
+void gor_limiter(const gor_params_t* p, const double* pll, double* pl, double* pr,
+                 const double* prr) {
+  limiter(p, pll, pl, pr, prr);
+}
+double gor_cooltab(const gor_params_t* p, double T) { return cooltab(p, T); }
+
+void gor_divb(const gor_state_t* s, double* divb) {
+  const gor_params_t* p = &s->p;
+  const int nx = p->nx, ny = p->ny, nz = p->nz;
+  for (int k = 1; k <= nz; ++k)
+    for (int j = 1; j <= ny; ++j)
+      for (int i = 1; i <= nx; ++i)
+        divb[((size_t)(k - 1) * ny + (j - 1)) * nx + (i - 1)] =
+            (AT(s, s->u, 6, i + 1, j, k) - AT(s, s->u, 6, i - 1, j, k)) / (2.0 * p->dx)
+            + (AT(s, s->u, 7, i, j + 1, k) - AT(s, s->u, 7, i, j - 1, k)) / (2.0 * p->dy)
+            + (AT(s, s->u, 8, i, j, k + 1) - AT(s, s->u, 8, i, j, k - 1)) / (2.0 * p->dz);
+}
+
+/* src/main.f90:94-125 */
+int gor_run(gor_state_t* s, double tmax, double dtprint, int max_steps, int n_iter, int* iter,
+            double* tprint) {
+  int steps = 0;
+  while (s->time <= tmax && steps < max_steps) {
+    double dt;
+    int dump = 0;
+    gor_get_timestep(s, *iter, n_iter, s->time, *tprint, &dt, &dump);
+    gor_tstep(s, dt);
+    s->time = s->time + dt;
+    if (dump) *tprint = *tprint + dtprint;
+    *iter = *iter + 1;
+    ++steps;
+    if (s->err) break;
+  }
+  return steps;
+}
