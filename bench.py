@@ -1,0 +1,386 @@
+#!/usr/bin/env python
+"""Benchmark: zone-updates/s of the Guacho timestep on GB300.
+
+Workload (N=1): decaying MHD turbulence on a 256^3 periodic box (seeded
+random-phase solenoidal velocity, E(k) ~ k^-2 on 2<=|k|<=8, RMS Mach 1;
+B = (0.1,0,0) + solenoidal perturbation of RMS 0.05), HLLD, van Leer,
+flux-CD, gamma = 5/3.  A step = get_timestep + tstep over the whole box.
+
+  value  : FP32-mixed zone-updates/s, state resident in HBM, CUDA-graph
+           device loop, timed with CUDA events (max over ranks)
+  e2e    : the same through the C ABI with the state in pinned HOST memory
+           (gch_step_host: H2D of u, get_timestep, tstep, D2H of u per step)
+  extra  : the plain FP64 path on the same box, the L1 error of FP32-mixed
+           against it, the live roofline of the dominant kernel, the CPU
+           oracle on a bounded sample, SM clocks sampled during the run.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+
+Under torchrun every rank advances its own replica box on its own GPU
+(the path does not shard: replicas only), timings are max-reduced.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "zone-updates/s on 1 GB300: FP64 plain vs FP32-mixed vs batched, at stated L1 err"
+UNIT = "zone-updates/s"
+WORKLOAD = ("decaying MHD turbulence 256^3, periodic, HLLD + van Leer + flux-CD, "
+            "seeded random-phase solenoidal velocity (E(k)~k^-2, 2<=|k|<=8, Mach 1)")
+
+
+def _dist():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+class Dist:
+    """Barrier and max-reduce across ranks (no-op at N=1)."""
+
+    def __init__(self):
+        self.ws, self.rank, self.local = _dist()
+        self.pg = None
+        if self.ws > 1:
+            import torch
+            import torch.distributed as td
+            backend = "nccl" if torch.cuda.is_available() else "gloo"
+            if backend == "nccl":
+                torch.cuda.set_device(0)  # one visible GPU per rank
+            td.init_process_group(backend=backend)
+            self.td, self.torch, self.backend = td, torch, backend
+
+    def barrier(self):
+        if self.ws > 1:
+            self.td.barrier()
+
+    def max(self, x: float) -> float:
+        if self.ws == 1:
+            return x
+        dev = "cuda" if self.backend == "nccl" else "cpu"
+        t = self.torch.tensor([x], dtype=self.torch.float64, device=dev)
+        self.td.all_reduce(t, op=self.td.ReduceOp.MAX)
+        return float(t.item())
+
+    def close(self):
+        if self.ws > 1:
+            self.td.destroy_process_group()
+
+
+class Clocks:
+    """nvidia-smi samples during the timed region (SM clock, reasons)."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self):
+        self.proc = None
+        self.out = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=self.out, stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        self.proc.wait()
+        self.out.flush()
+        rows = [r.split(",") for r in Path(self.out.name).read_text().splitlines() if r.strip()]
+        os.unlink(self.out.name)
+        vis = os.environ.get("CUDA_VISIBLE_DEVICES", "0").split(",")[0]
+        rows = [r for r in rows if r[0].strip() == vis] or rows
+        sm = [float(r[1]) for r in rows if r[1].strip().replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].strip().replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4)
+                          if len(r) > 5 + i and r[5 + i].strip().lower() == "active"})
+        load = [s for s in sm if mx and s > 0.5 * max(mx)] or sm
+        return {"sm_mhz": statistics.median(load) if load else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": reasons,
+                "samples": len(rows)}
+
+
+def peaks() -> dict:
+    f = ROOT / "MEASURED_PEAKS.json"
+    if f.exists():
+        d = json.loads(f.read_text())
+        return {"hbm_gbs": d["hbm_gbs"], "source": "measured"}
+    return {"hbm_gbs": 6800.0, "source": "fallback"}
+
+
+# ---------------------------------------------------------------------------
+# algorithmic bytes per cell of the dominant kernel (stage-2 k_flux) and per
+# zone-update of the whole step (two-sweep minimum 3 u + 2 up passes)
+def kernel_bytes_per_cell(prec: int, neq: int = 8) -> int:
+    tu = 8
+    ts = 8 if prec == 0 else 4
+    # read up (neq), read u(1:5), write u(1:5), write E (3)
+    return neq * ts + 5 * tu + 5 * tu + 3 * ts
+
+
+def step_bytes_per_zone(prec: int, neq: int = 8) -> int:
+    tu = 8
+    ts = 8 if prec == 0 else 4
+    return neq * (3 * tu + 2 * ts)
+
+
+def rel_l1(a, b):
+    import numpy as np
+    return float(np.abs(a - b).mean() / max(np.abs(b).mean(), 1e-300))
+
+
+def prim_fields(p, u):
+    import numpy as np
+    ui = u[2:-2, 2:-2, 2:-2]
+    rho = ui[..., 0]
+    v = ui[..., 1:4] / rho[..., None]
+    e = ui[..., 4] - 0.5 * rho * (v ** 2).sum(-1) - 0.5 * (ui[..., 5:8] ** 2).sum(-1)
+    return {"rho": rho, "p": e / p.cv, "vx": v[..., 0], "vy": v[..., 1], "vz": v[..., 2],
+            "Bx": ui[..., 5], "By": ui[..., 6], "Bz": ui[..., 7]}
+
+
+# ---------------------------------------------------------------------------
+def cpu_oracle_rate(n: int, steps: int, threads: int) -> dict:
+    """The oracle (the C restatement of the reference's CPU algorithm) on an
+    n^3 sample of the same turbulence problem, FP64, all threads."""
+    from guacho_gb300 import problems
+    from oracle.oracle import Oracle
+    p, u0 = problems.turbulence(n)
+    o = Oracle(p, threads=threads)
+    o.init(u0)
+    t, it = 0.0, 1
+    dt, _ = o.get_timestep(it, 10, t, 1e30)  # warm-up step
+    o.tstep(dt)
+    t += dt
+    it += 1
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        dt, _ = o.get_timestep(it, 10, t, 1e30)
+        o.tstep(dt)
+        t += dt
+        it += 1
+    el = time.perf_counter() - t0
+    return {"value": n ** 3 * steps / el, "seconds": el, "n": n, "steps": steps}
+
+
+def run_reference(args, dist: Dist) -> None:
+    if dist.rank != 0:
+        dist.close()
+        return
+    threads = os.cpu_count() or 1
+    from oracle.oracle import Oracle, build
+    from guacho_gb300 import problems
+    build()
+    n = args.ref_size
+    p, u0 = problems.turbulence(n)
+    o = Oracle(p, threads=threads)
+    o.init(u0)
+    t, it = 0.0, 1
+    for _ in range(args.warmup):
+        dt, _ = o.get_timestep(it, 10, t, 1e30)
+        o.tstep(dt)
+        t += dt
+        it += 1
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        dt, _ = o.get_timestep(it, 10, t, 1e30)
+        o.tstep(dt)
+        t += dt
+        it += 1
+    el = time.perf_counter() - t0
+    rate = n ** 3 * args.steps / el
+    sample = (f"{n}^3 sample of the same turbulence problem (same seed and spectrum), "
+              f"FP64, {args.steps} steps after {args.warmup} warm-up")
+    line = {"impl": "reference", "metric": METRIC, "value": rate, "unit": UNIT, "n_gpus": 1,
+            "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": 1e3 * el / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "reference_sample_n": n},
+            "cpu_baseline": {"value": rate, "unit": UNIT, "cores": threads, "kind": "port",
+                             "sample": sample + "; the reference Fortran+MPI build cannot "
+                                       "be compiled here (no Fortran compiler), so the C "
+                                       "restatement (oracle/) runs instead"},
+            "e2e": {"value": rate, "unit": UNIT, "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    dist.close()
+
+
+# ---------------------------------------------------------------------------
+def run_ours(args, dist: Dist) -> None:
+    import numpy as np
+
+    from guacho_gb300 import build as gbuild
+    if dist.rank == 0 or dist.ws == 1:
+        gbuild.build(verbose=False)
+    dist.barrier()
+    from guacho_gb300 import params as P
+    from guacho_gb300 import problems
+    from guacho_gb300.domain import Domain
+
+    n = args.size
+    K, W = args.steps, args.warmup
+    p, u0 = problems.turbulence(n)
+    pk = peaks()
+    out = {}
+
+    # ---- FP32-mixed, device resident --------------------------------------
+    pm = p.replace(precision=P.FP32_MIXED)
+    d = Domain(pm)
+    d.init(u0)
+    d.advance_timed(W)
+    clocks = Clocks()
+    dist.barrier()
+    clocks.start()
+    ms = d.advance_timed(K)
+    clk = clocks.stop()
+    ms = dist.max(ms)
+    launches = d.launches_per_step()
+    value = dist.ws * n ** 3 * K / (ms * 1e-3)
+    # live per-kernel durations (events between launches, same stream)
+    prof = {}
+    for _ in range(3):
+        for name, t in d.profile_step():
+            prof.setdefault(name, []).append(t)
+    um = d.download()
+    d.close()
+
+    # ---- plain FP64 on the same box (for the stated ratio and L1 error) ----
+    p64 = p.replace(precision=P.FP64)
+    d64 = Domain(p64)
+    d64.init(u0)
+    d64.advance_timed(1)
+    k64 = max(2, args.fp64_steps)
+    ms64 = d64.advance_timed(k64)
+    # same total step count as the mixed run for the error comparison
+    remaining = (W + K) - (1 + k64)
+    if remaining > 0:
+        d64.advance_timed(remaining)
+    u64 = d64.download()
+    d64.close()
+    fm, f64 = prim_fields(p, um), prim_fields(p, u64)
+    l1 = {k: rel_l1(fm[k], f64[k]) for k in ("rho", "p", "vx", "By", "Bx", "Bz")}
+
+    # ---- e2e through the C ABI with host buffers ----------------------------
+    import torch
+    host = torch.empty(p.shape, dtype=torch.float64, pin_memory=True).numpy()
+    host[...] = u0
+    de = Domain(pm)
+    de.init(u0)
+    t, it = 0.0, 1
+    for _ in range(2):
+        dt, _ = de.step_host(host, it, 10, t, 1e300)
+        t += dt
+        it += 1
+    ke = max(2, args.e2e_steps)
+    dist.barrier()
+    t0 = time.perf_counter()
+    for _ in range(ke):
+        dt, _ = de.step_host(host, it, 10, t, 1e300)
+        t += dt
+        it += 1
+    e2e_s = dist.max(time.perf_counter() - t0)
+    de.close()
+    e2e = {"value": dist.ws * n ** 3 * ke / e2e_s, "unit": UNIT,
+           "h2d_bytes_per_step": int(host.nbytes), "d2h_bytes_per_step": int(host.nbytes),
+           "steps": ke, "path": "gch_step_host: pinned host u -> H2D -> get_timestep + "
+                                "tstep -> D2H"}
+
+    # ---- roofline of the dominant kernel -----------------------------------
+    means = {k: sum(v) / len(v) for k, v in prof.items()}
+    total = sum(sum(v) for v in prof.values())
+    dom = max(means, key=lambda k: sum(prof[k]))
+    cells = n ** 3
+    bpc = kernel_bytes_per_cell(P.FP32_MIXED) if dom == "k_flux_stage2" else None
+    roof = None
+    if bpc:
+        ach = bpc * cells / (means[dom] * 1e-3) / 1e9
+        roof = {"kernel": dom, "bound": "hbm", "achieved": ach, "peak": pk["hbm_gbs"],
+                "unit": "GB/s", "frac": ach / pk["hbm_gbs"], "traffic": args.traffic,
+                "bytes_per_cell": bpc, "launch_ms": means[dom],
+                "share_of_step": sum(prof[dom]) / total, "peak_source": pk["source"]}
+    sbz = step_bytes_per_zone(P.FP32_MIXED)
+    step_gbs = value / dist.ws * sbz / 1e9
+    step_roof = {"bytes_per_zone_update": sbz, "achieved": step_gbs, "peak": pk["hbm_gbs"],
+                 "unit": "GB/s", "frac": step_gbs / pk["hbm_gbs"]}
+
+    # ---- CPU baseline (rank 0, N=1 only) ------------------------------------
+    cpu = None
+    if dist.rank == 0 and dist.ws == 1 and not args.no_cpu:
+        threads = os.cpu_count() or 1
+        r = cpu_oracle_rate(args.cpu_size, args.cpu_steps, threads)
+        cpu = {"value": r["value"], "unit": UNIT, "cores": threads, "kind": "port",
+               "sample": f"oracle (C restatement of the reference CPU algorithm), "
+                         f"{r['n']}^3 sample of the same problem, {r['steps']} steps, FP64, "
+                         f"{r['seconds']:.1f} s"}
+
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": dist.ws, "steps": K,
+        "warmup": W, "ms_per_step": ms / K, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32 (f64 pressure recovery, accumulation, dt)",
+        "data": "synthetic (seeded turbulence initial state, no dataset)",
+        "config": {"workload": WORKLOAD, "n": n, "precision": "fp32_mixed",
+                   "parallelism": f"replicas x{dist.ws}",
+                   "l2": "state 1.1 GB FP64 u + 0.56 GB FP32 up >> 129 MB L2 (no flush)"},
+        "fp64_plain": {"value": dist.ws * n ** 3 * k64 / (ms64 * 1e-3),
+                       "ms_per_step": ms64 / k64, "steps": k64},
+        "l1_err_fp32_vs_fp64": l1,
+        "kernel_ms": {k: round(v, 4) for k, v in means.items()},
+        "roofline": roof, "step_roofline": step_roof,
+        "cpu_baseline": cpu, "e2e": e2e, "clocks": clk,
+        "gpu_launches": launches * K,
+    }
+    if dist.rank == 0:
+        print(json.dumps(line), flush=True)
+    dist.close()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=40)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--size", type=int, default=256)
+    ap.add_argument("--fp64-steps", type=int, default=4)
+    ap.add_argument("--e2e-steps", type=int, default=6)
+    ap.add_argument("--cpu-size", type=int, default=96)
+    ap.add_argument("--cpu-steps", type=int, default=3)
+    ap.add_argument("--ref-size", type=int, default=128)
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--traffic", type=float, default=None,
+                    help="ncu dram bytes per launch of the dominant kernel, if known")
+    args = ap.parse_args()
+    ws, rank, local = _dist()
+    if ws > 1 and args.impl == "ours":
+        os.environ["CUDA_VISIBLE_DEVICES"] = str(local)
+    dist = Dist()
+    if args.impl == "reference":
+        run_reference(args, dist)
+    else:
+        run_ours(args, dist)
+
+
+if __name__ == "__main__":
+    main()

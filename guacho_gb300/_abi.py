@@ -118,6 +118,8 @@ def lib() -> C.CDLL:
         "gch_advance": (I, [P, I, D, D, I, DP, IP, DP, IP]),
         "gch_last_step_info": (I, [P, C.POINTER(C.c_longlong), IP]),
         "gch_launches_per_step": (I, [P]),
+        "gch_advance_timed": (I, [P, I, I, C.POINTER(C.c_float)]),
+        "gch_profile_step": (I, [P, I, C.POINTER(C.c_float), C.c_char_p, I, IP]),
         "gch_batch_create": (I, [I, C.POINTER(Params_t), P, VPP]),
         "gch_batch_destroy": (I, [P]),
         "gch_batch_upload": (I, [P, I, P]),
@@ -137,7 +139,8 @@ def exported_symbols() -> list[str]:
     return ["gch_params_default", "gch_params_check", "gch_create", "gch_destroy",
             "gch_upload", "gch_download", "gch_boundaryI", "gch_calcprim",
             "gch_get_timestep", "gch_tstep", "gch_step_host", "gch_advance",
-            "gch_last_step_info", "gch_launches_per_step", "gch_batch_create",
+            "gch_last_step_info", "gch_launches_per_step", "gch_advance_timed",
+            "gch_profile_step", "gch_batch_create",
             "gch_batch_destroy", "gch_batch_upload", "gch_batch_download",
             "gch_batch_advance", "gch_batch_time"]
 

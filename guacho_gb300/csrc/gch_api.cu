@@ -143,6 +143,8 @@ int gch_params_check(const gch_params_t* p) {
 int gch_destroy(gch_domain_t* d) {
   if (!d) return GCH_OK;
   if (d->graph) cudaGraphExecDestroy(d->graph);
+  for (int i = 0; i < 64; ++i)
+    if (d->prof_ev[i]) cudaEventDestroy(d->prof_ev[i]);
   cudaFree(d->u);
   cudaFree(d->up);
   cudaFree(d->w);
@@ -394,10 +396,22 @@ extern "C" {
 
 int gch_advance(gch_domain_t* d, int max_steps, double tmax, double dtprint, int n_iter,
                 double* time, int* iter, double* tprint, int* steps_done) {
-  if (!d || !time || !iter || !tprint) return GCH_ERR_PARAM;
+  if (!d || !time || !iter || !tprint || max_steps < 0) return GCH_ERR_PARAM;
   const int iter0 = *iter;
-  int st = gch_advance_enqueue(d, max_steps, tmax, dtprint, n_iter, *time, *iter, *tprint);
-  if (st) return st;
+  // Launch the step graph in chunks and stop as soon as the device loop
+  // condition (time <= tmax, no error) turns false: the host never queues
+  // more than one chunk of steps past the end of the run.
+  int st = gch_advance_enqueue(d, 0, tmax, dtprint, n_iter, *time, *iter, *tprint);
+  int left = max_steps;
+  int chunk = 8;
+  while (st == GCH_OK && left > 0) {
+    const int k = std::min(chunk, left);
+    for (int n = 0; n < k; ++n) st |= cuda_ok(cudaGraphLaunch(d->graph, d->stream));
+    left -= k;
+    st |= fetch_scalars(d);
+    if (!d->sc_host->active || d->sc_host->err) break;
+    chunk = std::min(chunk * 2, 256);
+  }
   st |= gch_advance_finish(d, time, iter, tprint);
   if (steps_done) *steps_done = *iter - iter0;
   return st;
@@ -409,6 +423,54 @@ int gch_last_step_info(gch_domain_t* d, long long* pfloor_hits, int* err_bits) {
   if (pfloor_hits) *pfloor_hits = (long long)d->sc_host->pfloor;
   if (err_bits) *err_bits = d->sc_host->err;
   k_clear_info<<<1, 1, 0, d->stream>>>(d->sc);
+  return st;
+}
+
+int gch_advance_timed(gch_domain_t* d, int steps, int n_iter, float* ms) {
+  if (!d || !ms || steps < 0) return GCH_ERR_PARAM;
+  const double inf = 1e300;
+  int st = fetch_scalars(d);
+  const double t0 = d->sc_host->time;
+  const int it0 = d->sc_host->iter > 0 ? d->sc_host->iter : 1;
+  cudaEvent_t a, b;
+  st |= cuda_ok(cudaEventCreate(&a));
+  st |= cuda_ok(cudaEventCreate(&b));
+  k_set_ctrl<<<1, 1, 0, d->stream>>>(d->sc, it0, n_iter, t0, inf, inf, inf, 1);
+  st |= gch_advance_enqueue(d, 0, inf, inf, n_iter, t0, it0, inf);  // capture only
+  st |= cuda_ok(cudaEventRecord(a, d->stream));
+  for (int n = 0; n < steps; ++n) st |= cuda_ok(cudaGraphLaunch(d->graph, d->stream));
+  st |= cuda_ok(cudaEventRecord(b, d->stream));
+  st |= cuda_ok(cudaEventSynchronize(b));
+  st |= cuda_ok(cudaEventElapsedTime(ms, a, b));
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  st |= fetch_scalars(d);
+  st |= d->sc_host->err;
+  return st;
+}
+
+int gch_profile_step(gch_domain_t* d, int cap, float* ms, char* names, int name_len, int* n) {
+  if (!d || !ms || !names || !n || cap < 1 || name_len < 2) return GCH_ERR_PARAM;
+  int st = fetch_scalars(d);
+  const double inf = 1e300;
+  const int it0 = d->sc_host->iter > 0 ? d->sc_host->iter : 1;
+  for (int i = 0; i < 64; ++i)
+    if (!d->prof_ev[i]) st |= cuda_ok(cudaEventCreate(&d->prof_ev[i]));
+  k_set_ctrl<<<1, 1, 0, d->stream>>>(d->sc, it0, 10, d->sc_host->time, inf, inf, inf, 1);
+  d->prof_on = true;
+  d->prof_n = 0;
+  st |= cuda_ok(cudaEventRecord(d->prof_ev[0], d->stream));
+  st |= engine(d).get_dt(d);
+  st |= engine(d).tstep(d);
+  d->prof_on = false;
+  st |= cuda_ok(cudaStreamSynchronize(d->stream));
+  const int m = std::min(cap, d->prof_n);
+  for (int i = 0; i < m; ++i) {
+    st |= cuda_ok(cudaEventElapsedTime(&ms[i], d->prof_ev[i], d->prof_ev[i + 1]));
+    strncpy(names + (size_t)i * name_len, d->prof_name[i], name_len - 1);
+    names[(size_t)i * name_len + name_len - 1] = 0;
+  }
+  *n = m;
   return st;
 }
 

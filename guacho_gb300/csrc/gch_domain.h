@@ -34,7 +34,21 @@ struct gch_domain {
   int launches = 0;             // kernel launches of the last tstep
   // CUDA graph of one device-resident step (get_timestep + tstep + loop tail)
   cudaGraphExec_t graph = nullptr;
+  // per-launch profiling: when prof_on, an event is recorded after every
+  // launch with the kernel's name (gch_profile_step)
+  bool prof_on = false;
+  int prof_n = 0;
+  cudaEvent_t prof_ev[64] = {};
+  const char* prof_name[64] = {};
 };
+
+// Record the end of the launch just issued (no-op unless profiling).
+inline void gch_mark(gch_domain* d, const char* name) {
+  if (!d->prof_on || d->prof_n >= 63) return;
+  d->prof_name[d->prof_n] = name;
+  cudaEventRecord(d->prof_ev[d->prof_n + 1], d->stream);
+  ++d->prof_n;
+}
 
 namespace gch {
 

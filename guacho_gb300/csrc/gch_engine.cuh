@@ -55,10 +55,12 @@ struct Engine {
       dim3 grid((N0 + 127) / 128, N1, 2 * layers);
       k_ghost<T><<<grid, 128, 0, d->stream>>>(p, a, p.neq, axis, layers, d->sc);
       ++d->launches;
+      gch_mark(d, "k_ghost");
     }
     if (p.bc_user && p.nsph > 0) {
       k_user_bc<T><<<dim3(64, p.nsph), 256, 0, d->stream>>>(p, a, p.neq, d->sc);
       ++d->launches;
+      gch_mark(d, "k_user_bc");
     }
   }
 
@@ -73,7 +75,9 @@ struct Engine {
       if (p.neq == 8) k_cfl<Pol, 8, false><<<grid, block, 0, d->stream>>>(p, (const TU*)d->u, d->sc);
       else k_cfl<Pol, 5, false><<<grid, block, 0, d->stream>>>(p, (const TU*)d->u, d->sc);
     }
+    gch_mark(d, "k_cfl");
     k_dtfin<<<1, 1, 0, d->stream>>>(d->sc, p.cfl);
+    gch_mark(d, "k_dtfin");
     return cuda_status(cudaGetLastError());
   }
 
@@ -88,10 +92,12 @@ struct Engine {
     if (d->prim_in) st |= flux<1, true>(d, d->primit, d->up);
     else st |= flux<1, false>(d, d->u, d->up);
     ++d->launches;
+    gch_mark(d, "k_flux_stage1");
     if (ct) {
       k_ct<Pol, 1><<<cgrid, cblock, 0, d->stream>>>(p, (const TU*)d->u, (TS*)d->up,
                                                      (const TS*)d->E, (const TS*)d->s678, d->sc);
       ++d->launches;
+      gch_mark(d, "k_ct_stage1");
     }
     // boundaryII on up (+ user spheres)
     ghost<TS>(d, (TS*)d->up, 2);
@@ -99,20 +105,24 @@ struct Engine {
     void* dst2 = p.eta != 0.0 ? d->w : d->u;
     st |= flux<2, false>(d, d->up, dst2);
     ++d->launches;
+    gch_mark(d, "k_flux_stage2");
     if (ct) {
       k_ct<Pol, 2><<<cgrid, cblock, 0, d->stream>>>(p, (const TU*)d->u, (TU*)dst2,
                                                      (const TS*)d->E, (const TS*)d->s678, d->sc);
       ++d->launches;
+      gch_mark(d, "k_ct_stage2");
     }
     if (p.eta != 0.0) {
       if (p.neq == 8) k_visc<Pol, 8><<<cgrid, cblock, 0, d->stream>>>(p, (TU*)d->u, (const TU*)d->w, (const TS*)d->up, d->sc);
       else k_visc<Pol, 5><<<cgrid, cblock, 0, d->stream>>>(p, (TU*)d->u, (const TU*)d->w, (const TS*)d->up, d->sc);
       ++d->launches;
+      gch_mark(d, "k_visc");
     }
     if (d->prim_in) {  // tabulated cooling (updates primit and u(5))
       if (p.neq == 8) k_cool<Pol, 8><<<cgrid, cblock, 0, d->stream>>>(p, (TU*)d->u, (TS*)d->primit, d->sc);
       else k_cool<Pol, 5><<<cgrid, cblock, 0, d->stream>>>(p, (TU*)d->u, (TS*)d->primit, d->sc);
       ++d->launches;
+      gch_mark(d, "k_cool");
     }
     // boundaryI on u (+ user spheres), then primitives of the ghost shell
     ghost<TU>(d, (TU*)d->u, 1);
@@ -121,6 +131,7 @@ struct Engine {
       if (p.neq == 8) k_calcprim<Pol, 8><<<g, cblock, 0, d->stream>>>(p, (const TU*)d->u, (TS*)d->primit, 1, d->sc);
       else k_calcprim<Pol, 5><<<g, cblock, 0, d->stream>>>(p, (const TU*)d->u, (TS*)d->primit, 1, d->sc);
       ++d->launches;
+      gch_mark(d, "k_calcprim");
     }
     st |= cuda_status(cudaGetLastError());
     return st;

@@ -99,7 +99,7 @@ class Domain:
         self.boundaryI()
         self.calcprim()
 
-    def run(self, tmax: float, dtprint: float, max_steps: int = 1 << 30, n_iter: int = 10,
+    def run(self, tmax: float, dtprint: float, max_steps: int = 1 << 20, n_iter: int = 10,
             device_loop: bool = True) -> int:
         """The time loop of src/main.f90:94-125 (without output)."""
         if self.tprint is None:
@@ -134,6 +134,25 @@ class Domain:
 
     def launches_per_step(self) -> int:
         return self._lib.gch_launches_per_step(self._h)
+
+    def advance_timed(self, steps: int, n_iter: int = 10) -> float:
+        """`steps` device-resident steps timed with CUDA events; GPU ms."""
+        ms = C.c_float()
+        check("gch_advance_timed", self._lib.gch_advance_timed(self._h, steps, n_iter,
+                                                                C.byref(ms)))
+        return ms.value
+
+    def profile_step(self) -> list[tuple[str, float]]:
+        """One step with an event after every launch: [(kernel, ms)]."""
+        cap, nl = 64, 32
+        ms = (C.c_float * cap)()
+        names = C.create_string_buffer(cap * nl)
+        n = C.c_int()
+        check("gch_profile_step", self._lib.gch_profile_step(self._h, cap, ms, names, nl,
+                                                              C.byref(n)))
+        raw = names.raw
+        return [(raw[i * nl:(i + 1) * nl].split(b"\0")[0].decode(), ms[i])
+                for i in range(n.value)]
 
 
 class Batch:

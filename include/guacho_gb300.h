@@ -221,6 +221,15 @@ int gch_last_step_info(gch_domain_t* d, long long* pfloor_hits, int* err_bits);
 /* Number of kernel launches one gch_tstep issues (for launch accounting). */
 int gch_launches_per_step(gch_domain_t* d);
 
+/* Profiling aids (no counterpart in the reference).
+ * gch_advance_timed: `steps` device-resident iterations without output
+ * clipping, timed with CUDA events on the domain's stream; *ms = GPU time.
+ * gch_profile_step: one get_timestep + tstep with an event after every
+ * launch; writes up to `cap` per-launch durations (ms) and kernel names
+ * (each a NUL-terminated string in a `name_len`-byte slot of `names`). */
+int gch_advance_timed(gch_domain_t* d, int steps, int n_iter, float* ms);
+int gch_profile_step(gch_domain_t* d, int cap, float* ms, char* names, int name_len, int* n);
+
 /* ---- batched boxes ------------------------------------------------------ */
 typedef struct gch_batch gch_batch_t;
 
