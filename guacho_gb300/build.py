@@ -29,7 +29,9 @@ COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", f"-I{INCLUDE}
 # unit -> extra flags
 UNITS = {
     "gch_fp64.cu": ["-fmad=false"],
-    "gch_fp32.cu": [],
+    # FP32 divide / sqrt through the hardware reciprocal and square-root
+    # approximations (FP64 operations are unaffected)
+    "gch_fp32.cu": ["-prec-div=false", "-prec-sqrt=false", "-ftz=true"],
     "gch_api.cu": [],
     "gch_batch.cu": [],
 }

@@ -39,9 +39,10 @@ __global__ void k_set_ctrl(StepScalars* sc, int iter, int n_iter, double time, d
   sc->active = active;
   sc->dump = 0;
 }
-__global__ void k_set_dt(StepScalars* sc, double dt) {
+__global__ void k_set_dt(StepScalars* sc, double dt, double dx, double dy, double dz) {
   sc->dt = dt;
   sc->active = 1;
+  gch::set_stage_ratios(sc, dx, dy, dz);
 }
 __global__ void k_set_active(StepScalars* sc) { sc->active = 1; }
 __global__ void k_clear_info(StepScalars* sc) {
@@ -198,6 +199,7 @@ int gch_create(const gch_params_t* p, void* stream, gch_domain_t** out) {
   k.bc_user = p->bc_user;
   k.dx = p->dx; k.dy = p->dy; k.dz = p->dz;
   k.cv = p->cv; k.gamma = p->gamma; k.cfl = p->cfl; k.eta = p->eta;
+  k.inv_cv = 1.0 / p->cv;
   k.Tempsc = p->Tempsc; k.Psc = p->Psc; k.tsc = p->tsc;
   k.ntab = p->ntab; k.tab_i0 = p->tab_i0;
   k.tab_inv_dlog = p->tab_inv_dlog; k.tab_tail = p->tab_tail; k.tab_Tmin = p->tab_Tmin;
@@ -335,7 +337,7 @@ int gch_get_timestep(gch_domain_t* d, int current_iter, int n_iter, double curre
 int gch_tstep(gch_domain_t* d, double dt) {
   if (!d) return GCH_ERR_PARAM;
   if (!(dt > 0.0) || !std::isfinite(dt)) return GCH_ERR_DT;
-  k_set_dt<<<1, 1, 0, d->stream>>>(d->sc, dt);
+  k_set_dt<<<1, 1, 0, d->stream>>>(d->sc, dt, d->kp.dx, d->kp.dy, d->kp.dz);
   return engine(d).tstep(d);
 }
 

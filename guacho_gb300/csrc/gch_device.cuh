@@ -30,12 +30,14 @@ struct PolFP64 {
   using TS = double;
   using TC = double;
   static constexpr int kMode = GCH_FP64;
+  static constexpr int kMinBlocks = 1;   // stage kernels: blocks per SM hint
 };
 struct PolMixed {
   using TU = double;
   using TS = float;
   using TC = float;
   static constexpr int kMode = GCH_FP32_MIXED;
+  static constexpr int kMinBlocks = 3;
 };
 
 // ---------------------------------------------------------------------------
@@ -53,6 +55,7 @@ struct KParams {
   int bc_user;
   double dx, dy, dz;
   double cv, gamma, cfl, eta;
+  double inv_cv;              // 1/cv for the mixed-precision paths
   double Tempsc, Psc, tsc;
   // cooling table (device pointers)
   int ntab, tab_i0;
@@ -81,7 +84,22 @@ struct StepScalars {
   int active;                 // loop condition of the device time loop
   int pad;
   unsigned long long pfloor;  // pressure-floor hits (u2prim)
+  // dt/dx, dt/dy, dt/dz of stage 1 (dtm = dt/2) and stage 2 (dt), computed
+  // once per step exactly as src/hydro_solver.f90:91-93 does
+  double dtd[2][3];
 };
+
+// Fill the per-stage ratios from sc->dt (one thread).
+__device__ __forceinline__ void set_stage_ratios(StepScalars* sc, double dx, double dy,
+                                                 double dz) {
+  const double dtm = sc->dt / 2.0;  // src/hydro_solver.f90:152
+  sc->dtd[0][0] = dtm / dx;
+  sc->dtd[0][1] = dtm / dy;
+  sc->dtd[0][2] = dtm / dz;
+  sc->dtd[1][0] = sc->dt / dx;
+  sc->dtd[1][1] = sc->dt / dy;
+  sc->dtd[1][2] = sc->dt / dz;
+}
 
 __host__ __device__ inline long long cell_index(const KParams& p, int ax, int ay, int az) {
   return ((long long)az * p.NY + ay) * p.pitch + ax;

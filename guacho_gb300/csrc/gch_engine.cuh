@@ -27,7 +27,15 @@ struct Engine {
     dim3 block(TX, TY);
     using TIn = typename Src<Pol, NEQ, STAGE, PRIM_IN>::TIn;
     using TD = typename std::conditional<STAGE == 1, TS, TU>::type;
-    k_flux<Pol, SOLVER, NEQ, STAGE, PRIM_IN><<<grid, block, 0, d->stream>>>(
+    using TC = typename Ops<Pol>::TC;
+    constexpr size_t smem = sizeof(FluxSmem<TC, NEQ, STAGE>);
+    static bool attr = false;  // once per instantiation
+    if (!attr) {
+      cudaFuncSetAttribute(k_flux<Pol, SOLVER, NEQ, STAGE, PRIM_IN>,
+                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      attr = true;
+    }
+    k_flux<Pol, SOLVER, NEQ, STAGE, PRIM_IN><<<grid, block, smem, d->stream>>>(
         p, (const TIn*)src, (const TU*)d->u, (TD*)dst, (TS*)d->E, (TS*)d->s678, d->sc, d->kz);
   }
 
@@ -76,7 +84,7 @@ struct Engine {
       else k_cfl<Pol, 5, false><<<grid, block, 0, d->stream>>>(p, (const TU*)d->u, d->sc);
     }
     gch_mark(d, "k_cfl");
-    k_dtfin<<<1, 1, 0, d->stream>>>(d->sc, p.cfl);
+    k_dtfin<<<1, 1, 0, d->stream>>>(d->sc, p.cfl, p.dx, p.dy, p.dz);
     gch_mark(d, "k_dtfin");
     return cuda_status(cudaGetLastError());
   }

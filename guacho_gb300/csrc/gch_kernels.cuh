@@ -45,18 +45,35 @@ struct Src {
   }
 };
 
+// Shared memory of the stage kernel (dynamic: up to 72 KB in FP32).
+template <class TC, int NEQ, int STAGE>
+struct FluxSmem {
+  static constexpr int H = STAGE == 1 ? 1 : 2;
+  static constexpr int NQ = STAGE == 1 ? 1 : 3;
+  TC P[NEQ][TY + 2 * H][TX + 2 * H];
+  TC F[NEQ][TY][TX + 1];
+  TC G[NEQ][TY + 1][TX];
+  TC Hz[2][NEQ][TY][TX];
+  TC Q[NQ][NEQ][TY][TX];
+};
+
 // ---------------------------------------------------------------------------
 // Stage kernel.  Block = TX x TY cells of one x-y tile; the block marches
-// over planes [kb, ke) of z.  Per plane:
-//   1. the prim plane with an H-cell halo (H = 1 first order, 2 limited)
-//      goes to shared memory (centre cells carried from the previous plane
-//      in registers, halo ring recomputed from global memory);
-//   2. x and y face fluxes of the tile -> shared memory; the z face k+1/2
-//      of each column in registers (face k-1/2 carried);
+// over planes [kb, ke) of z.  Per plane k:
+//   1. the primitive plane k with an H-cell halo (H = 1 first order, 2
+//      limited) is staged in shared memory: centre cells from the column
+//      ring (each thread owns one column), halo cells formed from global
+//      memory;
+//   2. one work loop solves every face the tile needs, through a single
+//      Riemann call site: first the z face k+1/2 of each thread's own
+//      column, then the tile's x faces and y faces; fluxes go to shared
+//      memory;
 //   3. each cell: hydro update (+ sources) and E from its six faces.
+// Column state (the next planes, z slopes, z fluxes) lives in shared
+// memory slots owned by one thread, which keeps registers for the solver.
 // Fluxes are never written to global memory.
 template <class Pol, int SOLVER, int NEQ, int STAGE, bool PRIM_IN>
-__global__ void __launch_bounds__(NT)
+__global__ void __launch_bounds__(NT, Pol::kMinBlocks)
 k_flux(KParams p, const typename Src<Pol, NEQ, STAGE, PRIM_IN>::TIn* __restrict__ src,
        const typename Pol::TU* u,
        typename std::conditional<STAGE == 1, typename Pol::TS, typename Pol::TU>::type* dst,
@@ -70,10 +87,14 @@ k_flux(KParams p, const typename Src<Pol, NEQ, STAGE, PRIM_IN>::TIn* __restrict_
   constexpr int PW = TX + 2 * H;
   constexpr int PH = TY + 2 * H;
   constexpr int NRING = 2 * H * (TX + TY);
-
-  __shared__ TC sP[NEQ][PH][PW];
-  __shared__ TC sF[NEQ][TY][TX + 1];
-  __shared__ TC sG[NEQ][TY + 1][TX];
+  using SM = FluxSmem<TC, NEQ, STAGE>;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  SM& sm = *reinterpret_cast<SM*>(smem_raw);
+  auto& sP = sm.P;    // primitive plane k with halo
+  auto& sF = sm.F;    // x-face fluxes (prologue: left z states)
+  auto& sG = sm.G;    // y-face fluxes (prologue: right z states)
+  auto& sH = sm.Hz;   // z-face fluxes, slot (face+1/2)&1
+  auto& sQ = sm.Q;    // column ring: [0] p(k+1), [1] p(k+2), [2] p(k-1)
 
   const int tx = threadIdx.x, ty = threadIdx.y;
   const int tid = ty * TX + tx;
@@ -86,7 +107,8 @@ k_flux(KParams p, const typename Src<Pol, NEQ, STAGE, PRIM_IN>::TIn* __restrict_
   const int lim = p.limiter;
 
   const double dt = STAGE == 1 ? sc->dt / 2.0 : sc->dt;  // dtm = dt_CFL/2.
-  const TC dtdx = (TC)(dt / p.dx), dtdy = (TC)(dt / p.dy), dtdz = (TC)(dt / p.dz);
+  const TC dtdx = (TC)sc->dtd[STAGE - 1][0], dtdy = (TC)sc->dtd[STAGE - 1][1],
+           dtdz = (TC)sc->dtd[STAGE - 1][2];
 
   int err = 0;
   unsigned pfl = 0;
@@ -100,96 +122,137 @@ k_flux(KParams p, const typename Src<Pol, NEQ, STAGE, PRIM_IN>::TIn* __restrict_
     return cell_index(p, ax, ay, az);
   };
   const int axc = ci + NG, ayc = cj + NG;
+  TC bzm = 0;  // Bz at k-1 of this column (eight-wave div B)
 
-  // column state
-  TC pcen[NEQ];   // prim at (ci, cj, k)
-  TC pn[NEQ];     // prim at k+1 (STAGE 2)
-  TC slc[NEQ];    // z slope at k (STAGE 2)
-  TC hprev[NEQ];  // z flux at k-1/2
-  TC bzm = 0;     // Bz at k-1 (eight-wave div B)
-
-  // ---- prologue: z face kb-1/2 -------------------------------------------
+  // ---- column prologue: states of the z face kb-1/2 -----------------------
   {
+    TC a[NEQ], b[NEQ], c[NEQ];
     if (STAGE == 1) {
-      TC pm[NEQ];
-      S::load(p, src, gidx(axc, ayc, kb - 1 + NG), pm, pfl);
-      S::load(p, src, gidx(axc, ayc, kb + NG), pcen, pfl);
-      if (NEQ >= 8) bzm = pm[7];
-      if (active) {
-        TC l[NEQ], r[NEQ], f[NEQ];
+      S::load(p, src, gidx(axc, ayc, kb - 1 + NG), a, pfl);
+      S::load(p, src, gidx(axc, ayc, kb + NG), b, pfl);
 #pragma unroll
-        for (int q = 0; q < NEQ; ++q) { l[q] = pm[perm<2>(q)]; r[q] = pcen[perm<2>(q)]; }
-        Riemann<SOLVER, NEQ>::solve(p, l, r, f, err);
-#pragma unroll
-        for (int q = 0; q < NEQ; ++q) hprev[perm<2>(q)] = f[q];
+      for (int q = 0; q < NEQ; ++q) {
+        sF[q][ty][tx] = a[q];
+        sG[q][ty][tx] = b[q];
+        sQ[0][q][ty][tx] = b[q];
       }
+      if (NEQ >= 8) bzm = a[7];
     } else {
-      TC pm2[NEQ], pm1[NEQ];
-      S::load(p, src, gidx(axc, ayc, kb - 2 + NG), pm2, pfl);
-      S::load(p, src, gidx(axc, ayc, kb - 1 + NG), pm1, pfl);
-      S::load(p, src, gidx(axc, ayc, kb + NG), pcen, pfl);
-      S::load(p, src, gidx(axc, ayc, kb + 1 + NG), pn, pfl);
-      if (NEQ >= 8) bzm = pm1[7];
-      if (active) {
-        TC l[NEQ], r[NEQ], f[NEQ];
+      S::load(p, src, gidx(axc, ayc, kb - 2 + NG), a, pfl);
+      S::load(p, src, gidx(axc, ayc, kb - 1 + NG), b, pfl);
+      S::load(p, src, gidx(axc, ayc, kb + NG), c, pfl);
+      if (NEQ >= 8) bzm = b[7];
 #pragma unroll
-        for (int q = 0; q < NEQ; ++q) {
-          const int s = perm<2>(q);
-          TC sm1 = average(lim, pm1[s] - pm2[s], pcen[s] - pm1[s]);
-          slc[s] = average(lim, pcen[s] - pm1[s], pn[s] - pcen[s]);
-          l[q] = pm1[s] + sm1 * TC(0.5);
-          r[q] = pcen[s] - slc[s] * TC(0.5);
-        }
-        Riemann<SOLVER, NEQ>::solve(p, l, r, f, err);
+      for (int q = 0; q < NEQ; ++q) {
+        const TC sm1 = average(lim, b[q] - a[q], c[q] - b[q]);
+        sF[q][ty][tx] = b[q] + sm1 * TC(0.5);
+        sQ[2][q][ty][tx] = b[q];
+        sQ[0][q][ty][tx] = c[q];
+      }
+      S::load(p, src, gidx(axc, ayc, kb + 1 + NG), a, pfl);  // a = p(kb+1)
 #pragma unroll
-        for (int q = 0; q < NEQ; ++q) hprev[perm<2>(q)] = f[q];
+      for (int q = 0; q < NEQ; ++q) {
+        const TC s0 = average(lim, c[q] - b[q], a[q] - c[q]);
+        sG[q][ty][tx] = c[q] - s0 * TC(0.5);
+        sQ[1][q][ty][tx] = a[q];
       }
     }
   }
 
-  for (int k = kb; k < ke; ++k) {
+  const int nfx = (TX + 1) * TY;
+  const int nfy = TX * (TY + 1);
+  for (int k = kb - 1; k < ke; ++k) {
+    const bool pro = k < kb;
     const int az = k + NG;
-    // next column value(s)
-    TC pnext[NEQ];  // STAGE 1: prim at k+1; STAGE 2: prim at k+2
-    S::load(p, src, gidx(axc, ayc, az + (STAGE == 1 ? 1 : 2)), pnext, pfl);
-
-    __syncthreads();  // previous plane's readers are done with sP/sF/sG
-    // 1. prim plane k: centre from registers, halo ring from global memory
+    if (!pro) {
+      __syncthreads();  // readers of the previous plane are done
+      // 1. plane k: the ring shifts (p(k-1) <- centre, centre <- p(k),
+      //    p(k+1) <- p(k+2)) and the next plane is formed from global memory
+      {
+        TC nx_[NEQ];
+        S::load(p, src, gidx(axc, ayc, az + (STAGE == 1 ? 1 : 2)), nx_, pfl);
 #pragma unroll
-    for (int q = 0; q < NEQ; ++q) sP[q][ty + H][tx + H] = pcen[q];
-    for (int r = tid; r < NRING; r += NT) {
-      int hx, hy;
-      if (r < 2 * H * TX) {  // rows below / above the tile
-        const int row = r / TX;
-        hx = r % TX;
-        hy = row < H ? row - H : TY + (row - H);
-      } else {  // columns left / right
-        const int rr = r - 2 * H * TX;
-        const int col = rr / TY;
-        hy = rr % TY;
-        hx = col < H ? col - H : TX + (col - H);
+        for (int q = 0; q < NEQ; ++q) {
+          if (STAGE == 2 && k > kb) sQ[2][q][ty][tx] = sP[q][ty + H][tx + H];
+          sP[q][ty + H][tx + H] = sQ[0][q][ty][tx];
+          if (STAGE == 1) {
+            sQ[0][q][ty][tx] = nx_[q];
+          } else {
+            sQ[0][q][ty][tx] = sQ[1][q][ty][tx];
+            sQ[1][q][ty][tx] = nx_[q];
+          }
+        }
       }
-      TC pr[NEQ];
-      S::load(p, src, gidx(i0 + hx + NG, j0 + hy + NG, az), pr, pfl);
+      for (int r = tid; r < NRING; r += NT) {
+        int hx, hy;
+        if (r < 2 * H * TX) {  // rows below / above the tile
+          const int row = r / TX;
+          hx = r % TX;
+          hy = row < H ? row - H : TY + (row - H);
+        } else {  // columns left / right
+          const int rr = r - 2 * H * TX;
+          const int col = rr / TY;
+          hy = rr % TY;
+          hx = col < H ? col - H : TX + (col - H);
+        }
+        TC pr[NEQ];
+        S::load(p, src, gidx(i0 + hx + NG, j0 + hy + NG, az), pr, pfl);
 #pragma unroll
-      for (int q = 0; q < NEQ; ++q) sP[q][hy + H][hx + H] = pr[q];
+        for (int q = 0; q < NEQ; ++q) sP[q][hy + H][hx + H] = pr[q];
+      }
+      __syncthreads();
     }
-    __syncthreads();
 
-    // 2a. x faces: face fx (0..TX) between tile cells fx-1 and fx
-    const int nfx = (TX + 1) * TY;
-    const int nfy = TX * (TY + 1);
-    for (int w = tid; w < nfx + nfy; w += NT) {
-      const bool isx = w < nfx;
+    // 2. all faces through one Riemann call site
+    const int nwork = pro ? NT : NT + nfx + nfy;
+    const int hslot = (k + 1) & 1;  // face k+1/2
+    for (int w = tid; w < nwork; w += NT) {
+      int kind;  // 0 = z (own column), 1 = x, 2 = y
       int fx, fy;
-      if (isx) { fx = w % (TX + 1); fy = w / (TX + 1); }
-      else { fx = (w - nfx) % TX; fy = (w - nfx) / TX; }
-      // needed only if an adjacent cell is inside the domain
-      const bool need = isx ? (j0 + fy < p.ny && i0 + fx - 1 < p.nx)
-                            : (i0 + fx < p.nx && j0 + fy - 1 < p.ny);
+      bool need;
+      if (w < NT) {
+        kind = 0; fx = tx; fy = ty; need = active;
+      } else if (w - NT < nfx) {
+        kind = 1;
+        fx = (w - NT) % (TX + 1);
+        fy = (w - NT) / (TX + 1);
+        need = j0 + fy < p.ny && i0 + fx - 1 < p.nx;
+      } else {
+        kind = 2;
+        fx = (w - NT - nfx) % TX;
+        fy = (w - NT - nfx) / TX;
+        need = i0 + fx < p.nx && j0 + fy - 1 < p.ny;
+      }
       if (!need) continue;
       TC l[NEQ], r[NEQ], f[NEQ];
-      if (isx) {
+      if (kind == 0) {
+        if (pro) {
+#pragma unroll
+          for (int q = 0; q < NEQ; ++q) {
+            l[q] = sF[perm<2>(q)][ty][tx];
+            r[q] = sG[perm<2>(q)][ty][tx];
+          }
+        } else if (STAGE == 1) {
+#pragma unroll
+          for (int q = 0; q < NEQ; ++q) {
+            l[q] = sP[perm<2>(q)][ty + H][tx + H];
+            r[q] = sQ[0][perm<2>(q)][ty][tx];
+          }
+        } else {
+          // limiter on p(k-1), p(k), p(k+1), p(k+2)
+#pragma unroll
+          for (int q = 0; q < NEQ; ++q) {
+            const int s = perm<2>(q);
+            const TC ll = sQ[2][s][ty][tx], rr = sQ[1][s][ty][tx];
+            l[q] = sP[s][ty + H][tx + H];
+            r[q] = sQ[0][s][ty][tx];
+            const TC dl = l[q] - ll, dm = r[q] - l[q], dr = rr - r[q];
+            const TC al = average(lim, dl, dm), ar = average(lim, dm, dr);
+            l[q] = l[q] + al * TC(0.5);
+            r[q] = r[q] - ar * TC(0.5);
+          }
+        }
+      } else if (kind == 1) {
         const int cy = fy + H, cl = fx - 1 + H;
 #pragma unroll
         for (int q = 0; q < NEQ; ++q) {
@@ -203,9 +266,6 @@ k_flux(KParams p, const typename Src<Pol, NEQ, STAGE, PRIM_IN>::TIn* __restrict_
             r[q] = r[q] - ar * TC(0.5);
           }
         }
-        Riemann<SOLVER, NEQ>::solve(p, l, r, f, err);
-#pragma unroll
-        for (int q = 0; q < NEQ; ++q) sF[q][fy][fx] = f[q];
       } else {
         const int cx = fx + H, cl = fy - 1 + H;
 #pragma unroll
@@ -221,44 +281,35 @@ k_flux(KParams p, const typename Src<Pol, NEQ, STAGE, PRIM_IN>::TIn* __restrict_
             r[q] = r[q] - ar * TC(0.5);
           }
         }
-        Riemann<SOLVER, NEQ>::solve(p, l, r, f, err);
+      }
+      Riemann<SOLVER, NEQ>::solve(p, l, r, f, err);
+      if (kind == 0) {
+#pragma unroll
+        for (int q = 0; q < NEQ; ++q) sH[hslot][perm<2>(q)][ty][tx] = f[q];
+      } else if (kind == 1) {
+#pragma unroll
+        for (int q = 0; q < NEQ; ++q) sF[q][fy][fx] = f[q];
+      } else {
 #pragma unroll
         for (int q = 0; q < NEQ; ++q) sG[perm<1>(q)][fy][fx] = f[q];
       }
     }
-
-    // 2b. z face k+1/2 of this column
-    TC hnext[NEQ];
-    TC slnext[NEQ];
-    if (active) {
-      TC l[NEQ], r[NEQ], f[NEQ];
-      if (STAGE == 1) {
-#pragma unroll
-        for (int q = 0; q < NEQ; ++q) { l[q] = pcen[perm<2>(q)]; r[q] = pnext[perm<2>(q)]; }
-      } else {
-#pragma unroll
-        for (int q = 0; q < NEQ; ++q) {
-          const int s = perm<2>(q);
-          slnext[s] = average(lim, pn[s] - pcen[s], pnext[s] - pn[s]);
-          l[q] = pcen[s] + slc[s] * TC(0.5);
-          r[q] = pn[s] - slnext[s] * TC(0.5);
-        }
-      }
-      Riemann<SOLVER, NEQ>::solve(p, l, r, f, err);
-#pragma unroll
-      for (int q = 0; q < NEQ; ++q) hnext[perm<2>(q)] = f[q];
-    }
+    if (pro) continue;  // z states of the prologue were private: no barrier
     __syncthreads();
 
     // 3. cell update and E
     if (active) {
       const long long c = cell_index(p, axc, ayc, az);
       const int nupd = ct ? 5 : NEQ;
+      const int hp = k & 1, hn = (k + 1) & 1;  // faces k-1/2, k+1/2
       TC sv[NEQ];
 #pragma unroll
       for (int q = 0; q < NEQ; ++q) sv[q] = TC(0);
       const bool src_terms = p.user_src || (NEQ >= 8 && p.eight_wave);
       if (src_terms) {
+        TC pcen[NEQ];
+#pragma unroll
+        for (int q = 0; q < NEQ; ++q) pcen[q] = sP[q][ty + H][tx + H];
         // src/sources.f90:190-220 with the cell's stage primitives
         if (p.user_src) {
           // EXO/user_mod.f90:158-206 point masses
@@ -280,7 +331,7 @@ k_flux(KParams p, const typename Src<Pol, NEQ, STAGE, PRIM_IN>::TIn* __restrict_
         }
         if (NEQ >= 8 && p.eight_wave) {
           // src/sources.f90:124-175
-          const TC bzp = STAGE == 1 ? pnext[7] : pn[7];
+          const TC bzp = sQ[0][7][ty][tx];
           const TC divB = (sP[5][ty + H][tx + H + 1] - sP[5][ty + H][tx + H - 1]) / (TC)(2.0 * p.dx)
                           + (sP[6][ty + H + 1][tx + H] - sP[6][ty + H - 1][tx + H]) / (TC)(2.0 * p.dy)
                           + (bzp - bzm) / (TC)(2.0 * p.dz);
@@ -298,16 +349,19 @@ k_flux(KParams p, const typename Src<Pol, NEQ, STAGE, PRIM_IN>::TIn* __restrict_
         if (q < nupd) {
           double unew = Ops<Pol>::update((double)u[q * p.fs + c], dtdx, dtdy, dtdz,
                                          sF[q][ty][tx], sF[q][ty][tx + 1], sG[q][ty][tx],
-                                         sG[q][ty + 1][tx], hprev[q], hnext[q]);
+                                         sG[q][ty + 1][tx], sH[hp][q][ty][tx], sH[hn][q][ty][tx]);
           if (src_terms) unew = unew + dt * (double)sv[q];
           dst[q * p.fs + c] = (TD)unew;
         }
       }
       if (ct) {
         // src/flux_cd_module.f90:258-265
-        const TC e1 = TC(0.25) * (-sG[7][ty][tx] - sG[7][ty + 1][tx] + hprev[6] + hnext[6]);
-        const TC e2 = TC(0.25) * (+sF[7][ty][tx] + sF[7][ty][tx + 1] - hprev[5] - hnext[5]);
-        const TC e3 = TC(0.25) * (-sF[6][ty][tx] - sF[6][ty][tx + 1] + sG[5][ty][tx] + sG[5][ty + 1][tx]);
+        const TC e1 = TC(0.25) * (-sG[7][ty][tx] - sG[7][ty + 1][tx] + sH[hp][6][ty][tx]
+                                  + sH[hn][6][ty][tx]);
+        const TC e2 = TC(0.25) * (+sF[7][ty][tx] + sF[7][ty][tx + 1] - sH[hp][5][ty][tx]
+                                  - sH[hn][5][ty][tx]);
+        const TC e3 = TC(0.25) * (-sF[6][ty][tx] - sF[6][ty][tx + 1] + sG[5][ty][tx]
+                                  + sG[5][ty + 1][tx]);
         E[c] = e1;
         E[p.fs + c] = e2;
         E[2 * p.fs + c] = e3;
@@ -318,24 +372,10 @@ k_flux(KParams p, const typename Src<Pol, NEQ, STAGE, PRIM_IN>::TIn* __restrict_
         }
       }
     }
-
-    // carry the column state to plane k+1
-    if (NEQ >= 8) bzm = pcen[7];
-#pragma unroll
-    for (int q = 0; q < NEQ; ++q) {
-      hprev[q] = hnext[q];
-      if (STAGE == 1) {
-        pcen[q] = pnext[q];
-      } else {
-        pcen[q] = pn[q];
-        pn[q] = pnext[q];
-        slc[q] = slnext[q];
-      }
-    }
+    if (NEQ >= 8) bzm = sP[7][ty + H][tx + H];
   }
   raise_err(&sc->err, err);
 }
-
 // ---------------------------------------------------------------------------
 // Constrained transport of B (src/flux_cd_module.f90:311-321) with the E
 // ghost layer of boundaryI_ef (:45-237) applied as an index map.
@@ -353,8 +393,8 @@ k_ct(KParams p, const typename Pol::TU* u,
   if (ci >= p.nx || cj >= p.ny || !sc->active) return;
   const int ax = ci + NG, ay = cj + NG, az = ck + NG;
   const double dt = STAGE == 1 ? sc->dt / 2.0 : sc->dt;
-  const double dtdx = dt / p.dx, dtdy = dt / p.dy, dtdz = dt / p.dz;
-  const TC hx = (TC)(0.5 * dtdx), hy = (TC)(0.5 * dtdy), hz = (TC)(0.5 * dtdz);
+  const TC hx = (TC)(0.5 * sc->dtd[STAGE - 1][0]), hy = (TC)(0.5 * sc->dtd[STAGE - 1][1]),
+           hz = (TC)(0.5 * sc->dtd[STAGE - 1][2]);
 
   // E component q at a face neighbour (the ghost layer follows boundaryI_ef:
   // periodic copy, outflow copy, closed copy with the normal component of the
@@ -558,7 +598,7 @@ k_cfl(KParams p, const typename std::conditional<PRIM_IN, typename Pol::TS, type
 
 // get_timestep's scalar tail (src/hydro_core.f90:677-694) and the bookkeeping
 // of the device time loop (src/main.f90:94-125).
-static __global__ void k_dtfin(StepScalars* sc, double cfl) {
+static __global__ void k_dtfin(StepScalars* sc, double cfl, double dx, double dy, double dz) {
   if (!sc->active) return;
   double dtp = __longlong_as_double((long long)sc->dtmin_bits);
   sc->dtmin_bits = 0x7FF0000000000000ull;  // +inf for the next reduction
@@ -575,6 +615,7 @@ static __global__ void k_dtfin(StepScalars* sc, double cfl) {
   if (!(dt > 0.0) || !(dt < 1e300)) sc->err |= GCH_ERR_DT;
   sc->dt = dt;
   sc->dump = dump;
+  set_stage_ratios(sc, dx, dy, dz);
 }
 
 // Time-loop tail after a tstep (src/main.f90:108-123): device-resident loop.

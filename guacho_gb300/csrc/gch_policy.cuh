@@ -87,38 +87,112 @@ struct Ops<PolFP64> {
 };
 
 // ---------------------------------------------------------------------------
+// Error-free FP32 transformations (compensated "double-float" arithmetic).
+// They contain no multiply-add pattern the compiler could contract, and the
+// products use explicit fmaf, so they stay exact under -fmad=true.
+struct DF {
+  float hi, lo;
+};
+__device__ __forceinline__ DF two_sum(float a, float b) {
+  const float s = a + b;
+  const float bb = s - a;
+  return {s, (a - (s - bb)) + (b - bb)};
+}
+__device__ __forceinline__ DF fast_two_sum(float a, float b) {  // |a| >= |b|
+  const float s = a + b;
+  return {s, b - (s - a)};
+}
+__device__ __forceinline__ DF two_prod(float a, float b) {
+  const float p = a * b;
+  return {p, fmaf(a, b, -p)};
+}
+__device__ __forceinline__ DF df_add(DF x, DF y) {
+  const DF s = two_sum(x.hi, y.hi);
+  return fast_two_sum(s.hi, s.lo + (x.lo + y.lo));
+}
+// a^2 + b^2 + c^2 of exact FP32 inputs, to ~2^-44 relative
+__device__ __forceinline__ DF df_sumsq(float a, float b, float c) {
+  return df_add(df_add(two_prod(a, a), two_prod(b, b)), two_prod(c, c));
+}
+
+// ---------------------------------------------------------------------------
 template <>
 struct Ops<PolMixed> {
   using TC = float;
 
-  // u2prim with the pressure recovery in FP64; inputs promoted exactly.
+  // u2prim with the pressure recovery p = (E - m.m/(2 rho) - B.B/2)/cv
+  // done at FP64-level accuracy:
+  //  - FP64 source (u): FP64 arithmetic, one reciprocal (FP32 estimate and a
+  //    Newton step in FP64 instead of an FP64 divide, which runs at 1/600 of
+  //    the FP32 FMA rate on this part);
+  //  - FP32 source (up): the inputs are exact FP32 numbers, so the products
+  //    are formed exactly with FMA-based two-products and the cancellation
+  //    E - KE - B^2/2 is taken in compensated FP32 ("double-float"), which
+  //    matches an FP64 evaluation to ~1e-13 relative of KE + B^2/2.
   template <int NEQ, class TIn>
   __device__ __forceinline__ static void load_prim(const KParams& p, const TIn* src,
                                                    long long idx, TC* prim, unsigned& pfl) {
-    double uu[NEQ];
+    if constexpr (sizeof(TIn) == 8) {
+      double uu[NEQ];
 #pragma unroll
-    for (int q = 0; q < NEQ; ++q) uu[q] = (double)src[q * p.fs + idx];
-    double r = tmax_(uu[0], 1e-15);
-    double ir = 1.0 / r;
-    double vx = uu[1] * ir, vy = uu[2] * ir, vz = uu[3] * ir;
-    double pr = uu[4] - 0.5 * r * (vx * vx + vy * vy + vz * vz);
-    if (NEQ >= 8 && p.mhd) pr = pr - 0.5 * (uu[5] * uu[5] + uu[6] * uu[6] + uu[7] * uu[7]);
-    pr = pr / p.cv;
-    if (!(pr >= 1e-16)) ++pfl;
-    pr = tmax_(pr, 1e-16);
-    if (p.eos == GCH_EOS_SINGLE_SPECIE) {
-      double t = tmax_(1.0, (pr / r) * p.Tempsc);
-      pr = r * t / p.Tempsc;
-    }
-    prim[0] = (float)r;
-    prim[1] = (float)vx;
-    prim[2] = (float)vy;
-    prim[3] = (float)vz;
-    prim[4] = (float)pr;
-    if (NEQ >= 8) {
-      prim[5] = (float)uu[5];
-      prim[6] = (float)uu[6];
-      prim[7] = (float)uu[7];
+      for (int q = 0; q < NEQ; ++q) uu[q] = (double)src[q * p.fs + idx];
+      const double r = tmax_(uu[0], 1e-15);
+      const float irf = 1.0f / (float)r;
+      double ir = (double)irf;
+      ir = ir * fma(-r, ir, 2.0);
+      const double m2 = fma(uu[3], uu[3], fma(uu[2], uu[2], uu[1] * uu[1]));
+      double kb = m2 * ir;
+      if (NEQ >= 8 && p.mhd) kb = fma(uu[7], uu[7], fma(uu[6], uu[6], fma(uu[5], uu[5], kb)));
+      double pr = fma(-0.5, kb, uu[4]) * p.inv_cv;
+      if (!(pr >= 1e-16)) ++pfl;
+      pr = tmax_(pr, 1e-16);
+      if (p.eos == GCH_EOS_SINGLE_SPECIE) {
+        const double t = tmax_(1.0, (pr * ir) * p.Tempsc);
+        pr = r * t / p.Tempsc;
+      }
+      const float rf = (float)r;
+      prim[0] = rf;
+      prim[1] = (float)uu[1] * irf;
+      prim[2] = (float)uu[2] * irf;
+      prim[3] = (float)uu[3] * irf;
+      prim[4] = (float)pr;
+      if (NEQ >= 8) {
+        prim[5] = (float)uu[5];
+        prim[6] = (float)uu[6];
+        prim[7] = (float)uu[7];
+      }
+    } else {
+      float uu[NEQ];
+#pragma unroll
+      for (int q = 0; q < NEQ; ++q) uu[q] = (float)src[q * p.fs + idx];
+      const float r = tmax_(uu[0], 1e-15f);
+      float ir = 1.0f / r;
+      ir = ir * fmaf(-r, ir, 2.0f);
+      // KE = (m.m)/r as a compensated pair
+      const DF m2 = df_sumsq(uu[1], uu[2], uu[3]);
+      const float q = m2.hi * ir;
+      const float rem = fmaf(-q, r, m2.hi) + m2.lo;
+      DF kb = fast_two_sum(q, rem * ir);
+      if (NEQ >= 8 && p.mhd) kb = df_add(kb, df_sumsq(uu[5], uu[6], uu[7]));
+      // E - kb/2 (halving is exact)
+      const DF d = two_sum(uu[4], -0.5f * kb.hi);
+      float pr = (d.hi + (d.lo - 0.5f * kb.lo)) * (float)p.inv_cv;
+      if (!(pr >= 1e-16f)) ++pfl;
+      pr = tmax_(pr, 1e-16f);
+      if (p.eos == GCH_EOS_SINGLE_SPECIE) {
+        const float t = tmax_(1.0f, (pr * ir) * (float)p.Tempsc);
+        pr = r * t / (float)p.Tempsc;
+      }
+      prim[0] = r;
+      prim[1] = uu[1] * ir;
+      prim[2] = uu[2] * ir;
+      prim[3] = uu[3] * ir;
+      prim[4] = pr;
+      if (NEQ >= 8) {
+        prim[5] = uu[5];
+        prim[6] = uu[6];
+        prim[7] = uu[7];
+      }
     }
   }
 
@@ -133,13 +207,13 @@ struct Ops<PolMixed> {
   __device__ __forceinline__ static double update(double u, float dtdx, float dtdy, float dtdz,
                                                   float fl, float fr, float gl, float gr,
                                                   float hl, float hr) {
-    float d = dtdx * (fr - fl) + dtdy * (gr - gl) + dtdz * (hr - hl);
+    const float d = dtdx * (fr - fl) + dtdy * (gr - gl) + dtdz * (hr - hl);
     return u - (double)d;
   }
 
   __device__ __forceinline__ static double ct(double u, float hdta, float a0, float a1,
                                               float hdtb, float b0, float b1, bool first_minus) {
-    float d = hdta * (a1 - a0) - hdtb * (b1 - b0);
+    const float d = hdta * (a1 - a0) - hdtb * (b1 - b0);
     return first_minus ? u - (double)d : u + (double)d;
   }
 };

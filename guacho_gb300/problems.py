@@ -53,9 +53,10 @@ def conserved(p: Params, rho, vx, vy, vz, pr, bx=None, by=None, bz=None) -> np.n
 def orszag_tang(nx=128, ny=128, nz=4, precision=FP64, cfl=0.4, b0_scale=1.0, **kw) -> tuple:
     """Orszag-Tang vortex, OT/orzag_tang.f90:14-70 and OT/parameters.f90
     (HLLD, minmod, flux-CD, periodic), with dz = dx (zmax = nz/nx)."""
+    opts = dict(riemann_solver=SOLVER_HLLD, slope_limiter=LIMITER_MINMOD)
+    opts.update(kw)
     p = Params(nx=nx, ny=ny, nz=nz, precision=precision, mhd=True,
-               riemann_solver=SOLVER_HLLD, slope_limiter=LIMITER_MINMOD,
-               xmax=1.0, ymax=ny / nx, zmax=nz / nx, cfl=cfl, **kw)
+               xmax=1.0, ymax=ny / nx, zmax=nz / nx, cfl=cfl, **opts)
     pi = math.acos(-1.0)
     rho = 25.0 / (36.0 * pi)
     pr = 5.0 / (12.0 * pi)
@@ -118,8 +119,9 @@ def turbulence(n=256, precision=FP64, seed=20260001, mach=1.0, b0=0.1, brms=0.05
     perturbation of RMS `brms` built as the centred-difference curl of a
     random vector potential (so its centred div B is round-off).  HLLD,
     van Leer, flux-CD."""
-    p = Params(nx=n, ny=n, nz=n, precision=precision, mhd=True, riemann_solver=SOLVER_HLLD,
-               slope_limiter=LIMITER_VAN_LEER, cfl=cfl, **kw)
+    opts = dict(riemann_solver=SOLVER_HLLD, slope_limiter=LIMITER_VAN_LEER)
+    opts.update(kw)
+    p = Params(nx=n, ny=n, nz=n, precision=precision, mhd=True, cfl=cfl, **opts)
     rng = np.random.default_rng(seed)
     v = _solenoidal_field(n, rng, 2.0, 8.0, -2.0)
     cs = math.sqrt(p.gamma * 1.0 / 1.0)
@@ -159,9 +161,9 @@ def blast(n=192, precision=FP64, p_in=10.0, p_out=0.1, radius=0.1, cfl=0.4, b_sc
     (cell-centre test).  HLLD, minmod, flux-CD."""
     bc = dict(bc_left=BC_OUTFLOW, bc_right=BC_OUTFLOW, bc_bottom=BC_OUTFLOW,
               bc_top=BC_OUTFLOW, bc_out=BC_OUTFLOW, bc_in=BC_OUTFLOW)
+    bc.update(riemann_solver=SOLVER_HLLD, slope_limiter=LIMITER_MINMOD)
     bc.update(kw)
-    p = Params(nx=n, ny=n, nz=n, precision=precision, mhd=True, riemann_solver=SOLVER_HLLD,
-               slope_limiter=LIMITER_MINMOD, cfl=cfl, **bc)
+    p = Params(nx=n, ny=n, nz=n, precision=precision, mhd=True, cfl=cfl, **bc)
     x, y, z = _centered_coords(p)
     r = np.sqrt(x * x + y * y + z * z)
     pr = np.where(r < radius, p_in, p_out)

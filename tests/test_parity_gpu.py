@@ -46,8 +46,8 @@ def _gpu_run(p, u0, steps, n_iter=10, dtprint=1e30):
 
 def _hydro_state(n, seed=7, closed=False, **kw):
     """A smooth random hydro state (neq = 5) on an n^3 box."""
-    p = P.Params(nx=n, ny=n, nz=n, mhd=False, riemann_solver=P.SOLVER_HLLC,
-                 enable_flux_cd=False, cfl=0.3, **kw)
+    kw.setdefault("riemann_solver", P.SOLVER_HLLC)
+    p = P.Params(nx=n, ny=n, nz=n, mhd=False, enable_flux_cd=False, cfl=0.3, **kw)
     if closed:
         p = p.replace(**{k: P.BC_CLOSED for k in
                          ("bc_left", "bc_right", "bc_bottom", "bc_top", "bc_out", "bc_in")})
