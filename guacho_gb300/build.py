@@ -32,6 +32,7 @@ UNITS = {
     # FP32 divide / sqrt through the hardware reciprocal and square-root
     # approximations (FP64 operations are unaffected)
     "gch_fp32.cu": ["-prec-div=false", "-prec-sqrt=false", "-ftz=true"],
+    "gch_kahan.cu": ["-prec-div=false", "-prec-sqrt=false", "-ftz=true"],
     "gch_api.cu": [],
     "gch_batch.cu": [],
 }

@@ -17,7 +17,9 @@ using gch::StepScalars;
 namespace {
 
 const EngineOps& engine(const gch_domain* d) {
-  return d->mode == GCH_FP64 ? gch::kEngineFP64 : gch::kEngineMixed;
+  if (d->mode == GCH_FP64) return gch::kEngineFP64;
+  if (d->mode == GCH_FP32_KAHAN) return gch::kEngineKahan;
+  return gch::kEngineMixed;
 }
 
 int cuda_ok(cudaError_t e) { return e == cudaSuccess ? GCH_OK : GCH_ERR_CUDA; }
@@ -95,7 +97,9 @@ void gch_params_default(gch_params_t* p, int nx, int ny, int nz) {
 
 int gch_params_check(const gch_params_t* p) {
   if (!p || p->abi_version != GCH_ABI_VERSION) return GCH_ERR_PARAM;
-  if (p->precision != GCH_FP64 && p->precision != GCH_FP32_MIXED) return GCH_ERR_PARAM;
+  if (p->precision != GCH_FP64 && p->precision != GCH_FP32_MIXED &&
+      p->precision != GCH_FP32_KAHAN)
+    return GCH_ERR_PARAM;
   if (p->nx < 1 || p->ny < 1 || p->nz < 1) return GCH_ERR_PARAM;
   if (p->neq != 5 && p->neq != 8) return GCH_ERR_PARAM;
   const bool bfield = p->neq == 8;

@@ -40,6 +40,43 @@ struct PolMixed {
   static constexpr int kMinBlocks = 3;
 };
 
+struct PolKahan {
+  using TU = float2;  // compensated (hi, lo) FP32 pair
+  using TS = float;
+  using TC = float;
+  static constexpr int kMode = GCH_FP32_KAHAN;
+  static constexpr int kMinBlocks = 3;
+};
+
+// Value conversions across the stored types: double, float, and the
+// compensated pair (hi, lo) whose value is hi + lo.
+__host__ __device__ __forceinline__ double to_d(double x) { return x; }
+__host__ __device__ __forceinline__ double to_d(float x) { return (double)x; }
+__host__ __device__ __forceinline__ double to_d(float2 x) { return (double)x.x + (double)x.y; }
+template <class T>
+__host__ __device__ __forceinline__ T from_d(double v);
+template <>
+__host__ __device__ __forceinline__ double from_d<double>(double v) { return v; }
+template <>
+__host__ __device__ __forceinline__ float from_d<float>(double v) { return (float)v; }
+template <>
+__host__ __device__ __forceinline__ float2 from_d<float2>(double v) {
+  const float h = (float)v;
+  return make_float2(h, (float)(v - (double)h));
+}
+__host__ __device__ __forceinline__ double neg(double x) { return -x; }
+__host__ __device__ __forceinline__ float neg(float x) { return -x; }
+__host__ __device__ __forceinline__ float2 neg(float2 x) { return make_float2(-x.x, -x.y); }
+// store an accumulator value (double or pair) in a stage array type
+template <class TD>
+__device__ __forceinline__ TD store_as(double v) { return from_d<TD>(v); }
+template <class TD>
+__device__ __forceinline__ TD store_as(float2 v);
+template <>
+__device__ __forceinline__ float store_as<float>(float2 v) { return v.x + v.y; }
+template <>
+__device__ __forceinline__ float2 store_as<float2>(float2 v) { return v; }
+
 // ---------------------------------------------------------------------------
 // Kernel parameter block (by value; tables live in device memory).
 struct KParams {
@@ -221,6 +258,15 @@ __device__ __forceinline__ T average(int lim, T a, T b) {
       return s * tmax_(tmax_(T(0), av1), av2);
   }
   return T(0);
+}
+
+// The limiter as a compile-time choice for the common ones; kLimRuntime
+// dispatches on the runtime value.
+constexpr int kLimRuntime = -99;
+template <int LIM, class T>
+__device__ __forceinline__ T average_t(int lim, T a, T b) {
+  if constexpr (LIM == kLimRuntime) return average(lim, a, b);
+  else return average(LIM, a, b);
 }
 
 // ---------------------------------------------------------------------------

@@ -65,6 +65,7 @@ struct EngineOps {
 
 extern const EngineOps kEngineFP64;
 extern const EngineOps kEngineMixed;
+extern const EngineOps kEngineKahan;
 
 }  // namespace gch
 

@@ -20,8 +20,8 @@ struct Engine {
   }
 
   // ---- stage kernels, dispatched on solver and neq ----------------------
-  template <int SOLVER, int NEQ, int STAGE, bool PRIM_IN>
-  static void flux_launch(gch_domain* d, const void* src, void* dst) {
+  template <int SOLVER, int NEQ, int STAGE, bool PRIM_IN, int LIM>
+  static void flux_launch_lim(gch_domain* d, const void* src, void* dst) {
     const KParams& p = d->kp;
     dim3 grid((p.nx + TX - 1) / TX, (p.ny + TY - 1) / TY, (p.nz + d->kz - 1) / d->kz);
     dim3 block(TX, TY);
@@ -31,12 +31,25 @@ struct Engine {
     constexpr size_t smem = sizeof(FluxSmem<TC, NEQ, STAGE>);
     static bool attr = false;  // once per instantiation
     if (!attr) {
-      cudaFuncSetAttribute(k_flux<Pol, SOLVER, NEQ, STAGE, PRIM_IN>,
+      cudaFuncSetAttribute(k_flux<Pol, SOLVER, NEQ, STAGE, PRIM_IN, LIM>,
                            cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
       attr = true;
     }
-    k_flux<Pol, SOLVER, NEQ, STAGE, PRIM_IN><<<grid, block, smem, d->stream>>>(
+    k_flux<Pol, SOLVER, NEQ, STAGE, PRIM_IN, LIM><<<grid, block, smem, d->stream>>>(
         p, (const TIn*)src, (const TU*)d->u, (TD*)dst, (TS*)d->E, (TS*)d->s678, d->sc, d->kz);
+  }
+
+  // stage 1 has no limiter; stage 2 specialises minmod and van Leer
+  template <int SOLVER, int NEQ, int STAGE, bool PRIM_IN>
+  static void flux_launch(gch_domain* d, const void* src, void* dst) {
+    if (STAGE == 1)
+      flux_launch_lim<SOLVER, NEQ, STAGE, PRIM_IN, kLimRuntime>(d, src, dst);
+    else if (d->kp.limiter == GCH_LIMITER_MINMOD)
+      flux_launch_lim<SOLVER, NEQ, STAGE, PRIM_IN, GCH_LIMITER_MINMOD>(d, src, dst);
+    else if (d->kp.limiter == GCH_LIMITER_VAN_LEER)
+      flux_launch_lim<SOLVER, NEQ, STAGE, PRIM_IN, GCH_LIMITER_VAN_LEER>(d, src, dst);
+    else
+      flux_launch_lim<SOLVER, NEQ, STAGE, PRIM_IN, kLimRuntime>(d, src, dst);
   }
 
   template <int STAGE, bool PRIM_IN>

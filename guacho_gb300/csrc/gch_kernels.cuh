@@ -38,7 +38,7 @@ struct Src {
                                         typename Pol::TS>::type;
   __device__ __forceinline__ static void load(const KParams& p, const TIn* src, long long idx,
                                               TC* prim, unsigned& pfl) {
-    if (PRIM_IN)
+    if constexpr (PRIM_IN)
       Ops<Pol>::template load_stored_prim<NEQ>(p, src, idx, prim);
     else
       Ops<Pol>::template load_prim<NEQ>(p, src, idx, prim, pfl);
@@ -72,7 +72,7 @@ struct FluxSmem {
 // Column state (the next planes, z slopes, z fluxes) lives in shared
 // memory slots owned by one thread, which keeps registers for the solver.
 // Fluxes are never written to global memory.
-template <class Pol, int SOLVER, int NEQ, int STAGE, bool PRIM_IN>
+template <class Pol, int SOLVER, int NEQ, int STAGE, bool PRIM_IN, int LIM>
 __global__ void __launch_bounds__(NT, Pol::kMinBlocks)
 k_flux(KParams p, const typename Src<Pol, NEQ, STAGE, PRIM_IN>::TIn* __restrict__ src,
        const typename Pol::TU* u,
@@ -144,7 +144,7 @@ k_flux(KParams p, const typename Src<Pol, NEQ, STAGE, PRIM_IN>::TIn* __restrict_
       if (NEQ >= 8) bzm = b[7];
 #pragma unroll
       for (int q = 0; q < NEQ; ++q) {
-        const TC sm1 = average(lim, b[q] - a[q], c[q] - b[q]);
+        const TC sm1 = average_t<LIM>(lim, b[q] - a[q], c[q] - b[q]);
         sF[q][ty][tx] = b[q] + sm1 * TC(0.5);
         sQ[2][q][ty][tx] = b[q];
         sQ[0][q][ty][tx] = c[q];
@@ -152,7 +152,7 @@ k_flux(KParams p, const typename Src<Pol, NEQ, STAGE, PRIM_IN>::TIn* __restrict_
       S::load(p, src, gidx(axc, ayc, kb + 1 + NG), a, pfl);  // a = p(kb+1)
 #pragma unroll
       for (int q = 0; q < NEQ; ++q) {
-        const TC s0 = average(lim, c[q] - b[q], a[q] - c[q]);
+        const TC s0 = average_t<LIM>(lim, c[q] - b[q], a[q] - c[q]);
         sG[q][ty][tx] = c[q] - s0 * TC(0.5);
         sQ[1][q][ty][tx] = a[q];
       }
@@ -247,7 +247,7 @@ k_flux(KParams p, const typename Src<Pol, NEQ, STAGE, PRIM_IN>::TIn* __restrict_
             l[q] = sP[s][ty + H][tx + H];
             r[q] = sQ[0][s][ty][tx];
             const TC dl = l[q] - ll, dm = r[q] - l[q], dr = rr - r[q];
-            const TC al = average(lim, dl, dm), ar = average(lim, dm, dr);
+            const TC al = average_t<LIM>(lim, dl, dm), ar = average_t<LIM>(lim, dm, dr);
             l[q] = l[q] + al * TC(0.5);
             r[q] = r[q] - ar * TC(0.5);
           }
@@ -261,7 +261,7 @@ k_flux(KParams p, const typename Src<Pol, NEQ, STAGE, PRIM_IN>::TIn* __restrict_
           if (STAGE == 2) {
             const TC ll = sP[q][cy][cl - 1], rr = sP[q][cy][cl + 2];
             const TC dl = l[q] - ll, dm = r[q] - l[q], dr = rr - r[q];
-            const TC al = average(lim, dl, dm), ar = average(lim, dm, dr);
+            const TC al = average_t<LIM>(lim, dl, dm), ar = average_t<LIM>(lim, dm, dr);
             l[q] = l[q] + al * TC(0.5);
             r[q] = r[q] - ar * TC(0.5);
           }
@@ -276,7 +276,7 @@ k_flux(KParams p, const typename Src<Pol, NEQ, STAGE, PRIM_IN>::TIn* __restrict_
           if (STAGE == 2) {
             const TC ll = sP[s][cl - 1][cx], rr = sP[s][cl + 2][cx];
             const TC dl = l[q] - ll, dm = r[q] - l[q], dr = rr - r[q];
-            const TC al = average(lim, dl, dm), ar = average(lim, dm, dr);
+            const TC al = average_t<LIM>(lim, dl, dm), ar = average_t<LIM>(lim, dm, dr);
             l[q] = l[q] + al * TC(0.5);
             r[q] = r[q] - ar * TC(0.5);
           }
@@ -347,11 +347,11 @@ k_flux(KParams p, const typename Src<Pol, NEQ, STAGE, PRIM_IN>::TIn* __restrict_
 #pragma unroll
       for (int q = 0; q < NEQ; ++q) {
         if (q < nupd) {
-          double unew = Ops<Pol>::update((double)u[q * p.fs + c], dtdx, dtdy, dtdz,
-                                         sF[q][ty][tx], sF[q][ty][tx + 1], sG[q][ty][tx],
-                                         sG[q][ty + 1][tx], sH[hp][q][ty][tx], sH[hn][q][ty][tx]);
-          if (src_terms) unew = unew + dt * (double)sv[q];
-          dst[q * p.fs + c] = (TD)unew;
+          auto unew = Ops<Pol>::update(Ops<Pol>::ld(u[q * p.fs + c]), dtdx, dtdy, dtdz,
+                                       sF[q][ty][tx], sF[q][ty][tx + 1], sG[q][ty][tx],
+                                       sG[q][ty + 1][tx], sH[hp][q][ty][tx], sH[hn][q][ty][tx]);
+          if (src_terms) unew = Ops<Pol>::add(unew, dt * (double)sv[q]);
+          dst[q * p.fs + c] = store_as<TD>(unew);
         }
       }
       if (ct) {
@@ -409,23 +409,23 @@ k_ct(KParams p, const typename Pol::TU* u,
     return v;
   };
   const long long c = cell_index(p, ax, ay, az);
-  const double u6 = (double)u[5 * p.fs + c];
-  const double u7 = (double)u[6 * p.fs + c];
-  const double u8 = (double)u[7 * p.fs + c];
-  double b6 = Ops<Pol>::ct(u6, hy, e_at(2, ax, ay - 1, az), e_at(2, ax, ay + 1, az), hz,
+  const auto u6 = Ops<Pol>::ld(u[5 * p.fs + c]);
+  const auto u7 = Ops<Pol>::ld(u[6 * p.fs + c]);
+  const auto u8 = Ops<Pol>::ld(u[7 * p.fs + c]);
+  auto b6 = Ops<Pol>::ct(u6, hy, e_at(2, ax, ay - 1, az), e_at(2, ax, ay + 1, az), hz,
                            e_at(1, ax, ay, az - 1), e_at(1, ax, ay, az + 1), true);
-  double b7 = Ops<Pol>::ct(u7, hx, e_at(2, ax - 1, ay, az), e_at(2, ax + 1, ay, az), hz,
+  auto b7 = Ops<Pol>::ct(u7, hx, e_at(2, ax - 1, ay, az), e_at(2, ax + 1, ay, az), hz,
                            e_at(0, ax, ay, az - 1), e_at(0, ax, ay, az + 1), false);
-  double b8 = Ops<Pol>::ct(u8, hx, e_at(1, ax - 1, ay, az), e_at(1, ax + 1, ay, az), hy,
+  auto b8 = Ops<Pol>::ct(u8, hx, e_at(1, ax - 1, ay, az), e_at(1, ax + 1, ay, az), hy,
                            e_at(0, ax, ay - 1, az), e_at(0, ax, ay + 1, az), true);
   if (p.eight_wave) {
-    b6 = b6 + dt * (double)s678[c];
-    b7 = b7 + dt * (double)s678[p.fs + c];
-    b8 = b8 + dt * (double)s678[2 * p.fs + c];
+    b6 = Ops<Pol>::add(b6, dt * (double)s678[c]);
+    b7 = Ops<Pol>::add(b7, dt * (double)s678[p.fs + c]);
+    b8 = Ops<Pol>::add(b8, dt * (double)s678[2 * p.fs + c]);
   }
-  dst[5 * p.fs + c] = (TD)b6;
-  dst[6 * p.fs + c] = (TD)b7;
-  dst[7 * p.fs + c] = (TD)b8;
+  dst[5 * p.fs + c] = store_as<TD>(b6);
+  dst[6 * p.fs + c] = store_as<TD>(b7);
+  dst[7 * p.fs + c] = store_as<TD>(b8);
 }
 
 // ---------------------------------------------------------------------------
@@ -456,7 +456,7 @@ __global__ void k_ghost(KParams p, T* a, int neq, int axis, int layers, const St
   const long long di = cell_index(p, dx, dy, dz), si = cell_index(p, sx, sy, sz);
   for (int q = 0; q < neq; ++q) {
     T v = a[q * p.fs + si];
-    if (flip && q == axis + 1) v = -v;
+    if (flip && q == axis + 1) v = neg(v);
     a[q * p.fs + di] = v;
   }
 }
@@ -508,10 +508,10 @@ __global__ void k_user_bc(KParams p, T* a, int neq, const StepScalars* sc) {
     const double velz = sp.vorb[2] + sp.vwind * zs / rads;
     const double dens = sp.dens;
     const long long c = cell_index(p, ax, ay, az);
-    a[c] = (T)dens;
-    a[p.fs + c] = (T)(dens * velx);
-    a[2 * p.fs + c] = (T)(dens * vely);
-    a[3 * p.fs + c] = (T)(dens * velz);
+    a[c] = from_d<T>(dens);
+    a[p.fs + c] = from_d<T>(dens * velx);
+    a[2 * p.fs + c] = from_d<T>(dens * vely);
+    a[3 * p.fs + c] = from_d<T>(dens * velz);
     double b2 = 0.0;
     if (neq >= 8) {
       const double rr = sp.radius / rads;
@@ -519,14 +519,14 @@ __global__ void k_user_bc(KParams p, T* a, int neq, const StepScalars* sc) {
       const double b5 = 3.0 * ys * xs * cpi;
       const double b6 = (3.0 * (ys * ys) - rads * rads) * cpi;
       const double b7 = 3.0 * ys * zs * cpi;
-      a[5 * p.fs + c] = (T)b5;
-      a[6 * p.fs + c] = (T)b6;
-      a[7 * p.fs + c] = (T)b7;
+      a[5 * p.fs + c] = from_d<T>(b5);
+      a[6 * p.fs + c] = from_d<T>(b6);
+      a[7 * p.fs + c] = from_d<T>(b7);
       b2 = b5 * b5 + b6 * b6 + b7 * b7;
     }
     double e = 0.5 * dens * (velx * velx + vely * vely + velz * velz) + p.cv * dens * sp.tfac;
     if (p.mhd) e = e + 0.5 * b2;
-    a[4 * p.fs + c] = (T)e;
+    a[4 * p.fs + c] = from_d<T>(e);
   }
 }
 
@@ -549,7 +549,7 @@ k_cfl(KParams p, const typename std::conditional<PRIM_IN, typename Pol::TS, type
     TC pr[NEQ];
     TC cand[3];
     unsigned pfl = 0;
-    if (PRIM_IN)
+    if constexpr (PRIM_IN)
       Ops<Pol>::template load_stored_prim<NEQ>(p, src, c, pr);
     else
       Ops<Pol>::template load_prim<NEQ>(p, src, c, pr, pfl);
@@ -644,7 +644,7 @@ __global__ void k_cool(KParams p, typename Pol::TU* u, typename Pol::TS* primit,
   const long long c = cell_index(p, ci + NG, cj + NG, ck + NG);
   double uu[NEQ], pp[NEQ];
 #pragma unroll
-  for (int q = 0; q < NEQ; ++q) uu[q] = (double)u[q * p.fs + c];
+  for (int q = 0; q < NEQ; ++q) uu[q] = to_d(u[q * p.fs + c]);
   unsigned pfl = 0;
   double T;
   Ops<PolFP64>::u2prim<NEQ>(p, uu, pp, pfl, &T);
@@ -663,7 +663,7 @@ __global__ void k_cool(KParams p, typename Pol::TU* u, typename Pol::TS* primit,
     const double dens = pp[0];
     const double ce = (aloss * (dens * dens)) / (Eth0 * p.Psc);
     pp[4] = pp[4] * exp(-ce * (sc->dt * p.tsc));
-    u[4 * p.fs + c] = (typename Pol::TU)(uu[4] - Eth0 + p.cv * pp[4]);
+    u[4 * p.fs + c] = from_d<typename Pol::TU>(uu[4] - Eth0 + p.cv * pp[4]);
   }
 #pragma unroll
   for (int q = 0; q < NEQ; ++q) primit[q * p.fs + c] = (typename Pol::TS)pp[q];
@@ -683,12 +683,12 @@ __global__ void k_visc(KParams p, typename Pol::TU* u, const typename Pol::TU* w
     const bool inside = x >= NG && x < NG + p.nx && y >= NG && y < NG + p.ny && z >= NG &&
                         z < NG + p.nz;
     const long long c = cell_index(p, x, y, z);
-    return inside ? (double)w[q * p.fs + c] : (double)up[q * p.fs + c];
+    return inside ? to_d(w[q * p.fs + c]) : to_d(up[q * p.fs + c]);
   };
   const long long c = cell_index(p, ax, ay, az);
   for (int q = 0; q < NEQ; ++q) {
     const double v = val(q, ax, ay, az);
-    u[q * p.fs + c] = (typename Pol::TU)(
+    u[q * p.fs + c] = from_d<typename Pol::TU>(
         v + p.eta * (val(q, ax + 1, ay, az) + val(q, ax - 1, ay, az) + val(q, ax, ay + 1, az) +
                      val(q, ax, ay - 1, az) + val(q, ax, ay, az + 1) + val(q, ax, ay, az - 1) -
                      6.0 * v));
@@ -716,7 +716,7 @@ __global__ void k_calcprim(KParams p, const typename Pol::TU* u, typename Pol::T
   const long long c = cell_index(p, ax, ay, az);
   double uu[NEQ], pp[NEQ];
 #pragma unroll
-  for (int q = 0; q < NEQ; ++q) uu[q] = (double)u[q * p.fs + c];
+  for (int q = 0; q < NEQ; ++q) uu[q] = to_d(u[q * p.fs + c]);
   unsigned pfl = 0;
   Ops<PolFP64>::u2prim<NEQ>(p, uu, pp, pfl);
 #pragma unroll
@@ -734,7 +734,7 @@ __global__ void k_aos_to_soa(KParams p, const double* __restrict__ aos, T* __res
     const int ay = (int)((t / p.NX) % p.NY);
     const int az = (int)(t / ((long long)p.NX * p.NY));
     const long long c = cell_index(p, ax, ay, az);
-    for (int q = 0; q < neq; ++q) soa[q * p.fs + c] = (T)aos[t * neq + q];
+    for (int q = 0; q < neq; ++q) soa[q * p.fs + c] = from_d<T>(aos[t * neq + q]);
   }
 }
 template <class T>
@@ -747,7 +747,7 @@ __global__ void k_soa_to_aos(KParams p, const T* __restrict__ soa, double* __res
     const int ay = (int)((t / p.NX) % p.NY);
     const int az = (int)(t / ((long long)p.NX * p.NY));
     const long long c = cell_index(p, ax, ay, az);
-    for (int q = 0; q < neq; ++q) aos[t * neq + q] = (double)soa[q * p.fs + c];
+    for (int q = 0; q < neq; ++q) aos[t * neq + q] = to_d(soa[q * p.fs + c]);
   }
 }
 // primit (full array, from u) straight into the host layout
@@ -762,7 +762,7 @@ __global__ void k_prim_to_aos(KParams p, const typename Pol::TU* __restrict__ u,
     const int az = (int)(t / ((long long)p.NX * p.NY));
     const long long c = cell_index(p, ax, ay, az);
     double uu[NEQ], pp[NEQ];
-    for (int q = 0; q < NEQ; ++q) uu[q] = (double)u[q * p.fs + c];
+    for (int q = 0; q < NEQ; ++q) uu[q] = to_d(u[q * p.fs + c]);
     unsigned pfl = 0;
     Ops<PolFP64>::u2prim<NEQ>(p, uu, pp, pfl);
     for (int q = 0; q < NEQ; ++q) aos[t * NEQ + q] = pp[q];

@@ -20,6 +20,10 @@ struct Ops;
 template <>
 struct Ops<PolFP64> {
   using TC = double;
+  using R = double;  // accumulator of u updates
+  __device__ __forceinline__ static double ld(double u) { return u; }
+  // up + dt*s (src/hydro_solver.f90:119)
+  __device__ __forceinline__ static double add(double u, double v) { return u + v; }
 
   // src/hydro_core.f90:46-129 u2prim, on a cell of any stored type
   template <int NEQ, class TIn>
@@ -115,10 +119,54 @@ __device__ __forceinline__ DF df_sumsq(float a, float b, float c) {
   return df_add(df_add(two_prod(a, a), two_prod(b, b)), two_prod(c, c));
 }
 
+// u2prim from exact FP32 inputs with the pressure recovery in compensated
+// FP32: m.m and B.B are formed exactly with FMA two-products, KE = m.m/rho is
+// a pair quotient, and E - KE/2 - B.B/2 is taken in double-float, matching an
+// FP64 evaluation to ~1e-13 relative of KE + B^2/2.
+template <int NEQ>
+__device__ __forceinline__ void prim_from_f32(const KParams& p, const float* uu, float* prim,
+                                              unsigned& pfl) {
+  const float r = tmax_(uu[0], 1e-15f);
+  float ir = 1.0f / r;
+  ir = ir * fmaf(-r, ir, 2.0f);
+  const DF m2 = df_sumsq(uu[1], uu[2], uu[3]);
+  const float q = m2.hi * ir;
+  const float rem = fmaf(-q, r, m2.hi) + m2.lo;
+  DF kb = fast_two_sum(q, rem * ir);
+  if (NEQ >= 8 && p.mhd) kb = df_add(kb, df_sumsq(uu[5], uu[6], uu[7]));
+  const DF d = two_sum(uu[4], -0.5f * kb.hi);
+  float pr = (d.hi + (d.lo - 0.5f * kb.lo)) * (float)p.inv_cv;
+  if (!(pr >= 1e-16f)) ++pfl;
+  pr = tmax_(pr, 1e-16f);
+  if (p.eos == GCH_EOS_SINGLE_SPECIE) {
+    const float t = tmax_(1.0f, (pr * ir) * (float)p.Tempsc);
+    pr = r * t / (float)p.Tempsc;
+  }
+  prim[0] = r;
+  prim[1] = uu[1] * ir;
+  prim[2] = uu[2] * ir;
+  prim[3] = uu[3] * ir;
+  prim[4] = pr;
+  if (NEQ >= 8) {
+    prim[5] = uu[5];
+    prim[6] = uu[6];
+    prim[7] = uu[7];
+  }
+}
+
+// (h + l)^2 of a compensated pair, as a pair (the l^2 term is below 2^-48)
+__device__ __forceinline__ DF df_sq(float2 x) {
+  const DF p = two_prod(x.x, x.x);
+  return fast_two_sum(p.hi, p.lo + 2.0f * x.x * x.y);
+}
+
 // ---------------------------------------------------------------------------
 template <>
 struct Ops<PolMixed> {
   using TC = float;
+  using R = double;
+  __device__ __forceinline__ static double ld(double u) { return u; }
+  __device__ __forceinline__ static double add(double u, double v) { return u + v; }
 
   // u2prim with the pressure recovery p = (E - m.m/(2 rho) - B.B/2)/cv
   // done at FP64-level accuracy:
@@ -165,34 +213,7 @@ struct Ops<PolMixed> {
       float uu[NEQ];
 #pragma unroll
       for (int q = 0; q < NEQ; ++q) uu[q] = (float)src[q * p.fs + idx];
-      const float r = tmax_(uu[0], 1e-15f);
-      float ir = 1.0f / r;
-      ir = ir * fmaf(-r, ir, 2.0f);
-      // KE = (m.m)/r as a compensated pair
-      const DF m2 = df_sumsq(uu[1], uu[2], uu[3]);
-      const float q = m2.hi * ir;
-      const float rem = fmaf(-q, r, m2.hi) + m2.lo;
-      DF kb = fast_two_sum(q, rem * ir);
-      if (NEQ >= 8 && p.mhd) kb = df_add(kb, df_sumsq(uu[5], uu[6], uu[7]));
-      // E - kb/2 (halving is exact)
-      const DF d = two_sum(uu[4], -0.5f * kb.hi);
-      float pr = (d.hi + (d.lo - 0.5f * kb.lo)) * (float)p.inv_cv;
-      if (!(pr >= 1e-16f)) ++pfl;
-      pr = tmax_(pr, 1e-16f);
-      if (p.eos == GCH_EOS_SINGLE_SPECIE) {
-        const float t = tmax_(1.0f, (pr * ir) * (float)p.Tempsc);
-        pr = r * t / (float)p.Tempsc;
-      }
-      prim[0] = r;
-      prim[1] = uu[1] * ir;
-      prim[2] = uu[2] * ir;
-      prim[3] = uu[3] * ir;
-      prim[4] = pr;
-      if (NEQ >= 8) {
-        prim[5] = uu[5];
-        prim[6] = uu[6];
-        prim[7] = uu[7];
-      }
+      prim_from_f32<NEQ>(p, uu, prim, pfl);
     }
   }
 
@@ -215,6 +236,89 @@ struct Ops<PolMixed> {
                                               float hdtb, float b0, float b1, bool first_minus) {
     const float d = hdta * (a1 - a0) - hdtb * (b1 - b0);
     return first_minus ? u - (double)d : u + (double)d;
+  }
+};
+
+
+// ---------------------------------------------------------------------------
+// FP32 with Kahan-compensated accumulation: u is a (hi, lo) FP32 pair per
+// value; every per-cell operation is FP32 (no FP64 instruction on the step
+// path), the pressure recovery is double-float.
+template <>
+struct Ops<PolKahan> {
+  using TC = float;
+  using R = float2;
+  __device__ __forceinline__ static float2 ld(float2 u) { return u; }
+  // pair + v: two-sum of the high parts, low parts folded in, renormalised
+  __device__ __forceinline__ static float2 addf(float2 u, float v) {
+    const DF s = two_sum(u.x, v);
+    const DF r = fast_two_sum(s.hi, s.lo + u.y);
+    return make_float2(r.hi, r.lo);
+  }
+  __device__ __forceinline__ static float2 add(float2 u, double v) { return addf(u, (float)v); }
+
+  template <int NEQ, class TIn>
+  __device__ __forceinline__ static void load_prim(const KParams& p, const TIn* src,
+                                                   long long idx, TC* prim, unsigned& pfl) {
+    if constexpr (sizeof(TIn) == 8) {
+      float2 uu[NEQ];
+#pragma unroll
+      for (int q = 0; q < NEQ; ++q) uu[q] = src[q * p.fs + idx];
+      const float rh = tmax_(uu[0].x + uu[0].y, 1e-15f);
+      const float rl = uu[0].x + uu[0].y == rh ? (uu[0].y - (rh - uu[0].x)) : 0.0f;
+      float ir = 1.0f / rh;
+      ir = ir * fmaf(-rh, ir, 2.0f);
+      // m.m / rho as a pair quotient of pair operands
+      const DF m2 = df_add(df_add(df_sq(uu[1]), df_sq(uu[2])), df_sq(uu[3]));
+      const float q = m2.hi * ir;
+      const float rem = (fmaf(-q, rh, m2.hi) - q * rl) + m2.lo;
+      DF kb = fast_two_sum(q, rem * ir);
+      if (NEQ >= 8 && p.mhd)
+        kb = df_add(kb, df_add(df_add(df_sq(uu[5]), df_sq(uu[6])), df_sq(uu[7])));
+      const DF d = two_sum(uu[4].x, -0.5f * kb.hi);
+      float pr = (d.hi + ((d.lo + uu[4].y) - 0.5f * kb.lo)) * (float)p.inv_cv;
+      if (!(pr >= 1e-16f)) ++pfl;
+      pr = tmax_(pr, 1e-16f);
+      if (p.eos == GCH_EOS_SINGLE_SPECIE) {
+        const float t = tmax_(1.0f, (pr * ir) * (float)p.Tempsc);
+        pr = rh * t / (float)p.Tempsc;
+      }
+      prim[0] = rh;
+      prim[1] = uu[1].x * ir;
+      prim[2] = uu[2].x * ir;
+      prim[3] = uu[3].x * ir;
+      prim[4] = pr;
+      if (NEQ >= 8) {
+        prim[5] = uu[5].x;
+        prim[6] = uu[6].x;
+        prim[7] = uu[7].x;
+      }
+    } else {
+      float uu[NEQ];
+#pragma unroll
+      for (int q = 0; q < NEQ; ++q) uu[q] = (float)src[q * p.fs + idx];
+      prim_from_f32<NEQ>(p, uu, prim, pfl);
+    }
+  }
+
+  template <int NEQ, class TIn>
+  __device__ __forceinline__ static void load_stored_prim(const KParams& p, const TIn* src,
+                                                          long long idx, TC* prim) {
+#pragma unroll
+    for (int q = 0; q < NEQ; ++q) prim[q] = (float)src[q * p.fs + idx];
+  }
+
+  __device__ __forceinline__ static float2 update(float2 u, float dtdx, float dtdy, float dtdz,
+                                                  float fl, float fr, float gl, float gr,
+                                                  float hl, float hr) {
+    const float d = dtdx * (fr - fl) + dtdy * (gr - gl) + dtdz * (hr - hl);
+    return addf(u, -d);
+  }
+
+  __device__ __forceinline__ static float2 ct(float2 u, float hdta, float a0, float a1,
+                                              float hdtb, float b0, float b1, bool first_minus) {
+    const float d = hdta * (a1 - a0) - hdtb * (b1 - b0);
+    return addf(u, first_minus ? -d : d);
   }
 };
 

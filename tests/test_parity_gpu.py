@@ -158,13 +158,16 @@ def _prims(p, u):
     return out
 
 
+@pytest.mark.parametrize("prec", [P.FP32_MIXED, P.FP32_KAHAN])
 @pytest.mark.parametrize("name", ["ot_hlld_minmod", "blast_hlld_outflow", "turbulence_16",
-                                  "hydro_hllc_periodic", "ot_hlle_vanleer"])
-def test_fp32_mixed_l1(gpu_lib, name):
+                                  "hydro_hllc_periodic", "ot_hlle_vanleer", "ot_limiter_4",
+                                  "hydro_hllc_closed", "ot_eta", "ot_eight_wave"])
+def test_fp32_l1(gpu_lib, name, prec):
+    """FP32-mixed (FP64 u) and FP32 + Kahan pairs against the FP64 oracle."""
     p, u0 = CASES[name]()
     steps = 20
     ur, dr = _oracle_run(p, u0, steps)
-    ug, dg = _gpu_run(p.replace(precision=P.FP32_MIXED), u0, steps)
+    ug, dg = _gpu_run(p.replace(precision=prec), u0, steps)
     np.testing.assert_allclose(dg, dr, rtol=1e-5)
     fr, fg = _prims(p, ur), _prims(p, ug)
     for k in ("rho", "p", "Bx", "By", "Bz"):
@@ -218,18 +221,20 @@ def test_step_host_matches_device(gpu_lib):
         assert np.array_equal(interior(uh), interior(b.download()))
 
 
-def test_deterministic(gpu_lib):
+@pytest.mark.parametrize("prec", [P.FP64, P.FP32_MIXED, P.FP32_KAHAN])
+def test_deterministic(gpu_lib, prec):
     p, u0 = problems.turbulence(16, seed=9)
-    pm = p.replace(precision=P.FP32_MIXED)
+    pm = p.replace(precision=prec)
     a, _ = _gpu_run(pm, u0, 5)
     b, _ = _gpu_run(pm, u0, 5)
     assert np.array_equal(a, b)
 
 
-def test_divb_roundoff_mixed(gpu_lib):
+@pytest.mark.parametrize("prec", [P.FP32_MIXED, P.FP32_KAHAN])
+def test_divb_roundoff_mixed(gpu_lib, prec):
     from guacho_gb300.domain import Domain
     p, u0 = problems.turbulence(32, seed=2)
-    with Domain(p.replace(precision=P.FP32_MIXED)) as d:
+    with Domain(p.replace(precision=prec)) as d:
         d.init(u0)
         d.run(1e30, 1e30, max_steps=20)
         u = d.download()
