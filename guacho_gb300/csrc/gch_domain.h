@@ -31,6 +31,11 @@ struct gch_domain {
   double* stage = nullptr;      // device staging buffer, host layout (FP64 AoS)
   size_t ncell_host = 0;        // NX*NY*NZ
   int kz = 8;                   // z planes per block of the stage kernels
+  // The next step's CFL reduction runs in the stage-2 CT epilogue when
+  // nothing modifies u after it (no viscosity, table cooling or user
+  // spheres); cfl_ready says the device min is current for get_timestep.
+  bool cfl_fused = false;
+  bool cfl_ready = false;
   int launches = 0;             // kernel launches of the last tstep
   // CUDA graph of one device-resident step (get_timestep + tstep + loop tail)
   cudaGraphExec_t graph = nullptr;
@@ -61,6 +66,7 @@ struct EngineOps {
   int (*download_u)(gch_domain*);     // u -> stage
   int (*download_prim)(gch_domain*);  // primit -> stage
   int (*loopfin)(gch_domain*);        // device time-loop tail
+  int (*cfl)(gch_domain*);            // CFL min of the current u only
 };
 
 extern const EngineOps kEngineFP64;

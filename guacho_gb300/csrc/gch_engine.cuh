@@ -86,7 +86,8 @@ struct Engine {
   }
 
   // ---- get_timestep --------------------------------------------------------
-  static int get_dt(gch_domain* d) {
+  // the CFL min over the interior into the device scalar block (k_cfl)
+  static int cfl(gch_domain* d) {
     const KParams& p = d->kp;
     dim3 grid = cell_grid(p), block(32, 8);
     if (d->prim_in) {
@@ -96,9 +97,26 @@ struct Engine {
       if (p.neq == 8) k_cfl<Pol, 8, false><<<grid, block, 0, d->stream>>>(p, (const TU*)d->u, d->sc);
       else k_cfl<Pol, 5, false><<<grid, block, 0, d->stream>>>(p, (const TU*)d->u, d->sc);
     }
-    gch_mark(d, "k_cfl");
+    d->cfl_ready = true;
+    return cuda_status(cudaGetLastError());
+  }
+
+  static int get_dt(gch_domain* d) {
+    const KParams& p = d->kp;
+    dim3 grid = cell_grid(p), block(32, 8);
+    if (d->cfl_fused && d->cfl_ready) {
+      // the min over cells was accumulated by the last step's k_ct<2>
+    } else if (d->prim_in) {
+      if (p.neq == 8) k_cfl<Pol, 8, true><<<grid, block, 0, d->stream>>>(p, (const TS*)d->primit, d->sc);
+      else k_cfl<Pol, 5, true><<<grid, block, 0, d->stream>>>(p, (const TS*)d->primit, d->sc);
+    } else {
+      if (p.neq == 8) k_cfl<Pol, 8, false><<<grid, block, 0, d->stream>>>(p, (const TU*)d->u, d->sc);
+      else k_cfl<Pol, 5, false><<<grid, block, 0, d->stream>>>(p, (const TU*)d->u, d->sc);
+    }
+    if (!(d->cfl_fused && d->cfl_ready)) gch_mark(d, "k_cfl");
     k_dtfin<<<1, 1, 0, d->stream>>>(d->sc, p.cfl, p.dx, p.dy, p.dz);
     gch_mark(d, "k_dtfin");
+    d->cfl_ready = false;  // k_dtfin consumed the min
     return cuda_status(cudaGetLastError());
   }
 
@@ -115,7 +133,7 @@ struct Engine {
     ++d->launches;
     gch_mark(d, "k_flux_stage1");
     if (ct) {
-      k_ct<Pol, 1><<<cgrid, cblock, 0, d->stream>>>(p, (const TU*)d->u, (TS*)d->up,
+      k_ct<Pol, 1, false><<<cgrid, cblock, 0, d->stream>>>(p, (const TU*)d->u, (TS*)d->up,
                                                      (const TS*)d->E, (const TS*)d->s678, d->sc);
       ++d->launches;
       gch_mark(d, "k_ct_stage1");
@@ -128,8 +146,12 @@ struct Engine {
     ++d->launches;
     gch_mark(d, "k_flux_stage2");
     if (ct) {
-      k_ct<Pol, 2><<<cgrid, cblock, 0, d->stream>>>(p, (const TU*)d->u, (TU*)dst2,
-                                                     (const TS*)d->E, (const TS*)d->s678, d->sc);
+      if (d->cfl_fused)
+        k_ct<Pol, 2, true><<<cgrid, cblock, 0, d->stream>>>(p, (const TU*)d->u, (TU*)dst2,
+                                                            (const TS*)d->E, (const TS*)d->s678, d->sc);
+      else
+        k_ct<Pol, 2, false><<<cgrid, cblock, 0, d->stream>>>(p, (const TU*)d->u, (TU*)dst2,
+                                                             (const TS*)d->E, (const TS*)d->s678, d->sc);
       ++d->launches;
       gch_mark(d, "k_ct_stage2");
     }
@@ -155,15 +177,18 @@ struct Engine {
       gch_mark(d, "k_calcprim");
     }
     st |= cuda_status(cudaGetLastError());
+    d->cfl_ready = d->cfl_fused;
     return st;
   }
 
   static int boundaryI(gch_domain* d) {
+    d->cfl_ready = false;
     ghost<TU>(d, (TU*)d->u, 1);
     return cuda_status(cudaGetLastError());
   }
 
   static int calcprim(gch_domain* d) {
+    d->cfl_ready = false;
     if (!d->prim_in) return GCH_OK;  // primitives are formed on the fly
     const KParams& p = d->kp;
     dim3 g((p.NX + 31) / 32, (p.NY + 7) / 8, p.NZ), b(32, 8);
@@ -173,6 +198,7 @@ struct Engine {
   }
 
   static int upload(gch_domain* d) {
+    d->cfl_ready = false;
     k_aos_to_soa<TU><<<1024, 256, 0, d->stream>>>(d->kp, d->stage, (TU*)d->u, d->kp.neq);
     return cuda_status(cudaGetLastError());
   }
@@ -198,7 +224,7 @@ struct Engine {
 
   static constexpr EngineOps ops() {
     return EngineOps{&get_dt, &tstep, &boundaryI, &calcprim,
-                     &upload, &download_u, &download_prim, &loopfin};
+                     &upload, &download_u, &download_prim, &loopfin, &cfl};
   }
 };
 

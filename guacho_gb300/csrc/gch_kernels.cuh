@@ -376,10 +376,58 @@ k_flux(KParams p, const typename Src<Pol, NEQ, STAGE, PRIM_IN>::TIn* __restrict_
   }
   raise_err(&sc->err, err);
 }
+// min(dx/(|vx|+cfx), dy/(|vy|+cfy), dz/(|vz|+cfz)) of one cell into dtp
+template <class TC, int NEQ>
+__device__ __forceinline__ void cfl_candidate(const KParams& p, const TC* pr, double& dtp,
+                                              int& bad) {
+  TC cand[3];
+  if (NEQ >= 8 && p.mhd) {
+    // src/hydro_core.f90:568-581 cfast
+    const TC g = (TC)p.gamma;
+    const TC bx = pr[5], by = pr[6], bz = pr[7];
+    const TC b2 = bx * bx + by * by + bz * bz;
+    const TC a = g * pr[4] + b2;
+    const TC cx = tsqrt(TC(0.5) * (a + tsqrt(a * a - TC(4.0) * g * pr[4] * bx * bx)) / pr[0]);
+    const TC cy = tsqrt(TC(0.5) * (a + tsqrt(a * a - TC(4.0) * g * pr[4] * by * by)) / pr[0]);
+    const TC cz = tsqrt(TC(0.5) * (a + tsqrt(a * a - TC(4.0) * g * pr[4] * bz * bz)) / pr[0]);
+    cand[0] = (TC)p.dx / (tabs(pr[1]) + cx);
+    cand[1] = (TC)p.dy / (tabs(pr[2]) + cy);
+    cand[2] = (TC)p.dz / (tabs(pr[3]) + cz);
+  } else {
+    const TC c0 = csound(p, pr[4], pr[0]);
+    cand[0] = (TC)p.dx / (tabs(pr[1]) + c0);
+    cand[1] = (TC)p.dy / (tabs(pr[2]) + c0);
+    cand[2] = (TC)p.dz / (tabs(pr[3]) + c0);
+  }
+#pragma unroll
+  for (int d = 0; d < 3; ++d) {
+    if (cand[d] == cand[d]) dtp = tmin_(dtp, (double)cand[d]);
+    else bad = 1;
+  }
+}
+
+// Block-wide min of dtp into sc->dtmin_bits; every thread of the block calls.
+__device__ __forceinline__ void cfl_block_reduce(double dtp, int bad, StepScalars* sc) {
+  if (__any_sync(0xffffffffu, bad) && (threadIdx.x & 31) == 0) atomicOr(&sc->err, GCH_ERR_DT);
+  for (int o = 16; o > 0; o >>= 1) dtp = tmin_(dtp, __shfl_xor_sync(0xffffffffu, dtp, o));
+  __shared__ double red[32];
+  const int t = threadIdx.y * blockDim.x + threadIdx.x;
+  const int lane = t & 31, wid = t >> 5;
+  if (lane == 0) red[wid] = dtp;
+  __syncthreads();
+  if (wid == 0) {
+    const int nw = (blockDim.x * blockDim.y) >> 5;
+    double v = lane < nw ? red[lane] : 1e30;
+    for (int o = 16; o > 0; o >>= 1) v = tmin_(v, __shfl_xor_sync(0xffffffffu, v, o));
+    // positive doubles order like their bit patterns
+    if (lane == 0) atomicMin(&sc->dtmin_bits, (unsigned long long)__double_as_longlong(v));
+  }
+}
+
 // ---------------------------------------------------------------------------
 // Constrained transport of B (src/flux_cd_module.f90:311-321) with the E
 // ghost layer of boundaryI_ef (:45-237) applied as an index map.
-template <class Pol, int STAGE>
+template <class Pol, int STAGE, bool CFL>
 __global__ void __launch_bounds__(256)
 k_ct(KParams p, const typename Pol::TU* u,
      typename std::conditional<STAGE == 1, typename Pol::TS, typename Pol::TU>::type* dst,
@@ -390,8 +438,10 @@ k_ct(KParams p, const typename Pol::TU* u,
   const int ci = blockIdx.x * blockDim.x + threadIdx.x;
   const int cj = blockIdx.y * blockDim.y + threadIdx.y;
   const int ck = blockIdx.z;
-  if (ci >= p.nx || cj >= p.ny || !sc->active) return;
-  const int ax = ci + NG, ay = cj + NG, az = ck + NG;
+  if (!sc->active) return;
+  const bool active = ci < p.nx && cj < p.ny;
+  if (!CFL && !active) return;
+  const int ax = min(ci, p.nx - 1) + NG, ay = min(cj, p.ny - 1) + NG, az = ck + NG;
   const double dt = STAGE == 1 ? sc->dt / 2.0 : sc->dt;
   const TC hx = (TC)(0.5 * sc->dtd[STAGE - 1][0]), hy = (TC)(0.5 * sc->dtd[STAGE - 1][1]),
            hz = (TC)(0.5 * sc->dtd[STAGE - 1][2]);
@@ -423,9 +473,31 @@ k_ct(KParams p, const typename Pol::TU* u,
     b7 = Ops<Pol>::add(b7, dt * (double)s678[p.fs + c]);
     b8 = Ops<Pol>::add(b8, dt * (double)s678[2 * p.fs + c]);
   }
-  dst[5 * p.fs + c] = store_as<TD>(b6);
-  dst[6 * p.fs + c] = store_as<TD>(b7);
-  dst[7 * p.fs + c] = store_as<TD>(b8);
+  if (active) {
+    dst[5 * p.fs + c] = store_as<TD>(b6);
+    dst[6 * p.fs + c] = store_as<TD>(b7);
+    dst[7 * p.fs + c] = store_as<TD>(b8);
+  }
+  if constexpr (CFL && STAGE == 2) {
+    // the next step's CFL candidate from the final state of this cell
+    // (same values and arithmetic as k_cfl on u)
+    double dtp = 1e30;
+    int bad = 0;
+    if (active) {
+      typename Ops<Pol>::R uu[8];
+#pragma unroll
+      for (int q = 0; q < 5; ++q) uu[q] = Ops<Pol>::ld(dst[q * p.fs + c]);
+      uu[5] = store_as<typename Pol::TU>(b6);
+      uu[6] = store_as<typename Pol::TU>(b7);
+      uu[7] = store_as<typename Pol::TU>(b8);
+      TC pr[8];
+      unsigned pfl = 0;
+      Ops<Pol>::template prim_vals<8>(p, uu, pr, pfl);
+      cfl_candidate<TC, 8>(p, pr, dtp, bad);
+      if (pfl) atomicAdd(&sc->pfloor, (unsigned long long)pfl);
+    }
+    cfl_block_reduce(dtp, bad, sc);
+  }
 }
 
 // ---------------------------------------------------------------------------
@@ -533,6 +605,7 @@ __global__ void k_user_bc(KParams p, T* a, int neq, const StepScalars* sc) {
 // ---------------------------------------------------------------------------
 // CFL reduction (src/hydro_core.f90:644-675): per-cell candidate, warp
 // shuffle min, one atomicMin per block on the bits of the positive double.
+
 template <class Pol, int NEQ, bool PRIM_IN>
 __global__ void __launch_bounds__(256)
 k_cfl(KParams p, const typename std::conditional<PRIM_IN, typename Pol::TS, typename Pol::TU>::type* src,
@@ -547,53 +620,15 @@ k_cfl(KParams p, const typename std::conditional<PRIM_IN, typename Pol::TS, type
   if (ci < p.nx && cj < p.ny) {
     const long long c = cell_index(p, ci + NG, cj + NG, ck + NG);
     TC pr[NEQ];
-    TC cand[3];
     unsigned pfl = 0;
     if constexpr (PRIM_IN)
       Ops<Pol>::template load_stored_prim<NEQ>(p, src, c, pr);
     else
       Ops<Pol>::template load_prim<NEQ>(p, src, c, pr, pfl);
-    if (NEQ >= 8 && p.mhd) {
-      // src/hydro_core.f90:568-581 cfast
-      const TC g = (TC)p.gamma;
-      const TC bx = pr[5], by = pr[6], bz = pr[7];
-      const TC b2 = bx * bx + by * by + bz * bz;
-      const TC a = g * pr[4] + b2;
-      const TC cx = tsqrt(TC(0.5) * (a + tsqrt(a * a - TC(4.0) * g * pr[4] * bx * bx)) / pr[0]);
-      const TC cy = tsqrt(TC(0.5) * (a + tsqrt(a * a - TC(4.0) * g * pr[4] * by * by)) / pr[0]);
-      const TC cz = tsqrt(TC(0.5) * (a + tsqrt(a * a - TC(4.0) * g * pr[4] * bz * bz)) / pr[0]);
-      cand[0] = (TC)p.dx / (tabs(pr[1]) + cx);
-      cand[1] = (TC)p.dy / (tabs(pr[2]) + cy);
-      cand[2] = (TC)p.dz / (tabs(pr[3]) + cz);
-    } else {
-      const TC c0 = csound(p, pr[4], pr[0]);
-      cand[0] = (TC)p.dx / (tabs(pr[1]) + c0);
-      cand[1] = (TC)p.dy / (tabs(pr[2]) + c0);
-      cand[2] = (TC)p.dz / (tabs(pr[3]) + c0);
-    }
-#pragma unroll
-    for (int d = 0; d < 3; ++d) {
-      if (cand[d] == cand[d]) dtp = tmin_(dtp, (double)cand[d]);
-      else bad = 1;
-    }
+    cfl_candidate<TC, NEQ>(p, pr, dtp, bad);
     if (pfl) atomicAdd(&sc->pfloor, (unsigned long long)pfl);
   }
-  if (__any_sync(0xffffffffu, bad) && (threadIdx.x & 31) == 0) atomicOr(&sc->err, GCH_ERR_DT);
-  for (int o = 16; o > 0; o >>= 1) dtp = tmin_(dtp, __shfl_xor_sync(0xffffffffu, dtp, o));
-  __shared__ double sm[8];
-  const int lane = (threadIdx.y * blockDim.x + threadIdx.x) & 31;
-  const int wid = (threadIdx.y * blockDim.x + threadIdx.x) >> 5;
-  if (lane == 0) sm[wid] = dtp;
-  __syncthreads();
-  if (wid == 0) {
-    const int nw = (blockDim.x * blockDim.y) >> 5;
-    double v = lane < nw ? sm[lane] : 1e30;
-    for (int o = 16; o > 0; o >>= 1) v = tmin_(v, __shfl_xor_sync(0xffffffffu, v, o));
-    if (lane == 0) {
-      // positive doubles order like their bit patterns
-      atomicMin(&sc->dtmin_bits, (unsigned long long)__double_as_longlong(v));
-    }
-  }
+  cfl_block_reduce(dtp, bad, sc);
 }
 
 // get_timestep's scalar tail (src/hydro_core.f90:677-694) and the bookkeeping

@@ -34,6 +34,12 @@ struct Ops<PolFP64> {
     for (int q = 0; q < NEQ; ++q) uu[q] = (double)src[q * p.fs + idx];
     u2prim<NEQ>(p, uu, prim, pfl);
   }
+  // the same from values already in registers
+  template <int NEQ>
+  __device__ __forceinline__ static void prim_vals(const KParams& p, const double* uu, TC* prim,
+                                                   unsigned& pfl) {
+    u2prim<NEQ>(p, uu, prim, pfl);
+  }
 
   template <int NEQ>
   __device__ __forceinline__ static void u2prim(const KParams& p, const double* uu, double* prim,
@@ -184,6 +190,19 @@ struct Ops<PolMixed> {
       double uu[NEQ];
 #pragma unroll
       for (int q = 0; q < NEQ; ++q) uu[q] = (double)src[q * p.fs + idx];
+      prim_vals<NEQ>(p, uu, prim, pfl);
+    } else {
+      float uu[NEQ];
+#pragma unroll
+      for (int q = 0; q < NEQ; ++q) uu[q] = (float)src[q * p.fs + idx];
+      prim_from_f32<NEQ>(p, uu, prim, pfl);
+    }
+  }
+
+  template <int NEQ>
+  __device__ __forceinline__ static void prim_vals(const KParams& p, const double* uu, TC* prim,
+                                                   unsigned& pfl) {
+    {
       const double r = tmax_(uu[0], 1e-15);
       const float irf = 1.0f / (float)r;
       double ir = (double)irf;
@@ -209,11 +228,6 @@ struct Ops<PolMixed> {
         prim[6] = (float)uu[6];
         prim[7] = (float)uu[7];
       }
-    } else {
-      float uu[NEQ];
-#pragma unroll
-      for (int q = 0; q < NEQ; ++q) uu[q] = (float)src[q * p.fs + idx];
-      prim_from_f32<NEQ>(p, uu, prim, pfl);
     }
   }
 
@@ -264,6 +278,19 @@ struct Ops<PolKahan> {
       float2 uu[NEQ];
 #pragma unroll
       for (int q = 0; q < NEQ; ++q) uu[q] = src[q * p.fs + idx];
+      prim_vals<NEQ>(p, uu, prim, pfl);
+    } else {
+      float uu[NEQ];
+#pragma unroll
+      for (int q = 0; q < NEQ; ++q) uu[q] = (float)src[q * p.fs + idx];
+      prim_from_f32<NEQ>(p, uu, prim, pfl);
+    }
+  }
+
+  template <int NEQ>
+  __device__ __forceinline__ static void prim_vals(const KParams& p, const float2* uu, TC* prim,
+                                                   unsigned& pfl) {
+    {
       const float rh = tmax_(uu[0].x + uu[0].y, 1e-15f);
       const float rl = uu[0].x + uu[0].y == rh ? (uu[0].y - (rh - uu[0].x)) : 0.0f;
       float ir = 1.0f / rh;
@@ -293,11 +320,6 @@ struct Ops<PolKahan> {
         prim[6] = uu[6].x;
         prim[7] = uu[7].x;
       }
-    } else {
-      float uu[NEQ];
-#pragma unroll
-      for (int q = 0; q < NEQ; ++q) uu[q] = (float)src[q * p.fs + idx];
-      prim_from_f32<NEQ>(p, uu, prim, pfl);
     }
   }
 

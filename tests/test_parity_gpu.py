@@ -170,9 +170,17 @@ def test_fp32_l1(gpu_lib, name, prec):
     ug, dg = _gpu_run(p.replace(precision=prec), u0, steps)
     np.testing.assert_allclose(dg, dr, rtol=1e-5)
     fr, fg = _prims(p, ur), _prims(p, ug)
+    # relative L1 per field; B components are normalised by the mean |B| so
+    # that a component that is round-off noise in the FP64 run (Bz of a
+    # z-independent vortex) does not divide by ~0
+    bmag = (np.sqrt(fr["Bx"] ** 2 + fr["By"] ** 2 + fr["Bz"] ** 2).mean()
+            if "Bx" in fr else None)
     for k in ("rho", "p", "Bx", "By", "Bz"):
-        if k in fr and np.abs(fr[k]).mean() > 1e-12:
-            assert _rel_l1(fg[k], fr[k]) < 1e-4, (k, _rel_l1(fg[k], fr[k]))
+        if k not in fr:
+            continue
+        den = bmag if k.startswith("B") else np.abs(fr[k]).mean()
+        err = np.abs(fg[k] - fr[k]).mean() / den
+        assert err < 1e-4, (k, err)
 
 
 def test_device_loop_matches_host_loop(gpu_lib):
@@ -202,6 +210,27 @@ def test_device_loop_matches_oracle_main_loop(gpu_lib):
         nd = d.run(0.1, 0.03)
         assert nd == no and d.time == o.time
         assert np.array_equal(interior(d.download()), interior(o.download()))
+
+
+@pytest.mark.parametrize("prec", [P.FP64, P.FP32_KAHAN])
+def test_fused_cfl_matches_separate_reduction(gpu_lib, prec):
+    """The next step's CFL min formed in the stage-2 CT epilogue equals a
+    fresh reduction over u: the same dt comes back either way."""
+    from guacho_gb300.domain import Domain
+    p, u0 = problems.turbulence(24, seed=8)
+    p = p.replace(precision=prec)
+    with Domain(p) as a, Domain(p) as b:
+        a.init(u0)
+        b.init(u0)
+        t = 0.0
+        for it in range(1, 5):
+            dta, _ = a.get_timestep(it, 10, t, 1e30)      # fused after step 1
+            b.upload(b.download())                        # forces a fresh k_cfl
+            dtb, _ = b.get_timestep(it, 10, t, 1e30)
+            assert dta == dtb
+            a.tstep(dta)
+            b.tstep(dtb)
+            t += dta
 
 
 def test_step_host_matches_device(gpu_lib):
