@@ -133,7 +133,7 @@ def peaks() -> dict:
 # algorithmic bytes per cell of the dominant kernel (stage-2 k_flux) and per
 # zone-update of the whole step (two-sweep minimum 3 u + 2 up passes)
 def kernel_bytes_per_cell(prec: int, neq: int = 8) -> int:
-    tu = 8
+    tu = 8  # FP64 u, or a (hi, lo) FP32 pair
     ts = 8 if prec == 0 else 4
     # read up (neq), read u(1:5), write u(1:5), write E (3)
     return neq * ts + 5 * tu + 5 * tu + 3 * ts
@@ -245,42 +245,62 @@ def run_ours(args, dist: Dist) -> None:
     pk = peaks()
     out = {}
 
-    # ---- FP32-mixed, device resident --------------------------------------
-    pm = p.replace(precision=P.FP32_MIXED)
-    d = Domain(pm)
-    d.init(u0)
-    d.advance_timed(W)
-    clocks = Clocks()
-    dist.barrier()
-    clocks.start()
-    ms = d.advance_timed(K)
-    clk = clocks.stop()
-    ms = dist.max(ms)
-    launches = d.launches_per_step()
+    # ---- FP32 paths, device resident ---------------------------------------
+    # headline: FP32 state/fluxes with Kahan-compensated FP32-pair u;
+    # also the variant with u in FP64 (FP64 accumulation and recovery)
+    variants = {}
+    headline = P.FP32_KAHAN
+    for prec in (P.FP32_KAHAN, P.FP32_MIXED):
+        d = Domain(p.replace(precision=prec))
+        d.init(u0)
+        d.advance_timed(W)
+        clocks = Clocks()
+        dist.barrier()
+        clocks.start()
+        ms_v = d.advance_timed(K)
+        clk_v = clocks.stop()
+        ms_v = dist.max(ms_v)
+        prof_v = {}
+        if prec == headline:
+            for _ in range(3):
+                for name, t in d.profile_step():
+                    prof_v.setdefault(name, []).append(t)
+        variants[prec] = dict(ms=ms_v, clk=clk_v, prof=prof_v, u=d.download(),
+                              launches=d.launches_per_step(), steps=W + K + (3 if prof_v else 0))
+        d.close()
+    ms = variants[headline]["ms"]
+    clk = variants[headline]["clk"]
+    prof = variants[headline]["prof"]
+    launches = variants[headline]["launches"]
     value = dist.ws * n ** 3 * K / (ms * 1e-3)
-    # live per-kernel durations (events between launches, same stream)
-    prof = {}
-    for _ in range(3):
-        for name, t in d.profile_step():
-            prof.setdefault(name, []).append(t)
-    um = d.download()
-    d.close()
 
-    # ---- plain FP64 on the same box (for the stated ratio and L1 error) ----
+    # ---- plain FP64 on the same box (ratio, and the reference for L1) -------
     p64 = p.replace(precision=P.FP64)
     d64 = Domain(p64)
     d64.init(u0)
     d64.advance_timed(1)
     k64 = max(2, args.fp64_steps)
     ms64 = d64.advance_timed(k64)
-    # same total step count as the mixed run for the error comparison
-    remaining = (W + K) - (1 + k64)
-    if remaining > 0:
-        d64.advance_timed(remaining)
-    u64 = d64.download()
+    done = 1 + k64
+    snaps = {}
+    for prec in sorted(variants, key=lambda q: variants[q]["steps"]):
+        need = variants[prec]["steps"] - done
+        if need > 0:
+            d64.advance_timed(need)
+            done += need
+        snaps[prec] = d64.download()
     d64.close()
-    fm, f64 = prim_fields(p, um), prim_fields(p, u64)
-    l1 = {k: rel_l1(fm[k], f64[k]) for k in ("rho", "p", "vx", "By", "Bx", "Bz")}
+    l1 = {}
+    for prec, v in variants.items():
+        fm, f64 = prim_fields(p, v["u"]), prim_fields(p, snaps[prec])
+        bmag = np.sqrt(f64["Bx"] ** 2 + f64["By"] ** 2 + f64["Bz"] ** 2).mean()
+        errs = {}
+        for k in ("rho", "p", "vx", "Bx", "By", "Bz"):
+            den = bmag if k.startswith("B") else np.abs(f64[k]).mean()
+            errs[k] = float(np.abs(fm[k] - f64[k]).mean() / den)
+        errs["steps"] = v["steps"]
+        l1[{P.FP32_KAHAN: "fp32_kahan", P.FP32_MIXED: "fp32_mixed_fp64u"}[prec]] = errs
+    pm = p.replace(precision=headline)
 
     # ---- e2e through the C ABI with host buffers ----------------------------
     import torch
@@ -312,7 +332,7 @@ def run_ours(args, dist: Dist) -> None:
     total = sum(sum(v) for v in prof.values())
     dom = max(means, key=lambda k: sum(prof[k]))
     cells = n ** 3
-    bpc = kernel_bytes_per_cell(P.FP32_MIXED) if dom == "k_flux_stage2" else None
+    bpc = kernel_bytes_per_cell(headline) if dom == "k_flux_stage2" else None
     roof = None
     if bpc:
         ach = bpc * cells / (means[dom] * 1e-3) / 1e9
@@ -320,7 +340,7 @@ def run_ours(args, dist: Dist) -> None:
                 "unit": "GB/s", "frac": ach / pk["hbm_gbs"], "traffic": args.traffic,
                 "bytes_per_cell": bpc, "launch_ms": means[dom],
                 "share_of_step": sum(prof[dom]) / total, "peak_source": pk["source"]}
-    sbz = step_bytes_per_zone(P.FP32_MIXED)
+    sbz = step_bytes_per_zone(headline)
     step_gbs = value / dist.ws * sbz / 1e9
     step_roof = {"bytes_per_zone_update": sbz, "achieved": step_gbs, "peak": pk["hbm_gbs"],
                  "unit": "GB/s", "frac": step_gbs / pk["hbm_gbs"]}
@@ -338,14 +358,18 @@ def run_ours(args, dist: Dist) -> None:
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": dist.ws, "steps": K,
         "warmup": W, "ms_per_step": ms / K, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f32 (f64 pressure recovery, accumulation, dt)",
+        "vs_baseline": None,
+        "dtype": "f32 (u as Kahan-compensated f32 pairs; double-float pressure recovery; f64 dt)",
         "data": "synthetic (seeded turbulence initial state, no dataset)",
-        "config": {"workload": WORKLOAD, "n": n, "precision": "fp32_mixed",
+        "config": {"workload": WORKLOAD, "n": n,
+                   "precision": "fp32 + Kahan-compensated pair accumulation (GCH_FP32_KAHAN)",
                    "parallelism": f"replicas x{dist.ws}",
                    "l2": "state 1.1 GB FP64 u + 0.56 GB FP32 up >> 129 MB L2 (no flush)"},
         "fp64_plain": {"value": dist.ws * n ** 3 * k64 / (ms64 * 1e-3),
                        "ms_per_step": ms64 / k64, "steps": k64},
-        "l1_err_fp32_vs_fp64": l1,
+        "fp32_mixed_fp64u": {"value": dist.ws * n ** 3 * K / (variants[P.FP32_MIXED]["ms"] * 1e-3),
+                             "ms_per_step": variants[P.FP32_MIXED]["ms"] / K},
+        "l1_err_vs_fp64_gpu": l1,
         "kernel_ms": {k: round(v, 4) for k, v in means.items()},
         "roofline": roof, "step_roofline": step_roof,
         "cpu_baseline": cpu, "e2e": e2e, "clocks": clk,
