@@ -96,7 +96,7 @@ class Clocks:
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
-                 "-lms", "200"], stdout=self.out, stderr=subprocess.DEVNULL)
+                 "-lms", "100"], stdout=self.out, stderr=subprocess.DEVNULL)
         except OSError:
             self.proc = None
 
@@ -383,14 +383,14 @@ def run_ours(args, dist: Dist) -> None:
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=40)
+    ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--size", type=int, default=256)
     ap.add_argument("--fp64-steps", type=int, default=4)
     ap.add_argument("--e2e-steps", type=int, default=6)
-    ap.add_argument("--cpu-size", type=int, default=96)
-    ap.add_argument("--cpu-steps", type=int, default=3)
+    ap.add_argument("--cpu-size", type=int, default=160)
+    ap.add_argument("--cpu-steps", type=int, default=40)
     ap.add_argument("--ref-size", type=int, default=128)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--traffic", type=float, default=None,

@@ -424,6 +424,117 @@ __device__ __forceinline__ void hlld(const KParams& p, const T* pl, const T* pr,
   err |= GCH_ERR_HLLD;
 }
 
+// HLLD for the FP32 paths: the same Miyoshi-Kusano states as hlld() above
+// (src/hlld.f90:48-319), but the four star regions are selected by
+// predicates instead of branches, so that a warp whose faces fall in
+// different regions runs one instruction stream.  Both single-star states
+// and the double-star state are formed; the energy and the flux are then
+// evaluated once for the selected side with the reference's expressions.
+template <class T>
+__device__ __forceinline__ void hlld_sel(const KParams& p, const T* pl, const T* pr, T* ff,
+                                         int& err) {
+  const T cv = (T)p.cv;
+  const T csl = cfastX(p, pl);
+  const T csr = cfastX(p, pr);
+  const T sr = tmax_(pl[1] + csl, pr[1] + csr);
+  const T sl = tmin_(pl[1] - csl, pr[1] - csr);
+  if (sl > T(0)) { prim2f<T, 8>(p, pl, ff); return; }
+  if (sr < T(0)) { prim2f<T, 8>(p, pr, ff); return; }
+
+  const T bx = T(0.5) * (pl[5] + pr[5]);
+  const T signBx = tcopysign(T(1), bx);
+  const T bx2 = bx * bx;
+  const T pTL = pl[4] + T(0.5) * (bx2 + pl[6] * pl[6] + pl[7] * pl[7]);
+  const T pTR = pr[4] + T(0.5) * (bx2 + pr[6] * pr[6] + pr[7] * pr[7]);
+  const T slmul = sl - pl[1];
+  const T srmur = sr - pr[1];
+  const T den = srmur * pr[0] - slmul * pl[0];
+  const T iden = T(1) / den;
+  const T sM = (srmur * (pr[0] * pr[1]) - slmul * (pl[0] * pl[1]) - pTR + pTL) * iden;
+  const T srmsM = sr - sM;
+  const T slmsM = sl - sM;
+  const T rhostl = pl[0] * slmul / slmsM;
+  const T rhostr = pr[0] * srmur / srmsM;
+  const T sql = tsqrt(rhostl), sqr = tsqrt(rhostr);
+  const T sstl = sM - tabs(bx) / sql;
+  const T sstr = sM + tabs(bx) / sqr;
+  const T pst = (srmur * pr[0] * pTL - slmul * pl[0] * pTR
+                 + pl[0] * pr[0] * srmur * slmul * (pr[1] - pl[1])) * iden;
+  // single-star states (with the reference's denl/denr == 0 fallbacks)
+  T vstl, wstl, bystl, bzstl, vstr, wstr, bystr, bzstr;
+  {
+    const T denl = pl[0] * slmul * slmsM - bx2;
+    const T ok = denl == T(0) ? T(0) : T(1);
+    const T idl = ok / (denl == T(0) ? T(1) : denl);
+    const T sMmul = sM - pl[1];
+    const T fb = (pl[0] * (slmul * slmul) - bx2) * idl;
+    vstl = pl[2] - bx * pl[6] * sMmul * idl;
+    wstl = pl[3] - bx * pl[7] * sMmul * idl;
+    bystl = pl[6] * fb;
+    bzstl = pl[7] * fb;
+  }
+  {
+    const T denr = pr[0] * srmur * srmsM - bx2;
+    const T ok = denr == T(0) ? T(0) : T(1);
+    const T idr = ok / (denr == T(0) ? T(1) : denr);
+    const T sMmur = sM - pr[1];
+    const T fb = (pr[0] * (srmur * srmur) - bx2) * idr;
+    vstr = pr[2] - bx * pr[6] * sMmur * idr;
+    wstr = pr[3] - bx * pr[7] * sMmur * idr;
+    bystr = pr[6] * fb;
+    bzstr = pr[7] * fb;
+  }
+  // region: UL* | UR* | UL** | UR**
+  const bool star_l = sstl >= T(0);
+  const bool star_r = !star_l && sstr <= T(0);
+  const bool dbl = !star_l && !star_r;
+  const bool left = star_l || (dbl && sM >= T(0));
+  if (dbl && !(sM >= T(0)) && !(sM <= T(0))) {  // src/hlld.f90:316-317
+#pragma unroll
+    for (int q = 0; q < 8; ++q) ff[q] = sM;
+    err |= GCH_ERR_HLLD;
+    return;
+  }
+  // double-star state
+  const T idd = T(1) / (sql + sqr);
+  const T sqlr = sql * sqr;
+  const T vstst = (sql * vstl + sqr * vstr + (bystr - bystl) * signBx) * idd;
+  const T wstst = (sql * wstl + sqr * wstr + (bzstr - bzstl) * signBx) * idd;
+  const T bystst = (sql * bystr + sqr * bystl + sqlr * (vstr - vstl) * signBx) * idd;
+  const T bzstst = (sql * bzstr + sqr * bzstl + sqlr * (wstr - wstl) * signBx) * idd;
+  const T vststdotbstst = sM * bx + vstst * bystst + wstst * bzstst;
+  // the selected side's single-star energy
+  // per-component selects keep pl/pr in registers
+  T q[8];
+#pragma unroll
+  for (int i = 0; i < 8; ++i) q[i] = left ? pl[i] : pr[i];
+  const T smu = left ? slmul : srmur;
+  const T smsM = left ? slmsM : srmsM;
+  const T pT = left ? pTL : pTR;
+  const T rhos = left ? rhostl : rhostr;
+  const T vst = left ? vstl : vstr, wst = left ? wstl : wstr;
+  const T byst = left ? bystl : bystr, bzst = left ? bzstl : bzstr;
+  const T e = T(0.5) * q[0] * (q[1] * q[1] + q[2] * q[2] + q[3] * q[3]) + cv * q[4]
+              + T(0.5) * (bx2 + q[6] * q[6] + q[7] * q[7]);
+  const T vdotb = q[1] * bx + q[2] * q[6] + q[3] * q[7];
+  const T vstdotbst = sM * bx + vst * byst + wst * bzst;
+  const T est = (smu * e - pT * q[1] + pst * sM + bx * (vdotb - vstdotbst)) / smsM;
+  // ** regions: eL** = eL* - sqrt(rhoL*)(..)signBx, eR** = eR* + ..
+  const T sqs = left ? -sql : sqr;
+  const T ex = dbl ? est + sqs * (vstdotbst - vststdotbstst) * signBx : est;
+  const T vx_ = dbl ? vstst : vst, wx_ = dbl ? wstst : wst;
+  const T byx = dbl ? bystst : byst, bzx = dbl ? bzstst : bzst;
+  const T vbx = dbl ? vststdotbstst : vstdotbst;
+  ff[0] = rhos * sM;
+  ff[1] = rhos * (sM * sM) + pst - bx2;
+  ff[2] = rhos * sM * vx_ - bx * byx;
+  ff[3] = rhos * sM * wx_ - bx * bzx;
+  ff[4] = sM * (ex + pst) - bx * vbx;
+  ff[5] = T(0);
+  ff[6] = byx * sM - bx * vx_;
+  ff[7] = bzx * sM - bx * wx_;
+}
+
 // src/hllc.f90:44-140  prim2fhllc (hydro, or passive B when NEQ == 8)
 template <class T, int NEQ>
 __device__ __forceinline__ void hllc(const KParams& p, const T* pl, const T* pr, T* ff, int& err) {
@@ -516,7 +627,10 @@ struct Riemann<GCH_SOLVER_HLLD, 8> {
   template <class T>
   __device__ __forceinline__ static void solve(const KParams& p, const T* l, const T* r, T* f,
                                                int& e) {
-    hlld<T>(p, l, r, f, e);
+    if constexpr (sizeof(T) == 4)
+      hlld_sel<T>(p, l, r, f, e);  // FP32 paths: branch-free star regions
+    else
+      hlld<T>(p, l, r, f, e);      // FP64: the reference's branch order
   }
 };
 template <int NEQ>

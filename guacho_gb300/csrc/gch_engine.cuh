@@ -18,6 +18,12 @@ struct Engine {
   static dim3 cell_grid(const KParams& p) {
     return dim3((p.nx + 31) / 32, (p.ny + 7) / 8, p.nz);
   }
+  // cell kernels that march over kzc planes per block (fewer blocks: one
+  // reduction atomic per block)
+  static constexpr int kzc = 8;
+  static dim3 column_grid(const KParams& p) {
+    return dim3((p.nx + 31) / 32, (p.ny + 7) / 8, (p.nz + kzc - 1) / kzc);
+  }
 
   // ---- stage kernels, dispatched on solver and neq ----------------------
   template <int SOLVER, int NEQ, int STAGE, bool PRIM_IN, int LIM>
@@ -89,13 +95,13 @@ struct Engine {
   // the CFL min over the interior into the device scalar block (k_cfl)
   static int cfl(gch_domain* d) {
     const KParams& p = d->kp;
-    dim3 grid = cell_grid(p), block(32, 8);
+    dim3 cgrid = column_grid(p), block(32, 8);
     if (d->prim_in) {
-      if (p.neq == 8) k_cfl<Pol, 8, true><<<grid, block, 0, d->stream>>>(p, (const TS*)d->primit, d->sc);
-      else k_cfl<Pol, 5, true><<<grid, block, 0, d->stream>>>(p, (const TS*)d->primit, d->sc);
+      if (p.neq == 8) k_cfl<Pol, 8, true><<<cgrid, block, 0, d->stream>>>(p, (const TS*)d->primit, d->sc, kzc);
+      else k_cfl<Pol, 5, true><<<cgrid, block, 0, d->stream>>>(p, (const TS*)d->primit, d->sc, kzc);
     } else {
-      if (p.neq == 8) k_cfl<Pol, 8, false><<<grid, block, 0, d->stream>>>(p, (const TU*)d->u, d->sc);
-      else k_cfl<Pol, 5, false><<<grid, block, 0, d->stream>>>(p, (const TU*)d->u, d->sc);
+      if (p.neq == 8) k_cfl<Pol, 8, false><<<cgrid, block, 0, d->stream>>>(p, (const TU*)d->u, d->sc, kzc);
+      else k_cfl<Pol, 5, false><<<cgrid, block, 0, d->stream>>>(p, (const TU*)d->u, d->sc, kzc);
     }
     d->cfl_ready = true;
     return cuda_status(cudaGetLastError());
@@ -103,15 +109,15 @@ struct Engine {
 
   static int get_dt(gch_domain* d) {
     const KParams& p = d->kp;
-    dim3 grid = cell_grid(p), block(32, 8);
+    dim3 cgrid = column_grid(p), block(32, 8);
     if (d->cfl_fused && d->cfl_ready) {
       // the min over cells was accumulated by the last step's k_ct<2>
     } else if (d->prim_in) {
-      if (p.neq == 8) k_cfl<Pol, 8, true><<<grid, block, 0, d->stream>>>(p, (const TS*)d->primit, d->sc);
-      else k_cfl<Pol, 5, true><<<grid, block, 0, d->stream>>>(p, (const TS*)d->primit, d->sc);
+      if (p.neq == 8) k_cfl<Pol, 8, true><<<cgrid, block, 0, d->stream>>>(p, (const TS*)d->primit, d->sc, kzc);
+      else k_cfl<Pol, 5, true><<<cgrid, block, 0, d->stream>>>(p, (const TS*)d->primit, d->sc, kzc);
     } else {
-      if (p.neq == 8) k_cfl<Pol, 8, false><<<grid, block, 0, d->stream>>>(p, (const TU*)d->u, d->sc);
-      else k_cfl<Pol, 5, false><<<grid, block, 0, d->stream>>>(p, (const TU*)d->u, d->sc);
+      if (p.neq == 8) k_cfl<Pol, 8, false><<<cgrid, block, 0, d->stream>>>(p, (const TU*)d->u, d->sc, kzc);
+      else k_cfl<Pol, 5, false><<<cgrid, block, 0, d->stream>>>(p, (const TU*)d->u, d->sc, kzc);
     }
     if (!(d->cfl_fused && d->cfl_ready)) gch_mark(d, "k_cfl");
     k_dtfin<<<1, 1, 0, d->stream>>>(d->sc, p.cfl, p.dx, p.dy, p.dz);
@@ -133,8 +139,8 @@ struct Engine {
     ++d->launches;
     gch_mark(d, "k_flux_stage1");
     if (ct) {
-      k_ct<Pol, 1, false><<<cgrid, cblock, 0, d->stream>>>(p, (const TU*)d->u, (TS*)d->up,
-                                                     (const TS*)d->E, (const TS*)d->s678, d->sc);
+      k_ct<Pol, 1, false><<<column_grid(p), cblock, 0, d->stream>>>(
+          p, (const TU*)d->u, (TS*)d->up, (const TS*)d->E, (const TS*)d->s678, d->sc, kzc);
       ++d->launches;
       gch_mark(d, "k_ct_stage1");
     }
@@ -147,11 +153,11 @@ struct Engine {
     gch_mark(d, "k_flux_stage2");
     if (ct) {
       if (d->cfl_fused)
-        k_ct<Pol, 2, true><<<cgrid, cblock, 0, d->stream>>>(p, (const TU*)d->u, (TU*)dst2,
-                                                            (const TS*)d->E, (const TS*)d->s678, d->sc);
+        k_ct<Pol, 2, true><<<column_grid(p), cblock, 0, d->stream>>>(
+            p, (const TU*)d->u, (TU*)dst2, (const TS*)d->E, (const TS*)d->s678, d->sc, kzc);
       else
-        k_ct<Pol, 2, false><<<cgrid, cblock, 0, d->stream>>>(p, (const TU*)d->u, (TU*)dst2,
-                                                             (const TS*)d->E, (const TS*)d->s678, d->sc);
+        k_ct<Pol, 2, false><<<column_grid(p), cblock, 0, d->stream>>>(
+            p, (const TU*)d->u, (TU*)dst2, (const TS*)d->E, (const TS*)d->s678, d->sc, kzc);
       ++d->launches;
       gch_mark(d, "k_ct_stage2");
     }

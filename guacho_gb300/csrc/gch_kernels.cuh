@@ -432,72 +432,98 @@ __global__ void __launch_bounds__(256)
 k_ct(KParams p, const typename Pol::TU* u,
      typename std::conditional<STAGE == 1, typename Pol::TS, typename Pol::TU>::type* dst,
      const typename Pol::TS* __restrict__ E, const typename Pol::TS* __restrict__ s678,
-     StepScalars* sc) {
+     StepScalars* sc, int kz) {
   using TC = typename Ops<Pol>::TC;
   using TD = typename std::conditional<STAGE == 1, typename Pol::TS, typename Pol::TU>::type;
+  if (!sc->active) return;
   const int ci = blockIdx.x * blockDim.x + threadIdx.x;
   const int cj = blockIdx.y * blockDim.y + threadIdx.y;
-  const int ck = blockIdx.z;
-  if (!sc->active) return;
+  const int kb = blockIdx.z * kz;
+  const int ke = min(p.nz, kb + kz);
   const bool active = ci < p.nx && cj < p.ny;
   if (!CFL && !active) return;
-  const int ax = min(ci, p.nx - 1) + NG, ay = min(cj, p.ny - 1) + NG, az = ck + NG;
+  const int ax = min(ci, p.nx - 1) + NG, ay = min(cj, p.ny - 1) + NG;
   const double dt = STAGE == 1 ? sc->dt / 2.0 : sc->dt;
   const TC hx = (TC)(0.5 * sc->dtd[STAGE - 1][0]), hy = (TC)(0.5 * sc->dtd[STAGE - 1][1]),
            hz = (TC)(0.5 * sc->dtd[STAGE - 1][2]);
+  const long long sx = 1, sy = p.pitch, sz = (long long)p.pitch * p.NY;
+  const bool inxy = ax > NG && ax < NG + p.nx - 1 && ay > NG && ay < NG + p.ny - 1;
 
-  // E component q at a face neighbour (the ghost layer follows boundaryI_ef:
-  // periodic copy, outflow copy, closed copy with the normal component of the
-  // x/y walls negated and nothing negated on z walls)
-  auto e_at = [&](int q, int bx, int by, int bz) -> TC {
+  // E component q at a face neighbour; the ghost layer follows
+  // boundaryI_ef (src/flux_cd_module.f90:45-237): periodic copy, outflow
+  // copy, closed copy with the normal component of the x/y walls negated
+  // and nothing negated on z walls
+  auto e_ghost = [&](int q, int bx, int by, int bz) -> TC {
     bool fx = false, fy = false, fz = false;
-    const int sx = ghost_src(bx, p.nx, p.bc[0], p.bc[1], fx);
-    const int sy = ghost_src(by, p.ny, p.bc[2], p.bc[3], fy);
-    const int sz = ghost_src(bz, p.nz, p.bc[4], p.bc[5], fz);
-    TC v = (TC)E[q * p.fs + cell_index(p, sx, sy, sz)];
+    const int gx = ghost_src(bx, p.nx, p.bc[0], p.bc[1], fx);
+    const int gy = ghost_src(by, p.ny, p.bc[2], p.bc[3], fy);
+    const int gz = ghost_src(bz, p.nz, p.bc[4], p.bc[5], fz);
+    TC v = (TC)E[q * p.fs + cell_index(p, gx, gy, gz)];
     if ((fx && q == 0) || (fy && q == 1)) v = -v;
     return v;
   };
-  const long long c = cell_index(p, ax, ay, az);
-  const auto u6 = Ops<Pol>::ld(u[5 * p.fs + c]);
-  const auto u7 = Ops<Pol>::ld(u[6 * p.fs + c]);
-  const auto u8 = Ops<Pol>::ld(u[7 * p.fs + c]);
-  auto b6 = Ops<Pol>::ct(u6, hy, e_at(2, ax, ay - 1, az), e_at(2, ax, ay + 1, az), hz,
-                           e_at(1, ax, ay, az - 1), e_at(1, ax, ay, az + 1), true);
-  auto b7 = Ops<Pol>::ct(u7, hx, e_at(2, ax - 1, ay, az), e_at(2, ax + 1, ay, az), hz,
-                           e_at(0, ax, ay, az - 1), e_at(0, ax, ay, az + 1), false);
-  auto b8 = Ops<Pol>::ct(u8, hx, e_at(1, ax - 1, ay, az), e_at(1, ax + 1, ay, az), hy,
-                           e_at(0, ax, ay - 1, az), e_at(0, ax, ay + 1, az), true);
-  if (p.eight_wave) {
-    b6 = Ops<Pol>::add(b6, dt * (double)s678[c]);
-    b7 = Ops<Pol>::add(b7, dt * (double)s678[p.fs + c]);
-    b8 = Ops<Pol>::add(b8, dt * (double)s678[2 * p.fs + c]);
-  }
-  if (active) {
-    dst[5 * p.fs + c] = store_as<TD>(b6);
-    dst[6 * p.fs + c] = store_as<TD>(b7);
-    dst[7 * p.fs + c] = store_as<TD>(b8);
-  }
-  if constexpr (CFL && STAGE == 2) {
-    // the next step's CFL candidate from the final state of this cell
-    // (same values and arithmetic as k_cfl on u)
-    double dtp = 1e30;
-    int bad = 0;
-    if (active) {
-      typename Ops<Pol>::R uu[8];
-#pragma unroll
-      for (int q = 0; q < 5; ++q) uu[q] = Ops<Pol>::ld(dst[q * p.fs + c]);
-      uu[5] = store_as<typename Pol::TU>(b6);
-      uu[6] = store_as<typename Pol::TU>(b7);
-      uu[7] = store_as<typename Pol::TU>(b8);
-      TC pr[8];
-      unsigned pfl = 0;
-      Ops<Pol>::template prim_vals<8>(p, uu, pr, pfl);
-      cfl_candidate<TC, 8>(p, pr, dtp, bad);
-      if (pfl) atomicAdd(&sc->pfloor, (unsigned long long)pfl);
+
+  double dtp = 1e30;
+  int bad = 0;
+  for (int k = kb; k < ke; ++k) {
+    const int az = k + NG;
+    const long long c = cell_index(p, ax, ay, az);
+    // the six face neighbours of E needed by the three components
+    TC e3ym, e3yp, e2zm, e2zp, e3xm, e3xp, e1zm, e1zp, e2xm, e2xp, e1ym, e1yp;
+    if (inxy && az > NG && az < NG + p.nz - 1) {
+      const typename Pol::TS* E1 = E;
+      const typename Pol::TS* E2 = E + p.fs;
+      const typename Pol::TS* E3 = E + 2 * p.fs;
+      e3ym = (TC)E3[c - sy]; e3yp = (TC)E3[c + sy];
+      e2zm = (TC)E2[c - sz]; e2zp = (TC)E2[c + sz];
+      e3xm = (TC)E3[c - sx]; e3xp = (TC)E3[c + sx];
+      e1zm = (TC)E1[c - sz]; e1zp = (TC)E1[c + sz];
+      e2xm = (TC)E2[c - sx]; e2xp = (TC)E2[c + sx];
+      e1ym = (TC)E1[c - sy]; e1yp = (TC)E1[c + sy];
+    } else {
+      e3ym = e_ghost(2, ax, ay - 1, az); e3yp = e_ghost(2, ax, ay + 1, az);
+      e2zm = e_ghost(1, ax, ay, az - 1); e2zp = e_ghost(1, ax, ay, az + 1);
+      e3xm = e_ghost(2, ax - 1, ay, az); e3xp = e_ghost(2, ax + 1, ay, az);
+      e1zm = e_ghost(0, ax, ay, az - 1); e1zp = e_ghost(0, ax, ay, az + 1);
+      e2xm = e_ghost(1, ax - 1, ay, az); e2xp = e_ghost(1, ax + 1, ay, az);
+      e1ym = e_ghost(0, ax, ay - 1, az); e1yp = e_ghost(0, ax, ay + 1, az);
     }
-    cfl_block_reduce(dtp, bad, sc);
+    const auto u6 = Ops<Pol>::ld(u[5 * p.fs + c]);
+    const auto u7 = Ops<Pol>::ld(u[6 * p.fs + c]);
+    const auto u8 = Ops<Pol>::ld(u[7 * p.fs + c]);
+    // src/flux_cd_module.f90:311-321
+    auto b6 = Ops<Pol>::ct(u6, hy, e3ym, e3yp, hz, e2zm, e2zp, true);
+    auto b7 = Ops<Pol>::ct(u7, hx, e3xm, e3xp, hz, e1zm, e1zp, false);
+    auto b8 = Ops<Pol>::ct(u8, hx, e2xm, e2xp, hy, e1ym, e1yp, true);
+    if (p.eight_wave) {
+      b6 = Ops<Pol>::add(b6, dt * (double)s678[c]);
+      b7 = Ops<Pol>::add(b7, dt * (double)s678[p.fs + c]);
+      b8 = Ops<Pol>::add(b8, dt * (double)s678[2 * p.fs + c]);
+    }
+    if (active) {
+      dst[5 * p.fs + c] = store_as<TD>(b6);
+      dst[6 * p.fs + c] = store_as<TD>(b7);
+      dst[7 * p.fs + c] = store_as<TD>(b8);
+    }
+    if constexpr (CFL && STAGE == 2) {
+      // the next step's CFL candidate from the final state of this cell
+      // (same values and arithmetic as k_cfl on u)
+      if (active) {
+        typename Ops<Pol>::R uu[8];
+#pragma unroll
+        for (int q = 0; q < 5; ++q) uu[q] = Ops<Pol>::ld(dst[q * p.fs + c]);
+        uu[5] = store_as<typename Pol::TU>(b6);
+        uu[6] = store_as<typename Pol::TU>(b7);
+        uu[7] = store_as<typename Pol::TU>(b8);
+        TC pr[8];
+        unsigned pfl = 0;
+        Ops<Pol>::template prim_vals<8>(p, uu, pr, pfl);
+        cfl_candidate<TC, 8>(p, pr, dtp, bad);
+        if (pfl) atomicAdd(&sc->pfloor, (unsigned long long)pfl);
+      }
+    }
   }
+  if constexpr (CFL && STAGE == 2) cfl_block_reduce(dtp, bad, sc);
 }
 
 // ---------------------------------------------------------------------------
@@ -609,23 +635,26 @@ __global__ void k_user_bc(KParams p, T* a, int neq, const StepScalars* sc) {
 template <class Pol, int NEQ, bool PRIM_IN>
 __global__ void __launch_bounds__(256)
 k_cfl(KParams p, const typename std::conditional<PRIM_IN, typename Pol::TS, typename Pol::TU>::type* src,
-      StepScalars* sc) {
+      StepScalars* sc, int kz) {
   using TC = typename Ops<Pol>::TC;
   if (!sc->active) return;
   const int ci = blockIdx.x * blockDim.x + threadIdx.x;
   const int cj = blockIdx.y * blockDim.y + threadIdx.y;
-  const int ck = blockIdx.z;
+  const int kb = blockIdx.z * kz;
+  const int ke = min(p.nz, kb + kz);
   double dtp = 1e30;
   int bad = 0;
   if (ci < p.nx && cj < p.ny) {
-    const long long c = cell_index(p, ci + NG, cj + NG, ck + NG);
-    TC pr[NEQ];
     unsigned pfl = 0;
-    if constexpr (PRIM_IN)
-      Ops<Pol>::template load_stored_prim<NEQ>(p, src, c, pr);
-    else
-      Ops<Pol>::template load_prim<NEQ>(p, src, c, pr, pfl);
-    cfl_candidate<TC, NEQ>(p, pr, dtp, bad);
+    for (int k = kb; k < ke; ++k) {
+      const long long c = cell_index(p, ci + NG, cj + NG, k + NG);
+      TC pr[NEQ];
+      if constexpr (PRIM_IN)
+        Ops<Pol>::template load_stored_prim<NEQ>(p, src, c, pr);
+      else
+        Ops<Pol>::template load_prim<NEQ>(p, src, c, pr, pfl);
+      cfl_candidate<TC, NEQ>(p, pr, dtp, bad);
+    }
     if (pfl) atomicAdd(&sc->pfloor, (unsigned long long)pfl);
   }
   cfl_block_reduce(dtp, bad, sc);
