@@ -17,9 +17,10 @@ MAX_SPHERES, MAX_GRAV, MAX_TABLE = 8, 4, 512
 
 ERR_PARAM, ERR_CUDA, ERR_HLLD, ERR_HLLC = 0x1, 0x2, 0x4, 0x8
 ERR_DT, ERR_TIMEOUT, ERR_NO_DEVICE, ERR_STATE = 0x10, 0x20, 0x40, 0x80
+ERR_TOO_LARGE = 0x100
 ERR_NAMES = {ERR_PARAM: "PARAM", ERR_CUDA: "CUDA", ERR_HLLD: "HLLD", ERR_HLLC: "HLLC",
              ERR_DT: "DT", ERR_TIMEOUT: "TIMEOUT", ERR_NO_DEVICE: "NO_DEVICE",
-             ERR_STATE: "STATE"}
+             ERR_STATE: "STATE", ERR_TOO_LARGE: "TOO_LARGE"}
 
 LIB_PATH = Path(__file__).resolve().parent / "lib" / "libguacho_gb300.so"
 
@@ -126,6 +127,7 @@ def lib() -> C.CDLL:
         "gch_batch_download": (I, [P, I, P]),
         "gch_batch_advance": (I, [P, I, I]),
         "gch_batch_time": (I, [P, DP, IP]),
+        "gch_get_timestep_noalloc": (I, [C.POINTER(Params_t), P, I, I, D, D, P, P, P]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)
@@ -142,7 +144,7 @@ def exported_symbols() -> list[str]:
             "gch_last_step_info", "gch_launches_per_step", "gch_advance_timed",
             "gch_profile_step", "gch_batch_create",
             "gch_batch_destroy", "gch_batch_upload", "gch_batch_download",
-            "gch_batch_advance", "gch_batch_time"]
+            "gch_batch_advance", "gch_batch_time", "gch_get_timestep_noalloc"]
 
 
 class GuachoError(RuntimeError):

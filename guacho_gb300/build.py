@@ -35,6 +35,8 @@ UNITS = {
     "gch_kahan.cu": ["-prec-div=false", "-prec-sqrt=false", "-ftz=true"],
     "gch_api.cu": [],
     "gch_batch.cu": [],
+    # FP64 arithmetic in the reference's order, as gch_fp64.cu
+    "gch_noalloc.cu": ["-fmad=false"],
 }
 
 

@@ -100,6 +100,7 @@ extern "C" {
 #define GCH_ERR_TIMEOUT 0x20         /* a bounded device wait ran out     */
 #define GCH_ERR_NO_DEVICE 0x40       /* no CUDA device / not sm_103       */
 #define GCH_ERR_STATE 0x80           /* call out of order                 */
+#define GCH_ERR_TOO_LARGE 0x100      /* box exceeds a fixed-size work area */
 
 #define GCH_MAX_SPHERES 8
 #define GCH_MAX_GRAV 4
@@ -229,6 +230,25 @@ int gch_launches_per_step(gch_domain_t* d);
  * (each a NUL-terminated string in a `name_len`-byte slot of `names`). */
 int gch_advance_timed(gch_domain_t* d, int steps, int n_iter, float* ms);
 int gch_profile_step(gch_domain_t* d, int cap, float* ms, char* names, int name_len, int* n);
+
+/* get_timestep for callers that cannot allocate device memory.  No
+ * counterpart in the reference: it exists for drivers that record their
+ * time loop with CUDA stream capture (an allocation cannot be captured) and
+ * for host codes that give the library a fixed memory budget and forbid
+ * hidden allocations.  It allocates nothing: the caller passes u in device
+ * memory in the reference layout u(neq, 1-2:nx+2, 1-2:ny+2, 1-2:nz+2)
+ * (FP64, ghost cells filled) and device slots for the outputs dt and
+ * dump_flag; the per-block partial minima go to a fixed array inside the
+ * library (512 KiB on every GPU that loads it, kept until exit).  Same
+ * result as gch_get_timestep in FP64 arithmetic.  Limits: boxes with
+ * ceil(nx/32)*ceil(ny/8)*ceil(nz/8) > 65536 (beyond 512^3 cells) return
+ * GCH_ERR_TOO_LARGE; table cooling returns GCH_ERR_PARAM.  All calls share
+ * the fixed array: calls that can overlap on the GPU race, so issue them on
+ * one stream.  The first call on a device looks up the array's address;
+ * make it before any stream capture.  Asynchronous on `stream`. */
+int gch_get_timestep_noalloc(const gch_params_t* p, const double* u_dev, int current_iter,
+                             int n_iter, double current_time, double tprint, double* dt_dev,
+                             int* dump_dev, void* stream);
 
 /* ---- batched boxes ------------------------------------------------------ */
 typedef struct gch_batch gch_batch_t;
