@@ -380,6 +380,27 @@ def run_ours(args, dist: Dist) -> None:
     dist.close()
 
 
+def run_ncu_case(args) -> None:
+    """A short host-driven step sequence (no CUDA graphs) of the benchmark
+    problem for profiler captures: --size, --precision, --steps."""
+    from guacho_gb300 import build as gbuild
+    gbuild.build(verbose=False)
+    from guacho_gb300 import params as P
+    from guacho_gb300 import problems
+    from guacho_gb300.domain import Domain
+    prec = {"kahan": P.FP32_KAHAN, "mixed": P.FP32_MIXED, "fp64": P.FP64}[args.precision]
+    p, u0 = problems.turbulence(args.size)
+    with Domain(p.replace(precision=prec)) as d:
+        d.init(u0)
+        t = 0.0
+        for it in range(1, args.steps + 1):
+            dt, _ = d.get_timestep(it, 10, t, 1e30)
+            d.tstep(dt)
+            t += dt
+        print(json.dumps({"ncu_case": args.precision, "size": args.size, "steps": args.steps,
+                          "time": t, "info": d.step_info()}))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -395,7 +416,13 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--traffic", type=float, default=None,
                     help="ncu dram bytes per launch of the dominant kernel, if known")
+    ap.add_argument("--ncu-case", action="store_true",
+                    help="run a short host-driven step sequence for profiler captures")
+    ap.add_argument("--precision", default="kahan", choices=["kahan", "mixed", "fp64"])
     args = ap.parse_args()
+    if args.ncu_case:
+        run_ncu_case(args)
+        return
     ws, rank, local = _dist()
     if ws > 1 and args.impl == "ours":
         os.environ["CUDA_VISIBLE_DEVICES"] = str(local)
