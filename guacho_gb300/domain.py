@@ -125,6 +125,28 @@ class Domain:
             steps += 1
         return steps
 
+    def write_output(self, outputpath, itprint: int, dump_divb: bool = True,
+                     scal=(1.0, 1.0, 1.0)) -> None:
+        """src/output.f90:40-53 write_output with out_bin: download u and
+        write BIN/points000.<itprint>.bin (+ the div B dump when MHD)."""
+        from . import binio
+        u = self.download()
+        binio.write_bin(binio.bin_path(outputpath, itprint), u, self.params, scal)
+        if dump_divb and self.params.bfield:
+            binio.write_divb(binio.bin_path(outputpath, itprint, base="divB-"), u,
+                             self.params, scal)
+
+    def read_warm_start(self, path) -> None:
+        """src/init.f90:437-467 (iwarm): read u from a BIN file, then
+        calcprim."""
+        from . import binio
+        hdr, u = binio.read_bin(path)
+        if (hdr["nx"], hdr["ny"], hdr["nz"], hdr["neq"]) != (
+                self.params.nx, self.params.ny, self.params.nz, self.params.neq):
+            raise ValueError(f"{path}: grid {hdr} does not match the domain")
+        self.upload(u)
+        self.calcprim()
+
     def step_info(self) -> tuple[int, int]:
         pf = C.c_longlong()
         err = C.c_int()
