@@ -194,7 +194,8 @@ def batched_run(args, precision: int) -> dict:
            "zones": zones, "steps": args.batch_steps,
            "step_ms_p50": 1e3 * float(np.percentile(times, 50)),
            "step_ms_p99": 1e3 * float(np.percentile(times, 99)),
-           "timing": "host wall clock per synchronous batch step"}
+           "timing": "host wall clock per synchronous batch step",
+           "tuning": b.tuning()}
     # per-box error against FP64 boxes advanced the same number of steps
     b64 = Batch([p.replace(precision=P.FP64) for p, _ in boxes])
     for i, (_, u) in enumerate(boxes):

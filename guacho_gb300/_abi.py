@@ -121,12 +121,16 @@ def lib() -> C.CDLL:
         "gch_launches_per_step": (I, [P]),
         "gch_advance_timed": (I, [P, I, I, C.POINTER(C.c_float)]),
         "gch_profile_step": (I, [P, I, C.POINTER(C.c_float), C.c_char_p, I, IP]),
+        "gch_get_kz": (I, [P]),
+        "gch_set_kz": (I, [P, I]),
+        "gch_autotune": (I, [P, I, IP, C.POINTER(C.c_float), IP]),
         "gch_batch_create": (I, [I, C.POINTER(Params_t), P, VPP]),
         "gch_batch_destroy": (I, [P]),
         "gch_batch_upload": (I, [P, I, P]),
         "gch_batch_download": (I, [P, I, P]),
         "gch_batch_advance": (I, [P, I, I]),
         "gch_batch_time": (I, [P, DP, IP]),
+        "gch_batch_tuning": (I, [P, IP, IP, I, IP, C.POINTER(C.c_float), IP]),
         "gch_get_timestep_noalloc": (I, [C.POINTER(Params_t), P, I, I, D, D, P, P, P]),
     }
     for name, (res, args) in sig.items():
@@ -142,9 +146,11 @@ def exported_symbols() -> list[str]:
             "gch_upload", "gch_download", "gch_boundaryI", "gch_calcprim",
             "gch_get_timestep", "gch_tstep", "gch_step_host", "gch_advance",
             "gch_last_step_info", "gch_launches_per_step", "gch_advance_timed",
-            "gch_profile_step", "gch_batch_create",
+            "gch_profile_step", "gch_get_kz", "gch_set_kz", "gch_autotune",
+            "gch_batch_create",
             "gch_batch_destroy", "gch_batch_upload", "gch_batch_download",
-            "gch_batch_advance", "gch_batch_time", "gch_get_timestep_noalloc"]
+            "gch_batch_advance", "gch_batch_time", "gch_batch_tuning",
+            "gch_get_timestep_noalloc"]
 
 
 class GuachoError(RuntimeError):

@@ -47,6 +47,11 @@ __global__ void k_set_dt(StepScalars* sc, double dt, double dx, double dy, doubl
   gch::set_stage_ratios(sc, dx, dy, dz);
 }
 __global__ void k_set_active(StepScalars* sc) { sc->active = 1; }
+__global__ void k_restore_info(StepScalars* sc, int active, int err, unsigned long long pfloor) {
+  sc->active = active;
+  sc->err = err;
+  sc->pfloor = pfloor;
+}
 __global__ void k_clear_info(StepScalars* sc) {
   sc->err = 0;
   sc->pfloor = 0;
@@ -491,6 +496,61 @@ int gch_profile_step(gch_domain_t* d, int cap, float* ms, char* names, int name_
 int gch_launches_per_step(gch_domain_t* d) {
   if (!d) return -1;
   return d->launches + 2;  // + k_cfl and k_dtfin of get_timestep
+}
+
+int gch_get_kz(gch_domain_t* d) { return d ? d->kz : -1; }
+
+int gch_set_kz(gch_domain_t* d, int kz) {
+  if (!d || kz < 1 || kz > d->kp.nz) return GCH_ERR_PARAM;
+  int st = cuda_ok(cudaStreamSynchronize(d->stream));
+  if (d->graph) {  // the captured step holds the old grid
+    cudaGraphExecDestroy(d->graph);
+    d->graph = nullptr;
+  }
+  d->kz = kz;
+  return st;
+}
+
+int gch_autotune(gch_domain_t* d, int cap, int* cand_kz, float* cand_ms, int* ncand) {
+  if (!d) return GCH_ERR_PARAM;
+  int st = fetch_scalars(d);
+  const StepScalars keep = *d->sc_host;
+  k_set_active<<<1, 1, 0, d->stream>>>(d->sc);
+  cudaEvent_t e0, e1;
+  st |= cuda_ok(cudaEventCreate(&e0));
+  st |= cuda_ok(cudaEventCreate(&e1));
+  int best_kz = d->kz, n = 0;
+  float best = 0.f;
+  for (int kz : {1, 2, 4, 8, 16, 32}) {
+    if (kz > d->kp.nz || st) break;
+    d->kz = kz;
+    st |= engine(d).probe(d);  // warm-up
+    st |= cuda_ok(cudaEventRecord(e0, d->stream));
+    for (int r = 0; r < 3; ++r) st |= engine(d).probe(d);
+    st |= cuda_ok(cudaEventRecord(e1, d->stream));
+    st |= cuda_ok(cudaEventSynchronize(e1));
+    float ms = 0.f;
+    st |= cuda_ok(cudaEventElapsedTime(&ms, e0, e1));
+    ms /= 3;
+    if (n < cap) {
+      if (cand_kz) cand_kz[n] = kz;
+      if (cand_ms) cand_ms[n] = ms;
+    }
+    if (n == 0 || ms < best) {
+      best = ms;
+      best_kz = kz;
+    }
+    ++n;
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (ncand) *ncand = std::min(n, cap);
+  // the probes counted the pressure floors of the stage-1 states: put the
+  // step information back as it was
+  k_restore_info<<<1, 1, 0, d->stream>>>(d->sc, keep.active, keep.err, keep.pfloor);
+  st |= cuda_ok(cudaGetLastError());
+  st |= gch_set_kz(d, best_kz);
+  return st;
 }
 
 }  // extern "C"

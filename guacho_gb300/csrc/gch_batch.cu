@@ -1,32 +1,176 @@
 // gch_batch.cu -- many independent boxes of uneven size, each with its own
-// CFL dt, advanced together.  Each box runs its captured step graph on its
-// own stream so that small boxes overlap on the 152 SMs.
+// CFL dt, advanced together.
+//
+// Grouped mode (FP32 policies; no table cooling, resistivity or user
+// spheres): one step of all boxes is one CUDA graph of grouped launches,
+// one launch per kernel of the step for up to 64 boxes (gch_group.cuh).
+// The z-march depth of the stage kernels is chosen by timing the stage-1
+// flux kernel over the whole batch for each candidate depth (the autotuner
+// runs once, before the first step; that kernel only writes the stage
+// arrays up and E, so timing it leaves the state untouched).  The loop state
+// of every box is gathered into one array and read back with one copy.
+//
+// Otherwise (FP64, or physics the grouped step does not carry) every box
+// runs its own captured step graph on its own stream.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <new>
 #include <vector>
 
 #include "gch_domain.h"
 
+namespace {
+
+using gch::StepScalars;
+
+// the loop controls of a batched advance: no output clip, no tmax
+__global__ void k_batch_begin(StepScalars* const* sc, int n, int n_iter) {
+  const int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= n) return;
+  StepScalars* s = sc[b];
+  s->n_iter = n_iter;
+  s->tprint = 1e300;
+  s->dtprint = 1e300;
+  s->tmax = 1e300;
+  s->dump = 0;
+  s->active = s->err == 0;
+}
+
+__global__ void k_batch_gather(StepScalars* const* sc, int n, StepScalars* out) {
+  const int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b < n) out[b] = *sc[b];
+}
+
+__global__ void k_batch_clear_info(StepScalars* const* sc, int n) {
+  const int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= n) return;
+  sc[b]->err = 0;
+  sc[b]->pfloor = 0;
+}
+
+int cuda_ok(cudaError_t e) { return e == cudaSuccess ? GCH_OK : GCH_ERR_CUDA; }
+
+}  // namespace
+
 struct gch_batch {
   std::vector<gch_domain*> boxes;
   std::vector<double> time;
   std::vector<int> iter;
+  // grouped mode
+  const gch::GroupOps* gops = nullptr;
+  cudaStream_t stream = nullptr;
+  bool own_stream = false;
+  int kz = 0;                                // 0 until the autotuner ran
+  std::vector<int> tune_kz;                  // candidates and their times
+  std::vector<float> tune_ms;
+  bool cfl_ready = false;
+  cudaGraphExec_t graph = nullptr;
+  StepScalars** sc_list = nullptr;           // device: the boxes' scalar blocks
+  StepScalars* sc_all = nullptr;             // device gather buffer
+  StepScalars* sc_all_host = nullptr;        // pinned
 };
+
+namespace {
+
+bool groupable(const gch_params_t& p) {
+  const bool prim_in = p.cooling == GCH_COOL_DMC || p.cooling == GCH_COOL_CHI;
+  return p.precision != GCH_FP64 && !prim_in && p.eta == 0.0 && !p.bc_user;
+}
+
+int grid_of(int n) { return (n + 127) / 128; }
+
+// Time the stage-1 flux kernel of all boxes for each candidate z-march
+// depth and keep the fastest.
+int autotune(gch_batch* b) {
+  const int n = (int)b->boxes.size();
+  int nzmax = 1;
+  for (gch_domain* d : b->boxes) nzmax = std::max(nzmax, d->kp.nz);
+  cudaEvent_t e0, e1;
+  int st = cuda_ok(cudaEventCreate(&e0));
+  st |= cuda_ok(cudaEventCreate(&e1));
+  b->tune_kz.clear();
+  b->tune_ms.clear();
+  float best = 0.f;
+  int best_kz = std::min(8, nzmax);
+  for (int kz : {2, 4, 8, 16, 32}) {
+    if (kz > nzmax && kz != 2) break;
+    st |= b->gops->probe(b->boxes.data(), n, kz, b->stream);  // warm-up
+    st |= cuda_ok(cudaEventRecord(e0, b->stream));
+    for (int r = 0; r < 3; ++r) st |= b->gops->probe(b->boxes.data(), n, kz, b->stream);
+    st |= cuda_ok(cudaEventRecord(e1, b->stream));
+    st |= cuda_ok(cudaEventSynchronize(e1));
+    float ms = 0.f;
+    st |= cuda_ok(cudaEventElapsedTime(&ms, e0, e1));
+    if (st) break;
+    b->tune_kz.push_back(kz);
+    b->tune_ms.push_back(ms / 3);
+    if (b->tune_kz.size() == 1 || ms < best) {
+      best = ms;
+      best_kz = kz;
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  // the probes counted pressure floors of the stage-1 states: clear them
+  k_batch_clear_info<<<grid_of(n), 128, 0, b->stream>>>(b->sc_list, n);
+  st |= cuda_ok(cudaGetLastError());
+  b->kz = best_kz;
+  return st;
+}
+
+int grouped_advance(gch_batch* b, int steps, int n_iter) {
+  const int n = (int)b->boxes.size();
+  int st = GCH_OK;
+  k_batch_begin<<<grid_of(n), 128, 0, b->stream>>>(b->sc_list, n, n_iter);
+  st |= cuda_ok(cudaGetLastError());
+  if (!b->kz) st |= autotune(b);
+  const bool fused = b->boxes[0]->cfl_fused;
+  if (fused && !b->cfl_ready) st |= b->gops->cfl(b->boxes.data(), n, b->kz, b->stream);
+  if (!b->graph && !st) {
+    cudaGraph_t g = nullptr;
+    st |= cuda_ok(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
+    st |= b->gops->step(b->boxes.data(), n, b->kz, b->stream);
+    st |= cuda_ok(cudaStreamEndCapture(b->stream, &g));
+    if (st == GCH_OK) st |= cuda_ok(cudaGraphInstantiate(&b->graph, g, 0));
+    if (g) cudaGraphDestroy(g);
+  }
+  if (st) return st;
+  for (int s = 0; s < steps; ++s) st |= cuda_ok(cudaGraphLaunch(b->graph, b->stream));
+  b->cfl_ready = fused;  // the last step's stage-2 CT left the CFL minima
+  k_batch_gather<<<grid_of(n), 128, 0, b->stream>>>(b->sc_list, n, b->sc_all);
+  st |= cuda_ok(cudaMemcpyAsync(b->sc_all_host, b->sc_all, n * sizeof(StepScalars),
+                                cudaMemcpyDeviceToHost, b->stream));
+  st |= cuda_ok(cudaStreamSynchronize(b->stream));
+  for (int i = 0; i < n; ++i) {
+    b->time[i] = b->sc_all_host[i].time;
+    b->iter[i] = b->sc_all_host[i].iter;
+    st |= b->sc_all_host[i].err;
+  }
+  return st;
+}
+
+}  // namespace
 
 extern "C" {
 
 int gch_batch_destroy(gch_batch_t* b) {
   if (!b) return GCH_OK;
+  if (b->stream) cudaStreamSynchronize(b->stream);
+  if (b->graph) cudaGraphExecDestroy(b->graph);
+  cudaFree(b->sc_list);
+  cudaFree(b->sc_all);
+  if (b->sc_all_host) cudaFreeHost(b->sc_all_host);
+  if (b->stream && b->own_stream) cudaStreamDestroy(b->stream);
   for (gch_domain* d : b->boxes) gch_destroy(d);
   delete b;
   return GCH_OK;
 }
 
 int gch_batch_create(int n, const gch_params_t* params, void* stream, gch_batch_t** out) {
-  (void)stream;  // every box gets its own stream
   if (!out || n < 1 || !params) return GCH_ERR_PARAM;
   *out = nullptr;
+  bool grouped = groupable(params[0]);
   for (int i = 1; i < n; ++i) {
     const gch_params_t& a = params[0];
     const gch_params_t& c = params[i];
@@ -34,6 +178,7 @@ int gch_batch_create(int n, const gch_params_t* params, void* stream, gch_batch_
         c.riemann_solver != a.riemann_solver || c.slope_limiter != a.slope_limiter ||
         c.enable_flux_cd != a.enable_flux_cd || c.cooling != a.cooling)
       return GCH_ERR_PARAM;
+    grouped = grouped && groupable(c);
   }
   gch_batch* b = new (std::nothrow) gch_batch();
   if (!b) return GCH_ERR_CUDA;
@@ -48,25 +193,51 @@ int gch_batch_create(int n, const gch_params_t* params, void* stream, gch_batch_
     b->time.push_back(0.0);
     b->iter.push_back(1);
   }
+  if (grouped) {
+    b->gops = params[0].precision == GCH_FP32_KAHAN ? &gch::kGroupKahan : &gch::kGroupMixed;
+    cudaStream_t s = (cudaStream_t)stream;
+    cudaError_t e = cudaSuccess;
+    if (!s) {  // capture needs a stream other than the legacy default stream
+      e = cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking);
+      b->own_stream = e == cudaSuccess;
+    }
+    b->stream = s;
+    std::vector<StepScalars*> sc(n);
+    for (int i = 0; i < n; ++i) sc[i] = b->boxes[i]->sc;
+    if (e == cudaSuccess) e = cudaMalloc((void**)&b->sc_list, n * sizeof(StepScalars*));
+    if (e == cudaSuccess) e = cudaMalloc((void**)&b->sc_all, n * sizeof(StepScalars));
+    if (e == cudaSuccess) e = cudaMallocHost((void**)&b->sc_all_host, n * sizeof(StepScalars));
+    if (e == cudaSuccess)
+      e = cudaMemcpy(b->sc_list, sc.data(), n * sizeof(StepScalars*), cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) {
+      gch_batch_destroy(b);
+      return GCH_ERR_CUDA;
+    }
+  }
   *out = b;
   return GCH_OK;
 }
 
 int gch_batch_upload(gch_batch_t* b, int box, const double* u) {
   if (!b || box < 0 || box >= (int)b->boxes.size()) return GCH_ERR_PARAM;
+  if (b->stream) cudaStreamSynchronize(b->stream);
   int st = gch_upload(b->boxes[box], u);
   st |= gch_boundaryI(b->boxes[box]);
   st |= gch_calcprim(b->boxes[box]);
+  st |= cuda_ok(cudaStreamSynchronize(b->boxes[box]->stream));
+  b->cfl_ready = false;  // the CFL minima must be formed from the new state
   return st;
 }
 
 int gch_batch_download(gch_batch_t* b, int box, double* u) {
   if (!b || box < 0 || box >= (int)b->boxes.size()) return GCH_ERR_PARAM;
+  if (b->stream) cudaStreamSynchronize(b->stream);
   return gch_download(b->boxes[box], u, nullptr);
 }
 
 int gch_batch_advance(gch_batch_t* b, int steps, int n_iter) {
   if (!b || steps < 0) return GCH_ERR_PARAM;
+  if (b->gops) return grouped_advance(b, steps, n_iter);
   int st = GCH_OK;
   const double inf = 1e300;
   for (size_t i = 0; i < b->boxes.size(); ++i)
@@ -84,6 +255,20 @@ int gch_batch_time(gch_batch_t* b, double* times, int* iters) {
     if (times) times[i] = b->time[i];
     if (iters) iters[i] = b->iter[i];
   }
+  return GCH_OK;
+}
+
+int gch_batch_tuning(gch_batch_t* b, int* grouped, int* kz, int cap, int* cand_kz,
+                     float* cand_ms, int* ncand) {
+  if (!b) return GCH_ERR_PARAM;
+  if (grouped) *grouped = b->gops != nullptr;
+  if (kz) *kz = b->gops ? b->kz : -1;
+  const int m = std::min(cap, (int)b->tune_kz.size());
+  for (int i = 0; i < m; ++i) {
+    if (cand_kz) cand_kz[i] = b->tune_kz[i];
+    if (cand_ms) cand_ms[i] = b->tune_ms[i];
+  }
+  if (ncand) *ncand = m;
   return GCH_OK;
 }
 

@@ -154,6 +154,11 @@ __device__ __forceinline__ double tsqrt(double a) { return sqrt(a); }
 __device__ __forceinline__ float tsqrt(float a) { return sqrtf(a); }
 __device__ __forceinline__ double tabs(double a) { return fabs(a); }
 __device__ __forceinline__ float tabs(float a) { return fabsf(a); }
+// Quotient with a denominator known to lie in [2^-126, 2^126]: the FP32
+// paths use the hardware reciprocal (__fdividef, 2 ulp); FP64 divides
+// exactly as the reference does.
+__device__ __forceinline__ double tdiv_pos(double a, double b) { return a / b; }
+__device__ __forceinline__ float tdiv_pos(float a, float b) { return __fdividef(a, b); }
 
 template <class T>
 __device__ __forceinline__ bool has_b(const KParams& p) { return p.neq >= 8; }
@@ -236,10 +241,12 @@ __device__ __forceinline__ T average(int lim, T a, T b) {
       s = tcopysign(T(1), a);
       return s * tmax_(T(0), tmin_(tabs(a), s * b));
     case GCH_LIMITER_VAN_LEER:
+      // a*b > 0 (a normal number after FTZ) bounds a*a + b*b >= 2ab from
+      // below; above, it is at most 2^126 while |a|, |b| < 6e18
       if (a * b <= T(0)) return T(0);
-      return a * b * (a + b) / (a * a + b * b);
+      return tdiv_pos(a * b * (a + b), a * a + b * b);
     case GCH_LIMITER_VAN_ALBADA:
-      return (a * (b * b + delta) + b * (a * a + delta)) / (a * a + b * b + delta);
+      return tdiv_pos(a * (b * b + delta) + b * (a * a + delta), a * a + b * b + delta);
     case GCH_LIMITER_UMIST:
       s = tcopysign(T(1), a);
       c = T(0.25) * a + T(0.75) * b;

@@ -67,11 +67,28 @@ struct EngineOps {
   int (*download_prim)(gch_domain*);  // primit -> stage
   int (*loopfin)(gch_domain*);        // device time-loop tail
   int (*cfl)(gch_domain*);            // CFL min of the current u only
+  int (*probe)(gch_domain*);          // stage-1 fluxes alone (autotuner)
 };
 
 extern const EngineOps kEngineFP64;
 extern const EngineOps kEngineMixed;
 extern const EngineOps kEngineKahan;
+
+// Grouped launches over many boxes of one precision (gch_group.cuh).  The
+// boxes share solver, neq, limiter and flux-CD, have no table cooling,
+// resistivity or user spheres, and are advanced on one stream.
+struct GroupOps {
+  // CFL min of the current u of every box (k_cfl)
+  int (*cfl)(gch_domain* const* boxes, int n, int kz, cudaStream_t s);
+  // one device-resident iteration of every box: [k_cfl], k_dtfin, both
+  // stages with their CT and ghost fills, k_loopfin
+  int (*step)(gch_domain* const* boxes, int n, int kz, cudaStream_t s);
+  // the stage-1 flux kernel alone (writes up and E, leaves u): the
+  // autotuner's timing probe
+  int (*probe)(gch_domain* const* boxes, int n, int kz, cudaStream_t s);
+};
+extern const GroupOps kGroupMixed;
+extern const GroupOps kGroupKahan;
 
 }  // namespace gch
 

@@ -228,9 +228,16 @@ struct Engine {
     return cuda_status(cudaGetLastError());
   }
 
+  // the stage-1 flux kernel alone: it writes the stage arrays up and E and
+  // leaves u and primit unchanged (the autotuner times it)
+  static int probe(gch_domain* d) {
+    int st = d->prim_in ? flux<1, true>(d, d->primit, d->up) : flux<1, false>(d, d->u, d->up);
+    return st | cuda_status(cudaGetLastError());
+  }
+
   static constexpr EngineOps ops() {
     return EngineOps{&get_dt, &tstep, &boundaryI, &calcprim,
-                     &upload, &download_u, &download_prim, &loopfin, &cfl};
+                     &upload, &download_u, &download_prim, &loopfin, &cfl, &probe};
   }
 };
 

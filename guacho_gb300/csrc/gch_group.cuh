@@ -1,0 +1,103 @@
+// gch_group.cuh -- grouped launches: one kernel launch advances a stage of
+// many independent boxes of uneven size.
+//
+// Every box keeps its own arrays, parameters and StepScalars (its own CFL
+// dt).  A grouped launch carries the per-box parameter blocks in its kernel
+// parameter space (__grid_constant__, up to kGroupMax boxes, 22 KB) and a
+// one-dimensional grid: block b belongs to the box whose first block blk0
+// is the largest one <= b, and is decoded to that box's tile coordinates.
+// The per-box bodies are the ones of the one-box kernels, so a box computes
+// exactly what it computes alone.
+#pragma once
+
+#include "gch_kernels.cuh"
+
+namespace gch {
+
+constexpr int kGroupMax = 64;  // boxes per grouped launch
+
+struct GroupBox {
+  KParams p;
+  const void* a0;  // kernel-specific arrays (see GroupEngine)
+  const void* a1;
+  void* a2;
+  void* a3;
+  void* a4;
+  StepScalars* sc;
+  int blk0;        // first linear block of this box in the launch
+  int gx, gy;      // blocks along the two fastest grid axes of the box
+  int kz;          // z planes per block (stage and CT kernels)
+};
+
+struct GroupArgs {
+  int nbox;
+  int i0, i1;      // kernel-specific integers (ghost fill: axis, layers)
+  GroupBox box[kGroupMax];
+};
+static_assert(sizeof(GroupArgs) <= 32000, "grouped launch exceeds the kernel parameter limit");
+
+// the box owning linear block `blk` (binary search over blk0)
+__device__ __forceinline__ int group_box(const GroupArgs& g, int blk) {
+  int lo = 0, hi = g.nbox - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (g.box[mid].blk0 <= blk) lo = mid;
+    else hi = mid - 1;
+  }
+  return lo;
+}
+
+// a0 = stage source, a1 = u, a2 = stage destination, a3 = E, a4 = s678
+template <class Pol, int SOLVER, int NEQ, int STAGE, int LIM>
+__global__ void __launch_bounds__(NT, Pol::kMinBlocks) k_flux_grp(const __grid_constant__ GroupArgs g) {
+  using TIn = typename Src<Pol, NEQ, STAGE, false>::TIn;
+  using TD = typename std::conditional<STAGE == 1, typename Pol::TS, typename Pol::TU>::type;
+  const GroupBox& x = g.box[group_box(g, blockIdx.x)];
+  const int l = blockIdx.x - x.blk0;
+  flux_body<Pol, SOLVER, NEQ, STAGE, false, LIM>(
+      x.p, (const TIn*)x.a0, (const typename Pol::TU*)x.a1, (TD*)x.a2, (typename Pol::TS*)x.a3,
+      (typename Pol::TS*)x.a4, x.sc, x.kz, l % x.gx, (l / x.gx) % x.gy, l / (x.gx * x.gy));
+}
+
+// a1 = u, a2 = destination of B, a3 = E, a4 = s678
+template <class Pol, int STAGE, bool CFL>
+__global__ void __launch_bounds__(256) k_ct_grp(const __grid_constant__ GroupArgs g) {
+  using TD = typename std::conditional<STAGE == 1, typename Pol::TS, typename Pol::TU>::type;
+  const GroupBox& x = g.box[group_box(g, blockIdx.x)];
+  const int l = blockIdx.x - x.blk0;
+  ct_body<Pol, STAGE, CFL>(x.p, (const typename Pol::TU*)x.a1, (TD*)x.a2,
+                           (const typename Pol::TS*)x.a3, (const typename Pol::TS*)x.a4, x.sc,
+                           x.kz, l % x.gx, (l / x.gx) % x.gy, l / (x.gx * x.gy));
+}
+
+// a2 = the array to fill; i0 = axis, i1 = layers
+template <class T>
+__global__ void __launch_bounds__(128) k_ghost_grp(const __grid_constant__ GroupArgs g) {
+  const GroupBox& x = g.box[group_box(g, blockIdx.x)];
+  const int l = blockIdx.x - x.blk0;
+  ghost_body<T>(x.p, (T*)x.a2, x.p.neq, g.i0, g.i1, x.sc, l % x.gx, (l / x.gx) % x.gy,
+                l / (x.gx * x.gy));
+}
+
+// a1 = u
+template <class Pol, int NEQ>
+__global__ void __launch_bounds__(256) k_cfl_grp(const __grid_constant__ GroupArgs g) {
+  const GroupBox& x = g.box[group_box(g, blockIdx.x)];
+  const int l = blockIdx.x - x.blk0;
+  cfl_body<Pol, NEQ, false>(x.p, (const typename Pol::TU*)x.a1, x.sc, x.kz, l % x.gx,
+                            (l / x.gx) % x.gy, l / (x.gx * x.gy));
+}
+
+// one thread per box
+static __global__ void k_dtfin_grp(const __grid_constant__ GroupArgs g) {
+  const int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= g.nbox) return;
+  const KParams& p = g.box[b].p;
+  dtfin_body(g.box[b].sc, p.cfl, p.dx, p.dy, p.dz);
+}
+static __global__ void k_loopfin_grp(const __grid_constant__ GroupArgs g) {
+  const int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b < g.nbox) loopfin_body(g.box[b].sc);
+}
+
+}  // namespace gch

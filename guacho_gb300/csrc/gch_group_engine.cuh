@@ -1,0 +1,198 @@
+// gch_group_engine.cuh -- launch orchestration of one timestep of many boxes
+// with grouped kernels (gch_group.cuh): one launch per kernel of the step
+// for up to kGroupMax boxes, whatever their sizes.  Included by exactly one
+// translation unit per FP32 policy, which defines that policy's GroupOps.
+#pragma once
+
+#include <algorithm>
+#include <climits>
+#include <cstring>
+#include <memory>
+
+#include "gch_engine.cuh"
+#include "gch_group.cuh"
+
+namespace gch {
+
+template <class Pol>
+struct GroupEngine {
+  using TU = typename Pol::TU;
+  using TS = typename Pol::TS;
+  using TC = typename Ops<Pol>::TC;
+  static constexpr int kzc = Engine<Pol>::kzc;
+
+  // Fill the argument block of each chunk of <= kGroupMax boxes and launch
+  // it: setup(GroupBox&, box) fills the kernel-specific fields and returns
+  // the box's block count; launch(GroupArgs&, total blocks) issues the kernel.
+  template <class Setup, class Launch>
+  static int chunks(gch_domain* const* boxes, int n, Setup setup, Launch launch) {
+    std::unique_ptr<GroupArgs> g(new GroupArgs);
+    for (int c0 = 0; c0 < n; c0 += kGroupMax) {
+      const int m = std::min(kGroupMax, n - c0);
+      std::memset(g.get(), 0, sizeof(GroupArgs));
+      g->nbox = m;
+      long long blocks = 0;
+      for (int i = 0; i < m; ++i) {
+        GroupBox& x = g->box[i];
+        gch_domain* d = boxes[c0 + i];
+        x.p = d->kp;
+        x.sc = d->sc;
+        x.blk0 = (int)blocks;
+        blocks += setup(x, d);
+        if (blocks > INT_MAX) return GCH_ERR_TOO_LARGE;
+      }
+      launch(*g, (unsigned)blocks);
+    }
+    return cuda_status(cudaGetLastError());
+  }
+
+  // ---- stage kernels ---------------------------------------------------------
+  template <int SOLVER, int NEQ, int STAGE, int LIM>
+  static void flux_lim(GroupArgs& g, unsigned blocks, cudaStream_t s) {
+    constexpr size_t smem = sizeof(FluxSmem<TC, NEQ, STAGE>);
+    static bool attr = false;  // once per instantiation
+    if (!attr) {
+      cudaFuncSetAttribute(k_flux_grp<Pol, SOLVER, NEQ, STAGE, LIM>,
+                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      attr = true;
+    }
+    if (blocks) k_flux_grp<Pol, SOLVER, NEQ, STAGE, LIM><<<blocks, dim3(TX, TY), smem, s>>>(g);
+  }
+  template <int SOLVER, int NEQ, int STAGE>
+  static void flux_solver(GroupArgs& g, unsigned blocks, cudaStream_t s, int lim) {
+    if (STAGE == 1) flux_lim<SOLVER, NEQ, STAGE, kLimRuntime>(g, blocks, s);
+    else if (lim == GCH_LIMITER_MINMOD) flux_lim<SOLVER, NEQ, STAGE, GCH_LIMITER_MINMOD>(g, blocks, s);
+    else if (lim == GCH_LIMITER_VAN_LEER) flux_lim<SOLVER, NEQ, STAGE, GCH_LIMITER_VAN_LEER>(g, blocks, s);
+    else flux_lim<SOLVER, NEQ, STAGE, kLimRuntime>(g, blocks, s);
+  }
+  template <int STAGE>
+  static int flux(gch_domain* const* boxes, int n, int kz, cudaStream_t s) {
+    const KParams& p0 = boxes[0]->kp;
+    const int sv = p0.solver, neq = p0.neq, lim = p0.limiter;
+    auto setup = [&](GroupBox& x, gch_domain* d) -> long long {
+      const KParams& p = d->kp;
+      x.a0 = STAGE == 1 ? d->u : d->up;  // u, or up for the second half step
+      x.a1 = d->u;
+      x.a2 = STAGE == 1 ? d->up : d->u;
+      x.a3 = d->E;
+      x.a4 = d->s678;
+      x.kz = std::max(1, std::min(kz, p.nz));
+      x.gx = (p.nx + TX - 1) / TX;
+      x.gy = (p.ny + TY - 1) / TY;
+      return (long long)x.gx * x.gy * ((p.nz + x.kz - 1) / x.kz);
+    };
+    auto go = [&](auto launch) { return chunks(boxes, n, setup, launch); };
+    if (sv == GCH_SOLVER_HLLD && neq == 8)
+      return go([&](GroupArgs& g, unsigned b) { flux_solver<GCH_SOLVER_HLLD, 8, STAGE>(g, b, s, lim); });
+    if (sv == GCH_SOLVER_HLLC && neq == 5)
+      return go([&](GroupArgs& g, unsigned b) { flux_solver<GCH_SOLVER_HLLC, 5, STAGE>(g, b, s, lim); });
+    if (sv == GCH_SOLVER_HLLC && neq == 8)
+      return go([&](GroupArgs& g, unsigned b) { flux_solver<GCH_SOLVER_HLLC, 8, STAGE>(g, b, s, lim); });
+    if (sv == GCH_SOLVER_HLLE && neq == 8)
+      return go([&](GroupArgs& g, unsigned b) { flux_solver<GCH_SOLVER_HLLE, 8, STAGE>(g, b, s, lim); });
+    if (sv == GCH_SOLVER_HLL && neq == 5)
+      return go([&](GroupArgs& g, unsigned b) { flux_solver<GCH_SOLVER_HLL, 5, STAGE>(g, b, s, lim); });
+    if (sv == GCH_SOLVER_HLL && neq == 8)
+      return go([&](GroupArgs& g, unsigned b) { flux_solver<GCH_SOLVER_HLL, 8, STAGE>(g, b, s, lim); });
+    return GCH_ERR_PARAM;
+  }
+
+  // column-marching cell kernels: tile 32 x 8, kzc planes per block
+  static long long column_setup(GroupBox& x, const KParams& p) {
+    x.kz = kzc;
+    x.gx = (p.nx + 31) / 32;
+    x.gy = (p.ny + 7) / 8;
+    return (long long)x.gx * x.gy * ((p.nz + kzc - 1) / kzc);
+  }
+
+  template <int STAGE, bool CFL>
+  static int ct(gch_domain* const* boxes, int n, cudaStream_t s) {
+    return chunks(
+        boxes, n,
+        [&](GroupBox& x, gch_domain* d) {
+          x.a1 = d->u;
+          x.a2 = STAGE == 1 ? d->up : d->u;
+          x.a3 = d->E;
+          x.a4 = d->s678;
+          return column_setup(x, d->kp);
+        },
+        [&](GroupArgs& g, unsigned b) {
+          if (b) k_ct_grp<Pol, STAGE, CFL><<<b, dim3(32, 8), 0, s>>>(g);
+        });
+  }
+
+  template <class T>
+  static int ghost(gch_domain* const* boxes, int n, bool on_up, int layers, cudaStream_t s) {
+    int st = GCH_OK;
+    for (int axis = 0; axis < 3; ++axis) {
+      st |= chunks(
+          boxes, n,
+          [&](GroupBox& x, gch_domain* d) -> long long {
+            const KParams& p = d->kp;
+            x.a2 = on_up ? d->up : d->u;
+            const int N0 = axis == 0 ? p.NY : p.NX;
+            const int N1 = axis == 2 ? p.NY : p.NZ;
+            x.gx = (N0 + 127) / 128;
+            x.gy = N1;
+            return (long long)x.gx * N1 * 2 * layers;
+          },
+          [&](GroupArgs& g, unsigned b) {
+            g.i0 = axis;
+            g.i1 = layers;
+            if (b) k_ghost_grp<T><<<b, 128, 0, s>>>(g);
+          });
+    }
+    return st;
+  }
+
+  static int cfl(gch_domain* const* boxes, int n, int, cudaStream_t s) {
+    const int neq = boxes[0]->kp.neq;
+    return chunks(
+        boxes, n,
+        [&](GroupBox& x, gch_domain* d) {
+          x.a1 = d->u;
+          return column_setup(x, d->kp);
+        },
+        [&](GroupArgs& g, unsigned b) {
+          if (!b) return;
+          if (neq == 8) k_cfl_grp<Pol, 8><<<b, dim3(32, 8), 0, s>>>(g);
+          else k_cfl_grp<Pol, 5><<<b, dim3(32, 8), 0, s>>>(g);
+        });
+  }
+
+  static int scalar_tail(gch_domain* const* boxes, int n, bool loop_tail, cudaStream_t s) {
+    return chunks(
+        boxes, n, [](GroupBox&, gch_domain*) { return 0LL; },
+        [&](GroupArgs& g, unsigned) {
+          if (loop_tail) k_loopfin_grp<<<1, kGroupMax, 0, s>>>(g);
+          else k_dtfin_grp<<<1, kGroupMax, 0, s>>>(g);
+        });
+  }
+
+  // get_timestep + tstep + the loop tail of every box (Engine<Pol>::get_dt,
+  // tstep and loopfin with resistivity, table cooling and spheres absent)
+  static int step(gch_domain* const* boxes, int n, int kz, cudaStream_t s) {
+    const KParams& p0 = boxes[0]->kp;
+    const bool ctp = p0.neq >= 8 && p0.flux_cd;
+    const bool fused = boxes[0]->cfl_fused;
+    int st = GCH_OK;
+    if (!fused) st |= cfl(boxes, n, kz, s);
+    st |= scalar_tail(boxes, n, false, s);
+    st |= flux<1>(boxes, n, kz, s);
+    if (ctp) st |= ct<1, false>(boxes, n, s);
+    st |= ghost<TS>(boxes, n, true, 2, s);
+    st |= flux<2>(boxes, n, kz, s);
+    if (ctp) st |= fused ? ct<2, true>(boxes, n, s) : ct<2, false>(boxes, n, s);
+    st |= ghost<TU>(boxes, n, false, 1, s);
+    st |= scalar_tail(boxes, n, true, s);
+    return st;
+  }
+
+  static int probe(gch_domain* const* boxes, int n, int kz, cudaStream_t s) {
+    return flux<1>(boxes, n, kz, s);
+  }
+
+  static constexpr GroupOps ops() { return GroupOps{&cfl, &step, &probe}; }
+};
+
+}  // namespace gch

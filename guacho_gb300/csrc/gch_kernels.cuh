@@ -72,34 +72,35 @@ struct FluxSmem {
 // Column state (the next planes, z slopes, z fluxes) lives in shared
 // memory slots owned by one thread, which keeps registers for the solver.
 // Fluxes are never written to global memory.
+// The body takes the block's tile coordinates (bx, by) and z chunk (bz) as
+// arguments: the one-box kernel passes blockIdx, the grouped kernel of many
+// boxes passes the coordinates decoded from its linear block index.
 template <class Pol, int SOLVER, int NEQ, int STAGE, bool PRIM_IN, int LIM>
-__global__ void __launch_bounds__(NT, Pol::kMinBlocks)
-k_flux(KParams p, const typename Src<Pol, NEQ, STAGE, PRIM_IN>::TIn* __restrict__ src,
-       const typename Pol::TU* u,
-       typename std::conditional<STAGE == 1, typename Pol::TS, typename Pol::TU>::type* dst,
-       typename Pol::TS* __restrict__ E, typename Pol::TS* __restrict__ s678,
-       StepScalars* sc, int kz) {
+__device__ __forceinline__ void
+flux_body(const KParams& p, const typename Src<Pol, NEQ, STAGE, PRIM_IN>::TIn* __restrict__ src,
+          const typename Pol::TU* u,
+          typename std::conditional<STAGE == 1, typename Pol::TS, typename Pol::TU>::type* dst,
+          typename Pol::TS* __restrict__ E, typename Pol::TS* __restrict__ s678,
+          StepScalars* sc, int kz, int bx, int by, int bz) {
   using TC = typename Ops<Pol>::TC;
   using TD = typename std::conditional<STAGE == 1, typename Pol::TS, typename Pol::TU>::type;
   using S = Src<Pol, NEQ, STAGE, PRIM_IN>;
   if (!sc->active) return;
   constexpr int H = STAGE == 1 ? 1 : 2;
-  constexpr int PW = TX + 2 * H;
-  constexpr int PH = TY + 2 * H;
   constexpr int NRING = 2 * H * (TX + TY);
   using SM = FluxSmem<TC, NEQ, STAGE>;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   SM& sm = *reinterpret_cast<SM*>(smem_raw);
   auto& sP = sm.P;    // primitive plane k with halo
-  auto& sF = sm.F;    // x-face fluxes (prologue: left z states)
-  auto& sG = sm.G;    // y-face fluxes (prologue: right z states)
+  auto& sF = sm.F;    // x-face fluxes
+  auto& sG = sm.G;    // y-face fluxes
   auto& sH = sm.Hz;   // z-face fluxes, slot (face+1/2)&1
-  auto& sQ = sm.Q;    // column ring: [0] p(k+1), [1] p(k+2), [2] p(k-1)
+  auto& sQ = sm.Q;    // column ring: [0] p(k+1), [1] p(k+2), [2] z slope of p(k)
 
   const int tx = threadIdx.x, ty = threadIdx.y;
   const int tid = ty * TX + tx;
-  const int i0 = blockIdx.x * TX, j0 = blockIdx.y * TY;
-  const int kb = blockIdx.z * kz;
+  const int i0 = bx * TX, j0 = by * TY;
+  const int kb = bz * kz;
   const int ke = min(p.nz, kb + kz);
   const int ci = i0 + tx, cj = j0 + ty;
   const bool active = ci < p.nx && cj < p.ny;
@@ -124,65 +125,39 @@ k_flux(KParams p, const typename Src<Pol, NEQ, STAGE, PRIM_IN>::TIn* __restrict_
   const int axc = ci + NG, ayc = cj + NG;
   TC bzm = 0;  // Bz at k-1 of this column (eight-wave div B)
 
-  // ---- column prologue: states of the z face kb-1/2 -----------------------
-  {
-    TC a[NEQ], b[NEQ], c[NEQ];
-    if (STAGE == 1) {
-      S::load(p, src, gidx(axc, ayc, kb - 1 + NG), a, pfl);
-      S::load(p, src, gidx(axc, ayc, kb + NG), b, pfl);
-#pragma unroll
-      for (int q = 0; q < NEQ; ++q) {
-        sF[q][ty][tx] = a[q];
-        sG[q][ty][tx] = b[q];
-        sQ[0][q][ty][tx] = b[q];
-      }
-      if (NEQ >= 8) bzm = a[7];
-    } else {
-      S::load(p, src, gidx(axc, ayc, kb - 2 + NG), a, pfl);
-      S::load(p, src, gidx(axc, ayc, kb - 1 + NG), b, pfl);
-      S::load(p, src, gidx(axc, ayc, kb + NG), c, pfl);
-      if (NEQ >= 8) bzm = b[7];
-#pragma unroll
-      for (int q = 0; q < NEQ; ++q) {
-        const TC sm1 = average_t<LIM>(lim, b[q] - a[q], c[q] - b[q]);
-        sF[q][ty][tx] = b[q] + sm1 * TC(0.5);
-        sQ[2][q][ty][tx] = b[q];
-        sQ[0][q][ty][tx] = c[q];
-      }
-      S::load(p, src, gidx(axc, ayc, kb + 1 + NG), a, pfl);  // a = p(kb+1)
-#pragma unroll
-      for (int q = 0; q < NEQ; ++q) {
-        const TC s0 = average_t<LIM>(lim, c[q] - b[q], a[q] - c[q]);
-        sG[q][ty][tx] = c[q] - s0 * TC(0.5);
-        sQ[1][q][ty][tx] = a[q];
-      }
-    }
-  }
-
+  // The march starts before kb so that every plane's column values, z
+  // slopes and z faces come from the same code as in the body of the march
+  // (one inlined instance each): the results of a plane do not depend on
+  // where a z chunk begins.  Iteration k loads p(k+H) into the column ring;
+  // stage 2 forms the z slope of p(k+1) from k >= kb-2 on; the z face k+1/2
+  // is solved from k >= kb-1 on; planes k >= kb are staged and updated.
+  const int k0 = kb - (STAGE == 1 ? 2 : 4);
   const int nfx = (TX + 1) * TY;
   const int nfy = TX * (TY + 1);
-  for (int k = kb - 1; k < ke; ++k) {
-    const bool pro = k < kb;
+  for (int k = k0; k < ke; ++k) {
+    const bool plane = k >= kb;
+    const bool zface = k >= kb - 1;
+    const bool zwork = STAGE == 1 ? zface : k >= kb - 2;
     const int az = k + NG;
-    if (!pro) {
-      __syncthreads();  // readers of the previous plane are done
-      // 1. plane k: the ring shifts (p(k-1) <- centre, centre <- p(k),
-      //    p(k+1) <- p(k+2)) and the next plane is formed from global memory
-      {
-        TC nx_[NEQ];
-        S::load(p, src, gidx(axc, ayc, az + (STAGE == 1 ? 1 : 2)), nx_, pfl);
+    if (plane) __syncthreads();  // readers of the previous plane are done
+    // 1. the column ring shifts (centre <- p(k), p(k+1) <- p(k+2)) and the
+    //    next plane of the column is formed from global memory
+    {
+      TC nx_[NEQ];
+      S::load(p, src, gidx(axc, ayc, az + H), nx_, pfl);
 #pragma unroll
-        for (int q = 0; q < NEQ; ++q) {
-          if (STAGE == 2 && k > kb) sQ[2][q][ty][tx] = sP[q][ty + H][tx + H];
-          sP[q][ty + H][tx + H] = sQ[0][q][ty][tx];
-          if (STAGE == 1) {
-            sQ[0][q][ty][tx] = nx_[q];
-          } else {
-            sQ[0][q][ty][tx] = sQ[1][q][ty][tx];
-            sQ[1][q][ty][tx] = nx_[q];
-          }
+      for (int q = 0; q < NEQ; ++q) {
+        sP[q][ty + H][tx + H] = sQ[0][q][ty][tx];
+        if (STAGE == 1) {
+          sQ[0][q][ty][tx] = nx_[q];
+        } else {
+          sQ[0][q][ty][tx] = sQ[1][q][ty][tx];
+          sQ[1][q][ty][tx] = nx_[q];
         }
       }
+    }
+    if (plane) {
+      //  the halo of plane k from global memory
       for (int r = tid; r < NRING; r += NT) {
         int hx, hy;
         if (r < 2 * H * TX) {  // rows below / above the tile
@@ -204,7 +179,7 @@ k_flux(KParams p, const typename Src<Pol, NEQ, STAGE, PRIM_IN>::TIn* __restrict_
     }
 
     // 2. all faces through one Riemann call site
-    const int nwork = pro ? NT : NT + nfx + nfy;
+    const int nwork = plane ? NT + nfx + nfy : (zwork ? NT : 0);
     const int hslot = (k + 1) & 1;  // face k+1/2
     for (int w = tid; w < nwork; w += NT) {
       int kind;  // 0 = z (own column), 1 = x, 2 = y
@@ -226,31 +201,29 @@ k_flux(KParams p, const typename Src<Pol, NEQ, STAGE, PRIM_IN>::TIn* __restrict_
       if (!need) continue;
       TC l[NEQ], r[NEQ], f[NEQ];
       if (kind == 0) {
-        if (pro) {
-#pragma unroll
-          for (int q = 0; q < NEQ; ++q) {
-            l[q] = sF[perm<2>(q)][ty][tx];
-            r[q] = sG[perm<2>(q)][ty][tx];
-          }
-        } else if (STAGE == 1) {
+        if (STAGE == 1) {
 #pragma unroll
           for (int q = 0; q < NEQ; ++q) {
             l[q] = sP[perm<2>(q)][ty + H][tx + H];
             r[q] = sQ[0][perm<2>(q)][ty][tx];
           }
         } else {
-          // limiter on p(k-1), p(k), p(k+1), p(k+2)
+          // the slope of p(k) comes from the ring (formed by the previous
+          // iteration); the slope of p(k+1) from p(k..k+2) is formed here
+          // once and kept for face k+3/2
 #pragma unroll
           for (int q = 0; q < NEQ; ++q) {
             const int s = perm<2>(q);
-            const TC ll = sQ[2][s][ty][tx], rr = sQ[1][s][ty][tx];
+            const TC al = sQ[2][s][ty][tx], rr = sQ[1][s][ty][tx];
             l[q] = sP[s][ty + H][tx + H];
             r[q] = sQ[0][s][ty][tx];
-            const TC dl = l[q] - ll, dm = r[q] - l[q], dr = rr - r[q];
-            const TC al = average_t<LIM>(lim, dl, dm), ar = average_t<LIM>(lim, dm, dr);
+            const TC dm = r[q] - l[q], dr = rr - r[q];
+            const TC ar = average_t<LIM>(lim, dm, dr);
+            sQ[2][s][ty][tx] = ar;
             l[q] = l[q] + al * TC(0.5);
             r[q] = r[q] - ar * TC(0.5);
           }
+          if (!zface) continue;  // slope of p(kb-1) only
         }
       } else if (kind == 1) {
         const int cy = fy + H, cl = fx - 1 + H;
@@ -294,7 +267,10 @@ k_flux(KParams p, const typename Src<Pol, NEQ, STAGE, PRIM_IN>::TIn* __restrict_
         for (int q = 0; q < NEQ; ++q) sG[perm<1>(q)][fy][fx] = f[q];
       }
     }
-    if (pro) continue;  // z states of the prologue were private: no barrier
+    if (!plane) {  // column-private work only: no barrier
+      if (NEQ >= 8) bzm = sP[7][ty + H][tx + H];
+      continue;
+    }
     __syncthreads();
 
     // 3. cell update and E
@@ -376,6 +352,17 @@ k_flux(KParams p, const typename Src<Pol, NEQ, STAGE, PRIM_IN>::TIn* __restrict_
   }
   raise_err(&sc->err, err);
 }
+
+template <class Pol, int SOLVER, int NEQ, int STAGE, bool PRIM_IN, int LIM>
+__global__ void __launch_bounds__(NT, Pol::kMinBlocks)
+k_flux(KParams p, const typename Src<Pol, NEQ, STAGE, PRIM_IN>::TIn* __restrict__ src,
+       const typename Pol::TU* u,
+       typename std::conditional<STAGE == 1, typename Pol::TS, typename Pol::TU>::type* dst,
+       typename Pol::TS* __restrict__ E, typename Pol::TS* __restrict__ s678,
+       StepScalars* sc, int kz) {
+  flux_body<Pol, SOLVER, NEQ, STAGE, PRIM_IN, LIM>(p, src, u, dst, E, s678, sc, kz, blockIdx.x,
+                                                   blockIdx.y, blockIdx.z);
+}
 // min(dx/(|vx|+cfx), dy/(|vy|+cfy), dz/(|vz|+cfz)) of one cell into dtp
 template <class TC, int NEQ>
 __device__ __forceinline__ void cfl_candidate(const KParams& p, const TC* pr, double& dtp,
@@ -428,17 +415,17 @@ __device__ __forceinline__ void cfl_block_reduce(double dtp, int bad, StepScalar
 // Constrained transport of B (src/flux_cd_module.f90:311-321) with the E
 // ghost layer of boundaryI_ef (:45-237) applied as an index map.
 template <class Pol, int STAGE, bool CFL>
-__global__ void __launch_bounds__(256)
-k_ct(KParams p, const typename Pol::TU* u,
-     typename std::conditional<STAGE == 1, typename Pol::TS, typename Pol::TU>::type* dst,
-     const typename Pol::TS* __restrict__ E, const typename Pol::TS* __restrict__ s678,
-     StepScalars* sc, int kz) {
+__device__ __forceinline__ void
+ct_body(const KParams& p, const typename Pol::TU* u,
+        typename std::conditional<STAGE == 1, typename Pol::TS, typename Pol::TU>::type* dst,
+        const typename Pol::TS* __restrict__ E, const typename Pol::TS* __restrict__ s678,
+        StepScalars* sc, int kz, int bx, int by, int bz) {
   using TC = typename Ops<Pol>::TC;
   using TD = typename std::conditional<STAGE == 1, typename Pol::TS, typename Pol::TU>::type;
   if (!sc->active) return;
-  const int ci = blockIdx.x * blockDim.x + threadIdx.x;
-  const int cj = blockIdx.y * blockDim.y + threadIdx.y;
-  const int kb = blockIdx.z * kz;
+  const int ci = bx * 32 + threadIdx.x;
+  const int cj = by * 8 + threadIdx.y;
+  const int kb = bz * kz;
   const int ke = min(p.nz, kb + kz);
   const bool active = ci < p.nx && cj < p.ny;
   if (!CFL && !active) return;
@@ -526,15 +513,26 @@ k_ct(KParams p, const typename Pol::TU* u,
   if constexpr (CFL && STAGE == 2) cfl_block_reduce(dtp, bad, sc);
 }
 
+// block (32, 8); grid (ceil(nx/32), ceil(ny/8), ceil(nz/kz))
+template <class Pol, int STAGE, bool CFL>
+__global__ void __launch_bounds__(256)
+k_ct(KParams p, const typename Pol::TU* u,
+     typename std::conditional<STAGE == 1, typename Pol::TS, typename Pol::TU>::type* dst,
+     const typename Pol::TS* __restrict__ E, const typename Pol::TS* __restrict__ s678,
+     StepScalars* sc, int kz) {
+  ct_body<Pol, STAGE, CFL>(p, u, dst, E, s678, sc, kz, blockIdx.x, blockIdx.y, blockIdx.z);
+}
+
 // ---------------------------------------------------------------------------
 // Ghost fill of one axis (src/boundaries.f90:44-512): `layers` ghost layers
 // on both sides of `axis`, over the whole transverse extent.
 template <class T>
-__global__ void k_ghost(KParams p, T* a, int neq, int axis, int layers, const StepScalars* sc) {
+__device__ __forceinline__ void ghost_body(const KParams& p, T* a, int neq, int axis, int layers,
+                                           const StepScalars* sc, int bx, int by, int bz) {
   if (!sc->active) return;
-  const int t0 = blockIdx.x * blockDim.x + threadIdx.x;  // transverse fast index
-  const int t1 = blockIdx.y;                              // transverse slow index
-  const int side_layer = blockIdx.z;                      // 2*layers entries
+  const int t0 = bx * 128 + threadIdx.x;  // transverse fast index
+  const int t1 = by;                      // transverse slow index
+  const int side_layer = bz;              // 2*layers entries
   const int side = side_layer & 1;
   const int l = side_layer >> 1;
   int n, N0, N1, blo, bhi;
@@ -557,6 +555,12 @@ __global__ void k_ghost(KParams p, T* a, int neq, int axis, int layers, const St
     if (flip && q == axis + 1) v = neg(v);
     a[q * p.fs + di] = v;
   }
+}
+
+// block 128; grid (ceil(N0/128), N1, 2*layers) over the transverse extent
+template <class T>
+__global__ void k_ghost(KParams p, T* a, int neq, int axis, int layers, const StepScalars* sc) {
+  ghost_body<T>(p, a, neq, axis, layers, sc, blockIdx.x, blockIdx.y, blockIdx.z);
 }
 
 // User boundary spheres (EXO/exoplanet.f90:125-266 pattern) over the box
@@ -633,14 +637,15 @@ __global__ void k_user_bc(KParams p, T* a, int neq, const StepScalars* sc) {
 // shuffle min, one atomicMin per block on the bits of the positive double.
 
 template <class Pol, int NEQ, bool PRIM_IN>
-__global__ void __launch_bounds__(256)
-k_cfl(KParams p, const typename std::conditional<PRIM_IN, typename Pol::TS, typename Pol::TU>::type* src,
-      StepScalars* sc, int kz) {
+__device__ __forceinline__ void
+cfl_body(const KParams& p,
+         const typename std::conditional<PRIM_IN, typename Pol::TS, typename Pol::TU>::type* src,
+         StepScalars* sc, int kz, int bx, int by, int bz) {
   using TC = typename Ops<Pol>::TC;
   if (!sc->active) return;
-  const int ci = blockIdx.x * blockDim.x + threadIdx.x;
-  const int cj = blockIdx.y * blockDim.y + threadIdx.y;
-  const int kb = blockIdx.z * kz;
+  const int ci = bx * 32 + threadIdx.x;
+  const int cj = by * 8 + threadIdx.y;
+  const int kb = bz * kz;
   const int ke = min(p.nz, kb + kz);
   double dtp = 1e30;
   int bad = 0;
@@ -660,9 +665,18 @@ k_cfl(KParams p, const typename std::conditional<PRIM_IN, typename Pol::TS, type
   cfl_block_reduce(dtp, bad, sc);
 }
 
+// block (32, 8); grid (ceil(nx/32), ceil(ny/8), ceil(nz/kz))
+template <class Pol, int NEQ, bool PRIM_IN>
+__global__ void __launch_bounds__(256)
+k_cfl(KParams p, const typename std::conditional<PRIM_IN, typename Pol::TS, typename Pol::TU>::type* src,
+      StepScalars* sc, int kz) {
+  cfl_body<Pol, NEQ, PRIM_IN>(p, src, sc, kz, blockIdx.x, blockIdx.y, blockIdx.z);
+}
+
 // get_timestep's scalar tail (src/hydro_core.f90:677-694) and the bookkeeping
 // of the device time loop (src/main.f90:94-125).
-static __global__ void k_dtfin(StepScalars* sc, double cfl, double dx, double dy, double dz) {
+__device__ __forceinline__ void dtfin_body(StepScalars* sc, double cfl, double dx, double dy,
+                                           double dz) {
   if (!sc->active) return;
   double dtp = __longlong_as_double((long long)sc->dtmin_bits);
   sc->dtmin_bits = 0x7FF0000000000000ull;  // +inf for the next reduction
@@ -681,9 +695,12 @@ static __global__ void k_dtfin(StepScalars* sc, double cfl, double dx, double dy
   sc->dump = dump;
   set_stage_ratios(sc, dx, dy, dz);
 }
+static __global__ void k_dtfin(StepScalars* sc, double cfl, double dx, double dy, double dz) {
+  dtfin_body(sc, cfl, dx, dy, dz);
+}
 
 // Time-loop tail after a tstep (src/main.f90:108-123): device-resident loop.
-static __global__ void k_loopfin(StepScalars* sc) {
+__device__ __forceinline__ void loopfin_body(StepScalars* sc) {
   if (!sc->active) return;
   sc->time = sc->time + sc->dt;
   if (sc->dump) {
@@ -693,6 +710,7 @@ static __global__ void k_loopfin(StepScalars* sc) {
   sc->iter = sc->iter + 1;
   sc->active = (sc->time <= sc->tmax) && sc->err == 0;
 }
+static __global__ void k_loopfin(StepScalars* sc) { loopfin_body(sc); }
 
 // ---------------------------------------------------------------------------
 // Tabulated cooling (src/cooling_dmc.f90:115-156, src/cooling_chi.f90:114-154),

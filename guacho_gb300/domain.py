@@ -157,6 +157,24 @@ class Domain:
     def launches_per_step(self) -> int:
         return self._lib.gch_launches_per_step(self._h)
 
+    @property
+    def kz(self) -> int:
+        """z planes per block of the stage kernels."""
+        return self._lib.gch_get_kz(self._h)
+
+    @kz.setter
+    def kz(self, value: int) -> None:
+        check("gch_set_kz", self._lib.gch_set_kz(self._h, int(value)))
+
+    def autotune(self) -> dict:
+        """Time the stage-1 kernel for each candidate depth on the current
+        state, keep the fastest; returns {kz: ms}."""
+        ck = (C.c_int * 8)()
+        cm = (C.c_float * 8)()
+        n = C.c_int()
+        check("gch_autotune", self._lib.gch_autotune(self._h, 8, ck, cm, C.byref(n)))
+        return {int(ck[i]): float(cm[i]) for i in range(n.value)}
+
     def advance_timed(self, steps: int, n_iter: int = 10) -> float:
         """`steps` device-resident steps timed with CUDA events; GPU ms."""
         ms = C.c_float()
@@ -219,3 +237,14 @@ class Batch:
         it = (C.c_int * n)()
         check("gch_batch_time", self._lib.gch_batch_time(self._h, t, it))
         return list(t), list(it)
+
+    def tuning(self) -> dict:
+        """Grouped mode, the z-march depth chosen by the autotuner and the
+        measured stage-1 time of each candidate depth."""
+        g, kz, n = C.c_int(), C.c_int(), C.c_int()
+        ck = (C.c_int * 16)()
+        cm = (C.c_float * 16)()
+        check("gch_batch_tuning", self._lib.gch_batch_tuning(self._h, C.byref(g), C.byref(kz),
+                                                              16, ck, cm, C.byref(n)))
+        return {"grouped": bool(g.value), "kz": kz.value,
+                "candidates": {int(ck[i]): float(cm[i]) for i in range(n.value)}}

@@ -26,8 +26,9 @@
  *
  *   gch_advance        <- the time loop of src/main.f90:94-125, with dt kept
  *                         on the device, steps captured as a CUDA graph
- *   gch_batch_*        <- many independent boxes of uneven size advanced in
- *                         one persistent launch, each with its own dt
+ *   gch_batch_*        <- many independent boxes of uneven size, each with
+ *                         its own dt, advanced by one CUDA graph per step
+ *                         whose kernels each cover all boxes
  *
  * Every call returns 0 (GCH_OK) or a bitmask of GCH_ERR_* bits.  The Fortran
  * shim prints and stops on a non-zero status, as the reference does
@@ -222,6 +223,19 @@ int gch_last_step_info(gch_domain_t* d, long long* pfloor_hits, int* err_bits);
 /* Number of kernel launches one gch_tstep issues (for launch accounting). */
 int gch_launches_per_step(gch_domain_t* d);
 
+/* ---- z-march depth of the stage kernels (no reference counterpart) -------
+ * Each block of the stage kernels marches over kz planes of z.  Results are
+ * identical for every depth (every plane is computed by the same code); the
+ * depth trades the column warm-up per block against the number of blocks.
+ * gch_create picks kz from the box size; gch_autotune times the stage-1
+ * flux kernel (it writes only the stage arrays up and E) for kz in
+ * {1,2,4,8,16,32} <= nz on the current state, keeps the fastest, and
+ * reports up to `cap` candidates with their times in ms (outputs may be
+ * NULL).  gch_set_kz sets the depth directly (1 <= kz <= nz). */
+int gch_get_kz(gch_domain_t* d);
+int gch_set_kz(gch_domain_t* d, int kz);
+int gch_autotune(gch_domain_t* d, int cap, int* cand_kz, float* cand_ms, int* ncand);
+
 /* Profiling aids (no counterpart in the reference).
  * gch_advance_timed: `steps` device-resident iterations without output
  * clipping, timed with CUDA events on the domain's stream; *ms = GPU time.
@@ -255,7 +269,14 @@ typedef struct gch_batch gch_batch_t;
 
 /* n independent domains (each its own params, size and dt) advanced
  * together.  All boxes must share precision, neq and the physics switches;
- * sizes, spacings, boundary kinds and problem data may differ. */
+ * sizes, spacings, boundary kinds and problem data may differ.
+ *
+ * FP32 boxes without table cooling, resistivity or user spheres are advanced
+ * in grouped mode on `stream` (0 = a stream of the batch's own): one launch
+ * per kernel of the step covers up to 64 boxes, one CUDA graph holds the
+ * step, and the z-march depth is chosen by timing before the first step.
+ * Other batches run each box's own step graph on its own stream.  No
+ * reference counterpart: the reference advances one domain per process. */
 int gch_batch_create(int n, const gch_params_t* params, void* stream, gch_batch_t** out);
 int gch_batch_destroy(gch_batch_t* b);
 int gch_batch_upload(gch_batch_t* b, int box, const double* u);
@@ -265,6 +286,12 @@ int gch_batch_download(gch_batch_t* b, int box, double* u);
 int gch_batch_advance(gch_batch_t* b, int steps, int n_iter);
 /* Per-box simulated time and iteration count. */
 int gch_batch_time(gch_batch_t* b, double* times, int* iters);
+/* How the batch runs: grouped (1/0), the z-march depth the autotuner chose
+ * (-1 when not grouped, 0 before the first advance) and up to `cap`
+ * candidate depths with their measured stage-1 times in ms (ncand of them).
+ * Any output pointer may be NULL. */
+int gch_batch_tuning(gch_batch_t* b, int* grouped, int* kz, int cap, int* cand_kz,
+                     float* cand_ms, int* ncand);
 
 #ifdef __cplusplus
 }
