@@ -12,7 +12,7 @@ import numpy as np
 
 from .params import Params
 
-ABI_VERSION = 1
+ABI_VERSION = 2
 MAX_SPHERES, MAX_GRAV, MAX_TABLE = 8, 4, 512
 
 ERR_PARAM, ERR_CUDA, ERR_HLLD, ERR_HLLC = 0x1, 0x2, 0x4, 0x8
@@ -53,6 +53,9 @@ class Params_t(C.Structure):
         ("sph", Sphere_t * MAX_SPHERES),
         ("grav_GM", C.c_double * MAX_GRAV), ("grav_x", C.c_double * MAX_GRAV),
         ("grav_y", C.c_double * MAX_GRAV), ("grav_z", C.c_double * MAX_GRAV),
+        ("th_cond", C.c_int32), ("tc_saturation", C.c_int32),
+        ("rsc", C.c_double), ("rhosc", C.c_double), ("vsc2", C.c_double), ("bsc", C.c_double),
+        ("mu", C.c_double),
     ]
 
 
@@ -87,6 +90,8 @@ def to_struct(p: Params) -> Params_t:
     s.ngrav = len(p.grav)
     for i, (gm, x, y, z) in enumerate(p.grav):
         s.grav_GM[i], s.grav_x[i], s.grav_y[i], s.grav_z[i] = gm, x, y, z
+    s.th_cond, s.tc_saturation = p.th_cond, int(p.tc_saturation)
+    s.rsc, s.rhosc, s.vsc2, s.bsc, s.mu = p.rsc, p.rhosc, p.vsc2, p.bsc, p.mu
     return s
 
 
@@ -115,6 +120,7 @@ def lib() -> C.CDLL:
         "gch_calcprim": (I, [P]),
         "gch_get_timestep": (I, [P, I, I, D, D, DP, IP]),
         "gch_tstep": (I, [P, D]),
+        "gch_tc_info": (I, [P, IP, DP]),
         "gch_step_host": (I, [P, P, I, I, D, D, DP, IP]),
         "gch_advance": (I, [P, I, D, D, I, DP, IP, DP, IP]),
         "gch_last_step_info": (I, [P, C.POINTER(C.c_longlong), IP]),
@@ -144,7 +150,7 @@ def lib() -> C.CDLL:
 def exported_symbols() -> list[str]:
     return ["gch_params_default", "gch_params_check", "gch_create", "gch_destroy",
             "gch_upload", "gch_download", "gch_boundaryI", "gch_calcprim",
-            "gch_get_timestep", "gch_tstep", "gch_step_host", "gch_advance",
+            "gch_get_timestep", "gch_tstep", "gch_tc_info", "gch_step_host", "gch_advance",
             "gch_last_step_info", "gch_launches_per_step", "gch_advance_timed",
             "gch_profile_step", "gch_get_kz", "gch_set_kz", "gch_autotune",
             "gch_batch_create",

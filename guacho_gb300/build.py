@@ -43,6 +43,9 @@ UNITS = {
     "gch_batch.cu": [],
     # FP64 arithmetic in the reference's order, as gch_fp64.cu
     "gch_noalloc.cu": ["-fmad=false"],
+    # thermal conduction: FP64 device arithmetic and host-side super-step
+    # scalars, neither contracted into multiply-adds
+    "gch_tc.cu": ["-fmad=false", "-Xcompiler", "-ffp-contract=off"],
 }
 
 

@@ -98,6 +98,13 @@ void gch_params_default(gch_params_t* p, int nx, int ny, int nz) {
   p->Psc = 1.0;
   p->tsc = 1.0;
   p->tab_Tmin = 1e4;
+  p->th_cond = GCH_TC_OFF;
+  p->tc_saturation = 0;
+  p->rsc = 1.0;
+  p->rhosc = 1.0;
+  p->vsc2 = 1.0;
+  p->bsc = std::sqrt(4.0 * std::acos(-1.0));  // sqrt(4 pi Psc), Psc = 1
+  p->mu = 1.0;
 }
 
 int gch_params_check(const gch_params_t* p) {
@@ -147,6 +154,16 @@ int gch_params_check(const gch_params_t* p) {
   if (!(p->dx > 0 && p->dy > 0 && p->dz > 0 && p->cv > 0 && p->gamma > 0 && p->cfl > 0))
     return GCH_ERR_PARAM;
   if (!(p->eta >= 0.0)) return GCH_ERR_PARAM;
+  if (p->th_cond != GCH_TC_OFF) {
+    if (p->th_cond != GCH_TC_ISOTROPIC && p->th_cond != GCH_TC_ANISOTROPIC) return GCH_ERR_PARAM;
+    if (p->th_cond == GCH_TC_ANISOTROPIC && !bfield) return GCH_ERR_PARAM;
+    // with table cooling the reference's interior Temp is not refreshed
+    // before conduction reads it
+    if (p->cooling != GCH_COOL_NONE) return GCH_ERR_PARAM;
+    if (!(p->rsc > 0 && p->rhosc > 0 && p->vsc2 > 0 && p->bsc > 0 && p->mu > 0 && p->Psc > 0 &&
+          p->tsc > 0))
+      return GCH_ERR_PARAM;
+  }
   return GCH_OK;
 }
 
@@ -166,6 +183,9 @@ int gch_destroy(gch_domain_t* d) {
   cudaFree(d->grav);
   cudaFree(d->sc);
   cudaFree(d->stage);
+  cudaFree(d->tcw);
+  cudaFree(d->tc_min);
+  if (d->tc_min_host) cudaFreeHost(d->tc_min_host);
   if (d->sc_host) cudaFreeHost(d->sc_host);
   if (d->stream && d->own_stream) cudaStreamDestroy(d->stream);
   delete d;
@@ -213,7 +233,8 @@ int gch_create(const gch_params_t* p, void* stream, gch_domain_t** out) {
   k.ntab = p->ntab; k.tab_i0 = p->tab_i0;
   k.tab_inv_dlog = p->tab_inv_dlog; k.tab_tail = p->tab_tail; k.tab_Tmin = p->tab_Tmin;
   k.nsph = p->bc_user ? p->nsph : 0;
-  d->cfl_fused = p->neq == 8 && p->enable_flux_cd && p->eta == 0.0 && !d->prim_in && !p->bc_user;
+  d->cfl_fused = p->neq == 8 && p->enable_flux_cd && p->eta == 0.0 && !d->prim_in &&
+                 !p->bc_user && p->th_cond == GCH_TC_OFF;
   k.ngrav = p->user_source_terms ? p->ngrav : 0;
 
   // z planes per block: enough blocks to fill the 152 SMs several times
@@ -250,6 +271,11 @@ int gch_create(const gch_params_t* p, void* stream, gch_domain_t** out) {
   d->ncell_host = (size_t)k.NX * k.NY * k.NZ;
   alloc((void**)&d->stage, d->ncell_host * k.neq * sizeof(double));
   alloc((void**)&d->sc, sizeof(StepScalars));
+  if (p->th_cond != GCH_TC_OFF) {
+    alloc((void**)&d->tcw, fs * 6 * sizeof(double));
+    alloc((void**)&d->tc_min, sizeof(unsigned long long));
+    if (e == cudaSuccess) e = cudaMallocHost((void**)&d->tc_min_host, sizeof(unsigned long long));
+  }
   if (e == cudaSuccess && p->cooling != GCH_COOL_NONE) {
     e = cudaMalloc((void**)&d->tab, 2 * p->ntab * sizeof(double));
     if (e == cudaSuccess) e = cudaMemcpy(d->tab, p->tab_T, p->ntab * sizeof(double), cudaMemcpyHostToDevice);
@@ -348,7 +374,16 @@ int gch_tstep(gch_domain_t* d, double dt) {
   if (!d) return GCH_ERR_PARAM;
   if (!(dt > 0.0) || !std::isfinite(dt)) return GCH_ERR_DT;
   k_set_dt<<<1, 1, 0, d->stream>>>(d->sc, dt, d->kp.dx, d->kp.dy, d->kp.dz);
-  return engine(d).tstep(d);
+  int st = engine(d).tstep(d);
+  if (d->hp.th_cond != GCH_TC_OFF && st == GCH_OK) st |= gch::tc_run(d, dt);
+  return st;
+}
+
+int gch_tc_info(gch_domain_t* d, int* nsteps, double* dt_cond) {
+  if (!d) return GCH_ERR_PARAM;
+  if (nsteps) *nsteps = d->tc_nsteps;
+  if (dt_cond) *dt_cond = d->tc_dt_cond;
+  return GCH_OK;
 }
 
 int gch_step_host(gch_domain_t* d, double* u, int current_iter, int n_iter, double current_time,
@@ -361,6 +396,10 @@ int gch_step_host(gch_domain_t* d, double* u, int current_iter, int n_iter, doub
   k_set_ctrl<<<1, 1, 0, d->stream>>>(d->sc, current_iter, n_iter, current_time, tprint, 0.0, 0.0, 1);
   st |= engine(d).get_dt(d);
   st |= engine(d).tstep(d);
+  if (d->hp.th_cond != GCH_TC_OFF && st == GCH_OK) {
+    st |= fetch_scalars(d);  // the conduction substeps need dt on the host
+    st |= gch::tc_run(d, d->sc_host->dt);
+  }
   st |= engine(d).download_u(d);
   st |= cuda_ok(cudaMemcpyAsync(u, d->stage, bytes, cudaMemcpyDeviceToHost, d->stream));
   st |= fetch_scalars(d);
@@ -372,9 +411,35 @@ int gch_step_host(gch_domain_t* d, double* u, int current_iter, int n_iter, doub
 
 }  // extern "C"
 
-// Enqueue up to max_steps device-resident iterations (no host sync).
+namespace {
+// The time loop of src/main.f90:94-125 driven from the host, for domains
+// whose step needs the host (thermal conduction); leaves the loop state in
+// the device scalars as the device loop's tail does.
+int host_loop(gch_domain* d, int max_steps, double tmax, double dtprint, int n_iter,
+              double time, int iter, double tprint) {
+  int st = GCH_OK;
+  for (int n = 0; n < max_steps && time <= tmax && st == GCH_OK; ++n) {
+    double dt = 0.0;
+    int dump = 0;
+    st |= gch_get_timestep(d, iter, n_iter, time, tprint, &dt, &dump);
+    if (st) break;
+    st |= gch_tstep(d, dt);
+    time = time + dt;
+    if (dump) tprint = tprint + dtprint;
+    iter = iter + 1;
+  }
+  k_set_ctrl<<<1, 1, 0, d->stream>>>(d->sc, iter, n_iter, time, tprint, dtprint, tmax,
+                                     time <= tmax ? 1 : 0);
+  return st | cuda_ok(cudaGetLastError());
+}
+}  // namespace
+
+// Enqueue up to max_steps device-resident iterations (no host sync; with
+// thermal conduction the steps run from the host before this returns).
 int gch_advance_enqueue(gch_domain* d, int max_steps, double tmax, double dtprint, int n_iter,
                         double time, int iter, double tprint) {
+  if (d->hp.th_cond != GCH_TC_OFF)
+    return host_loop(d, max_steps, tmax, dtprint, n_iter, time, iter, tprint);
   k_set_ctrl<<<1, 1, 0, d->stream>>>(d->sc, iter, n_iter, time, tprint, dtprint, tmax,
                                      time <= tmax ? 1 : 0);
   int st = cuda_ok(cudaGetLastError());
@@ -417,6 +482,12 @@ int gch_advance(gch_domain_t* d, int max_steps, double tmax, double dtprint, int
                 double* time, int* iter, double* tprint, int* steps_done) {
   if (!d || !time || !iter || !tprint || max_steps < 0) return GCH_ERR_PARAM;
   const int iter0 = *iter;
+  if (d->hp.th_cond != GCH_TC_OFF) {
+    int st = host_loop(d, max_steps, tmax, dtprint, n_iter, *time, *iter, *tprint);
+    st |= gch_advance_finish(d, time, iter, tprint);
+    if (steps_done) *steps_done = *iter - iter0;
+    return st;
+  }
   // Launch the step graph in chunks and stop as soon as the device loop
   // condition (time <= tmax, no error) turns false: the host never queues
   // more than one chunk of steps past the end of the run.
@@ -455,9 +526,14 @@ int gch_advance_timed(gch_domain_t* d, int steps, int n_iter, float* ms) {
   st |= cuda_ok(cudaEventCreate(&a));
   st |= cuda_ok(cudaEventCreate(&b));
   k_set_ctrl<<<1, 1, 0, d->stream>>>(d->sc, it0, n_iter, t0, inf, inf, inf, 1);
-  st |= gch_advance_enqueue(d, 0, inf, inf, n_iter, t0, it0, inf);  // capture only
-  st |= cuda_ok(cudaEventRecord(a, d->stream));
-  for (int n = 0; n < steps; ++n) st |= cuda_ok(cudaGraphLaunch(d->graph, d->stream));
+  if (d->hp.th_cond != GCH_TC_OFF) {  // host-driven steps
+    st |= cuda_ok(cudaEventRecord(a, d->stream));
+    st |= host_loop(d, steps, inf, inf, n_iter, t0, it0, inf);
+  } else {
+    st |= gch_advance_enqueue(d, 0, inf, inf, n_iter, t0, it0, inf);  // capture only
+    st |= cuda_ok(cudaEventRecord(a, d->stream));
+    for (int n = 0; n < steps; ++n) st |= cuda_ok(cudaGraphLaunch(d->graph, d->stream));
+  }
   st |= cuda_ok(cudaEventRecord(b, d->stream));
   st |= cuda_ok(cudaEventSynchronize(b));
   st |= cuda_ok(cudaEventElapsedTime(ms, a, b));

@@ -1,7 +1,7 @@
 // gch_batch.cu -- many independent boxes of uneven size, each with its own
 // CFL dt, advanced together.
 //
-// Grouped mode (FP32 policies; no table cooling, resistivity or user
+// Grouped mode (FP32 policies; no table cooling, conduction, resistivity or user
 // spheres): one step of all boxes is one CUDA graph of grouped launches,
 // one launch per kernel of the step for up to 64 boxes (gch_group.cuh).
 // The z-march depth of the stage kernels is chosen by timing the stage-1
@@ -75,7 +75,8 @@ namespace {
 
 bool groupable(const gch_params_t& p) {
   const bool prim_in = p.cooling == GCH_COOL_DMC || p.cooling == GCH_COOL_CHI;
-  return p.precision != GCH_FP64 && !prim_in && p.eta == 0.0 && !p.bc_user;
+  return p.precision != GCH_FP64 && !prim_in && p.eta == 0.0 && !p.bc_user &&
+         p.th_cond == GCH_TC_OFF;
 }
 
 int grid_of(int n) { return (n + 127) / 128; }

@@ -542,6 +542,117 @@ __device__ __forceinline__ void hlld_sel(const KParams& p, const T* pl, const T*
   ff[7] = bzx * sM - bx * wx_;
 }
 
+// Paired FP32 arithmetic: the left and right states of an interface in the
+// two lanes of a float2, one FADD2/FMUL2/FFMA2 instruction for both.
+__device__ __forceinline__ float2 f2(float a, float b) { return make_float2(a, b); }
+__device__ __forceinline__ float2 f2(float a) { return make_float2(a, a); }
+__device__ __forceinline__ float2 add2(float2 a, float2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ float2 sub2(float2 a, float2 b) {
+  return __fadd2_rn(a, make_float2(-b.x, -b.y));
+}
+__device__ __forceinline__ float2 mul2(float2 a, float2 b) { return __fmul2_rn(a, b); }
+__device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+
+// HLLD for the FP32 paths with the left/right-symmetric work paired: the
+// states of hlld_sel (the same Miyoshi-Kusano star states of
+// src/hlld.f90:48-319, regions selected by predicates), with the fast speeds,
+// total pressures, star densities and single-star states of both sides
+// formed in the two lanes of float2 operations.
+__device__ __forceinline__ void hlld_pair(const KParams& p, const float* pl, const float* pr,
+                                          float* ff, int& err) {
+  const float cv = (float)p.cv, g = (float)p.gamma;
+  const float2 rho = f2(pl[0], pr[0]), vx = f2(pl[1], pr[1]);
+  const float2 vy = f2(pl[2], pr[2]), vz = f2(pl[3], pr[3]), pg = f2(pl[4], pr[4]);
+  const float2 bn = f2(pl[5], pr[5]), by = f2(pl[6], pr[6]), bz = f2(pl[7], pr[7]);
+  // cfastX of both states (src/hydro_core.f90:591-604)
+  const float2 irho = f2(1.0f / pl[0], 1.0f / pr[0]);
+  const float2 gp = mul2(f2(g), pg);
+  const float2 btt = fma2(by, by, mul2(bz, bz));
+  const float2 cs2va2 = mul2(add2(gp, fma2(bn, bn, btt)), irho);
+  const float2 t4 = mul2(mul2(f2(4.0f), gp), mul2(mul2(bn, bn), mul2(irho, irho)));
+  const float2 disc = fma2(cs2va2, cs2va2, f2(-t4.x, -t4.y));
+  const float2 h = mul2(f2(0.5f), add2(cs2va2, f2(sqrtf(disc.x), sqrtf(disc.y))));
+  const float2 cf = f2(sqrtf(h.x), sqrtf(h.y));
+  const float2 lo = sub2(vx, cf), hi = add2(vx, cf);
+  const float sl = tmin_(lo.x, lo.y), sr = tmax_(hi.x, hi.y);
+  if (sl > 0.0f) { prim2f<float, 8>(p, pl, ff); return; }
+  if (sr < 0.0f) { prim2f<float, 8>(p, pr, ff); return; }
+
+  const float bx = 0.5f * (pl[5] + pr[5]);
+  const float signBx = copysignf(1.0f, bx);
+  const float bx2 = bx * bx;
+  const float2 pT = fma2(f2(0.5f), add2(f2(bx2), btt), pg);  // total pressures
+  const float2 sv = f2(sl, sr);
+  const float2 smu = sub2(sv, vx);                           // S - u
+  const float2 m = mul2(smu, rho);                           // rho (S - u)
+  const float iden = 1.0f / (m.y - m.x);
+  const float2 mv = mul2(m, vx);
+  const float sM = (mv.y - mv.x - pT.y + pT.x) * iden;
+  const float2 ssM = sub2(sv, f2(sM));                       // S - sM
+  const float2 rhost = mul2(m, f2(1.0f / ssM.x, 1.0f / ssM.y));
+  const float2 isq = f2(rsqrtf(rhost.x), rsqrtf(rhost.y));
+  const float2 sq = mul2(rhost, isq);                        // sqrt(rho*)
+  const float abx = fabsf(bx);
+  const float sstl = sM - abx * isq.x, sstr = sM + abx * isq.y;
+  const float pst = (m.y * pT.x - m.x * pT.y + m.x * m.y * (pr[1] - pl[1])) * iden;
+  // single-star states with the reference's den == 0 fallbacks
+  const float2 dlr = fma2(m, ssM, f2(-bx2));
+  const float2 id = f2(dlr.x == 0.0f ? 0.0f : 1.0f / dlr.x, dlr.y == 0.0f ? 0.0f : 1.0f / dlr.y);
+  const float2 sMmu = sub2(f2(sM), vx);
+  const float2 fb = mul2(fma2(m, smu, f2(-bx2)), id);
+  const float2 t1 = mul2(mul2(f2(bx), sMmu), id);
+  const float2 vst = fma2(f2(-by.x, -by.y), t1, vy);
+  const float2 wst = fma2(f2(-bz.x, -bz.y), t1, vz);
+  const float2 byst = mul2(by, fb), bzst = mul2(bz, fb);
+  // region: UL* | UR* | UL** | UR**
+  const bool star_l = sstl >= 0.0f;
+  const bool star_r = !star_l && sstr <= 0.0f;
+  const bool dbl = !star_l && !star_r;
+  const bool left = star_l || (dbl && sM >= 0.0f);
+  if (dbl && !(sM >= 0.0f) && !(sM <= 0.0f)) {  // src/hlld.f90:316-317
+#pragma unroll
+    for (int q = 0; q < 8; ++q) ff[q] = sM;
+    err |= GCH_ERR_HLLD;
+    return;
+  }
+  // double-star state
+  const float idd = 1.0f / (sq.x + sq.y);
+  const float sqlr = sq.x * sq.y;
+  const float2 av = mul2(sq, vst), aw = mul2(sq, wst);
+  const float2 ab = mul2(sq, f2(byst.y, byst.x)), ac = mul2(sq, f2(bzst.y, bzst.x));
+  const float vstst = (av.x + av.y + (byst.y - byst.x) * signBx) * idd;
+  const float wstst = (aw.x + aw.y + (bzst.y - bzst.x) * signBx) * idd;
+  const float bystst = (ab.x + ab.y + sqlr * (vst.y - vst.x) * signBx) * idd;
+  const float bzstst = (ac.x + ac.y + sqlr * (wst.y - wst.x) * signBx) * idd;
+  const float vststdotbstst = sM * bx + vstst * bystst + wstst * bzstst;
+  // the selected side's single-star energy
+  const float q0 = left ? pl[0] : pr[0], q1 = left ? pl[1] : pr[1];
+  const float q2 = left ? pl[2] : pr[2], q3 = left ? pl[3] : pr[3];
+  const float q4 = left ? pl[4] : pr[4], q6 = left ? pl[6] : pr[6], q7 = left ? pl[7] : pr[7];
+  const float smu_s = left ? smu.x : smu.y, ssM_s = left ? ssM.x : ssM.y;
+  const float pT_s = left ? pT.x : pT.y, rhos = left ? rhost.x : rhost.y;
+  const float vst_s = left ? vst.x : vst.y, wst_s = left ? wst.x : wst.y;
+  const float byst_s = left ? byst.x : byst.y, bzst_s = left ? bzst.x : bzst.y;
+  const float e = 0.5f * q0 * (q1 * q1 + q2 * q2 + q3 * q3) + cv * q4
+                  + 0.5f * (bx2 + q6 * q6 + q7 * q7);
+  const float vdotb = q1 * bx + q2 * q6 + q3 * q7;
+  const float vstdotbst = sM * bx + vst_s * byst_s + wst_s * bzst_s;
+  const float est = (smu_s * e - pT_s * q1 + pst * sM + bx * (vdotb - vstdotbst)) / ssM_s;
+  const float sqs = left ? -sq.x : sq.y;
+  const float ex = dbl ? est + sqs * (vstdotbst - vststdotbstst) * signBx : est;
+  const float vx_ = dbl ? vstst : vst_s, wx_ = dbl ? wstst : wst_s;
+  const float byx = dbl ? bystst : byst_s, bzx = dbl ? bzstst : bzst_s;
+  const float vbx = dbl ? vststdotbstst : vstdotbst;
+  ff[0] = rhos * sM;
+  ff[1] = rhos * (sM * sM) + pst - bx2;
+  ff[2] = rhos * sM * vx_ - bx * byx;
+  ff[3] = rhos * sM * wx_ - bx * bzx;
+  ff[4] = sM * (ex + pst) - bx * vbx;
+  ff[5] = 0.0f;
+  ff[6] = byx * sM - bx * vx_;
+  ff[7] = bzx * sM - bx * wx_;
+}
+
 // src/hllc.f90:44-140  prim2fhllc (hydro, or passive B when NEQ == 8)
 template <class T, int NEQ>
 __device__ __forceinline__ void hllc(const KParams& p, const T* pl, const T* pr, T* ff, int& err) {
@@ -634,8 +745,13 @@ struct Riemann<GCH_SOLVER_HLLD, 8> {
   template <class T>
   __device__ __forceinline__ static void solve(const KParams& p, const T* l, const T* r, T* f,
                                                int& e) {
-    if constexpr (sizeof(T) == 4)
+    if constexpr (sizeof(T) == 4) {
+#if GCH_HLLD_PAIR
+      hlld_pair(p, l, r, f, e);    // FP32 paths: paired left/right work
+#else
       hlld_sel<T>(p, l, r, f, e);  // FP32 paths: branch-free star regions
+#endif
+    }
     else
       hlld<T>(p, l, r, f, e);      // FP64: the reference's branch order
   }

@@ -37,6 +37,14 @@ struct gch_domain {
   bool cfl_fused = false;
   bool cfl_ready = false;
   int launches = 0;             // kernel launches of the last tstep
+  // thermal conduction (th_cond != 0): rho, p, T and the three face fluxes
+  // (6 fields, FP64), the device min of the conduction timescale and its
+  // pinned copy, and the substep count / timescale of the last tstep
+  double* tcw = nullptr;
+  unsigned long long* tc_min = nullptr;
+  unsigned long long* tc_min_host = nullptr;
+  int tc_nsteps = 0;
+  double tc_dt_cond = 0.0;
   // CUDA graph of one device-resident step (get_timestep + tstep + loop tail)
   cudaGraphExec_t graph = nullptr;
   // per-launch profiling: when prof_on, an event is recorded after every
@@ -89,6 +97,13 @@ struct GroupOps {
 };
 extern const GroupOps kGroupMixed;
 extern const GroupOps kGroupKahan;
+
+// Thermal conduction after a tstep of dt_CFL (gch_tc.cu): synchronises once.
+int tc_run(gch_domain* d, double dt_CFL);
+// The super-time-stepping scalars of src/thermal_cond.f90:625-681.
+double tc_superstep(int N, double snu);
+double tc_substep(int j, int N, double nu);
+void tc_st_steps(double fs, int* Ns, double* fstep);
 
 }  // namespace gch
 

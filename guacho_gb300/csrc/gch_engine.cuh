@@ -48,7 +48,7 @@ struct Engine {
   // stage 1 has no limiter; stage 2 specialises minmod and van Leer
   template <int SOLVER, int NEQ, int STAGE, bool PRIM_IN>
   static void flux_launch(gch_domain* d, const void* src, void* dst) {
-    if (STAGE == 1)
+    if constexpr (STAGE == 1)
       flux_launch_lim<SOLVER, NEQ, STAGE, PRIM_IN, kLimRuntime>(d, src, dst);
     else if (d->kp.limiter == GCH_LIMITER_MINMOD)
       flux_launch_lim<SOLVER, NEQ, STAGE, PRIM_IN, GCH_LIMITER_MINMOD>(d, src, dst);

@@ -61,7 +61,7 @@ __global__ void __launch_bounds__(NT, Pol::kMinBlocks) k_flux_grp(const __grid_c
 
 // a1 = u, a2 = destination of B, a3 = E, a4 = s678
 template <class Pol, int STAGE, bool CFL>
-__global__ void __launch_bounds__(256) k_ct_grp(const __grid_constant__ GroupArgs g) {
+__global__ void __launch_bounds__(256, 4) k_ct_grp(const __grid_constant__ GroupArgs g) {
   using TD = typename std::conditional<STAGE == 1, typename Pol::TS, typename Pol::TU>::type;
   const GroupBox& x = g.box[group_box(g, blockIdx.x)];
   const int l = blockIdx.x - x.blk0;

@@ -60,7 +60,7 @@ struct GroupEngine {
   }
   template <int SOLVER, int NEQ, int STAGE>
   static void flux_solver(GroupArgs& g, unsigned blocks, cudaStream_t s, int lim) {
-    if (STAGE == 1) flux_lim<SOLVER, NEQ, STAGE, kLimRuntime>(g, blocks, s);
+    if constexpr (STAGE == 1) flux_lim<SOLVER, NEQ, STAGE, kLimRuntime>(g, blocks, s);
     else if (lim == GCH_LIMITER_MINMOD) flux_lim<SOLVER, NEQ, STAGE, GCH_LIMITER_MINMOD>(g, blocks, s);
     else if (lim == GCH_LIMITER_VAN_LEER) flux_lim<SOLVER, NEQ, STAGE, GCH_LIMITER_VAN_LEER>(g, blocks, s);
     else flux_lim<SOLVER, NEQ, STAGE, kLimRuntime>(g, blocks, s);

@@ -43,6 +43,25 @@ struct Src {
     else
       Ops<Pol>::template load_prim<NEQ>(p, src, idx, prim, pfl);
   }
+  // the same in two halves: the stored values of a cell into registers
+  // (issued early, so their latency overlaps other work), then the
+  // conversion, with the arithmetic of load()
+  __device__ __forceinline__ static void fetch(const KParams& p, const TIn* src, long long idx,
+                                               TIn* raw) {
+#pragma unroll
+    for (int q = 0; q < NEQ; ++q) raw[q] = src[q * p.fs + idx];
+  }
+  __device__ __forceinline__ static void convert(const KParams& p, const TIn* raw, TC* prim,
+                                                 unsigned& pfl) {
+    if constexpr (PRIM_IN) {
+#pragma unroll
+      for (int q = 0; q < NEQ; ++q) prim[q] = (TC)raw[q];
+    } else if constexpr (std::is_same<TIn, float>::value) {
+      prim_from_f32<NEQ>(p, raw, prim, pfl);  // FP32 stage state (up)
+    } else {
+      Ops<Pol>::template prim_vals<NEQ>(p, raw, prim, pfl);  // u: FP64 or pairs
+    }
+  }
 };
 
 // Shared memory of the stage kernel (dynamic: up to 72 KB in FP32).
@@ -134,6 +153,36 @@ flux_body(const KParams& p, const typename Src<Pol, NEQ, STAGE, PRIM_IN>::TIn* _
   const int k0 = kb - (STAGE == 1 ? 2 : 4);
   const int nfx = (TX + 1) * TY;
   const int nfy = TX * (TY + 1);
+
+  // The halo ring of a plane has fewer cells than the block has threads:
+  // thread tid < NRING owns halo cell (hx, hy) of every plane.
+  static_assert(NRING <= NT, "one halo cell per thread");
+  const bool has_halo = tid < NRING;
+  int hx = 0, hy = 0;
+  if (tid < 2 * H * TX) {  // rows below / above the tile
+    const int row = tid / TX;
+    hx = tid % TX;
+    hy = row < H ? row - H : TY + (row - H);
+  } else {  // columns left / right
+    const int rr = tid - 2 * H * TX;
+    const int col = rr / TY;
+    hy = rr % TY;
+    hx = col < H ? col - H : TX + (col - H);
+  }
+
+  // Stored values are fetched into registers before they are needed: the
+  // next column value after the faces of a plane are solved (converted at
+  // the start of the next iteration), and this plane's u before the barrier
+  // that precedes the update.  Their load latency overlaps the barrier wait
+  // and the update instead of stalling the start of a plane.  (Fetching the
+  // next halo cell as well costs more in register spills than it saves.)
+  using TIn = typename S::TIn;
+  TIn colr[NEQ];
+  S::fetch(p, src, gidx(axc, ayc, k0 + NG + H), colr);
+  auto prefetch_next = [&](int k) {
+    if (k + 1 < ke) S::fetch(p, src, gidx(axc, ayc, k + 1 + NG + H), colr);
+  };
+
   for (int k = k0; k < ke; ++k) {
     const bool plane = k >= kb;
     const bool zface = k >= kb - 1;
@@ -141,10 +190,10 @@ flux_body(const KParams& p, const typename Src<Pol, NEQ, STAGE, PRIM_IN>::TIn* _
     const int az = k + NG;
     if (plane) __syncthreads();  // readers of the previous plane are done
     // 1. the column ring shifts (centre <- p(k), p(k+1) <- p(k+2)) and the
-    //    next plane of the column is formed from global memory
+    //    next plane of the column is formed from the fetched values
     {
       TC nx_[NEQ];
-      S::load(p, src, gidx(axc, ayc, az + H), nx_, pfl);
+      S::convert(p, colr, nx_, pfl);
 #pragma unroll
       for (int q = 0; q < NEQ; ++q) {
         sP[q][ty + H][tx + H] = sQ[0][q][ty][tx];
@@ -157,19 +206,8 @@ flux_body(const KParams& p, const typename Src<Pol, NEQ, STAGE, PRIM_IN>::TIn* _
       }
     }
     if (plane) {
-      //  the halo of plane k from global memory
-      for (int r = tid; r < NRING; r += NT) {
-        int hx, hy;
-        if (r < 2 * H * TX) {  // rows below / above the tile
-          const int row = r / TX;
-          hx = r % TX;
-          hy = row < H ? row - H : TY + (row - H);
-        } else {  // columns left / right
-          const int rr = r - 2 * H * TX;
-          const int col = rr / TY;
-          hy = rr % TY;
-          hx = col < H ? col - H : TX + (col - H);
-        }
+      //  the halo of plane k
+      if (has_halo) {
         TC pr[NEQ];
         S::load(p, src, gidx(i0 + hx + NG, j0 + hy + NG, az), pr, pfl);
 #pragma unroll
@@ -269,14 +307,22 @@ flux_body(const KParams& p, const typename Src<Pol, NEQ, STAGE, PRIM_IN>::TIn* _
     }
     if (!plane) {  // column-private work only: no barrier
       if (NEQ >= 8) bzm = sP[7][ty + H][tx + H];
+      prefetch_next(k);
       continue;
     }
+    const int nupd = ct ? 5 : NEQ;
+    const long long c = cell_index(p, axc, ayc, az);
+    typename Pol::TU uq[NEQ];
+    if (active) {
+#pragma unroll
+      for (int q = 0; q < NEQ; ++q)
+        if (q < nupd) uq[q] = u[q * p.fs + c];
+    }
     __syncthreads();
+    prefetch_next(k);
 
     // 3. cell update and E
     if (active) {
-      const long long c = cell_index(p, axc, ayc, az);
-      const int nupd = ct ? 5 : NEQ;
       const int hp = k & 1, hn = (k + 1) & 1;  // faces k-1/2, k+1/2
       TC sv[NEQ];
 #pragma unroll
@@ -323,7 +369,7 @@ flux_body(const KParams& p, const typename Src<Pol, NEQ, STAGE, PRIM_IN>::TIn* _
 #pragma unroll
       for (int q = 0; q < NEQ; ++q) {
         if (q < nupd) {
-          auto unew = Ops<Pol>::update(Ops<Pol>::ld(u[q * p.fs + c]), dtdx, dtdy, dtdz,
+          auto unew = Ops<Pol>::update(Ops<Pol>::ld(uq[q]), dtdx, dtdy, dtdz,
                                        sF[q][ty][tx], sF[q][ty][tx + 1], sG[q][ty][tx],
                                        sG[q][ty + 1][tx], sH[hp][q][ty][tx], sH[hn][q][ty][tx]);
           if (src_terms) unew = Ops<Pol>::add(unew, dt * (double)sv[q]);
@@ -363,6 +409,12 @@ k_flux(KParams p, const typename Src<Pol, NEQ, STAGE, PRIM_IN>::TIn* __restrict_
   flux_body<Pol, SOLVER, NEQ, STAGE, PRIM_IN, LIM>(p, src, u, dst, E, s678, sc, kz, blockIdx.x,
                                                    blockIdx.y, blockIdx.z);
 }
+// Products rounded on their own (never fused into a following sum), so the
+// CFL candidate rounds the same way in every kernel that inlines it: the
+// stage-2 CT epilogue (fused reduction) and k_cfl agree bit for bit.
+__device__ __forceinline__ float mul_rn(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ double mul_rn(double a, double b) { return __dmul_rn(a, b); }
+
 // min(dx/(|vx|+cfx), dy/(|vy|+cfy), dz/(|vz|+cfz)) of one cell into dtp
 template <class TC, int NEQ>
 __device__ __forceinline__ void cfl_candidate(const KParams& p, const TC* pr, double& dtp,
@@ -372,11 +424,13 @@ __device__ __forceinline__ void cfl_candidate(const KParams& p, const TC* pr, do
     // src/hydro_core.f90:568-581 cfast
     const TC g = (TC)p.gamma;
     const TC bx = pr[5], by = pr[6], bz = pr[7];
-    const TC b2 = bx * bx + by * by + bz * bz;
-    const TC a = g * pr[4] + b2;
-    const TC cx = tsqrt(TC(0.5) * (a + tsqrt(a * a - TC(4.0) * g * pr[4] * bx * bx)) / pr[0]);
-    const TC cy = tsqrt(TC(0.5) * (a + tsqrt(a * a - TC(4.0) * g * pr[4] * by * by)) / pr[0]);
-    const TC cz = tsqrt(TC(0.5) * (a + tsqrt(a * a - TC(4.0) * g * pr[4] * bz * bz)) / pr[0]);
+    const TC b2 = mul_rn(bx, bx) + mul_rn(by, by) + mul_rn(bz, bz);
+    const TC gp = mul_rn(g, pr[4]);
+    const TC a = gp + b2;
+    const TC a2 = mul_rn(a, a), g4 = mul_rn(TC(4.0), gp);
+    const TC cx = tsqrt(mul_rn(TC(0.5), a + tsqrt(a2 - mul_rn(mul_rn(g4, bx), bx))) / pr[0]);
+    const TC cy = tsqrt(mul_rn(TC(0.5), a + tsqrt(a2 - mul_rn(mul_rn(g4, by), by))) / pr[0]);
+    const TC cz = tsqrt(mul_rn(TC(0.5), a + tsqrt(a2 - mul_rn(mul_rn(g4, bz), bz))) / pr[0]);
     cand[0] = (TC)p.dx / (tabs(pr[1]) + cx);
     cand[1] = (TC)p.dy / (tabs(pr[2]) + cy);
     cand[2] = (TC)p.dz / (tabs(pr[3]) + cz);
@@ -452,32 +506,49 @@ ct_body(const KParams& p, const typename Pol::TU* u,
 
   double dtp = 1e30;
   int bad = 0;
+  // E1 and E2 of this column at planes k-1 and k: the z neighbours march
+  // with the column, so each plane loads only its k+1 values
+  TC e1m = e_ghost(0, ax, ay, kb + NG - 1), e2m = e_ghost(1, ax, ay, kb + NG - 1);
+  TC e1c = e_ghost(0, ax, ay, kb + NG), e2c = e_ghost(1, ax, ay, kb + NG);
   for (int k = kb; k < ke; ++k) {
     const int az = k + NG;
     const long long c = cell_index(p, ax, ay, az);
-    // the six face neighbours of E needed by the three components
-    TC e3ym, e3yp, e2zm, e2zp, e3xm, e3xp, e1zm, e1zp, e2xm, e2xp, e1ym, e1yp;
-    if (inxy && az > NG && az < NG + p.nz - 1) {
+    // the face neighbours of E needed by the three components
+    TC e1p, e2p;
+    if (k + 1 < p.nz) {
+      e1p = (TC)E[c + sz];
+      e2p = (TC)E[p.fs + c + sz];
+    } else {
+      e1p = e_ghost(0, ax, ay, az + 1);
+      e2p = e_ghost(1, ax, ay, az + 1);
+    }
+    const TC e2zm = e2m, e2zp = e2p, e1zm = e1m, e1zp = e1p;
+    e1m = e1c; e2m = e2c; e1c = e1p; e2c = e2p;
+    TC e3ym, e3yp, e3xm, e3xp, e2xm, e2xp, e1ym, e1yp;
+    if (inxy) {
       const typename Pol::TS* E1 = E;
       const typename Pol::TS* E2 = E + p.fs;
       const typename Pol::TS* E3 = E + 2 * p.fs;
       e3ym = (TC)E3[c - sy]; e3yp = (TC)E3[c + sy];
-      e2zm = (TC)E2[c - sz]; e2zp = (TC)E2[c + sz];
       e3xm = (TC)E3[c - sx]; e3xp = (TC)E3[c + sx];
-      e1zm = (TC)E1[c - sz]; e1zp = (TC)E1[c + sz];
       e2xm = (TC)E2[c - sx]; e2xp = (TC)E2[c + sx];
       e1ym = (TC)E1[c - sy]; e1yp = (TC)E1[c + sy];
     } else {
       e3ym = e_ghost(2, ax, ay - 1, az); e3yp = e_ghost(2, ax, ay + 1, az);
-      e2zm = e_ghost(1, ax, ay, az - 1); e2zp = e_ghost(1, ax, ay, az + 1);
       e3xm = e_ghost(2, ax - 1, ay, az); e3xp = e_ghost(2, ax + 1, ay, az);
-      e1zm = e_ghost(0, ax, ay, az - 1); e1zp = e_ghost(0, ax, ay, az + 1);
       e2xm = e_ghost(1, ax - 1, ay, az); e2xp = e_ghost(1, ax + 1, ay, az);
       e1ym = e_ghost(0, ax, ay - 1, az); e1yp = e_ghost(0, ax, ay + 1, az);
     }
     const auto u6 = Ops<Pol>::ld(u[5 * p.fs + c]);
     const auto u7 = Ops<Pol>::ld(u[6 * p.fs + c]);
     const auto u8 = Ops<Pol>::ld(u[7 * p.fs + c]);
+    typename Ops<Pol>::R uu[8];
+    if constexpr (CFL && STAGE == 2) {
+      // u(1:5) of this cell (this kernel writes only B): loaded with the
+      // other inputs of the plane, ahead of the stores of B
+#pragma unroll
+      for (int q = 0; q < 5; ++q) uu[q] = Ops<Pol>::ld(dst[q * p.fs + c]);
+    }
     // src/flux_cd_module.f90:311-321
     auto b6 = Ops<Pol>::ct(u6, hy, e3ym, e3yp, hz, e2zm, e2zp, true);
     auto b7 = Ops<Pol>::ct(u7, hx, e3xm, e3xp, hz, e1zm, e1zp, false);
@@ -496,9 +567,6 @@ ct_body(const KParams& p, const typename Pol::TU* u,
       // the next step's CFL candidate from the final state of this cell
       // (same values and arithmetic as k_cfl on u)
       if (active) {
-        typename Ops<Pol>::R uu[8];
-#pragma unroll
-        for (int q = 0; q < 5; ++q) uu[q] = Ops<Pol>::ld(dst[q * p.fs + c]);
         uu[5] = store_as<typename Pol::TU>(b6);
         uu[6] = store_as<typename Pol::TU>(b7);
         uu[7] = store_as<typename Pol::TU>(b8);
@@ -513,9 +581,14 @@ ct_body(const KParams& p, const typename Pol::TU* u,
   if constexpr (CFL && STAGE == 2) cfl_block_reduce(dtp, bad, sc);
 }
 
-// block (32, 8); grid (ceil(nx/32), ceil(ny/8), ceil(nz/kz))
+// block (32, 8); grid (ceil(nx/32), ceil(ny/8), ceil(nz/kz)).  Four blocks
+// per SM keep enough loads in flight for the plain CT update; the variant
+// with the fused CFL candidate (pressure recovery and three fast speeds per
+// cell) runs fastest with the registers of two blocks per SM (measured on
+// the 256^3 turbulence box: 0.54 ms against 0.58 ms with four, 0.60 ms with
+// three).
 template <class Pol, int STAGE, bool CFL>
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(256, CFL ? 2 : 4)
 k_ct(KParams p, const typename Pol::TU* u,
      typename std::conditional<STAGE == 1, typename Pol::TS, typename Pol::TU>::type* dst,
      const typename Pol::TS* __restrict__ E, const typename Pol::TS* __restrict__ s678,

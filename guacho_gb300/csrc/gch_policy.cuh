@@ -98,8 +98,13 @@ struct Ops<PolFP64> {
 
 // ---------------------------------------------------------------------------
 // Error-free FP32 transformations (compensated "double-float" arithmetic).
-// They contain no multiply-add pattern the compiler could contract, and the
-// products use explicit fmaf, so they stay exact under -fmad=true.
+// The FP32 units are compiled with multiply-add contraction, which could
+// fuse a product into a following sum once these are inlined: every product
+// that feeds a sum here is rounded on its own (__fmul_rn, never contracted)
+// and the exact products use explicit fmaf.  That keeps the transformations
+// exact, and it makes the pressure recovery round the same way in every
+// kernel that inlines it (the dt of the fused and the separate CFL
+// reductions agree bit for bit).
 struct DF {
   float hi, lo;
 };
@@ -138,10 +143,10 @@ __device__ __forceinline__ void prim_from_f32(const KParams& p, const float* uu,
   const DF m2 = df_sumsq(uu[1], uu[2], uu[3]);
   const float q = m2.hi * ir;
   const float rem = fmaf(-q, r, m2.hi) + m2.lo;
-  DF kb = fast_two_sum(q, rem * ir);
+  DF kb = fast_two_sum(q, __fmul_rn(rem, ir));
   if (NEQ >= 8 && p.mhd) kb = df_add(kb, df_sumsq(uu[5], uu[6], uu[7]));
-  const DF d = two_sum(uu[4], -0.5f * kb.hi);
-  float pr = (d.hi + (d.lo - 0.5f * kb.lo)) * (float)p.inv_cv;
+  const DF d = two_sum(uu[4], __fmul_rn(-0.5f, kb.hi));
+  float pr = (d.hi + (d.lo - __fmul_rn(0.5f, kb.lo))) * (float)p.inv_cv;
   if (!(pr >= 1e-16f)) ++pfl;
   pr = tmax_(pr, 1e-16f);
   if (p.eos == GCH_EOS_SINGLE_SPECIE) {
@@ -163,7 +168,7 @@ __device__ __forceinline__ void prim_from_f32(const KParams& p, const float* uu,
 // (h + l)^2 of a compensated pair, as a pair (the l^2 term is below 2^-48)
 __device__ __forceinline__ DF df_sq(float2 x) {
   const DF p = two_prod(x.x, x.x);
-  return fast_two_sum(p.hi, p.lo + 2.0f * x.x * x.y);
+  return fast_two_sum(p.hi, p.lo + __fmul_rn(2.0f * x.x, x.y));
 }
 
 // ---------------------------------------------------------------------------
@@ -298,12 +303,12 @@ struct Ops<PolKahan> {
       // m.m / rho as a pair quotient of pair operands
       const DF m2 = df_add(df_add(df_sq(uu[1]), df_sq(uu[2])), df_sq(uu[3]));
       const float q = m2.hi * ir;
-      const float rem = (fmaf(-q, rh, m2.hi) - q * rl) + m2.lo;
-      DF kb = fast_two_sum(q, rem * ir);
+      const float rem = (fmaf(-q, rh, m2.hi) - __fmul_rn(q, rl)) + m2.lo;
+      DF kb = fast_two_sum(q, __fmul_rn(rem, ir));
       if (NEQ >= 8 && p.mhd)
         kb = df_add(kb, df_add(df_add(df_sq(uu[5]), df_sq(uu[6])), df_sq(uu[7])));
-      const DF d = two_sum(uu[4].x, -0.5f * kb.hi);
-      float pr = (d.hi + ((d.lo + uu[4].y) - 0.5f * kb.lo)) * (float)p.inv_cv;
+      const DF d = two_sum(uu[4].x, __fmul_rn(-0.5f, kb.hi));
+      float pr = (d.hi + ((d.lo + uu[4].y) - __fmul_rn(0.5f, kb.lo))) * (float)p.inv_cv;
       if (!(pr >= 1e-16f)) ++pfl;
       pr = tmax_(pr, 1e-16f);
       if (p.eos == GCH_EOS_SINGLE_SPECIE) {

@@ -154,6 +154,14 @@ class Domain:
                                                                   C.byref(err)))
         return pf.value, err.value
 
+    def tc_info(self) -> tuple[int, float]:
+        """Conduction substeps of the last tstep and the conduction
+        timescale in seconds (src/thermal_cond.f90:690-733)."""
+        n = C.c_int()
+        dtc = C.c_double()
+        check("gch_tc_info", self._lib.gch_tc_info(self._h, C.byref(n), C.byref(dtc)))
+        return n.value, dtc.value
+
     def launches_per_step(self) -> int:
         return self._lib.gch_launches_per_step(self._h)
 

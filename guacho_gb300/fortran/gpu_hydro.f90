@@ -38,6 +38,8 @@ module gpu_hydro
     type(gch_sphere_t) :: sph(GCH_MAX_SPHERES)
     real(c_double) :: grav_GM(GCH_MAX_GRAV), grav_x(GCH_MAX_GRAV)
     real(c_double) :: grav_y(GCH_MAX_GRAV), grav_z(GCH_MAX_GRAV)
+    integer(c_int32_t) :: th_cond, tc_saturation
+    real(c_double) :: rsc, rhosc, vsc2, bsc, mu
   end type gch_params_t
 
   interface
@@ -87,6 +89,12 @@ module gpu_hydro
       import :: c_int, c_ptr, c_double
       type(c_ptr), value :: dom
       real(c_double), value :: dt
+    end function
+    integer(c_int) function gch_tc_info(dom, nsteps, dt_cond) bind(C, name="gch_tc_info")
+      import :: c_int, c_ptr, c_double
+      type(c_ptr), value :: dom
+      integer(c_int), intent(out) :: nsteps
+      real(c_double), intent(out) :: dt_cond
     end function
   end interface
 

@@ -14,6 +14,7 @@ from dataclasses import dataclass, field
 SOLVER_HLL, SOLVER_HLLC, SOLVER_HLLE, SOLVER_HLLD = 1, 2, 3, 4
 EOS_ADIABATIC, EOS_SINGLE_SPECIE = 1, 2
 COOL_NONE, COOL_DMC, COOL_CHI = 0, 3, 4
+TC_OFF, TC_ISOTROPIC, TC_ANISOTROPIC = 0, 1, 2
 BC_OUTFLOW, BC_CLOSED, BC_PERIODIC, BC_OTHER = 1, 2, 3, 4
 (LIMITER_NO_AVERAGE, LIMITER_NO_LIMIT, LIMITER_MINMOD, LIMITER_VAN_LEER,
  LIMITER_VAN_ALBADA, LIMITER_UMIST, LIMITER_WOODWARD, LIMITER_SUPERBEE) = range(-1, 7)
@@ -78,6 +79,16 @@ class Params:
     spheres: list = field(default_factory=list)
     # point masses: (GM, x, y, z)
     grav: list = field(default_factory=list)
+    # thermal conduction (src/thermal_cond.f90) and the cgs scalings it
+    # converts with (parameters.f90:159-170: rsc = xphys/xmax, rhosc,
+    # vsc2, bsc = sqrt(4 pi Psc), mu)
+    th_cond: int = TC_OFF
+    tc_saturation: bool = False
+    rsc: float = 1.0
+    rhosc: float = 1.0
+    vsc2: float = 1.0
+    bsc: float = math.sqrt(4.0 * math.pi)
+    mu: float = 1.0
 
     @property
     def bfield(self) -> bool:

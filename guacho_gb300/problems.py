@@ -230,6 +230,49 @@ def wind_cooling(n=256, precision=FP64, xphys=3.0e13, nsc=1.0e5, cfl=0.4, **kw) 
     return p, u
 
 
+def conduction_blob(n=32, precision=FP64, th_cond=1, saturation=False, mhd=False, b0=1.0,
+                    xphys=3.0e17, nsc=1.0, T_hot=1.0e6, T_amb=1.0e4, radius=0.3, cfl=0.4,
+                    bc=BC_OUTFLOW, ny=None, nz=None, **kw) -> tuple:
+    """A hot sphere in a cool medium at rest with thermal conduction
+    (src/thermal_cond.f90): T = T_amb + (T_hot - T_amb)(1 - (r/radius)^2)^2
+    inside `radius` and exactly T_amb outside (so no heat crosses the walls
+    while the blob is small), rho = 1.  Guacho's cgs scalings with T0 = 1e4 K
+    and mu = 1 (parameters.f90:159-170); xphys is the box size in cm.  Hydro
+    HLLC, or MHD HLLD + flux-CD with B = (b0, 0, 0) in code units
+    (anisotropic conduction, th_cond = 2, needs mhd=True)."""
+    cv = 1.5
+    gamma = (cv + 1.0) / cv
+    T0, mu = 1.0e4, 1.0
+    rsc = xphys
+    rhosc = AMH * mu * nsc
+    Tempsc = T0 * gamma
+    vsc2 = gamma * RG * T0 / mu
+    Psc = rhosc * vsc2
+    tsc = rsc / math.sqrt(vsc2)
+    bsc = math.sqrt(4.0 * math.pi * Psc)
+    walls = dict(bc_left=bc, bc_right=bc, bc_bottom=bc, bc_top=bc, bc_out=bc, bc_in=bc)
+    if mhd:
+        phys = dict(mhd=True, riemann_solver=SOLVER_HLLD, enable_flux_cd=True)
+    else:
+        phys = dict(mhd=False, pmhd=False, riemann_solver=SOLVER_HLLC, enable_flux_cd=False)
+    phys.update(walls)
+    phys.update(kw)
+    p = Params(nx=n, ny=ny or n, nz=nz or n, precision=precision, slope_limiter=LIMITER_MINMOD,
+               cfl=cfl, cv=cv, Tempsc=Tempsc, Psc=Psc, tsc=tsc, th_cond=th_cond,
+               tc_saturation=saturation, rsc=rsc, rhosc=rhosc, vsc2=vsc2, bsc=bsc, mu=mu, **phys)
+    x, y, z = _centered_coords(p)
+    r = np.sqrt(x * x + y * y + z * z)
+    prof = np.clip(1.0 - (r / radius) ** 2, 0.0, None) ** 2
+    T = T_amb + (T_hot - T_amb) * prof
+    sh = p.shape[:3]
+    rho = np.ones(sh)
+    pr = rho * T / Tempsc
+    zero = np.zeros(sh)
+    if mhd:
+        return p, conserved(p, rho, zero, zero, zero, pr, np.full(sh, b0), zero, zero)
+    return p, conserved(p, rho, zero, zero, zero, pr)
+
+
 # ---------------------------------------------------------------------------
 def batch_boxes(nbox=64, seed=20260004, sizes=(32, 48, 64, 96), precision=FP64, cfl=0.4):
     """The batched set: `nbox` boxes with sizes drawn from `sizes`, each an

@@ -50,7 +50,7 @@
 extern "C" {
 #endif
 
-#define GCH_ABI_VERSION 1
+#define GCH_ABI_VERSION 2
 
 /* ---- switch ids: identical values to src/constants.f90:56-98 ----------- */
 #define GCH_SOLVER_HLL 1
@@ -64,6 +64,10 @@ extern "C" {
 #define GCH_COOL_NONE 0
 #define GCH_COOL_DMC 3
 #define GCH_COOL_CHI 4
+
+#define GCH_TC_OFF 0
+#define GCH_TC_ISOTROPIC 1
+#define GCH_TC_ANISOTROPIC 2
 
 #define GCH_BC_OUTFLOW 1
 #define GCH_BC_CLOSED 2
@@ -163,6 +167,14 @@ typedef struct {
   /* user source terms: point masses (EXO/user_mod.f90:158-206) */
   double grav_GM[GCH_MAX_GRAV];
   double grav_x[GCH_MAX_GRAV], grav_y[GCH_MAX_GRAV], grav_z[GCH_MAX_GRAV];
+  /* thermal conduction (th_cond and tc_saturation of parameters.f90:114-119;
+   * src/thermal_cond.f90) and the cgs scalings it converts with
+   * (parameters.f90:159-170): rsc = xphys/xmax, rhosc = amh*mu,
+   * vsc2 = gamma*Rg*T0/mu, bsc = sqrt(4*pi*Psc), mu.  Anisotropic
+   * conduction needs B; conduction with table cooling is rejected. */
+  int32_t th_cond;          /* GCH_TC_OFF | GCH_TC_ISOTROPIC | GCH_TC_ANISOTROPIC */
+  int32_t tc_saturation;
+  double rsc, rhosc, vsc2, bsc, mu;
 } gch_params_t;
 
 typedef struct gch_domain gch_domain_t;
@@ -200,8 +212,15 @@ int gch_get_timestep(gch_domain_t* d, int current_iter, int n_iter, double curre
                      double tprint, double* dt, int* dump_flag);
 
 /* src/hydro_solver.f90:134 tstep: advance u by dt (both stages, flux-CD,
- * sources, viscosity, cooling, boundaries, primitives). */
+ * sources, viscosity, cooling, boundaries, primitives, and thermal
+ * conduction when th_cond != 0).  With conduction the call waits for the
+ * device once (the super-step count depends on the state); otherwise it is
+ * asynchronous. */
 int gch_tstep(gch_domain_t* d, double dt);
+
+/* The conduction substeps of the last tstep (src/thermal_cond.f90:690-768:
+ * Nsteps and dt_cond in seconds); 0 and 0.0 when conduction is off. */
+int gch_tc_info(gch_domain_t* d, int* nsteps, double* dt_cond);
 
 /* gch_get_timestep + gch_tstep with the state in HOST memory: uploads u,
  * steps once and downloads u, for callers whose hooks need the host arrays
@@ -271,8 +290,9 @@ typedef struct gch_batch gch_batch_t;
  * together.  All boxes must share precision, neq and the physics switches;
  * sizes, spacings, boundary kinds and problem data may differ.
  *
- * FP32 boxes without table cooling, resistivity or user spheres are advanced
- * in grouped mode on `stream` (0 = a stream of the batch's own): one launch
+ * FP32 boxes without table cooling, thermal conduction, resistivity or user
+ * spheres are advanced in grouped mode on `stream` (0 = a stream of the
+ * batch's own): one launch
  * per kernel of the step covers up to 64 boxes, one CUDA graph holds the
  * step, and the z-march depth is chosen by timing before the first step.
  * Other batches run each box's own step graph on its own stream.  No

@@ -40,6 +40,7 @@ struct gor_state {
   int NX, NY, NZ;     /* with ghosts */
   size_t ncell;
   double *u, *up, *primit, *f, *g, *h, *e;
+  double* temp;       /* Temp (src/globals.f90), filled by calcprim */
   double time;
   int err;
 };
@@ -881,27 +882,30 @@ static void boundaryII(gor_state_t* s) { boundary_fill(s, s->up, 2); }
 static void calcprim_arr(gor_state_t* s, const double* uarr, int only_ghost) {
   const gor_params_t* p = &s->p;
   const int neq = p->neq, nx = p->nx, ny = p->ny, nz = p->nz;
+#define CP(i, j, k) \
+  u2prim(p, &uarr[CID(s, i, j, k) * neq], &s->primit[CID(s, i, j, k) * neq], &s->temp[CID(s, i, j, k)])
   if (only_ghost) {
     for (int j = 0; j <= ny + 1; ++j)
       for (int i = 0; i <= nx + 1; ++i) {
-        u2prim(p, &uarr[CID(s, i, j, 0) * neq], &s->primit[CID(s, i, j, 0) * neq], NULL);
-        u2prim(p, &uarr[CID(s, i, j, nz + 1) * neq], &s->primit[CID(s, i, j, nz + 1) * neq], NULL);
+        CP(i, j, 0);
+        CP(i, j, nz + 1);
       }
     for (int k = 0; k <= nz + 1; ++k)
       for (int i = 0; i <= nx + 1; ++i) {
-        u2prim(p, &uarr[CID(s, i, 0, k) * neq], &s->primit[CID(s, i, 0, k) * neq], NULL);
-        u2prim(p, &uarr[CID(s, i, ny + 1, k) * neq], &s->primit[CID(s, i, ny + 1, k) * neq], NULL);
+        CP(i, 0, k);
+        CP(i, ny + 1, k);
       }
     for (int k = 0; k <= nz + 1; ++k)
       for (int j = 0; j <= ny + 1; ++j) {
-        u2prim(p, &uarr[CID(s, 0, j, k) * neq], &s->primit[CID(s, 0, j, k) * neq], NULL);
-        u2prim(p, &uarr[CID(s, nx + 1, j, k) * neq], &s->primit[CID(s, nx + 1, j, k) * neq], NULL);
+        CP(0, j, k);
+        CP(nx + 1, j, k);
       }
     return;
   }
+#undef CP
   const size_t n = s->ncell;
 #pragma omp parallel for schedule(static)
-  for (size_t c = 0; c < n; ++c) u2prim(p, &uarr[c * neq], &s->primit[c * neq], NULL);
+  for (size_t c = 0; c < n; ++c) u2prim(p, &uarr[c * neq], &s->primit[c * neq], &s->temp[c]);
 }
 
 void gor_calcprim(gor_state_t* s, int only_ghost) { calcprim_arr(s, s->u, only_ghost); }
@@ -978,6 +982,259 @@ void gor_get_timestep(gor_state_t* s, int iter, int n_iter, double t, double tpr
   }
 }
 
+/* ---------------------------------------------------------------------- */
+/* src/thermal_cond.f90: Spitzer thermal conduction (isotropic, or split
+ * along and across B), optionally saturated, advanced with Chebyshev super
+ * time steps.  The heat fluxes live in component 5 of the face flux arrays
+ * f, g, h, as in the reference. */
+#define TC_RG 8.3145e7   /* gas constant, src/constants.f90:35 */
+#define TC_PH 0.4        /* saturation parameter, thermal_cond.f90:36 */
+#define TC_NU 0.01       /* super-step damping factor, :37 */
+#define TC_RED 0.25      /* tstep_red_factor, :41 */
+#define TC_CLIGHT 3.e10  /* :195, :281 */
+
+/* real**integer with a variable exponent: gfortran evaluates it by binary
+ * (square-and-multiply) exponentiation, which this restates */
+static double powi_sq(double x, int m) {
+  unsigned n = m < 0 ? 0u - (unsigned)m : (unsigned)m;
+  double y = (n % 2u) ? x : 1.0;
+  while (n >>= 1) {
+    x = x * x;
+    if (n % 2u) y = y * x;
+  }
+  return m < 0 ? 1.0 / y : y;
+}
+
+/* :625-636 superstep: length of a super step of N substeps */
+double gor_superstep(int N, double snu) {
+  const double a = powi_sq(1.0 + snu, 2 * N), b = powi_sq(1.0 - snu, 2 * N);
+  return (double)N / (2.0 * snu) * (a - b) / (a + b);
+}
+
+/* :646-654 substep: size of substep j of N */
+double gor_substep(int j, int N, double nu) {
+  const double pi = acos(-1.0);
+  return 1.0 / ((nu - 1.0) * cos(pi * (double)(2 * j - 1) / (2.0 * (double)N)) + nu + 1.0);
+}
+
+/* :664-681 ST_steps: the first N whose super step exceeds fs (200 when none
+ * of 1..199 does, the value of the Fortran DO index after the loop) */
+void gor_st_steps(double fs, int* Ns, double* fstep) {
+  const double snu = sqrt(TC_NU);
+  int j;
+  for (j = 1; j <= 199; ++j)
+    if (gor_superstep(j, snu) > fs) break;
+  *Ns = j;
+  *fstep = fs / gor_superstep(j, snu);
+}
+
+/* :142-178 Spitzer conductivities */
+static double ksp(double T) { return 6.e-7 * pow(T, 2.5); }
+static double ksp_parl(double T) { return 9.2181e-7 * pow(T, 2.5); }
+static double ksp_perp(double T, double dens, double B2) {
+  return 0.30089e+33 * dens / (B2 * sqrt(T)) * dens;
+}
+
+/* :78-110 get_dt_cond (seconds) */
+static double get_dt_cond(gor_state_t* s) {
+  const gor_params_t* p = &s->p;
+  double dtp = 1.7976931348623157e308; /* huge(1.) */
+  double ddx = dmin(p->dx, p->dy);
+  ddx = dmin(ddx, p->dz);
+  for (int k = 1; k <= p->nz; ++k)
+    for (int j = 1; j <= p->ny; ++j)
+      for (int i = 1; i <= p->nx; ++i)
+        dtp = dmin(dtp, AT(s, s->primit, 1, i, j, k) / ksp(s->temp[CID(s, i, j, k)]));
+  const double x = ddx * p->rsc;
+  return TC_RED * 0.5 * (x * x) * p->cv * TC_RG * dtp * p->rhosc / p->mu;
+}
+
+/* One face of :189-267 heatfluxes: the flux from cell a to cell b (b = a + 1
+ * along the face normal), spacing d */
+static double heatflux_iso(const gor_state_t* s, size_t a, size_t b, double d) {
+  const gor_params_t* p = &s->p;
+  const int neq = p->neq;
+  const double yhp = 1.0;
+  const double Ta = s->temp[a], Tb = s->temp[b];
+  if (Ta == Tb) return 0.0;
+  const double meanP = 0.5 * (s->primit[a * neq + 4] + s->primit[b * neq + 4]);
+  const double meanDens = 0.5 * (s->primit[a * neq] + s->primit[b * neq]);
+  const double meanT = 0.5 * (Ta + Tb);
+  const double dT = (Tb - Ta) / (d * p->rsc);
+  double coef;
+  if (p->tc_saturation) {
+    double cs = csound(p, meanP, meanDens);
+    cs = dmin(cs * sqrt(p->vsc2), TC_CLIGHT);
+    coef = dmin(ksp(meanT), 5. * TC_PH * cs * meanP * p->Psc / fabs(dT));
+  } else {
+    coef = ksp(meanT);
+  }
+  return -coef * dT * yhp;
+}
+
+static void heatfluxes(gor_state_t* s) {
+  const gor_params_t* p = &s->p;
+  const int neq = p->neq;
+#pragma omp parallel for schedule(static)
+  for (int k = 0; k <= p->nz; ++k)
+    for (int j = 0; j <= p->ny; ++j)
+      for (int i = 0; i <= p->nx; ++i) {
+        const size_t c = CID(s, i, j, k);
+        s->f[c * neq + 4] = heatflux_iso(s, c, CID(s, i + 1, j, k), p->dx);
+        s->g[c * neq + 4] = heatflux_iso(s, c, CID(s, i, j + 1, k), p->dy);
+        s->h[c * neq + 4] = heatflux_iso(s, c, CID(s, i, j, k + 1), p->dz);
+      }
+}
+
+/* :277-487 MHD_heatfluxes: conduction along and across the unit vector of B
+ * of the cell on the left of the three faces */
+static void mhd_heatfluxes(gor_state_t* s) {
+  const gor_params_t* p = &s->p;
+  const int neq = p->neq;
+  const double phi = 0.3, alpha = 5.0 * phi;
+  const double bsc2 = p->bsc * p->bsc;
+  const double vsc = sqrt(p->vsc2);
+#pragma omp parallel for schedule(static)
+  for (int k = 0; k <= p->nz; ++k)
+    for (int j = 0; j <= p->ny; ++j)
+      for (int i = 0; i <= p->nx; ++i) {
+        const size_t c = CID(s, i, j, k);
+        const size_t nb[3] = {CID(s, i + 1, j, k), CID(s, i, j + 1, k), CID(s, i, j, k + 1)};
+        const double dd[3] = {p->dx, p->dy, p->dz};
+        double bx = s->primit[c * neq + 5], by = s->primit[c * neq + 6], bz = s->primit[c * neq + 7];
+        const double B2 = bx * bx + by * by + bz * bz;
+        const double modB = sqrt(B2);
+        bx = bx / modB;
+        by = by / modB;
+        bz = bz / modB;
+        double grad[3], kpar[3], kperp[3], csat[3];
+        for (int a = 0; a < 3; ++a) {
+          const double Tc = s->temp[c], Tn = s->temp[nb[a]];
+          if (fabs(Tc - Tn) < 1.0e-14) {
+            grad[a] = 0.0;
+            kpar[a] = 0.0;
+            kperp[a] = 0.0;
+            csat[a] = 0.0;
+            continue;
+          }
+          const double meanDens = 0.5 * (s->primit[c * neq] + s->primit[nb[a] * neq]);
+          const double meanTemp = 0.5 * (Tc + Tn);
+          if (p->tc_saturation) {
+            const double meanPres = 0.5 * (s->primit[c * neq + 4] + s->primit[nb[a] * neq + 4]);
+            double cs = csound(p, meanPres, meanDens);
+            cs = dmin(cs * vsc, TC_CLIGHT);
+            csat[a] = alpha * meanDens * (cs * cs * cs);
+          } else {
+            csat[a] = 0.0;
+          }
+          grad[a] = (Tn - Tc) / (dd[a] * p->rsc);
+          kpar[a] = ksp_parl(meanTemp);
+          kperp[a] = ksp_perp(meanTemp, meanDens * p->rhosc, B2 * bsc2);
+        }
+        const double bgradT = bx * grad[0] + by * grad[1] + bz * grad[2];
+        const double gpar[3] = {bgradT * bx, bgradT * by, bgradT * bz};
+        const double gperp[3] = {grad[0] - gpar[0], grad[1] - gpar[1], grad[2] - gpar[2]};
+        double out[3];
+        if (!p->tc_saturation) {
+          for (int a = 0; a < 3; ++a) out[a] = -kpar[a] * gpar[a] - kperp[a] * gperp[a];
+        } else {
+          const double gpar_n = bgradT;
+          const double gperp_n = sqrt(gperp[0] * gperp[0] + gperp[1] * gperp[1] + gperp[2] * gperp[2]);
+          for (int a = 0; a < 3; ++a)
+            out[a] = -1. / (1. / (kpar[a] + 1.e-14) + gpar_n / (csat[a] + 1.e-14)) * gpar[a]
+                     - 1. / (1. / (kperp[a] + 1.e-14) + gperp_n / (csat[a] + 1.e-14)) * gperp[a];
+        }
+        s->f[c * neq + 4] = out[0];
+        s->g[c * neq + 4] = out[1];
+        s->h[c * neq + 4] = out[2];
+      }
+}
+
+/* :496-616 thermal_bounds, serial build: the periodic copies of the first
+ * ghost layer of u(5), then, unconditionally, the outflow copies of the
+ * physical walls, which overwrite the periodic ones over 0:n+1 */
+static void thermal_bounds(gor_state_t* s) {
+  const gor_params_t* p = &s->p;
+  const int neq = p->neq, nx = p->nx, ny = p->ny, nz = p->nz;
+#define U5(i, j, k) s->u[CID(s, i, j, k) * neq + 4]
+  if (p->bc_left == GOR_BC_PERIODIC && p->bc_right == GOR_BC_PERIODIC)
+    for (int k = 1 - NG; k <= nz + NG; ++k)
+      for (int j = 1 - NG; j <= ny + NG; ++j) {
+        U5(0, j, k) = U5(nx, j, k);
+        U5(nx + 1, j, k) = U5(1, j, k);
+      }
+  if (p->bc_bottom == GOR_BC_PERIODIC && p->bc_top == GOR_BC_PERIODIC)
+    for (int k = 1 - NG; k <= nz + NG; ++k)
+      for (int i = 1 - NG; i <= nx + NG; ++i) {
+        U5(i, 0, k) = U5(i, ny, k);
+        U5(i, ny + 1, k) = U5(i, 1, k);
+      }
+  if (p->bc_out == GOR_BC_PERIODIC && p->bc_in == GOR_BC_PERIODIC)
+    for (int j = 1 - NG; j <= ny + NG; ++j)
+      for (int i = 1 - NG; i <= nx + NG; ++i) {
+        U5(i, j, 0) = U5(i, j, nz);
+        U5(i, j, nz + 1) = U5(i, j, 1);
+      }
+  for (int k = 0; k <= nz + 1; ++k)
+    for (int j = 0; j <= ny + 1; ++j) U5(0, j, k) = U5(1, j, k);
+  for (int k = 0; k <= nz + 1; ++k)
+    for (int j = 0; j <= ny + 1; ++j) U5(nx + 1, j, k) = U5(nx, j, k);
+  for (int k = 0; k <= nz + 1; ++k)
+    for (int i = 0; i <= nx + 1; ++i) U5(i, 0, k) = U5(i, 1, k);
+  for (int k = 0; k <= nz + 1; ++k)
+    for (int i = 0; i <= nx + 1; ++i) U5(i, ny + 1, k) = U5(i, ny, k);
+  for (int j = 0; j <= ny + 1; ++j)
+    for (int i = 0; i <= nx + 1; ++i) U5(i, j, 0) = U5(i, j, 1);
+  for (int j = 0; j <= ny + 1; ++j)
+    for (int i = 0; i <= nx + 1; ++i) U5(i, j, nz + 1) = U5(i, j, nz);
+#undef U5
+}
+
+/* :690-768 thermal_conduction, from primit and Temp of the last calcprim */
+void gor_thermal_conduction(gor_state_t* s, double dt_CFL, int* nsteps_out, double* dt_cond_out) {
+  const gor_params_t* p = &s->p;
+  const int neq = p->neq;
+  const double dt_hydro = dt_CFL * p->tsc;
+  const double dt_cond = get_dt_cond(s);
+  int SuperStep = 1, Nsteps;
+  double fstep;
+  if (dt_cond < dt_hydro) {
+    gor_st_steps(dt_hydro / dt_cond, &Nsteps, &fstep);
+  } else {
+    SuperStep = 0;
+    fstep = dt_hydro / dt_cond;
+    Nsteps = 1;
+  }
+  if (nsteps_out) *nsteps_out = Nsteps;
+  if (dt_cond_out) *dt_cond_out = dt_cond;
+  for (int n = 1; n <= Nsteps; ++n) {
+    double dts;
+    if (SuperStep)
+      dts = dt_cond * fstep * gor_substep(n, Nsteps, TC_NU) / p->Psc / p->rsc;
+    else
+      dts = dt_hydro / (double)Nsteps / p->Psc / p->rsc;
+    if (p->th_cond == 2) mhd_heatfluxes(s);
+    if (p->th_cond == 1) heatfluxes(s);
+#pragma omp parallel for schedule(static)
+    for (int k = 1; k <= p->nz; ++k)
+      for (int j = 1; j <= p->ny; ++j)
+        for (int i = 1; i <= p->nx; ++i) {
+          const size_t c = CID(s, i, j, k);
+          s->u[c * neq + 4] =
+              s->u[c * neq + 4] -
+              dts * ((s->f[c * neq + 4] - s->f[CID(s, i - 1, j, k) * neq + 4]) / p->dx +
+                     (s->g[c * neq + 4] - s->g[CID(s, i, j - 1, k) * neq + 4]) / p->dy +
+                     (s->h[c * neq + 4] - s->h[CID(s, i, j, k - 1) * neq + 4]) / p->dz);
+        }
+    thermal_bounds(s);
+    calcprim_arr(s, s->u, 0);
+  }
+}
+
+void gor_get_temp(const gor_state_t* s, double* temp) {
+  memcpy(temp, s->temp, s->ncell * sizeof(double));
+}
+
 /* src/hydro_solver.f90:134-229  tstep */
 void gor_tstep(gor_state_t* s, double dt_CFL) {
   const gor_params_t* p = &s->p;
@@ -993,6 +1250,7 @@ void gor_tstep(gor_state_t* s, double dt_CFL) {
   if (table) cooling_table(s, dt_CFL);
   gor_boundaryI(s);
   calcprim_arr(s, s->u, table);
+  if (p->th_cond != 0) gor_thermal_conduction(s, dt_CFL, NULL, NULL);
 }
 
 /* ---------------------------------------------------------------------- */
@@ -1013,7 +1271,8 @@ gor_state_t* gor_create(const gor_params_t* p) {
   s->g = (double*)calloc(nv, sizeof(double));
   s->h = (double*)calloc(nv, sizeof(double));
   s->e = (double*)calloc(s->ncell * 3, sizeof(double));
-  if (!s->u || !s->up || !s->primit || !s->f || !s->g || !s->h || !s->e) {
+  s->temp = (double*)calloc(s->ncell, sizeof(double));
+  if (!s->u || !s->up || !s->primit || !s->f || !s->g || !s->h || !s->e || !s->temp) {
     gor_destroy(s);
     return NULL;
   }
@@ -1023,7 +1282,7 @@ gor_state_t* gor_create(const gor_params_t* p) {
 void gor_destroy(gor_state_t* s) {
   if (!s) return;
   free(s->u); free(s->up); free(s->primit);
-  free(s->f); free(s->g); free(s->h); free(s->e);
+  free(s->f); free(s->g); free(s->h); free(s->e); free(s->temp);
   free(s);
 }
 

@@ -84,6 +84,11 @@ typedef struct {
   int ngrav;
   double grav_GM[GOR_MAX_GRAV], grav_x[GOR_MAX_GRAV], grav_y[GOR_MAX_GRAV],
          grav_z[GOR_MAX_GRAV];
+  /* thermal conduction (src/thermal_cond.f90): th_cond = TC_OFF 0,
+   * TC_ISOTROPIC 1, TC_ANISOTROPIC 2 (src/constants.f90:96-98); the cgs
+   * scalings of parameters.f90:159-170 it converts with */
+  int th_cond, tc_saturation;
+  double rsc, rhosc, vsc2, bsc, mu;
 } gor_params_t;
 
 typedef struct gor_state gor_state_t;
@@ -117,6 +122,19 @@ void gor_prim2u(const gor_params_t* p, const double* prim, double* uu);
 void gor_limiter(const gor_params_t* p, const double* pll, double* pl, double* pr,
                  const double* prr);
 double gor_cooltab(const gor_params_t* p, double T);
+
+/* src/thermal_cond.f90:690-768 thermal_conduction: the conduction substeps
+ * that tstep runs after the hydro step when th_cond != 0 (called by
+ * gor_tstep; exposed for tests with the hydro step's dt_CFL).  *nsteps and
+ * *dt_cond (may be NULL) report the substep count and the conduction
+ * timescale in seconds. */
+void gor_thermal_conduction(gor_state_t* s, double dt_CFL, int* nsteps, double* dt_cond);
+/* Temperature of every cell from the last calcprim (src/globals.f90 Temp). */
+void gor_get_temp(const gor_state_t* s, double* temp /* NX*NY*NZ, x fastest */);
+/* The super-time-stepping helpers (src/thermal_cond.f90:625-681). */
+double gor_superstep(int n, double snu);
+double gor_substep(int j, int n, double nu);
+void gor_st_steps(double fs, int* ns, double* fstep);
 
 /* Diagnostics: centred div B over the interior (src/Out_BIN_Module.f90:214-222). */
 void gor_divb(const gor_state_t* s, double* divb /* nx*ny*nz */);

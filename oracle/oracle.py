@@ -58,6 +58,9 @@ class GorParams(C.Structure):
         ("nsph", C.c_int), ("sph", Sph * MAXSPH),
         ("ngrav", C.c_int), ("grav_GM", C.c_double * MAXGRAV), ("grav_x", C.c_double * MAXGRAV),
         ("grav_y", C.c_double * MAXGRAV), ("grav_z", C.c_double * MAXGRAV),
+        ("th_cond", C.c_int), ("tc_saturation", C.c_int),
+        ("rsc", C.c_double), ("rhosc", C.c_double), ("vsc2", C.c_double), ("bsc", C.c_double),
+        ("mu", C.c_double),
     ]
 
 
@@ -91,6 +94,8 @@ def params_struct(p) -> GorParams:
     s.ngrav = len(p.grav)
     for i, (gm, x, y, z) in enumerate(p.grav):
         s.grav_GM[i], s.grav_x[i], s.grav_y[i], s.grav_z[i] = gm, x, y, z
+    s.th_cond, s.tc_saturation = p.th_cond, int(p.tc_saturation)
+    s.rsc, s.rhosc, s.vsc2, s.bsc, s.mu = p.rsc, p.rhosc, p.vsc2, p.bsc, p.mu
     return s
 
 
@@ -118,6 +123,10 @@ def lib() -> C.CDLL:
             "gor_limiter": (None, [GP, P, P, P, P]), "gor_cooltab": (D, [GP, D]),
             "gor_divb": (None, [P, P]),
             "gor_run": (I, [P, D, D, I, I, IP, DP]),
+            "gor_thermal_conduction": (None, [P, D, IP, DP]),
+            "gor_get_temp": (None, [P, P]),
+            "gor_superstep": (D, [I, D]), "gor_substep": (D, [I, I, D]),
+            "gor_st_steps": (None, [D, IP, DP]),
         }
         for name, (res, args) in sigs.items():
             f = getattr(L, name)
@@ -213,6 +222,21 @@ class Oracle:
         self.L.gor_divb(self.h, _p(out))
         return out
 
+    def thermal_conduction(self, dt_cfl: float) -> tuple[int, float]:
+        """src/thermal_cond.f90:690-768 on the current state; returns the
+        substep count and the conduction timescale (seconds)."""
+        n = C.c_int()
+        dtc = C.c_double()
+        self.L.gor_thermal_conduction(self.h, dt_cfl, C.byref(n), C.byref(dtc))
+        return n.value, dtc.value
+
+    def temp(self) -> np.ndarray:
+        """Temp of every cell, (z, y, x) with ghosts."""
+        p = self.params
+        out = np.empty(p.shape[:3])
+        self.L.gor_get_temp(self.h, _p(out))
+        return out
+
 
 def riemann(params, pl, pr):
     ps = params_struct(params)
@@ -259,3 +283,18 @@ def limiter(params, pll, pl, pr, prr):
 def cooltab(params, T: float) -> float:
     ps = params_struct(params)
     return lib().gor_cooltab(C.byref(ps), T)
+
+
+def superstep(n: int, snu: float) -> float:
+    return lib().gor_superstep(n, snu)
+
+
+def substep(j: int, n: int, nu: float) -> float:
+    return lib().gor_substep(j, n, nu)
+
+
+def st_steps(fs: float) -> tuple[int, float]:
+    ns = C.c_int()
+    fstep = C.c_double()
+    lib().gor_st_steps(fs, C.byref(ns), C.byref(fstep))
+    return ns.value, fstep.value

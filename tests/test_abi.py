@@ -68,9 +68,20 @@ def test_params_check_accepts_configs(gpu_lib, make):
     dict(user_source_terms=True),                  # no point masses
     dict(precision=7),
     dict(cooling=2),                               # COOL_BBC is not on this path
+    dict(th_cond=3),
+    dict(th_cond=P.TC_ISOTROPIC, rsc=0.0),          # conduction needs the cgs scalings
 ])
 def test_params_check_rejects(gpu_lib, bad):
     p = problems.orszag_tang(16, 16, 4)[0].replace(**bad)
+    assert _check(p) == _abi.ERR_PARAM
+
+
+def test_conduction_params(gpu_lib):
+    assert _check(problems.conduction_blob(8)[0]) == 0
+    assert _check(problems.conduction_blob(8, th_cond=P.TC_ANISOTROPIC, mhd=True)[0]) == 0
+    # anisotropic conduction needs B; conduction with table cooling is rejected
+    assert _check(problems.conduction_blob(8, th_cond=P.TC_ANISOTROPIC)[0]) == _abi.ERR_PARAM
+    p = problems.wind_cooling(16)[0].replace(th_cond=P.TC_ISOTROPIC)
     assert _check(p) == _abi.ERR_PARAM
 
 
@@ -119,7 +130,8 @@ def test_switch_ids_match_reference_constants():
             "COOL_CHI": 4, "BC_OUTFLOW": 1, "BC_CLOSED": 2, "BC_PERIODIC": 3, "BC_OTHER": 4,
             "LIMITER_NO_AVERAGE": -1, "LIMITER_NO_LIMIT": 0, "LIMITER_MINMOD": 1,
             "LIMITER_VAN_LEER": 2, "LIMITER_VAN_ALBADA": 3, "LIMITER_UMIST": 4,
-            "LIMITER_WOODWARD": 5, "LIMITER_SUPERBEE": 6}
+            "LIMITER_WOODWARD": 5, "LIMITER_SUPERBEE": 6,
+            "TC_OFF": 0, "TC_ISOTROPIC": 1, "TC_ANISOTROPIC": 2}
     for k, v in want.items():
         m = re.search(rf"#define GCH_{k} \(?(-?\d+)\)?", text)
         assert m and int(m.group(1)) == v, k

@@ -317,6 +317,9 @@ def test_divb_roundoff_mixed(gpu_lib, prec):
 
 
 def test_batch_matches_single_domains(gpu_lib):
+    """A grouped FP32 batch runs the one-box kernel bodies in other kernel
+    instantiations, where the compiler may contract a*b+c differently: each
+    box matches its single-domain run to a few FP32 roundings per field."""
     from guacho_gb300.domain import Batch, Domain
     boxes = problems.batch_boxes(nbox=4, sizes=(16, 24), precision=P.FP32_MIXED)
     b = Batch([p for p, _ in boxes])
@@ -327,5 +330,9 @@ def test_batch_matches_single_domains(gpu_lib):
         with Domain(p) as d:
             d.init(u)
             d.run(1e300, 1e300, max_steps=5)
-            assert np.array_equal(b.download(i), d.download())
+            ref = d.download()
+        got = b.download(i)
+        scale = np.abs(ref).reshape(-1, p.neq).max(axis=0)
+        err = np.abs(got - ref).reshape(-1, p.neq).max(axis=0)
+        assert np.all(err <= 1e-5 * np.maximum(scale, 1e-30)), (i, err / scale)
     b.close()

@@ -1,0 +1,173 @@
+"""Thermal conduction (src/thermal_cond.f90): known answers of the oracle's
+restatement (CPU), then the GB300 path against the oracle (GPU).
+
+The reference ships no conduction test.  The oracle is pinned by:
+  - the super-time-stepping identity: the N substeps of
+    substep(j, N, nu) (:646-654) add up to superstep(N, sqrt(nu)) (:625-636),
+    the closed form of the Chebyshev sum (Alexiades, Amiez & Gremaud 1996);
+  - ST_steps (:664-681) picks the first N whose super step exceeds the ratio;
+  - a uniform temperature conducts nothing (every face takes the
+    Temp == Temp branch and the update adds exact zeros);
+  - a blob that has not reached the walls conserves the energy of the box
+    (the face fluxes telescope) and cools its peak;
+  - isotropic conduction is symmetric under x <-> y;
+  - anisotropic conduction with B along x carries heat along x and almost
+    none along y (Spitzer K_perp / K_parl ~ 1e-17 here).
+The CUDA path then matches the oracle through whole timesteps (hydro +
+conduction) on every precision path."""
+import math
+
+import numpy as np
+import pytest
+
+from guacho_gb300 import params as P
+from guacho_gb300 import problems
+from oracle import oracle as O
+
+INT = (slice(2, -2),) * 3
+
+
+def _oracle_after_tc(p, u, dt=None):
+    o = O.Oracle(p)
+    o.init(u)
+    if dt is None:
+        dt, _ = o.get_timestep(20, 10, 0.0, 1e30)
+    n, dtc = o.thermal_conduction(dt)
+    return o, n, dtc
+
+
+@pytest.mark.parametrize("N", [1, 2, 3, 7, 13, 40, 120])
+def test_substeps_sum_to_superstep(N):
+    s = sum(O.substep(j, N, 0.01) for j in range(1, N + 1))
+    assert s == pytest.approx(O.superstep(N, math.sqrt(0.01)), rel=1e-12)
+
+
+@pytest.mark.parametrize("fs", [1.5, 10.0, 59.5, 300.0, 1e4])
+def test_st_steps_first_superstep_above_ratio(fs):
+    ns, fstep = O.st_steps(fs)
+    snu = math.sqrt(0.01)
+    if ns <= 199:
+        assert O.superstep(ns, snu) > fs
+        assert ns == 1 or O.superstep(ns - 1, snu) <= fs
+    else:  # the search ran out: the Fortran loop index is 200
+        assert ns == 200 and all(O.superstep(j, snu) <= fs for j in range(1, 200))
+    assert fstep == fs / O.superstep(ns, snu)
+
+
+def test_uniform_temperature_conducts_nothing():
+    p, u = problems.conduction_blob(12, T_hot=1.0e4)  # T = T_amb everywhere
+    o, n, _ = _oracle_after_tc(p, u)
+    assert n >= 1
+    assert np.array_equal(o.download()[INT], u[INT])
+
+
+@pytest.mark.parametrize("sat", [False, True])
+def test_blob_conserves_energy_and_cools(sat):
+    p, u = problems.conduction_blob(24, saturation=sat)
+    o = O.Oracle(p)
+    o.init(u)
+    t0 = o.temp()[INT].copy()
+    dt, _ = o.get_timestep(20, 10, 0.0, 1e30)
+    n, dtc = o.thermal_conduction(dt)
+    assert n > 1 and dtc < dt * p.tsc       # super steps were needed
+    u1 = o.download()
+    e0, e1 = u[INT][..., 4].sum(), u1[INT][..., 4].sum()
+    assert abs(e1 - e0) <= 1e-13 * e0
+    t1 = o.temp()[INT]
+    assert t1.max() < t0.max() and np.abs(t1 - t0).max() > 1e-3 * t0.max()
+    # only the energy changes
+    assert np.array_equal(u1[INT][..., :4], u[INT][..., :4])
+
+
+def test_isotropic_xy_symmetry():
+    p, u = problems.conduction_blob(16, ny=20, nz=8, radius=0.25)
+    pt = p.replace(nx=p.ny, ny=p.nx)
+    ut = np.ascontiguousarray(np.swapaxes(u, 1, 2))
+    o, _, _ = _oracle_after_tc(p, u, dt=1e-3)
+    ot, _, _ = _oracle_after_tc(pt, ut, dt=1e-3)
+    a = o.download()[..., 4]
+    b = np.swapaxes(ot.download()[..., 4], 1, 2)
+    assert np.allclose(a, b, rtol=1e-13, atol=0)
+
+
+def test_anisotropic_conducts_along_b():
+    p, u = problems.conduction_blob(20, th_cond=P.TC_ANISOTROPIC, mhd=True, b0=1.0)
+    o, n, _ = _oracle_after_tc(p, u, dt=1e-3)
+    assert n >= 1
+    de = o.download()[INT][..., 4] - u[INT][..., 4]
+    c = p.nx // 2
+    # cells on the x line through the centre (along B) gain heat; cells on
+    # the y line gain nothing beyond round-off
+    gain_x = de[c, c, :].max()
+    gain_y = de[c, :, c].max()
+    assert gain_x > 1.0 and gain_y < 1e-9 * gain_x
+
+
+# ---------------------------------------------------------------------------
+def _gpu_vs_oracle(p, u, steps):
+    from guacho_gb300.domain import Domain
+    o = O.Oracle(p.replace(precision=P.FP64))
+    o.init(u)
+    with Domain(p) as d:
+        d.init(u)
+        t = 0.0
+        for it in range(1, steps + 1):
+            dto, _ = o.get_timestep(it, 10, t, 1e30)
+            dtg, _ = d.get_timestep(it, 10, t, 1e30)
+            o.tstep(dto)
+            d.tstep(dtg)
+            ng, dtcg = d.tc_info()
+            t += dto
+        ug = d.download()
+    return ug, o.download(), dtg / dto - 1.0, ng
+
+
+def _rel_field_err(a, b):
+    a, b = a[INT], b[INT]
+    scale = np.abs(b).reshape(-1, b.shape[-1]).max(axis=0)
+    return (np.abs(a - b).reshape(-1, b.shape[-1]).max(axis=0) / np.maximum(scale, 1e-300))
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("case", ["iso", "iso_sat", "aniso", "aniso_sat", "iso_periodic"])
+def test_gpu_fp64_matches_oracle(gpu_lib, case):
+    """FP64: only pow() (T^2.5) rounds differently from the host libm, so
+    the GPU matches the oracle to ~1e-12 after 3 steps of hydro + conduction,
+    with the same substep counts."""
+    kw = dict(saturation="sat" in case)
+    if case.startswith("aniso"):
+        kw.update(th_cond=P.TC_ANISOTROPIC, mhd=True)
+    if case == "iso_periodic":
+        kw.update(bc=P.BC_PERIODIC)
+    p, u = problems.conduction_blob(20, ny=16, nz=12, **kw)
+    ug, uo, ddt, ng = _gpu_vs_oracle(p, u, 3)
+    assert ng > 1
+    assert abs(ddt) < 1e-12
+    assert _rel_field_err(ug, uo).max() < 1e-11
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("prec", [P.FP32_MIXED, P.FP32_KAHAN])
+def test_gpu_fp32_paths_with_conduction(gpu_lib, prec):
+    """The FP32 paths run conduction in FP64 on their stored u: per-field
+    error against the FP64 oracle after 3 steps within the FP32 tolerance."""
+    p, u = problems.conduction_blob(20, ny=16, nz=12, th_cond=P.TC_ANISOTROPIC, mhd=True)
+    ug, uo, _, _ = _gpu_vs_oracle(p.replace(precision=prec), u, 3)
+    err = _rel_field_err(ug, uo)
+    assert err.max() < 1e-4, err
+
+
+@pytest.mark.gpu
+def test_gpu_device_loop_with_conduction(gpu_lib):
+    """gch_advance with conduction runs the main loop from the host and
+    lands on the oracle's main loop (time, steps, state)."""
+    from guacho_gb300.domain import Domain
+    p, u = problems.conduction_blob(16, ny=12, nz=8)
+    o = O.Oracle(p)
+    o.init(u)
+    no = o.run(0.004, 0.0015)
+    with Domain(p) as d:
+        d.init(u)
+        nd = d.run(0.004, 0.0015)
+        assert nd == no and d.time == pytest.approx(o.time, rel=1e-12)
+        assert _rel_field_err(d.download(), o.download()).max() < 1e-11
