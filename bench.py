@@ -133,8 +133,8 @@ def peaks() -> dict:
 # algorithmic bytes per cell of the dominant kernel (stage-2 k_flux) and per
 # zone-update of the whole step (two-sweep minimum 3 u + 2 up passes)
 # ncu, 256^3 turbulence, one k_flux<PolKahan,4,8,2,0,2> launch:
-# dram__bytes_read.sum 1293642240 + dram__bytes_write.sum 834974208
-STAGE2_KAHAN_TRAFFIC_PER_CELL = (1293642240 + 834974208) / 256 ** 3
+# dram__bytes_read.sum 1281655040 + dram__bytes_write.sum 842233344
+STAGE2_KAHAN_TRAFFIC_PER_CELL = (1281655040 + 842233344) / 256 ** 3
 
 
 def kernel_bytes_per_cell(prec: int, neq: int = 8) -> int:
@@ -395,7 +395,7 @@ def run_ours(args, dist: Dist) -> None:
         if traffic is None and headline == P.FP32_KAHAN:
             # dram__bytes_read.sum + dram__bytes_write.sum of one stage-2
             # k_flux launch (FP32 + Kahan, HLLD, van Leer) measured by ncu on
-            # the 256^3 box: 126.88 bytes per cell, scaled by the cell count
+            # the 256^3 box: 126.59 bytes per cell, scaled by the cell count
             traffic = STAGE2_KAHAN_TRAFFIC_PER_CELL * cells
         roof = {"kernel": dom, "bound": "hbm", "achieved": ach, "peak": pk["hbm_gbs"],
                 "unit": "GB/s", "frac": ach / pk["hbm_gbs"], "traffic": traffic,

@@ -64,6 +64,12 @@ struct Src {
   }
 };
 
+// FP32 x/y-face reconstruction with minmod or van Leer runs paired
+// (muscl_pair); FP64 and the other limiters take the scalar expressions.
+template <class TC, int LIM>
+constexpr bool kPairedMuscl = sizeof(TC) == 4 &&
+                              (LIM == GCH_LIMITER_VAN_LEER || LIM == GCH_LIMITER_MINMOD);
+
 // Shared memory of the stage kernel (dynamic: up to 72 KB in FP32).
 template <class TC, int NEQ, int STAGE>
 struct FluxSmem {
@@ -271,10 +277,16 @@ flux_body(const KParams& p, const typename Src<Pol, NEQ, STAGE, PRIM_IN>::TIn* _
           r[q] = sP[q][cy][cl + 1];
           if (STAGE == 2) {
             const TC ll = sP[q][cy][cl - 1], rr = sP[q][cy][cl + 2];
-            const TC dl = l[q] - ll, dm = r[q] - l[q], dr = rr - r[q];
-            const TC al = average_t<LIM>(lim, dl, dm), ar = average_t<LIM>(lim, dm, dr);
-            l[q] = l[q] + al * TC(0.5);
-            r[q] = r[q] - ar * TC(0.5);
+            if constexpr (kPairedMuscl<TC, LIM>) {
+              const float2 o = muscl_pair<LIM>(ll, l[q], r[q], rr);
+              l[q] = o.x;
+              r[q] = o.y;
+            } else {
+              const TC dl = l[q] - ll, dm = r[q] - l[q], dr = rr - r[q];
+              const TC al = average_t<LIM>(lim, dl, dm), ar = average_t<LIM>(lim, dm, dr);
+              l[q] = l[q] + al * TC(0.5);
+              r[q] = r[q] - ar * TC(0.5);
+            }
           }
         }
       } else {
@@ -286,10 +298,16 @@ flux_body(const KParams& p, const typename Src<Pol, NEQ, STAGE, PRIM_IN>::TIn* _
           r[q] = sP[s][cl + 1][cx];
           if (STAGE == 2) {
             const TC ll = sP[s][cl - 1][cx], rr = sP[s][cl + 2][cx];
-            const TC dl = l[q] - ll, dm = r[q] - l[q], dr = rr - r[q];
-            const TC al = average_t<LIM>(lim, dl, dm), ar = average_t<LIM>(lim, dm, dr);
-            l[q] = l[q] + al * TC(0.5);
-            r[q] = r[q] - ar * TC(0.5);
+            if constexpr (kPairedMuscl<TC, LIM>) {
+              const float2 o = muscl_pair<LIM>(ll, l[q], r[q], rr);
+              l[q] = o.x;
+              r[q] = o.y;
+            } else {
+              const TC dl = l[q] - ll, dm = r[q] - l[q], dr = rr - r[q];
+              const TC al = average_t<LIM>(lim, dl, dm), ar = average_t<LIM>(lim, dm, dr);
+              l[q] = l[q] + al * TC(0.5);
+              r[q] = r[q] - ar * TC(0.5);
+            }
           }
         }
       }
@@ -428,9 +446,16 @@ __device__ __forceinline__ void cfl_candidate(const KParams& p, const TC* pr, do
     const TC gp = mul_rn(g, pr[4]);
     const TC a = gp + b2;
     const TC a2 = mul_rn(a, a), g4 = mul_rn(TC(4.0), gp);
-    const TC cx = tsqrt(mul_rn(TC(0.5), a + tsqrt(a2 - mul_rn(mul_rn(g4, bx), bx))) / pr[0]);
-    const TC cy = tsqrt(mul_rn(TC(0.5), a + tsqrt(a2 - mul_rn(mul_rn(g4, by), by))) / pr[0]);
-    const TC cz = tsqrt(mul_rn(TC(0.5), a + tsqrt(a2 - mul_rn(mul_rn(g4, bz), bz))) / pr[0]);
+    // a^2 - 4 g p b_n^2 >= 0 exactly; in FP32 rounding can take it below
+    // zero where the sound speed meets the normal Alfven speed (clamped);
+    // FP64 keeps the reference's expression
+    auto disc = [&](TC bn) {
+      const TC d = a2 - mul_rn(mul_rn(g4, bn), bn);
+      return sizeof(TC) == 4 ? tmax_(d, TC(0)) : d;
+    };
+    const TC cx = tsqrt(mul_rn(TC(0.5), a + tsqrt(disc(bx))) / pr[0]);
+    const TC cy = tsqrt(mul_rn(TC(0.5), a + tsqrt(disc(by))) / pr[0]);
+    const TC cz = tsqrt(mul_rn(TC(0.5), a + tsqrt(disc(bz))) / pr[0]);
     cand[0] = (TC)p.dx / (tabs(pr[1]) + cx);
     cand[1] = (TC)p.dy / (tabs(pr[2]) + cy);
     cand[2] = (TC)p.dz / (tabs(pr[3]) + cz);

