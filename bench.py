@@ -368,7 +368,7 @@ def run_ours(args, dist: Dist) -> None:
         dt, _ = de.step_host(host, it, 10, t, 1e300)
         t += dt
         it += 1
-    ke = max(2, args.e2e_steps)
+    ke = max(2, args.e2e_steps)  # each step moves 2 x 1.12 GB over the host link
     dist.barrier()
     t0 = time.perf_counter()
     for _ in range(ke):
@@ -379,8 +379,9 @@ def run_ours(args, dist: Dist) -> None:
     de.close()
     e2e = {"value": dist.ws * n ** 3 * ke / e2e_s, "unit": UNIT,
            "h2d_bytes_per_step": int(host.nbytes), "d2h_bytes_per_step": int(host.nbytes),
-           "steps": ke, "path": "gch_step_host: pinned host u -> H2D -> get_timestep + "
-                                "tstep -> D2H"}
+           "steps": ke, "path": "gch_step_host: page-locked host u (reference layout, FP64) "
+                                "read by the layout kernel over the host link -> "
+                                "get_timestep + tstep -> written back over the link"}
 
     # ---- roofline of the dominant kernel -----------------------------------
     means = {k: sum(v) / len(v) for k, v in prof.items()}
@@ -476,7 +477,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--size", type=int, default=256)
     ap.add_argument("--fp64-steps", type=int, default=4)
-    ap.add_argument("--e2e-steps", type=int, default=6)
+    ap.add_argument("--e2e-steps", type=int, default=10)
     ap.add_argument("--cpu-size", type=int, default=160)
     ap.add_argument("--cpu-steps", type=int, default=40)
     ap.add_argument("--ref-size", type=int, default=128)

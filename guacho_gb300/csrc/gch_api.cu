@@ -57,6 +57,38 @@ __global__ void k_clear_info(StepScalars* sc) {
   sc->pfloor = 0;
 }
 
+// A host array in the reference's layout moves to and from the device
+// either straight through the layout kernels, when the GPU can address it
+// (page-locked memory mapped into the device address space: the kernels
+// read or write it over the host link, which also does the transposition),
+// or through a cudaMemcpy into the device staging buffer and the same
+// kernels on that buffer (pageable memory).
+const double* host_in(gch_domain* d, const double* h, int& st) {
+  cudaPointerAttributes a;
+  if (cudaPointerGetAttributes(&a, h) == cudaSuccess && a.type == cudaMemoryTypeHost &&
+      a.devicePointer)
+    return (const double*)a.devicePointer;
+  cudaGetLastError();  // an unregistered pointer is not an error here
+  st |= cuda_ok(cudaMemcpyAsync(d->stage, h, d->ncell_host * d->kp.neq * sizeof(double),
+                                cudaMemcpyHostToDevice, d->stream));
+  return d->stage;
+}
+// the device view of a host output array, or the staging buffer (then
+// host_out_finish copies it to the host)
+double* host_out(gch_domain* d, double* h) {
+  cudaPointerAttributes a;
+  if (cudaPointerGetAttributes(&a, h) == cudaSuccess && a.type == cudaMemoryTypeHost &&
+      a.devicePointer)
+    return (double*)a.devicePointer;
+  cudaGetLastError();
+  return d->stage;
+}
+int host_out_finish(gch_domain* d, double* h, const double* view) {
+  if (view != d->stage) return GCH_OK;
+  return cuda_ok(cudaMemcpyAsync(h, d->stage, d->ncell_host * d->kp.neq * sizeof(double),
+                                 cudaMemcpyDeviceToHost, d->stream));
+}
+
 int fetch_scalars(gch_domain* d) {
   int st = cuda_ok(cudaMemcpyAsync(d->sc_host, d->sc, sizeof(StepScalars), cudaMemcpyDeviceToHost,
                                    d->stream));
@@ -323,24 +355,25 @@ int gch_create(const gch_params_t* p, void* stream, gch_domain_t** out) {
 
 int gch_upload(gch_domain_t* d, const double* u) {
   if (!d || !u) return GCH_ERR_PARAM;
-  int st = cuda_ok(cudaMemcpyAsync(d->stage, u, d->ncell_host * d->kp.neq * sizeof(double),
-                                   cudaMemcpyHostToDevice, d->stream));
-  st |= engine(d).upload(d);
+  int st = GCH_OK;
+  const double* src = host_in(d, u, st);
+  st |= engine(d).upload(d, src);
   st |= cuda_ok(cudaStreamSynchronize(d->stream));
   return st;
 }
 
 int gch_download(gch_domain_t* d, double* u, double* primit) {
   if (!d) return GCH_ERR_PARAM;
-  const size_t bytes = d->ncell_host * d->kp.neq * sizeof(double);
   int st = GCH_OK;
   if (u) {
-    st |= engine(d).download_u(d);
-    st |= cuda_ok(cudaMemcpyAsync(u, d->stage, bytes, cudaMemcpyDeviceToHost, d->stream));
+    double* dst = host_out(d, u);
+    st |= engine(d).download_u(d, dst);
+    st |= host_out_finish(d, u, dst);
   }
   if (primit) {
-    st |= engine(d).download_prim(d);
-    st |= cuda_ok(cudaMemcpyAsync(primit, d->stage, bytes, cudaMemcpyDeviceToHost, d->stream));
+    double* dst = host_out(d, primit);
+    st |= engine(d).download_prim(d, dst);
+    st |= host_out_finish(d, primit, dst);
   }
   st |= cuda_ok(cudaStreamSynchronize(d->stream));
   return st;
@@ -389,9 +422,9 @@ int gch_tc_info(gch_domain_t* d, int* nsteps, double* dt_cond) {
 int gch_step_host(gch_domain_t* d, double* u, int current_iter, int n_iter, double current_time,
                   double tprint, double* dt, int* dump_flag) {
   if (!d || !u || !dt || !dump_flag) return GCH_ERR_PARAM;
-  const size_t bytes = d->ncell_host * d->kp.neq * sizeof(double);
-  int st = cuda_ok(cudaMemcpyAsync(d->stage, u, bytes, cudaMemcpyHostToDevice, d->stream));
-  st |= engine(d).upload(d);
+  int st = GCH_OK;
+  const double* src = host_in(d, u, st);
+  st |= engine(d).upload(d, src);
   if (d->prim_in) st |= engine(d).calcprim(d);
   k_set_ctrl<<<1, 1, 0, d->stream>>>(d->sc, current_iter, n_iter, current_time, tprint, 0.0, 0.0, 1);
   st |= engine(d).get_dt(d);
@@ -400,8 +433,9 @@ int gch_step_host(gch_domain_t* d, double* u, int current_iter, int n_iter, doub
     st |= fetch_scalars(d);  // the conduction substeps need dt on the host
     st |= gch::tc_run(d, d->sc_host->dt);
   }
-  st |= engine(d).download_u(d);
-  st |= cuda_ok(cudaMemcpyAsync(u, d->stage, bytes, cudaMemcpyDeviceToHost, d->stream));
+  double* dst = host_out(d, u);
+  st |= engine(d).download_u(d, dst);
+  st |= host_out_finish(d, u, dst);
   st |= fetch_scalars(d);
   *dt = d->sc_host->dt;
   if (d->sc_host->dump) *dump_flag = 1;

@@ -70,9 +70,10 @@ struct EngineOps {
   int (*tstep)(gch_domain*);          // both stages + boundaries
   int (*boundaryI)(gch_domain*);      // ghost layer of u + user spheres
   int (*calcprim)(gch_domain*);       // primit from u (tabulated cooling)
-  int (*upload)(gch_domain*);         // stage (host layout) -> u
-  int (*download_u)(gch_domain*);     // u -> stage
-  int (*download_prim)(gch_domain*);  // primit -> stage
+  // host layout (staging buffer or mapped host memory) <-> u / primit
+  int (*upload)(gch_domain*, const double*);
+  int (*download_u)(gch_domain*, double*);
+  int (*download_prim)(gch_domain*, double*);
   int (*loopfin)(gch_domain*);        // device time-loop tail
   int (*cfl)(gch_domain*);            // CFL min of the current u only
   int (*probe)(gch_domain*);          // stage-1 fluxes alone (autotuner)

@@ -203,23 +203,26 @@ struct Engine {
     return cuda_status(cudaGetLastError());
   }
 
-  static int upload(gch_domain* d) {
+  // host layout <-> u: `aos` is the staging buffer or mapped host memory
+  static constexpr int kLayoutGrid = 152 * 8;
+  static int upload(gch_domain* d, const double* aos) {
     d->cfl_ready = false;
-    k_aos_to_soa<TU><<<1024, 256, 0, d->stream>>>(d->kp, d->stage, (TU*)d->u, d->kp.neq);
+    k_aos_to_soa<TU><<<kLayoutGrid, kLayoutCells, 0, d->stream>>>(d->kp, aos, (TU*)d->u, d->kp.neq);
     return cuda_status(cudaGetLastError());
   }
-  static int download_u(gch_domain* d) {
-    k_soa_to_aos<TU><<<1024, 256, 0, d->stream>>>(d->kp, (const TU*)d->u, d->stage, d->kp.neq);
+  static int download_u(gch_domain* d, double* aos) {
+    k_soa_to_aos<TU><<<kLayoutGrid, kLayoutCells, 0, d->stream>>>(d->kp, (const TU*)d->u, aos,
+                                                                   d->kp.neq);
     return cuda_status(cudaGetLastError());
   }
-  static int download_prim(gch_domain* d) {
+  static int download_prim(gch_domain* d, double* aos) {
     const KParams& p = d->kp;
     if (d->prim_in) {
-      k_soa_to_aos<TS><<<1024, 256, 0, d->stream>>>(p, (const TS*)d->primit, d->stage, p.neq);
+      k_soa_to_aos<TS><<<kLayoutGrid, kLayoutCells, 0, d->stream>>>(p, (const TS*)d->primit, aos, p.neq);
     } else if (p.neq == 8) {
-      k_prim_to_aos<Pol, 8><<<1024, 256, 0, d->stream>>>(p, (const TU*)d->u, d->stage);
+      k_prim_to_aos<Pol, 8><<<kLayoutGrid, kLayoutCells, 0, d->stream>>>(p, (const TU*)d->u, aos);
     } else {
-      k_prim_to_aos<Pol, 5><<<1024, 256, 0, d->stream>>>(p, (const TU*)d->u, d->stage);
+      k_prim_to_aos<Pol, 5><<<kLayoutGrid, kLayoutCells, 0, d->stream>>>(p, (const TU*)d->u, aos);
     }
     return cuda_status(cudaGetLastError());
   }

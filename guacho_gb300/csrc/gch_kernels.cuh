@@ -904,48 +904,92 @@ __global__ void k_calcprim(KParams p, const typename Pol::TU* u, typename Pol::T
 }
 
 // Host layout (Fortran u(neq, x, y, z), FP64, no pitch) <-> device SoA.
+// A block moves kLayoutCells consecutive cells per pass: their neq doubles
+// each are read (or written) on the host-layout side with consecutive
+// threads on consecutive doubles, and exchanged through shared memory with
+// the per-field arrays, which are written (or read) one field at a time
+// with consecutive threads on consecutive cells.  The host-layout side may
+// be the device staging buffer or page-locked host memory mapped into the
+// device address space (then these kernels are the host-link transfer).
+constexpr int kLayoutCells = 256;
+constexpr int kLayoutPad = kMaxNeq + 1;  // odd row stride of the shared tile
+
+__device__ __forceinline__ long long layout_cell(const KParams& p, long long t) {
+  const int ax = (int)(t % p.NX);
+  const int ay = (int)((t / p.NX) % p.NY);
+  const int az = (int)(t / ((long long)p.NX * p.NY));
+  return cell_index(p, ax, ay, az);
+}
+
+// block 256; any grid (grid-stride over the cells)
 template <class T>
-__global__ void k_aos_to_soa(KParams p, const double* __restrict__ aos, T* __restrict__ soa,
-                             int neq) {
+__global__ void __launch_bounds__(kLayoutCells)
+k_aos_to_soa(KParams p, const double* __restrict__ aos, T* __restrict__ soa, int neq) {
+  __shared__ double buf[kLayoutCells * kLayoutPad];
   const long long n = (long long)p.NX * p.NY * p.NZ;
-  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n;
-       t += (long long)gridDim.x * blockDim.x) {
-    const int ax = (int)(t % p.NX);
-    const int ay = (int)((t / p.NX) % p.NY);
-    const int az = (int)(t / ((long long)p.NX * p.NY));
-    const long long c = cell_index(p, ax, ay, az);
-    for (int q = 0; q < neq; ++q) soa[q * p.fs + c] = from_d<T>(aos[t * neq + q]);
+  for (long long c0 = (long long)blockIdx.x * kLayoutCells; c0 < n;
+       c0 += (long long)gridDim.x * kLayoutCells) {
+    const int m = (int)min((long long)kLayoutCells, n - c0);
+    for (int i = threadIdx.x; i < m * neq; i += kLayoutCells) {
+      const int cell = i / neq;
+      buf[cell * kLayoutPad + (i - cell * neq)] = aos[c0 * neq + i];
+    }
+    __syncthreads();
+    if (threadIdx.x < m) {
+      const long long c = layout_cell(p, c0 + threadIdx.x);
+      for (int q = 0; q < neq; ++q)
+        soa[q * p.fs + c] = from_d<T>(buf[threadIdx.x * kLayoutPad + q]);
+    }
+    __syncthreads();
   }
 }
+
 template <class T>
-__global__ void k_soa_to_aos(KParams p, const T* __restrict__ soa, double* __restrict__ aos,
-                             int neq) {
+__global__ void __launch_bounds__(kLayoutCells)
+k_soa_to_aos(KParams p, const T* __restrict__ soa, double* __restrict__ aos, int neq) {
+  __shared__ double buf[kLayoutCells * kLayoutPad];
   const long long n = (long long)p.NX * p.NY * p.NZ;
-  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n;
-       t += (long long)gridDim.x * blockDim.x) {
-    const int ax = (int)(t % p.NX);
-    const int ay = (int)((t / p.NX) % p.NY);
-    const int az = (int)(t / ((long long)p.NX * p.NY));
-    const long long c = cell_index(p, ax, ay, az);
-    for (int q = 0; q < neq; ++q) aos[t * neq + q] = to_d(soa[q * p.fs + c]);
+  for (long long c0 = (long long)blockIdx.x * kLayoutCells; c0 < n;
+       c0 += (long long)gridDim.x * kLayoutCells) {
+    const int m = (int)min((long long)kLayoutCells, n - c0);
+    if (threadIdx.x < m) {
+      const long long c = layout_cell(p, c0 + threadIdx.x);
+      for (int q = 0; q < neq; ++q) buf[threadIdx.x * kLayoutPad + q] = to_d(soa[q * p.fs + c]);
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < m * neq; i += kLayoutCells) {
+      const int cell = i / neq;
+      aos[c0 * neq + i] = buf[cell * kLayoutPad + (i - cell * neq)];
+    }
+    __syncthreads();
   }
 }
+
 // primit (full array, from u) straight into the host layout
 template <class Pol, int NEQ>
-__global__ void k_prim_to_aos(KParams p, const typename Pol::TU* __restrict__ u,
-                              double* __restrict__ aos) {
+__global__ void __launch_bounds__(kLayoutCells)
+k_prim_to_aos(KParams p, const typename Pol::TU* __restrict__ u, double* __restrict__ aos) {
+  __shared__ double buf[kLayoutCells * kLayoutPad];
   const long long n = (long long)p.NX * p.NY * p.NZ;
-  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n;
-       t += (long long)gridDim.x * blockDim.x) {
-    const int ax = (int)(t % p.NX);
-    const int ay = (int)((t / p.NX) % p.NY);
-    const int az = (int)(t / ((long long)p.NX * p.NY));
-    const long long c = cell_index(p, ax, ay, az);
-    double uu[NEQ], pp[NEQ];
-    for (int q = 0; q < NEQ; ++q) uu[q] = to_d(u[q * p.fs + c]);
-    unsigned pfl = 0;
-    Ops<PolFP64>::u2prim<NEQ>(p, uu, pp, pfl);
-    for (int q = 0; q < NEQ; ++q) aos[t * NEQ + q] = pp[q];
+  for (long long c0 = (long long)blockIdx.x * kLayoutCells; c0 < n;
+       c0 += (long long)gridDim.x * kLayoutCells) {
+    const int m = (int)min((long long)kLayoutCells, n - c0);
+    if (threadIdx.x < m) {
+      const long long c = layout_cell(p, c0 + threadIdx.x);
+      double uu[NEQ], pp[NEQ];
+#pragma unroll
+      for (int q = 0; q < NEQ; ++q) uu[q] = to_d(u[q * p.fs + c]);
+      unsigned pfl = 0;
+      Ops<PolFP64>::u2prim<NEQ>(p, uu, pp, pfl);
+#pragma unroll
+      for (int q = 0; q < NEQ; ++q) buf[threadIdx.x * kLayoutPad + q] = pp[q];
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < m * NEQ; i += kLayoutCells) {
+      const int cell = i / NEQ;
+      aos[c0 * NEQ + i] = buf[cell * kLayoutPad + (i - cell * NEQ)];
+    }
+    __syncthreads();
   }
 }
 

@@ -291,6 +291,41 @@ def test_step_host_matches_device(gpu_lib):
         assert np.array_equal(interior(uh), interior(b.download()))
 
 
+@pytest.mark.parametrize("prec", [P.FP64, P.FP32_KAHAN])
+def test_pinned_and_pageable_host_arrays_agree(gpu_lib, prec):
+    """Page-locked host arrays are read and written by the layout kernels
+    over the host link; pageable ones go through the staging buffer: both
+    routes move the same bytes (upload, download with primit, step_host)."""
+    torch = pytest.importorskip("torch")
+    from guacho_gb300.domain import Domain
+    p, u0 = problems.turbulence(20, seed=6)
+    p = p.replace(precision=prec)
+
+    def pinned(a):
+        t = torch.empty(a.shape, dtype=torch.float64, pin_memory=True).numpy()
+        t[...] = a
+        return t
+
+    with Domain(p) as a, Domain(p) as b:
+        a.upload(u0)
+        b.upload(pinned(u0))
+        ua, pa = a.download(with_primit=True)
+        ub = pinned(np.zeros(p.shape))
+        pb = pinned(np.zeros(p.shape))
+        assert b._lib.gch_download(b._h, ub.ctypes.data, pb.ctypes.data) == 0
+        assert np.array_equal(ua, ub) and np.array_equal(pa, pb)
+        a.init(u0)
+        b.init(u0)
+        ha, hb = a.download(), pinned(b.download())
+        t = 0.0
+        for it in range(1, 3):
+            dta, _ = a.step_host(ha, it, 10, t, 1e30)
+            dtb, _ = b.step_host(hb, it, 10, t, 1e30)
+            assert dta == dtb
+            t += dta
+        assert np.array_equal(ha, hb)
+
+
 @pytest.mark.parametrize("prec", [P.FP64, P.FP32_MIXED, P.FP32_KAHAN])
 def test_deterministic(gpu_lib, prec):
     p, u0 = problems.turbulence(16, seed=9)
