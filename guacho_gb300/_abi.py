@@ -56,6 +56,7 @@ class Params_t(C.Structure):
         ("th_cond", C.c_int32), ("tc_saturation", C.c_int32),
         ("rsc", C.c_double), ("rhosc", C.c_double), ("vsc2", C.c_double), ("bsc", C.c_double),
         ("mu", C.c_double),
+        ("npas", C.c_int32),
     ]
 
 
@@ -92,6 +93,7 @@ def to_struct(p: Params) -> Params_t:
         s.grav_GM[i], s.grav_x[i], s.grav_y[i], s.grav_z[i] = gm, x, y, z
     s.th_cond, s.tc_saturation = p.th_cond, int(p.tc_saturation)
     s.rsc, s.rhosc, s.vsc2, s.bsc, s.mu = p.rsc, p.rhosc, p.vsc2, p.bsc, p.mu
+    s.npas = p.npas
     return s
 
 

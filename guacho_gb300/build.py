@@ -39,6 +39,10 @@ UNITS = {
     # grouped many-box kernels of the two FP32 policies (same flags)
     "gch_fp32_grp.cu": ["-use_fast_math"],
     "gch_kahan_grp.cu": ["-use_fast_math"],
+    # the passive-scalar stage kernels of each policy (same flags)
+    "gch_fp64_pas.cu": ["-fmad=false"],
+    "gch_fp32_pas.cu": ["-use_fast_math"],
+    "gch_kahan_pas.cu": ["-use_fast_math"],
     "gch_api.cu": [],
     "gch_batch.cu": [],
     # FP64 arithmetic in the reference's order, as gch_fp64.cu

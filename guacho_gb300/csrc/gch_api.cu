@@ -137,6 +137,7 @@ void gch_params_default(gch_params_t* p, int nx, int ny, int nz) {
   p->vsc2 = 1.0;
   p->bsc = std::sqrt(4.0 * std::acos(-1.0));  // sqrt(4 pi Psc), Psc = 1
   p->mu = 1.0;
+  p->npas = 0;
 }
 
 int gch_params_check(const gch_params_t* p) {
@@ -145,8 +146,11 @@ int gch_params_check(const gch_params_t* p) {
       p->precision != GCH_FP32_KAHAN)
     return GCH_ERR_PARAM;
   if (p->nx < 1 || p->ny < 1 || p->nz < 1) return GCH_ERR_PARAM;
-  if (p->neq != 5 && p->neq != 8) return GCH_ERR_PARAM;
-  const bool bfield = p->neq == 8;
+  // 5 or 8 dynamical equations and 0 or 2 passive scalars
+  if (p->npas != 0 && p->npas != 2) return GCH_ERR_PARAM;
+  const int neqdyn = p->neq - p->npas;
+  if (neqdyn != 5 && neqdyn != 8) return GCH_ERR_PARAM;
+  const bool bfield = neqdyn == 8;
   if (p->mhd && !bfield) return GCH_ERR_PARAM;
   if (bfield && !(p->mhd || p->pmhd)) return GCH_ERR_PARAM;
   if (p->mhd && p->pmhd) return GCH_ERR_PARAM;
@@ -164,11 +168,19 @@ int gch_params_check(const gch_params_t* p) {
   }
   if (p->slope_limiter < GCH_LIMITER_NO_AVERAGE || p->slope_limiter > GCH_LIMITER_SUPERBEE)
     return GCH_ERR_PARAM;
-  if (p->eq_of_state != GCH_EOS_ADIABATIC && p->eq_of_state != GCH_EOS_SINGLE_SPECIE)
+  if (p->eq_of_state != GCH_EOS_ADIABATIC && p->eq_of_state != GCH_EOS_SINGLE_SPECIE &&
+      p->eq_of_state != GCH_EOS_H_RATE)
     return GCH_ERR_PARAM;
-  if (p->cooling != GCH_COOL_NONE && p->cooling != GCH_COOL_DMC && p->cooling != GCH_COOL_CHI)
+  if (p->cooling != GCH_COOL_NONE && p->cooling != GCH_COOL_H && p->cooling != GCH_COOL_DMC &&
+      p->cooling != GCH_COOL_CHI)
     return GCH_ERR_PARAM;
-  if (p->cooling != GCH_COOL_NONE &&
+  // the H-rate EOS and COOL_H read the neutral hydrogen density from the
+  // first passive scalar (src/hydro_core.f90:106-111, src/cooling_h.f90:331)
+  if ((p->eq_of_state == GCH_EOS_H_RATE || p->cooling == GCH_COOL_H) && p->npas < 1)
+    return GCH_ERR_PARAM;
+  // the user spheres set the dynamical fields only
+  if (p->bc_user && p->npas != 0) return GCH_ERR_PARAM;
+  if ((p->cooling == GCH_COOL_DMC || p->cooling == GCH_COOL_CHI) &&
       (p->ntab < 2 || p->ntab > GCH_MAX_TABLE || !(p->tab_inv_dlog > 0.0)))
     return GCH_ERR_PARAM;
   // flux-CD needs B (the reference's hydro build leaves up untouched then)
@@ -191,7 +203,7 @@ int gch_params_check(const gch_params_t* p) {
     if (p->th_cond == GCH_TC_ANISOTROPIC && !bfield) return GCH_ERR_PARAM;
     // with table cooling the reference's interior Temp is not refreshed
     // before conduction reads it
-    if (p->cooling != GCH_COOL_NONE) return GCH_ERR_PARAM;
+    if (p->cooling == GCH_COOL_DMC || p->cooling == GCH_COOL_CHI) return GCH_ERR_PARAM;
     if (!(p->rsc > 0 && p->rhosc > 0 && p->vsc2 > 0 && p->bsc > 0 && p->mu > 0 && p->Psc > 0 &&
           p->tsc > 0))
       return GCH_ERR_PARAM;
@@ -265,8 +277,9 @@ int gch_create(const gch_params_t* p, void* stream, gch_domain_t** out) {
   k.ntab = p->ntab; k.tab_i0 = p->tab_i0;
   k.tab_inv_dlog = p->tab_inv_dlog; k.tab_tail = p->tab_tail; k.tab_Tmin = p->tab_Tmin;
   k.nsph = p->bc_user ? p->nsph : 0;
-  d->cfl_fused = p->neq == 8 && p->enable_flux_cd && p->eta == 0.0 && !d->prim_in &&
-                 !p->bc_user && p->th_cond == GCH_TC_OFF;
+  d->cfl_fused = p->neq >= 8 && p->enable_flux_cd && p->eta == 0.0 && !d->prim_in &&
+                 !p->bc_user && p->th_cond == GCH_TC_OFF && p->cooling == GCH_COOL_NONE &&
+                 p->npas == 0;  // the epilogue recovers the 8 dynamical fields only
   k.ngrav = p->user_source_terms ? p->ngrav : 0;
 
   // z planes per block: enough blocks to fill the 152 SMs several times
@@ -297,7 +310,7 @@ int gch_create(const gch_params_t* p, void* stream, gch_domain_t** out) {
   alloc(&d->u, fs * k.neq * d->tu_size);
   alloc(&d->up, fs * k.neq * d->ts_size);
   if (p->eta != 0.0) alloc(&d->w, fs * k.neq * d->tu_size);
-  if (k.neq == 8 && p->enable_flux_cd) alloc(&d->E, fs * 3 * d->ts_size);
+  if (k.neq >= 8 && p->enable_flux_cd) alloc(&d->E, fs * 3 * d->ts_size);
   if (p->eight_wave) alloc(&d->s678, fs * 3 * d->ts_size);
   if (d->prim_in) alloc(&d->primit, fs * k.neq * d->ts_size);
   d->ncell_host = (size_t)k.NX * k.NY * k.NZ;
@@ -308,7 +321,7 @@ int gch_create(const gch_params_t* p, void* stream, gch_domain_t** out) {
     alloc((void**)&d->tc_min, sizeof(unsigned long long));
     if (e == cudaSuccess) e = cudaMallocHost((void**)&d->tc_min_host, sizeof(unsigned long long));
   }
-  if (e == cudaSuccess && p->cooling != GCH_COOL_NONE) {
+  if (e == cudaSuccess && d->prim_in) {  // the tabulated cooling curve
     e = cudaMalloc((void**)&d->tab, 2 * p->ntab * sizeof(double));
     if (e == cudaSuccess) e = cudaMemcpy(d->tab, p->tab_T, p->ntab * sizeof(double), cudaMemcpyHostToDevice);
     if (e == cudaSuccess)

@@ -1,8 +1,8 @@
 // gch_batch.cu -- many independent boxes of uneven size, each with its own
 // CFL dt, advanced together.
 //
-// Grouped mode (FP32 policies; no table cooling, conduction, resistivity or user
-// spheres): one step of all boxes is one CUDA graph of grouped launches,
+// Grouped mode (FP32 policies; no cooling, conduction, resistivity, passive
+// scalars or user spheres): one step of all boxes is one CUDA graph of grouped launches,
 // one launch per kernel of the step for up to 64 boxes (gch_group.cuh).
 // The z-march depth of the stage kernels is chosen by timing the stage-1
 // flux kernel over the whole batch for each candidate depth (the autotuner
@@ -76,7 +76,7 @@ namespace {
 bool groupable(const gch_params_t& p) {
   const bool prim_in = p.cooling == GCH_COOL_DMC || p.cooling == GCH_COOL_CHI;
   return p.precision != GCH_FP64 && !prim_in && p.eta == 0.0 && !p.bc_user &&
-         p.th_cond == GCH_TC_OFF;
+         p.th_cond == GCH_TC_OFF && p.cooling == GCH_COOL_NONE && p.npas == 0;
 }
 
 int grid_of(int n) { return (n + 127) / 128; }

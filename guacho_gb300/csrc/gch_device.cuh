@@ -10,12 +10,33 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <type_traits>
+
 #include "guacho_gb300.h"
 
 namespace gch {
 
 constexpr int NG = 2;            // ghost cells per side (OT/parameters.f90:193)
-constexpr int kMaxNeq = 8;
+constexpr int kMaxNeq = 10;      // 8 dynamical equations + 2 passive scalars
+
+// Equation counts (parameters.f90:131-135, 197-202): 5 dynamical equations
+// (hydro) or 8 (with B), followed by npas = 0 or 2 passive scalars, so NEQ
+// is one of 5, 7, 8, 10 and NEQ >= 8 exactly when B is carried.
+template <int NEQ>
+constexpr int kNeqDyn = NEQ >= 8 ? 8 : 5;
+
+// Call f(std::integral_constant<int, NEQ>) for the runtime equation count
+// (host side: selects the kernel instantiation).
+template <class F>
+inline void with_neq(int neq, F&& f) {
+  switch (neq) {
+    case 5: f(std::integral_constant<int, 5>()); break;
+    case 7: f(std::integral_constant<int, 7>()); break;
+    case 8: f(std::integral_constant<int, 8>()); break;
+    case 10: f(std::integral_constant<int, 10>()); break;
+    default: break;
+  }
+}
 constexpr int TX = 32;           // stage-kernel tile width (one warp along x)
 constexpr int TY = 8;            // stage-kernel tile height
 constexpr int NT = TX * TY;
@@ -160,9 +181,6 @@ __device__ __forceinline__ float tabs(float a) { return fabsf(a); }
 __device__ __forceinline__ double tdiv_pos(double a, double b) { return a / b; }
 __device__ __forceinline__ float tdiv_pos(float a, float b) { return __fdividef(a, b); }
 
-template <class T>
-__device__ __forceinline__ bool has_b(const KParams& p) { return p.neq >= 8; }
-
 // src/hydro_core.f90:395-476  prim2f (x direction)
 template <class T, int NEQ>
 __device__ __forceinline__ void prim2f(const KParams& p, const T* prim, T* ff) {
@@ -193,6 +211,8 @@ __device__ __forceinline__ void prim2f(const KParams& p, const T* prim, T* ff) {
     ff[6] = prim[1] * prim[6] - prim[5] * prim[2];
     ff[7] = prim[1] * prim[7] - prim[5] * prim[3];
   }
+#pragma unroll
+  for (int q = kNeqDyn<NEQ>; q < NEQ; ++q) ff[q] = prim[q] * prim[1];  // passives, :471-473
 }
 
 // src/hydro_core.f90:331-383  prim2u
@@ -210,6 +230,8 @@ __device__ __forceinline__ void prim2u(const KParams& p, const T* prim, T* uu) {
     uu[6] = prim[6];
     uu[7] = prim[7];
   }
+#pragma unroll
+  for (int q = kNeqDyn<NEQ>; q < NEQ; ++q) uu[q] = prim[q];  // passives, :378-380
 }
 
 // src/hydro_core.f90:591-604  cfastX
@@ -282,15 +304,15 @@ __device__ __forceinline__ T average_t(int lim, T a, T b) {
 // Riemann solvers, x direction.  `err` collects GCH_ERR_* bits.
 
 // src/hlld.f90:48-319  prim2fhlld
-template <class T>
+template <class T, int NEQ>
 __device__ __forceinline__ void hlld(const KParams& p, const T* pl, const T* pr, T* ff, int& err) {
   const T cv = (T)p.cv;
   T csl = cfastX(p, pl);
   T csr = cfastX(p, pr);
   T sr = tmax_(pl[1] + csl, pr[1] + csr);
   T sl = tmin_(pl[1] - csl, pr[1] - csr);
-  if (sl > T(0)) { prim2f<T, 8>(p, pl, ff); return; }
-  if (sr < T(0)) { prim2f<T, 8>(p, pr, ff); return; }
+  if (sl > T(0)) { prim2f<T, NEQ>(p, pl, ff); return; }
+  if (sr < T(0)) { prim2f<T, NEQ>(p, pr, ff); return; }
 
   T bx = T(0.5) * (pl[5] + pr[5]);
   T signBx = tcopysign(T(1), bx);
@@ -336,6 +358,8 @@ __device__ __forceinline__ void hlld(const KParams& p, const T* pl, const T* pr,
     ff[5] = T(0);
     ff[6] = bystl * sM - bx * vstl;
     ff[7] = bzstl * sM - bx * wstl;
+#pragma unroll
+    for (int q = 8; q < NEQ; ++q) ff[q] = sM * pl[q] * slmul / slmsM;  // :150-152
     return;
   }
   if (sstr <= T(0)) {  // UR* region
@@ -364,6 +388,8 @@ __device__ __forceinline__ void hlld(const KParams& p, const T* pl, const T* pr,
     ff[5] = T(0);
     ff[6] = bystr * sM - bx * vstr;
     ff[7] = bzstr * sM - bx * wstr;
+#pragma unroll
+    for (int q = 8; q < NEQ; ++q) ff[q] = sM * pr[q] * srmur / srmsM;  // :198-200
     return;
   }
   T sMmul = sM - pl[1];
@@ -409,6 +435,8 @@ __device__ __forceinline__ void hlld(const KParams& p, const T* pl, const T* pr,
     ff[5] = T(0);
     ff[6] = bystst * sM - bx * vstst;
     ff[7] = bzstst * sM - bx * wstst;
+#pragma unroll
+    for (int q = 8; q < NEQ; ++q) ff[q] = sM * pl[q] * slmul / slmsM;  // :277-279
     return;
   }
   if (sM <= T(0)) {  // UR** region
@@ -426,10 +454,12 @@ __device__ __forceinline__ void hlld(const KParams& p, const T* pl, const T* pr,
     ff[5] = T(0);
     ff[6] = bystst * sM - bx * vstst;
     ff[7] = bzstst * sM - bx * wstst;
+#pragma unroll
+    for (int q = 8; q < NEQ; ++q) ff[q] = sM * pr[q] * srmur / srmsM;  // :308-310
     return;
   }
   // src/hlld.f90:316-317 prints and stops here (sM not finite)
-  for (int q = 0; q < 8; ++q) ff[q] = sM;
+  for (int q = 0; q < NEQ; ++q) ff[q] = sM;
   err |= GCH_ERR_HLLD;
 }
 
@@ -481,6 +511,7 @@ __device__ __forceinline__ float2 muscl_pair(float ll, float l, float r, float r
 //    operations, one paired instruction for both sides (measured: 4-7%
 //    fewer instructions in the stage kernels);
 //  - quotients by the same denominator share one hardware reciprocal.
+template <int NEQ>
 __device__ __forceinline__ void hlld_pair(const KParams& p, const float* pl, const float* pr,
                                           float* ff, int& err) {
   const float cv = (float)p.cv, g = (float)p.gamma;
@@ -501,8 +532,8 @@ __device__ __forceinline__ void hlld_pair(const KParams& p, const float* pl, con
   const float2 cf = f2(sqrtf(h.x), sqrtf(h.y));
   const float2 lo = sub2(vx, cf), hi = add2(vx, cf);
   const float sl = tmin_(lo.x, lo.y), sr = tmax_(hi.x, hi.y);
-  if (sl > 0.0f) { prim2f<float, 8>(p, pl, ff); return; }
-  if (sr < 0.0f) { prim2f<float, 8>(p, pr, ff); return; }
+  if (sl > 0.0f) { prim2f<float, NEQ>(p, pl, ff); return; }
+  if (sr < 0.0f) { prim2f<float, NEQ>(p, pr, ff); return; }
 
   const float bx = 0.5f * (pl[5] + pr[5]);
   const float signBx = copysignf(1.0f, bx);
@@ -537,7 +568,7 @@ __device__ __forceinline__ void hlld_pair(const KParams& p, const float* pl, con
   const bool left = star_l || (dbl && sM >= 0.0f);
   if (dbl && !(sM >= 0.0f) && !(sM <= 0.0f)) {  // src/hlld.f90:316-317
 #pragma unroll
-    for (int q = 0; q < 8; ++q) ff[q] = sM;
+    for (int q = 0; q < NEQ; ++q) ff[q] = sM;
     err |= GCH_ERR_HLLD;
     return;
   }
@@ -577,6 +608,9 @@ __device__ __forceinline__ void hlld_pair(const KParams& p, const float* pl, con
   ff[5] = 0.0f;
   ff[6] = byx * sM - bx * vx_;
   ff[7] = bzx * sM - bx * wx_;
+  // passives: the star density of the side (src/hlld.f90:150-152, 198-200)
+#pragma unroll
+  for (int q = 8; q < NEQ; ++q) ff[q] = sM * (left ? pl[q] : pr[q]) * smu_s / ssM_s;
 }
 
 // src/hllc.f90:44-140  prim2fhllc (hydro, or passive B when NEQ == 8)
@@ -608,6 +642,8 @@ __device__ __forceinline__ void hllc(const KParams& p, const T* pl, const T* pr,
       uuk[6] = rhost * pl[6] / pl[0];
       uuk[7] = rhost * pl[7] / pl[0];
     }
+#pragma unroll
+    for (int q = kNeqDyn<NEQ>; q < NEQ; ++q) uuk[q] = rhost * pl[q] / pl[0];  // :95-97
     prim2f<T, NEQ>(p, pl, ff);
     prim2u<T, NEQ>(p, pl, uu);
 #pragma unroll
@@ -627,6 +663,8 @@ __device__ __forceinline__ void hllc(const KParams& p, const T* pl, const T* pr,
       uuk[6] = rhost * pr[6] / pr[0];
       uuk[7] = rhost * pr[7] / pr[0];
     }
+#pragma unroll
+    for (int q = kNeqDyn<NEQ>; q < NEQ; ++q) uuk[q] = rhost * pr[q] / pr[0];  // :124-126
     prim2f<T, NEQ>(p, pr, ff);
     prim2u<T, NEQ>(p, pr, uu);
 #pragma unroll
@@ -666,15 +704,16 @@ __device__ __forceinline__ void hll2(const KParams& p, const T* pl, const T* pr,
 
 template <int SOLVER, int NEQ>
 struct Riemann;
-template <>
-struct Riemann<GCH_SOLVER_HLLD, 8> {
+template <int NEQ>
+struct Riemann<GCH_SOLVER_HLLD, NEQ> {
+  static_assert(NEQ >= 8, "HLLD needs B");
   template <class T>
   __device__ __forceinline__ static void solve(const KParams& p, const T* l, const T* r, T* f,
                                                int& e) {
     if constexpr (sizeof(T) == 4)
-      hlld_pair(p, l, r, f, e);  // FP32 paths: predicated regions, paired sides
+      hlld_pair<NEQ>(p, l, r, f, e);  // FP32 paths: predicated regions, paired sides
     else
-      hlld<T>(p, l, r, f, e);      // FP64: the reference's branch order
+      hlld<T, NEQ>(p, l, r, f, e);    // FP64: the reference's branch order
   }
 };
 template <int NEQ>
@@ -685,12 +724,13 @@ struct Riemann<GCH_SOLVER_HLLC, NEQ> {
     hllc<T, NEQ>(p, l, r, f, e);
   }
 };
-template <>
-struct Riemann<GCH_SOLVER_HLLE, 8> {
+template <int NEQ>
+struct Riemann<GCH_SOLVER_HLLE, NEQ> {
+  static_assert(NEQ >= 8, "HLLE uses the fast magnetosonic speed");
   template <class T>
   __device__ __forceinline__ static void solve(const KParams& p, const T* l, const T* r, T* f,
                                                int&) {
-    hll2<T, 8, true>(p, l, r, f);
+    hll2<T, NEQ, true>(p, l, r, f);
   }
 };
 template <int NEQ>
@@ -705,10 +745,12 @@ struct Riemann<GCH_SOLVER_HLL, NEQ> {
 // ---------------------------------------------------------------------------
 // Field permutations of swapy / swapz (src/hydro_core.f90:485-534):
 // component q of the rotated state is component perm(q) of the original.
-template <int DIR>
+// Passive scalars are not permuted; B is only where it is carried.
+template <int DIR, int NEQ>
 __device__ __forceinline__ int perm(int q) {
-  if (DIR == 1) return q == 1 ? 2 : q == 2 ? 1 : q == 5 ? 6 : q == 6 ? 5 : q;
-  if (DIR == 2) return q == 1 ? 3 : q == 3 ? 1 : q == 5 ? 7 : q == 7 ? 5 : q;
+  constexpr bool b = NEQ >= 8;
+  if (DIR == 1) return q == 1 ? 2 : q == 2 ? 1 : (b && q == 5) ? 6 : (b && q == 6) ? 5 : q;
+  if (DIR == 2) return q == 1 ? 3 : q == 3 ? 1 : (b && q == 5) ? 7 : (b && q == 7) ? 5 : q;
   return q;
 }
 

@@ -58,17 +58,21 @@ struct Engine {
       flux_launch_lim<SOLVER, NEQ, STAGE, PRIM_IN, kLimRuntime>(d, src, dst);
   }
 
+  // the stage kernels of one equation count, dispatched on the solver
+  // (the passive-scalar counts are instantiated in their own translation
+  // units, see GCH_PASSIVE_FLUX below)
+  template <int NEQ, int STAGE, bool PRIM_IN>
+  static int flux_n(gch_domain* d, const void* src, void* dst);  // defined below
+
   template <int STAGE, bool PRIM_IN>
   static int flux(gch_domain* d, const void* src, void* dst) {
-    const int s = d->kp.solver, neq = d->kp.neq;
-    if (s == GCH_SOLVER_HLLD && neq == 8) flux_launch<GCH_SOLVER_HLLD, 8, STAGE, PRIM_IN>(d, src, dst);
-    else if (s == GCH_SOLVER_HLLC && neq == 5) flux_launch<GCH_SOLVER_HLLC, 5, STAGE, PRIM_IN>(d, src, dst);
-    else if (s == GCH_SOLVER_HLLC && neq == 8) flux_launch<GCH_SOLVER_HLLC, 8, STAGE, PRIM_IN>(d, src, dst);
-    else if (s == GCH_SOLVER_HLLE && neq == 8) flux_launch<GCH_SOLVER_HLLE, 8, STAGE, PRIM_IN>(d, src, dst);
-    else if (s == GCH_SOLVER_HLL && neq == 5) flux_launch<GCH_SOLVER_HLL, 5, STAGE, PRIM_IN>(d, src, dst);
-    else if (s == GCH_SOLVER_HLL && neq == 8) flux_launch<GCH_SOLVER_HLL, 8, STAGE, PRIM_IN>(d, src, dst);
-    else return GCH_ERR_PARAM;
-    return GCH_OK;
+    switch (d->kp.neq) {
+      case 5: return flux_n<5, STAGE, PRIM_IN>(d, src, dst);
+      case 7: return flux_n<7, STAGE, PRIM_IN>(d, src, dst);
+      case 8: return flux_n<8, STAGE, PRIM_IN>(d, src, dst);
+      case 10: return flux_n<10, STAGE, PRIM_IN>(d, src, dst);
+    }
+    return GCH_ERR_PARAM;
   }
 
   template <class T>
@@ -97,11 +101,13 @@ struct Engine {
     const KParams& p = d->kp;
     dim3 cgrid = column_grid(p), block(32, 8);
     if (d->prim_in) {
-      if (p.neq == 8) k_cfl<Pol, 8, true><<<cgrid, block, 0, d->stream>>>(p, (const TS*)d->primit, d->sc, kzc);
-      else k_cfl<Pol, 5, true><<<cgrid, block, 0, d->stream>>>(p, (const TS*)d->primit, d->sc, kzc);
+      with_neq(p.neq, [&](auto N) {
+        k_cfl<Pol, decltype(N)::value, true><<<cgrid, block, 0, d->stream>>>(p, (const TS*)d->primit, d->sc, kzc);
+      });
     } else {
-      if (p.neq == 8) k_cfl<Pol, 8, false><<<cgrid, block, 0, d->stream>>>(p, (const TU*)d->u, d->sc, kzc);
-      else k_cfl<Pol, 5, false><<<cgrid, block, 0, d->stream>>>(p, (const TU*)d->u, d->sc, kzc);
+      with_neq(p.neq, [&](auto N) {
+        k_cfl<Pol, decltype(N)::value, false><<<cgrid, block, 0, d->stream>>>(p, (const TU*)d->u, d->sc, kzc);
+      });
     }
     d->cfl_ready = true;
     return cuda_status(cudaGetLastError());
@@ -113,11 +119,13 @@ struct Engine {
     if (d->cfl_fused && d->cfl_ready) {
       // the min over cells was accumulated by the last step's k_ct<2>
     } else if (d->prim_in) {
-      if (p.neq == 8) k_cfl<Pol, 8, true><<<cgrid, block, 0, d->stream>>>(p, (const TS*)d->primit, d->sc, kzc);
-      else k_cfl<Pol, 5, true><<<cgrid, block, 0, d->stream>>>(p, (const TS*)d->primit, d->sc, kzc);
+      with_neq(p.neq, [&](auto N) {
+        k_cfl<Pol, decltype(N)::value, true><<<cgrid, block, 0, d->stream>>>(p, (const TS*)d->primit, d->sc, kzc);
+      });
     } else {
-      if (p.neq == 8) k_cfl<Pol, 8, false><<<cgrid, block, 0, d->stream>>>(p, (const TU*)d->u, d->sc, kzc);
-      else k_cfl<Pol, 5, false><<<cgrid, block, 0, d->stream>>>(p, (const TU*)d->u, d->sc, kzc);
+      with_neq(p.neq, [&](auto N) {
+        k_cfl<Pol, decltype(N)::value, false><<<cgrid, block, 0, d->stream>>>(p, (const TU*)d->u, d->sc, kzc);
+      });
     }
     if (!(d->cfl_fused && d->cfl_ready)) gch_mark(d, "k_cfl");
     k_dtfin<<<1, 1, 0, d->stream>>>(d->sc, p.cfl, p.dx, p.dy, p.dz);
@@ -162,14 +170,25 @@ struct Engine {
       gch_mark(d, "k_ct_stage2");
     }
     if (p.eta != 0.0) {
-      if (p.neq == 8) k_visc<Pol, 8><<<cgrid, cblock, 0, d->stream>>>(p, (TU*)d->u, (const TU*)d->w, (const TS*)d->up, d->sc);
-      else k_visc<Pol, 5><<<cgrid, cblock, 0, d->stream>>>(p, (TU*)d->u, (const TU*)d->w, (const TS*)d->up, d->sc);
+      with_neq(p.neq, [&](auto N) {
+        k_visc<Pol, decltype(N)::value><<<cgrid, cblock, 0, d->stream>>>(p, (TU*)d->u, (const TU*)d->w, (const TS*)d->up, d->sc);
+      });
       ++d->launches;
       gch_mark(d, "k_visc");
     }
+    if (p.cooling == GCH_COOL_H) {  // ionisation of H and its cooling (u(5), n_HI)
+      with_neq(p.neq, [&](auto N) {
+        constexpr int n = decltype(N)::value;
+        if constexpr (n > kNeqDyn<n>)
+          k_cool_h<Pol, n><<<cgrid, cblock, 0, d->stream>>>(p, (TU*)d->u, d->sc);
+      });
+      ++d->launches;
+      gch_mark(d, "k_cool_h");
+    }
     if (d->prim_in) {  // tabulated cooling (updates primit and u(5))
-      if (p.neq == 8) k_cool<Pol, 8><<<cgrid, cblock, 0, d->stream>>>(p, (TU*)d->u, (TS*)d->primit, d->sc);
-      else k_cool<Pol, 5><<<cgrid, cblock, 0, d->stream>>>(p, (TU*)d->u, (TS*)d->primit, d->sc);
+      with_neq(p.neq, [&](auto N) {
+        k_cool<Pol, decltype(N)::value><<<cgrid, cblock, 0, d->stream>>>(p, (TU*)d->u, (TS*)d->primit, d->sc);
+      });
       ++d->launches;
       gch_mark(d, "k_cool");
     }
@@ -177,8 +196,9 @@ struct Engine {
     ghost<TU>(d, (TU*)d->u, 1);
     if (d->prim_in) {
       dim3 g((p.NX + 31) / 32, (p.NY + 7) / 8, p.NZ);
-      if (p.neq == 8) k_calcprim<Pol, 8><<<g, cblock, 0, d->stream>>>(p, (const TU*)d->u, (TS*)d->primit, 1, d->sc);
-      else k_calcprim<Pol, 5><<<g, cblock, 0, d->stream>>>(p, (const TU*)d->u, (TS*)d->primit, 1, d->sc);
+      with_neq(p.neq, [&](auto N) {
+        k_calcprim<Pol, decltype(N)::value><<<g, cblock, 0, d->stream>>>(p, (const TU*)d->u, (TS*)d->primit, 1, d->sc);
+      });
       ++d->launches;
       gch_mark(d, "k_calcprim");
     }
@@ -198,8 +218,9 @@ struct Engine {
     if (!d->prim_in) return GCH_OK;  // primitives are formed on the fly
     const KParams& p = d->kp;
     dim3 g((p.NX + 31) / 32, (p.NY + 7) / 8, p.NZ), b(32, 8);
-    if (p.neq == 8) k_calcprim<Pol, 8><<<g, b, 0, d->stream>>>(p, (const TU*)d->u, (TS*)d->primit, 0, d->sc);
-    else k_calcprim<Pol, 5><<<g, b, 0, d->stream>>>(p, (const TU*)d->u, (TS*)d->primit, 0, d->sc);
+    with_neq(p.neq, [&](auto N) {
+      k_calcprim<Pol, decltype(N)::value><<<g, b, 0, d->stream>>>(p, (const TU*)d->u, (TS*)d->primit, 0, d->sc);
+    });
     return cuda_status(cudaGetLastError());
   }
 
@@ -219,10 +240,11 @@ struct Engine {
     const KParams& p = d->kp;
     if (d->prim_in) {
       k_soa_to_aos<TS><<<kLayoutGrid, kLayoutCells, 0, d->stream>>>(p, (const TS*)d->primit, aos, p.neq);
-    } else if (p.neq == 8) {
-      k_prim_to_aos<Pol, 8><<<kLayoutGrid, kLayoutCells, 0, d->stream>>>(p, (const TU*)d->u, aos);
     } else {
-      k_prim_to_aos<Pol, 5><<<kLayoutGrid, kLayoutCells, 0, d->stream>>>(p, (const TU*)d->u, aos);
+      with_neq(p.neq, [&](auto N) {
+        k_prim_to_aos<Pol, decltype(N)::value><<<kLayoutGrid, kLayoutCells, 0, d->stream>>>(
+            p, (const TU*)d->u, aos);
+      });
     }
     return cuda_status(cudaGetLastError());
   }
@@ -243,5 +265,36 @@ struct Engine {
                      &upload, &download_u, &download_prim, &loopfin, &cfl, &probe};
   }
 };
+
+// Not inline, so that an explicit instantiation declaration keeps the
+// passive-scalar instantiations out of the policy's main translation unit.
+template <class Pol>
+template <int NEQ, int STAGE, bool PRIM_IN>
+int Engine<Pol>::flux_n(gch_domain* d, const void* src, void* dst) {
+  const int s = d->kp.solver;
+  if constexpr (NEQ >= 8) {  // with B: all four solvers (HLLC/HLL carry it passively)
+    if (s == GCH_SOLVER_HLLD) flux_launch<GCH_SOLVER_HLLD, NEQ, STAGE, PRIM_IN>(d, src, dst);
+    else if (s == GCH_SOLVER_HLLE) flux_launch<GCH_SOLVER_HLLE, NEQ, STAGE, PRIM_IN>(d, src, dst);
+    else if (s == GCH_SOLVER_HLLC) flux_launch<GCH_SOLVER_HLLC, NEQ, STAGE, PRIM_IN>(d, src, dst);
+    else if (s == GCH_SOLVER_HLL) flux_launch<GCH_SOLVER_HLL, NEQ, STAGE, PRIM_IN>(d, src, dst);
+    else return GCH_ERR_PARAM;
+  } else {  // hydro
+    if (s == GCH_SOLVER_HLLC) flux_launch<GCH_SOLVER_HLLC, NEQ, STAGE, PRIM_IN>(d, src, dst);
+    else if (s == GCH_SOLVER_HLL) flux_launch<GCH_SOLVER_HLL, NEQ, STAGE, PRIM_IN>(d, src, dst);
+    else return GCH_ERR_PARAM;
+  }
+  return GCH_OK;
+}
+
+// The stage kernels with passive scalars (7 and 10 equations) of policy POL,
+// declared `extern` in the policy's main translation unit and instantiated
+// in a second one, so the two compile in parallel.
+#define GCH_PASSIVE_FLUX(EXTERN, POL)                                                 \
+  EXTERN template int Engine<POL>::flux_n<7, 1, false>(gch_domain*, const void*, void*); \
+  EXTERN template int Engine<POL>::flux_n<7, 1, true>(gch_domain*, const void*, void*);  \
+  EXTERN template int Engine<POL>::flux_n<7, 2, false>(gch_domain*, const void*, void*); \
+  EXTERN template int Engine<POL>::flux_n<10, 1, false>(gch_domain*, const void*, void*); \
+  EXTERN template int Engine<POL>::flux_n<10, 1, true>(gch_domain*, const void*, void*);  \
+  EXTERN template int Engine<POL>::flux_n<10, 2, false>(gch_domain*, const void*, void*);
 
 }  // namespace gch

@@ -3,5 +3,6 @@
 #include "gch_engine.cuh"
 
 namespace gch {
+GCH_PASSIVE_FLUX(extern, PolMixed)
 const EngineOps kEngineMixed = Engine<PolMixed>::ops();
 }

@@ -4,5 +4,6 @@
 #include "gch_engine.cuh"
 
 namespace gch {
+GCH_PASSIVE_FLUX(extern, PolFP64)
 const EngineOps kEngineFP64 = Engine<PolFP64>::ops();
 }

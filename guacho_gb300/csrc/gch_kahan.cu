@@ -4,5 +4,6 @@
 #include "gch_engine.cuh"
 
 namespace gch {
+GCH_PASSIVE_FLUX(extern, PolKahan)
 const EngineOps kEngineKahan = Engine<PolKahan>::ops();
 }

@@ -248,8 +248,8 @@ flux_body(const KParams& p, const typename Src<Pol, NEQ, STAGE, PRIM_IN>::TIn* _
         if (STAGE == 1) {
 #pragma unroll
           for (int q = 0; q < NEQ; ++q) {
-            l[q] = sP[perm<2>(q)][ty + H][tx + H];
-            r[q] = sQ[0][perm<2>(q)][ty][tx];
+            l[q] = sP[perm<2, NEQ>(q)][ty + H][tx + H];
+            r[q] = sQ[0][perm<2, NEQ>(q)][ty][tx];
           }
         } else {
           // the slope of p(k) comes from the ring (formed by the previous
@@ -257,7 +257,7 @@ flux_body(const KParams& p, const typename Src<Pol, NEQ, STAGE, PRIM_IN>::TIn* _
           // once and kept for face k+3/2
 #pragma unroll
           for (int q = 0; q < NEQ; ++q) {
-            const int s = perm<2>(q);
+            const int s = perm<2, NEQ>(q);
             const TC al = sQ[2][s][ty][tx], rr = sQ[1][s][ty][tx];
             l[q] = sP[s][ty + H][tx + H];
             r[q] = sQ[0][s][ty][tx];
@@ -293,7 +293,7 @@ flux_body(const KParams& p, const typename Src<Pol, NEQ, STAGE, PRIM_IN>::TIn* _
         const int cx = fx + H, cl = fy - 1 + H;
 #pragma unroll
         for (int q = 0; q < NEQ; ++q) {
-          const int s = perm<1>(q);
+          const int s = perm<1, NEQ>(q);
           l[q] = sP[s][cl][cx];
           r[q] = sP[s][cl + 1][cx];
           if (STAGE == 2) {
@@ -314,13 +314,13 @@ flux_body(const KParams& p, const typename Src<Pol, NEQ, STAGE, PRIM_IN>::TIn* _
       Riemann<SOLVER, NEQ>::solve(p, l, r, f, err);
       if (kind == 0) {
 #pragma unroll
-        for (int q = 0; q < NEQ; ++q) sH[hslot][perm<2>(q)][ty][tx] = f[q];
+        for (int q = 0; q < NEQ; ++q) sH[hslot][perm<2, NEQ>(q)][ty][tx] = f[q];
       } else if (kind == 1) {
 #pragma unroll
         for (int q = 0; q < NEQ; ++q) sF[q][fy][fx] = f[q];
       } else {
 #pragma unroll
-        for (int q = 0; q < NEQ; ++q) sG[perm<1>(q)][fy][fx] = f[q];
+        for (int q = 0; q < NEQ; ++q) sG[perm<1, NEQ>(q)][fy][fx] = f[q];
       }
     }
     if (!plane) {  // column-private work only: no barrier
@@ -328,13 +328,15 @@ flux_body(const KParams& p, const typename Src<Pol, NEQ, STAGE, PRIM_IN>::TIn* _
       prefetch_next(k);
       continue;
     }
-    const int nupd = ct ? 5 : NEQ;
+    // with flux-CD, B comes from the CT kernel: the flux update covers the
+    // hydro fields and the passives (src/flux_cd_module.f90:299-308)
+    auto upd = [&](int q) { return !ct || q < 5 || q >= 8; };
     const long long c = cell_index(p, axc, ayc, az);
     typename Pol::TU uq[NEQ];
     if (active) {
 #pragma unroll
       for (int q = 0; q < NEQ; ++q)
-        if (q < nupd) uq[q] = u[q * p.fs + c];
+        if (upd(q)) uq[q] = u[q * p.fs + c];
     }
     __syncthreads();
     prefetch_next(k);
@@ -386,7 +388,7 @@ flux_body(const KParams& p, const typename Src<Pol, NEQ, STAGE, PRIM_IN>::TIn* _
       }
 #pragma unroll
       for (int q = 0; q < NEQ; ++q) {
-        if (q < nupd) {
+        if (upd(q)) {
           auto unew = Ops<Pol>::update(Ops<Pol>::ld(uq[q]), dtdx, dtdy, dtdz,
                                        sF[q][ty][tx], sF[q][ty][tx + 1], sG[q][ty][tx],
                                        sG[q][ty + 1][tx], sH[hp][q][ty][tx], sH[hn][q][ty][tx]);
@@ -847,6 +849,108 @@ __global__ void k_cool(KParams p, typename Pol::TU* u, typename Pol::TS* primit,
   }
 #pragma unroll
   for (int q = 0; q < NEQ; ++q) primit[q * p.fs + c] = (typename Pol::TS)pp[q];
+}
+
+// COOL_H (src/cooling_h.f90): non-equilibrium ionisation of hydrogen and
+// the parametrised cooling tied to it, per interior cell, FP64 (the
+// reference computes it in real(8)).  The first passive scalar is the
+// neutral hydrogen density.
+namespace coolh {
+__device__ __forceinline__ double alpha(double T) { return 2.55e-13 * pow(1.e4 / T, 0.79); }
+__device__ __forceinline__ double colf(double T) { return 5.83e-11 * sqrt(T) * exp(-157828. / T); }
+__device__ __forceinline__ double betah(double T) {
+  const double a = 157890. / T;
+  return 1.133e-24 / sqrt(a) * (-0.0713 + 0.5 * log(a) + 0.640 * pow(a, -0.33333));
+}
+// :155-242 ALOSS (X2 and DT enter only a quantity the reference does not use)
+__device__ __forceinline__ double aloss(double X1, double DEN, double DH0, double TE0) {
+  const double XION = 2.179e-11, XO = 1.e-3;
+  const double C0 = 0.5732, C1 = 1.8288e-5, C2 = -1.15822e-10, C3 = 9.4288e-16;
+  const double D0 = 0.5856, D1 = 1.55083e-5, D2 = -9.669e-12, D3 = 5.716e-19;
+  const double ENK = 118409., EN = 1.634E-11;
+  const double TE = tmax_(TE0, 10.);
+  const double DH = DEN;
+  const double DHP = (1. - X1) * DH;
+  const double DE = DHP + 1.E-4 * DH;
+  const double DOI = XO * DH0;
+  const double DOII = XO * DHP;
+  if (TE <= 1e4) return 0.;
+  double OMEGA = 0.0;
+  if (TE <= 55000.) OMEGA = C0 + TE * (C1 + TE * (C2 + TE * C3));
+  if (TE >= 72000.) OMEGA = D0 + TE * (D1 + TE * (D2 + TE * D3));
+  if (TE > 55000. && TE < 72000.) {
+    const double OMEGAL = C0 + TE * (C1 + TE * (C2 + TE * C3));
+    const double OMEGAH = D0 + TE * (D1 + TE * (D2 + TE * D3));
+    const double FRAC = (TE - 55000.) / 17000.;
+    OMEGA = (1. - FRAC) * OMEGAL + FRAC * OMEGAH;
+  }
+  const double QLA = 8.6287E-6 / (2. * sqrt(TE)) * OMEGA * exp(-ENK / TE);
+  const double ECOLL = tmax_(DE * DH0 * QLA * EN, 0.);
+  const double CION = 5.834E-11 * sqrt(TE) * exp(-1.579E5 / TE);
+  const double EION = DE * DH0 * CION * XION;
+  const double EREC = tmax_(DE * DHP * (betah(TE)), 0.);
+  const double TM = 1. / TE;
+  const double T2 = TM * TM;
+  const double EOI = tmax_(DE * DOI * pow(10., 1381465 * T2 - 12328.69 * TM - 19.82621), 0.);
+  const double EOII = tmax_(DE * DOII * pow(10., -2061075. * T2 - 14596.24 * TM - 19.01402), 0.);
+  const double BETAF = 1.3 * 1.42E-27 * pow(TE, 0.5);
+  const double HIICOOL = DE * DHP * BETAF;
+  const double EQUIL =
+      (1.0455E-18 / pow(TE, 0.63)) * (1. - exp(-pow(TE * 1.E-5, 1.63))) * DE * DEN + HIICOOL;
+  double FR = 0.0;
+  if (TE >= 54770.) FR = 1.;
+  if (TE > 44770. && TE < 54770.) {
+    const double EX2 = exp(-2. * (TE - 49770.) / 500.);
+    const double TANH = (1. - EX2) / (1. + EX2);
+    FR = 0.5 * (1. + TANH);
+  }
+  return ECOLL + EION + (EREC + 7.033 * (EOI + EOII)) * (1. - FR) + EQUIL * FR;
+}
+}  // namespace coolh
+
+template <class Pol, int NEQ>
+__global__ void k_cool_h(KParams p, typename Pol::TU* u, const StepScalars* sc) {
+  static_assert(NEQ > kNeqDyn<NEQ>, "COOL_H needs the neutral hydrogen passive");
+  constexpr int ND = kNeqDyn<NEQ>;
+  const int ci = blockIdx.x * blockDim.x + threadIdx.x;
+  const int cj = blockIdx.y * blockDim.y + threadIdx.y;
+  const int ck = blockIdx.z;
+  if (ci >= p.nx || cj >= p.ny || !sc->active) return;
+  const long long c = cell_index(p, ci + NG, cj + NG, ck + NG);
+  // :259-371 atomic, without diffuse radiation (radphi = 1, tprime = 10 K)
+  const double dt = sc->dt * p.tsc;
+  const double xi = 1.e-4, boltzm = 1.3807e-16;
+  double uu[NEQ], prim[NEQ], T;
+#pragma unroll
+  for (int q = 0; q < NEQ; ++q) uu[q] = to_d(u[q * p.fs + c]);
+  unsigned pfl = 0;
+  Ops<PolFP64>::u2prim<NEQ>(p, uu, prim, pfl, &T);
+  const double col = coolh::colf(T);
+  const double rec = coolh::alpha(T);
+  const double y0 = uu[ND] / uu[0];
+  const double dh = uu[0];
+  const double a = rec + col;
+  const double b = -((2. + xi) * rec + (1. + xi) * col);
+  const double cc = (1. + xi) * rec;
+  const double d = sqrt(b * b - 4. * a * cc);
+  const double g0 = (2. * a * y0 + b + d) / (2. * a * y0 + b - d);
+  const double e = exp(-d * dh * dt);
+  double y1 = (-b - d * (1. + g0 * e) / (1. - g0 * e)) / (2. * a);
+  y1 = tmin_(y1, 0.9999);
+  y1 = tmax_(y1, 0.);
+  const double dh0 = uu[ND];
+  const double al = coolh::aloss(y0, dh, dh0, T) / (dh * dh);
+  const double tprime = 10.;
+  const double ce = (2. * dh * al) / (3. * boltzm * T);
+  double t1 = tprime + (T - tprime) * exp(-ce * dt);
+  t1 = tmax_(t1, 0.1 * T);
+  t1 = tmin_(t1, 10. * T);
+  uu[ND] = y1 * uu[0];
+  double e5 = p.cv * (2. * uu[0] - uu[ND]) * t1 / p.Tempsc
+              + 0.5 * prim[0] * (prim[1] * prim[1] + prim[2] * prim[2] + prim[3] * prim[3]);
+  if (NEQ >= 8 && p.mhd) e5 = e5 + 0.5 * (prim[5] * prim[5] + prim[6] * prim[6] + prim[7] * prim[7]);
+  u[ND * p.fs + c] = from_d<typename Pol::TU>(uu[ND]);
+  u[4 * p.fs + c] = from_d<typename Pol::TU>(e5);
 }
 
 // src/hydro_solver.f90:47-65 viscous_copy: u = w + eta*(sum of the six

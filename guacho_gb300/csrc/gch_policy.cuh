@@ -63,9 +63,18 @@ struct Ops<PolFP64> {
       prim[6] = uu[6];
       prim[7] = uu[7];
     }
+#pragma unroll
+    for (int q = kNeqDyn<NEQ>; q < NEQ; ++q) prim[q] = uu[q];  // passives (:86-89)
     if (p.eos == GCH_EOS_SINGLE_SPECIE) {
       double t = tmax_(1.0, (prim[4] / r) * p.Tempsc);
       prim[4] = r * t / p.Tempsc;
+      if (T) *T = t;
+    } else if (NEQ > kNeqDyn<NEQ> && p.eos == GCH_EOS_H_RATE) {
+      // :106-111, n_HI in the first passive scalar
+      double dentot = (2.0 * r - prim[kNeqDyn<NEQ>]);
+      dentot = tmax_(dentot, 1e-15);
+      const double t = tmax_(1.0, (prim[4] / dentot) * p.Tempsc);
+      prim[4] = dentot * t / p.Tempsc;
       if (T) *T = t;
     } else if (T) {
       *T = (prim[4] / r) * p.Tempsc;
@@ -152,6 +161,10 @@ __device__ __forceinline__ void prim_from_f32(const KParams& p, const float* uu,
   if (p.eos == GCH_EOS_SINGLE_SPECIE) {
     const float t = tmax_(1.0f, (pr * ir) * (float)p.Tempsc);
     pr = r * t / (float)p.Tempsc;
+  } else if (NEQ > kNeqDyn<NEQ> && p.eos == GCH_EOS_H_RATE) {
+    const float dentot = tmax_(2.0f * r - uu[kNeqDyn<NEQ>], 1e-15f);
+    const float t = tmax_(1.0f, (pr / dentot) * (float)p.Tempsc);
+    pr = dentot * t / (float)p.Tempsc;
   }
   prim[0] = r;
   prim[1] = uu[1] * ir;
@@ -163,6 +176,8 @@ __device__ __forceinline__ void prim_from_f32(const KParams& p, const float* uu,
     prim[6] = uu[6];
     prim[7] = uu[7];
   }
+#pragma unroll
+  for (int q = kNeqDyn<NEQ>; q < NEQ; ++q) prim[q] = uu[q];
 }
 
 // (h + l)^2 of a compensated pair, as a pair (the l^2 term is below 2^-48)
@@ -221,6 +236,10 @@ struct Ops<PolMixed> {
       if (p.eos == GCH_EOS_SINGLE_SPECIE) {
         const double t = tmax_(1.0, (pr * ir) * p.Tempsc);
         pr = r * t / p.Tempsc;
+      } else if (NEQ > kNeqDyn<NEQ> && p.eos == GCH_EOS_H_RATE) {
+        const double dentot = tmax_(2.0 * r - uu[kNeqDyn<NEQ>], 1e-15);
+        const double t = tmax_(1.0, (pr / dentot) * p.Tempsc);
+        pr = dentot * t / p.Tempsc;
       }
       const float rf = (float)r;
       prim[0] = rf;
@@ -233,6 +252,8 @@ struct Ops<PolMixed> {
         prim[6] = (float)uu[6];
         prim[7] = (float)uu[7];
       }
+#pragma unroll
+      for (int q = kNeqDyn<NEQ>; q < NEQ; ++q) prim[q] = (float)uu[q];
     }
   }
 
@@ -314,6 +335,10 @@ struct Ops<PolKahan> {
       if (p.eos == GCH_EOS_SINGLE_SPECIE) {
         const float t = tmax_(1.0f, (pr * ir) * (float)p.Tempsc);
         pr = rh * t / (float)p.Tempsc;
+      } else if (NEQ > kNeqDyn<NEQ> && p.eos == GCH_EOS_H_RATE) {
+        const float dentot = tmax_(2.0f * rh - uu[kNeqDyn<NEQ>].x, 1e-15f);
+        const float t = tmax_(1.0f, (pr / dentot) * (float)p.Tempsc);
+        pr = dentot * t / (float)p.Tempsc;
       }
       prim[0] = rh;
       prim[1] = uu[1].x * ir;
@@ -325,6 +350,8 @@ struct Ops<PolKahan> {
         prim[6] = uu[6].x;
         prim[7] = uu[7].x;
       }
+#pragma unroll
+      for (int q = kNeqDyn<NEQ>; q < NEQ; ++q) prim[q] = uu[q].x;
     }
   }
 

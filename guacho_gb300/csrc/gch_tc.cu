@@ -251,8 +251,7 @@ int tc_run_t(gch_domain* d, double dt_CFL) {
   const dim3 gint((p.nx + 31) / 32, (p.ny + 7) / 8, p.nz);
   const dim3 gface((p.nx + 1 + 31) / 32, (p.ny + 1 + 7) / 8, p.nz + 1);
   auto prim = [&]() {
-    if (p.neq == 8) k_tc_prim<TU, 8><<<gall, b, 0, s>>>(p, u, w);
-    else k_tc_prim<TU, 5><<<gall, b, 0, s>>>(p, u, w);
+    with_neq(p.neq, [&](auto N) { k_tc_prim<TU, decltype(N)::value><<<gall, b, 0, s>>>(p, u, w); });
   };
   TcArgs t;
   t.rsc = hp.rsc;

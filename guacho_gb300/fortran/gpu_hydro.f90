@@ -40,6 +40,7 @@ module gpu_hydro
     real(c_double) :: grav_y(GCH_MAX_GRAV), grav_z(GCH_MAX_GRAV)
     integer(c_int32_t) :: th_cond, tc_saturation
     real(c_double) :: rsc, rhosc, vsc2, bsc, mu
+    integer(c_int32_t) :: npas
   end type gch_params_t
 
   interface

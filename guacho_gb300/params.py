@@ -12,8 +12,8 @@ from dataclasses import dataclass, field
 
 # src/constants.f90:56-98
 SOLVER_HLL, SOLVER_HLLC, SOLVER_HLLE, SOLVER_HLLD = 1, 2, 3, 4
-EOS_ADIABATIC, EOS_SINGLE_SPECIE = 1, 2
-COOL_NONE, COOL_DMC, COOL_CHI = 0, 3, 4
+EOS_ADIABATIC, EOS_SINGLE_SPECIE, EOS_H_RATE = 1, 2, 3
+COOL_NONE, COOL_H, COOL_DMC, COOL_CHI = 0, 1, 3, 4
 TC_OFF, TC_ISOTROPIC, TC_ANISOTROPIC = 0, 1, 2
 BC_OUTFLOW, BC_CLOSED, BC_PERIODIC, BC_OTHER = 1, 2, 3, 4
 (LIMITER_NO_AVERAGE, LIMITER_NO_LIMIT, LIMITER_MINMOD, LIMITER_VAN_LEER,
@@ -89,14 +89,21 @@ class Params:
     vsc2: float = 1.0
     bsc: float = math.sqrt(4.0 * math.pi)
     mu: float = 1.0
+    # passive scalars (parameters.f90:131-135): the last npas equations;
+    # with EOS_H_RATE / COOL_H the first is the neutral hydrogen density
+    npas: int = 0
 
     @property
     def bfield(self) -> bool:
         return self.mhd or self.pmhd
 
     @property
-    def neq(self) -> int:
+    def neqdyn(self) -> int:
         return 8 if self.bfield else 5
+
+    @property
+    def neq(self) -> int:
+        return self.neqdyn + self.npas
 
     @property
     def gamma(self) -> float:

@@ -18,9 +18,9 @@ import math
 
 import numpy as np
 
-from .params import (BC_OUTFLOW, BC_PERIODIC, COOL_DMC, FP64, LIMITER_MINMOD,
-                     LIMITER_VAN_LEER, NGHOST, SOLVER_HLLC, SOLVER_HLLD, Params, Sphere,
-                     table_from_log)
+from .params import (BC_OUTFLOW, BC_PERIODIC, COOL_DMC, COOL_H, EOS_H_RATE, FP64,
+                     LIMITER_MINMOD, LIMITER_VAN_LEER, NGHOST, SOLVER_HLLC, SOLVER_HLLD,
+                     Params, Sphere, table_from_log)
 
 G = NGHOST
 
@@ -274,6 +274,62 @@ def conduction_blob(n=32, precision=FP64, th_cond=1, saturation=False, mhd=False
     if mhd:
         return p, conserved(p, rho, zero, zero, zero, pr, np.full(sh, b0), zero, zero)
     return p, conserved(p, rho, zero, zero, zero, pr)
+
+
+def with_passives(p: Params, u: np.ndarray, *fields) -> tuple:
+    """Append passive scalars (conserved values, e.g. a species density) to
+    a state: npas = len(fields) extra equations after the dynamical ones."""
+    sh = p.shape[:3]
+    cols = [np.broadcast_to(np.asarray(f, dtype=np.float64), sh)[..., None] for f in fields]
+    return p.replace(npas=p.npas + len(fields)), np.ascontiguousarray(
+        np.concatenate([u] + cols, axis=-1))
+
+
+def h_cooling_blob(n=24, precision=FP64, T_hot=1.0e6, T_amb=8.0e3, radius=0.3, nsc=1.0,
+                   xphys=3.0e18, cfl=0.4, mhd=False, b0=0.2, **kw) -> tuple:
+    """Hot ionised gas cooling into a warm neutral medium with the
+    hydrogen-rate EOS and COOL_H (src/hydro_core.f90:106-111,
+    src/cooling_h.f90): two passive scalars, the neutral hydrogen density
+    n_HI (neutral fraction 0.999 in the warm gas, 1e-4 in the hot blob) and
+    a tracer equal to the blob's density.  T = T_amb + (T_hot - T_amb)
+    (1 - (r/radius)^2)^2 inside the blob, rho = 1 (nsc cm^-3), outflow
+    walls, HLLC hydro or HLLD MHD with B = (b0, 0, 0); Guacho's cgs scalings
+    with T0 = 1e4 K (parameters.f90:159-170)."""
+    cv = 1.5
+    gamma = (cv + 1.0) / cv
+    T0, mu = 1.0e4, 1.0
+    rhosc = AMH * mu * nsc
+    Tempsc = T0 * gamma
+    vsc2 = gamma * RG * T0 / mu
+    Psc = rhosc * vsc2
+    tsc = xphys / math.sqrt(vsc2)
+    walls = dict(bc_left=BC_OUTFLOW, bc_right=BC_OUTFLOW, bc_bottom=BC_OUTFLOW,
+                 bc_top=BC_OUTFLOW, bc_out=BC_OUTFLOW, bc_in=BC_OUTFLOW)
+    if mhd:
+        phys = dict(mhd=True, riemann_solver=SOLVER_HLLD, enable_flux_cd=True)
+    else:
+        phys = dict(mhd=False, pmhd=False, riemann_solver=SOLVER_HLLC, enable_flux_cd=False)
+    phys.update(walls)
+    phys.update(kw)
+    p = Params(nx=n, ny=n, nz=n, precision=precision, slope_limiter=LIMITER_MINMOD, cfl=cfl,
+               cv=cv, Tempsc=Tempsc, Psc=Psc, tsc=tsc, rsc=xphys, rhosc=rhosc, vsc2=vsc2,
+               bsc=math.sqrt(4.0 * math.pi * Psc), mu=mu, eq_of_state=EOS_H_RATE,
+               cooling=COOL_H, **phys)
+    x, y, z = _centered_coords(p)
+    r = np.sqrt(x * x + y * y + z * z)
+    prof = np.clip(1.0 - (r / radius) ** 2, 0.0, None) ** 2
+    T = T_amb + (T_hot - T_amb) * prof
+    sh = p.shape[:3]
+    rho = np.ones(sh)
+    xn = np.where(prof > 0.5, 1e-4, 0.999) * np.ones(sh)
+    nhi = xn * rho
+    pr = (2.0 * rho - nhi) * T / Tempsc  # the H-rate EOS: n = 2 rho - n_HI
+    zero = np.zeros(sh)
+    if mhd:
+        u = conserved(p, rho, zero, zero, zero, pr, np.full(sh, b0), zero, zero)
+    else:
+        u = conserved(p, rho, zero, zero, zero, pr)
+    return with_passives(p, u, nhi, rho * (prof > 0))
 
 
 # ---------------------------------------------------------------------------

@@ -60,8 +60,10 @@ extern "C" {
 
 #define GCH_EOS_ADIABATIC 1
 #define GCH_EOS_SINGLE_SPECIE 2
+#define GCH_EOS_H_RATE 3
 
 #define GCH_COOL_NONE 0
+#define GCH_COOL_H 1
 #define GCH_COOL_DMC 3
 #define GCH_COOL_CHI 4
 
@@ -175,6 +177,11 @@ typedef struct {
   int32_t th_cond;          /* GCH_TC_OFF | GCH_TC_ISOTROPIC | GCH_TC_ANISOTROPIC */
   int32_t tc_saturation;
   double rsc, rhosc, vsc2, bsc, mu;
+  /* passive scalars (npas of parameters.f90:131-135, 0 or 2): the last npas
+   * of the neq equations, neq = 5 or 8 dynamical + npas.  With
+   * GCH_EOS_H_RATE (src/hydro_core.f90:106-111) or GCH_COOL_H
+   * (src/cooling_h.f90) the first passive is the neutral hydrogen density. */
+  int32_t npas;
 } gch_params_t;
 
 typedef struct gch_domain gch_domain_t;
@@ -275,9 +282,9 @@ int gch_profile_step(gch_domain_t* d, int cap, float* ms, char* names, int name_
  * library (512 KiB on every GPU that loads it, kept until exit).  Same
  * result as gch_get_timestep in FP64 arithmetic.  Limits: boxes with
  * ceil(nx/32)*ceil(ny/8)*ceil(nz/8) > 65536 (beyond 512^3 cells) return
- * GCH_ERR_TOO_LARGE; table cooling returns GCH_ERR_PARAM.  All calls share
- * the fixed array: calls that can overlap on the GPU race, so issue them on
- * one stream.  The first call on a device looks up the array's address;
+ * GCH_ERR_TOO_LARGE; table cooling and passive scalars return GCH_ERR_PARAM.
+ * All calls share the fixed array: calls that can overlap on the GPU race,
+ * so issue them on one stream.  The first call on a device looks up the array's address;
  * make it before any stream capture.  Asynchronous on `stream`. */
 int gch_get_timestep_noalloc(const gch_params_t* p, const double* u_dev, int current_iter,
                              int n_iter, double current_time, double tprint, double* dt_dev,
@@ -290,8 +297,8 @@ typedef struct gch_batch gch_batch_t;
  * together.  All boxes must share precision, neq and the physics switches;
  * sizes, spacings, boundary kinds and problem data may differ.
  *
- * FP32 boxes without table cooling, thermal conduction, resistivity or user
- * spheres are advanced in grouped mode on `stream` (0 = a stream of the
+ * FP32 boxes without cooling, thermal conduction, resistivity, passive
+ * scalars or user spheres are advanced in grouped mode on `stream` (0 = a stream of the
  * batch's own): one launch
  * per kernel of the step covers up to 64 boxes, one CUDA graph holds the
  * step, and the z-march depth is chosen by timing before the first step.

@@ -54,7 +54,8 @@ struct gor_state {
 
 static inline double dmax(double a, double b) { return a > b ? a : b; }
 static inline double dmin(double a, double b) { return a < b ? a : b; }
-static inline int bfield(const gor_params_t* p) { return p->neq >= 8; }
+static inline int neqdyn(const gor_params_t* p) { return p->neq - p->npas; }
+static inline int bfield(const gor_params_t* p) { return neqdyn(p) >= 8; }
 
 /* ---------------------------------------------------------------------- */
 /* src/hydro_core.f90:46-129  u2prim                                        */
@@ -77,12 +78,21 @@ static void u2prim(const gor_params_t* p, const double* uu, double* prim, double
     prim[6] = uu[6];
     prim[7] = uu[7];
   }
+  const int nd = neqdyn(p);
+  for (int q = nd; q < p->neq; ++q) prim[q] = uu[q];  /* passives (:86-89) */
   double t = 0.0;
   if (p->eq_of_state == GOR_EOS_ADIABATIC) t = (prim[4] / r) * p->Tempsc;
   if (p->eq_of_state == GOR_EOS_SINGLE_SPECIE) {
     r = dmax(r, 1e-15);
     t = dmax(1.0, (prim[4] / r) * p->Tempsc);
     prim[4] = r * t / p->Tempsc;
+  }
+  if (p->eq_of_state == GOR_EOS_H_RATE && p->npas > 0) {
+    /* :106-111: n_HI + 2 n_HII = 2 rho - n_HI particles */
+    double dentot = (2.0 * r - prim[nd]);
+    dentot = dmax(dentot, 1e-15);
+    t = dmax(1.0, (prim[4] / dentot) * p->Tempsc);
+    prim[4] = dentot * t / p->Tempsc;
   }
   if (T) *T = t;
 }
@@ -102,6 +112,7 @@ static void prim2u(const gor_params_t* p, const double* prim, double* uu) {
     uu[6] = prim[6];
     uu[7] = prim[7];
   }
+  for (int q = neqdyn(p); q < p->neq; ++q) uu[q] = prim[q];  /* :378-380 */
 }
 
 /* src/hydro_core.f90:395-476  prim2f (non-split branch) */
@@ -132,6 +143,7 @@ static void prim2f(const gor_params_t* p, const double* prim, double* ff) {
     ff[6] = prim[1] * prim[6] - prim[5] * prim[2];
     ff[7] = prim[1] * prim[7] - prim[5] * prim[3];
   }
+  for (int q = neqdyn(p); q < p->neq; ++q) ff[q] = prim[q] * prim[1];  /* :471-473 */
 }
 
 /* src/hydro_core.f90:485-534  swapy / swapz */
@@ -276,6 +288,7 @@ static void prim2fhlld(const gor_params_t* p, const double* pl, const double* pr
     ff[5] = 0.0;
     ff[6] = bystl * sM - bx * vstl;
     ff[7] = bzstl * sM - bx * wstl;
+    for (int q = 8; q < p->neq; ++q) ff[q] = sM * pl[q] * slmul / slmsM;  /* :150-152 */
     return;
   }
 
@@ -305,6 +318,7 @@ static void prim2fhlld(const gor_params_t* p, const double* pl, const double* pr
     ff[5] = 0.0;
     ff[6] = bystr * sM - bx * vstr;
     ff[7] = bzstr * sM - bx * wstr;
+    for (int q = 8; q < p->neq; ++q) ff[q] = sM * pr[q] * srmur / srmsM;  /* :198-200 */
     return;
   }
 
@@ -353,6 +367,7 @@ static void prim2fhlld(const gor_params_t* p, const double* pl, const double* pr
     ff[5] = 0.0;
     ff[6] = bystst * sM - bx * vstst;
     ff[7] = bzstst * sM - bx * wstst;
+    for (int q = 8; q < p->neq; ++q) ff[q] = sM * pl[q] * slmul / slmsM;  /* :277-279 */
     return;
   }
   /* UR** region */
@@ -371,6 +386,7 @@ static void prim2fhlld(const gor_params_t* p, const double* pl, const double* pr
     ff[5] = 0.0;
     ff[6] = bystst * sM - bx * vstst;
     ff[7] = bzstst * sM - bx * wstst;
+    for (int q = 8; q < p->neq; ++q) ff[q] = sM * pr[q] * srmur / srmsM;  /* :308-310 */
     return;
   }
   /* src/hlld.f90:316-317: print and stop */
@@ -382,7 +398,7 @@ static void prim2fhlld(const gor_params_t* p, const double* pl, const double* pr
 static void prim2fhllc(const gor_params_t* p, const double* pl, const double* pr, double* ff,
                        int* err) {
   const int neq = p->neq;
-  double uu[8], uuk[8];
+  double uu[GOR_MAX_NEQ], uuk[GOR_MAX_NEQ];
   double csl = csound(p, pl[4], pl[0]);
   double csr = csound(p, pr[4], pr[0]);
   double sr = dmax(pl[1] + csl, pr[1] + csr);
@@ -411,6 +427,7 @@ static void prim2fhllc(const gor_params_t* p, const double* pl, const double* pr
        * HLLC is not used with full MHD */
       uuk[5] = uuk[6] = uuk[7] = 0.0;
     }
+    for (int q = neqdyn(p); q < neq; ++q) uuk[q] = rhost * pl[q] / pl[0];  /* :95-97 */
     prim2f(p, pl, ff);
     prim2u(p, pl, uu);
     for (int q = 0; q < neq; ++q) ff[q] = ff[q] + sl * (uuk[q] - uu[q]);
@@ -431,6 +448,7 @@ static void prim2fhllc(const gor_params_t* p, const double* pl, const double* pr
     } else if (bfield(p)) {
       uuk[5] = uuk[6] = uuk[7] = 0.0;
     }
+    for (int q = neqdyn(p); q < neq; ++q) uuk[q] = rhost * pr[q] / pr[0];  /* :124-126 */
     prim2f(p, pr, ff);
     prim2u(p, pr, uu);
     for (int q = 0; q < neq; ++q) ff[q] = ff[q] + sr * (uuk[q] - uu[q]);
@@ -444,7 +462,7 @@ static void prim2fhllc(const gor_params_t* p, const double* pl, const double* pr
  * the same two-wave formula with fast (HLLE) or sound (HLL) speeds. */
 static void prim2fhll_common(const gor_params_t* p, const double* pl, const double* pr,
                              double* ff, int fast) {
-  double fL[8], fR[8], uL[8], uR[8];
+  double fL[GOR_MAX_NEQ], fR[GOR_MAX_NEQ], uL[GOR_MAX_NEQ], uR[GOR_MAX_NEQ];
   double csl, csr;
   if (fast) {
     csl = cfastX(p, pl);
@@ -485,7 +503,7 @@ static void fluxes(gor_state_t* s, int choice) {
   int err = 0;
 #pragma omp parallel for schedule(static) reduction(| : err)
   for (int k = 0; k <= nz; ++k) {
-    double pl[8], pr[8], pll[8], prr[8], ff[8];
+    double pl[GOR_MAX_NEQ], pr[GOR_MAX_NEQ], pll[GOR_MAX_NEQ], prr[GOR_MAX_NEQ], ff[GOR_MAX_NEQ];
     for (int j = 0; j <= ny; ++j) {
       for (int i = 0; i <= nx; ++i) {
         /* x direction */
@@ -704,7 +722,7 @@ static void step(gor_state_t* s, double dt) {
   int src = p->user_source_terms || p->eight_wave;
 #pragma omp parallel for schedule(static)
   for (int k = 1; k <= nz; ++k) {
-    double sv[8], prim[8];
+    double sv[GOR_MAX_NEQ], prim[GOR_MAX_NEQ];
     for (int j = 1; j <= ny; ++j)
       for (int i = 1; i <= nx; ++i) {
         if (!ct) {
@@ -715,12 +733,15 @@ static void step(gor_state_t* s, double dt) {
                 - dtdy * (AT(s, s->g, q, i, j, k) - AT(s, s->g, q, i, j - 1, k))
                 - dtdz * (AT(s, s->h, q, i, j, k) - AT(s, s->h, q, i, j, k - 1));
         } else {
-          for (int q = 1; q <= 5; ++q)
+          /* hydro (:299-301) and passives (:304-308) upwind, B by CT */
+          for (int q = 1; q <= neq; ++q) {
+            if (q >= 6 && q <= 8) continue;
             AT(s, s->up, q, i, j, k) =
                 AT(s, s->u, q, i, j, k)
                 - dtdx * (AT(s, s->f, q, i, j, k) - AT(s, s->f, q, i - 1, j, k))
                 - dtdy * (AT(s, s->g, q, i, j, k) - AT(s, s->g, q, i, j - 1, k))
                 - dtdz * (AT(s, s->h, q, i, j, k) - AT(s, s->h, q, i, j, k - 1));
+          }
           AT(s, s->up, 6, i, j, k) = AT(s, s->u, 6, i, j, k)
                                      - 0.5 * dtdy * (EAT(s, 3, i, j + 1, k) - EAT(s, 3, i, j - 1, k))
                                      + 0.5 * dtdz * (EAT(s, 2, i, j, k + 1) - EAT(s, 2, i, j, k - 1));
@@ -945,6 +966,115 @@ static void cooling_table(gor_state_t* s, double dt) {
           uu[4] = uu[4] - Eth0 + p->cv * pp[4];
         }
       }
+}
+
+/* src/cooling_h.f90: parametrised cooling with the non-equilibrium
+ * ionisation of hydrogen (COOL_H); the first passive scalar is the neutral
+ * hydrogen density.  All arithmetic FP64, as in the reference build. */
+static double alpha_rec(double T) { return 2.55e-13 * pow(1.e4 / T, 0.79); } /* :75-84 */
+static double colf(double T) { return 5.83e-11 * sqrt(T) * exp(-157828. / T); } /* :108-117 */
+static double betah(double T) {                                               /* :125-136 */
+  const double a = 157890. / T;
+  return 1.133e-24 / sqrt(a) * (-0.0713 + 0.5 * log(a) + 0.640 * pow(a, -0.33333));
+}
+
+/* :155-242 ALOSS: energy loss rate of the cell */
+static double aloss(double X1, double X2, double DT, double DEN, double DH0, double TE0) {
+  const double XION = 2.179e-11, XO = 1.e-3;
+  const double C0 = 0.5732, C1 = 1.8288e-5, C2 = -1.15822e-10, C3 = 9.4288e-16;
+  const double D0 = 0.5856, D1 = 1.55083e-5, D2 = -9.669e-12, D3 = 5.716e-19;
+  const double ENK = 118409., EN = 1.634E-11;
+  (void)X2;
+  (void)DT;
+  const double TE = dmax(TE0, 10.);
+  const double DH = DEN;
+  const double DHP = (1. - X1) * DH;
+  const double DE = DHP + 1.E-4 * DH;
+  const double DOI = XO * DH0;
+  const double DOII = XO * DHP;
+  if (TE <= 1e4) return 0.;
+  double OMEGA = 0.0;
+  if (TE <= 55000.) OMEGA = C0 + TE * (C1 + TE * (C2 + TE * C3));
+  if (TE >= 72000.) OMEGA = D0 + TE * (D1 + TE * (D2 + TE * D3));
+  if (TE > 55000. && TE < 72000.) {
+    const double OMEGAL = C0 + TE * (C1 + TE * (C2 + TE * C3));
+    const double OMEGAH = D0 + TE * (D1 + TE * (D2 + TE * D3));
+    const double FRAC = (TE - 55000.) / 17000.;
+    OMEGA = (1. - FRAC) * OMEGAL + FRAC * OMEGAH;
+  }
+  const double QLA = 8.6287E-6 / (2. * sqrt(TE)) * OMEGA * exp(-ENK / TE);
+  double ECOLL = DE * DH0 * QLA * EN;
+  ECOLL = dmax(ECOLL, 0.);
+  const double CION = 5.834E-11 * sqrt(TE) * exp(-1.579E5 / TE);
+  const double EION = DE * DH0 * CION * XION;
+  double EREC = DE * DHP * (betah(TE));
+  EREC = dmax(EREC, 0.);
+  const double TM = 1. / TE;
+  const double T2 = TM * TM;
+  double EOI = DE * DOI * pow(10., 1381465 * T2 - 12328.69 * TM - 19.82621);
+  double EOII = DE * DOII * pow(10., -2061075. * T2 - 14596.24 * TM - 19.01402);
+  EOI = dmax(EOI, 0.);
+  EOII = dmax(EOII, 0.);
+  const double BETAF = 1.3 * 1.42E-27 * pow(TE, 0.5);
+  const double HIICOOL = DE * DHP * BETAF;
+  const double EQUIL =
+      (1.0455E-18 / pow(TE, 0.63)) * (1. - exp(-pow(TE * 1.E-5, 1.63))) * DE * DEN + HIICOOL;
+  double FR = 0.0;
+  if (TE <= 44770.) FR = 0.;
+  if (TE >= 54770.) FR = 1.;
+  if (TE > 44770. && TE < 54770.) {
+    const double EX2 = exp(-2. * (TE - 49770.) / 500.);
+    const double TANH = (1. - EX2) / (1. + EX2);
+    FR = 0.5 * (1. + TANH);
+  }
+  return ECOLL + EION + (EREC + 7.033 * (EOI + EOII)) * (1. - FR) + EQUIL * FR;
+}
+
+/* :259-371 atomic (no diffuse radiation: radphi = 1, tprime = 10 K) */
+static void atomic(const gor_params_t* p, double dt, double* uu) {
+  const double xi = 1.e-4, boltzm = 1.3807e-16;
+  const int nd = neqdyn(p);
+  double prim[GOR_MAX_NEQ], T;
+  u2prim(p, uu, prim, &T);
+  const double col = colf(T);
+  const double rec = alpha_rec(T);
+  const double y0 = uu[nd] / uu[0];
+  const double dh = uu[0];
+  const double a = rec + col;
+  const double b = -((2. + xi) * rec + (1. + xi) * col);
+  const double c = (1. + xi) * rec;
+  const double d = sqrt(b * b - 4. * a * c);
+  const double g0 = (2. * a * y0 + b + d) / (2. * a * y0 + b - d);
+  const double e = exp(-d * dh * dt);
+  double y1 = (-b - d * (1. + g0 * e) / (1. - g0 * e)) / (2. * a);
+  y1 = dmin(y1, 0.9999);
+  y1 = dmax(y1, 0.);
+  const double dh0 = uu[nd];
+  const double al = aloss(y0, y1, dt, dh, dh0, T) / (dh * dh);
+  const double tprime = 10.;
+  const double ce = (2. * dh * al) / (3. * boltzm * T);
+  double t1 = tprime + (T - tprime) * exp(-ce * dt);
+  t1 = dmax(t1, 0.1 * T);
+  t1 = dmin(t1, 10. * T);
+  uu[nd] = y1 * uu[0];
+  if (p->mhd)
+    uu[4] = p->cv * (2. * uu[0] - uu[nd]) * t1 / p->Tempsc
+            + 0.5 * prim[0] * (prim[1] * prim[1] + prim[2] * prim[2] + prim[3] * prim[3])
+            + 0.5 * (prim[5] * prim[5] + prim[6] * prim[6] + prim[7] * prim[7]);
+  else
+    uu[4] = p->cv * (2. * uu[0] - uu[nd]) * t1 / p->Tempsc
+            + 0.5 * prim[0] * (prim[1] * prim[1] + prim[2] * prim[2] + prim[3] * prim[3]);
+}
+
+/* :41-67 coolingh */
+static void coolingh(gor_state_t* s, double dt_CFL) {
+  const gor_params_t* p = &s->p;
+  const int neq = p->neq;
+  const double dt_seconds = dt_CFL * p->tsc;
+#pragma omp parallel for schedule(static)
+  for (int k = 1; k <= p->nz; ++k)
+    for (int j = 1; j <= p->ny; ++j)
+      for (int i = 1; i <= p->nx; ++i) atomic(p, dt_seconds, &s->u[CID(s, i, j, k) * neq]);
 }
 
 /* src/hydro_core.f90:623-697  get_timestep */
@@ -1246,6 +1376,7 @@ void gor_tstep(gor_state_t* s, double dt_CFL) {
   fluxes(s, 2);
   step(s, dt_CFL);
   viscous_copy(s);
+  if (p->cooling == GOR_COOL_H) coolingh(s, dt_CFL);
   int table = p->cooling == GOR_COOL_DMC || p->cooling == GOR_COOL_CHI;
   if (table) cooling_table(s, dt_CFL);
   gor_boundaryI(s);
@@ -1256,7 +1387,8 @@ void gor_tstep(gor_state_t* s, double dt_CFL) {
 /* ---------------------------------------------------------------------- */
 gor_state_t* gor_create(const gor_params_t* p) {
   if (p->nx < 1 || p->ny < 1 || p->nz < 1) return NULL;
-  if (p->neq != 5 && p->neq != 8) return NULL;
+  if (p->npas < 0 || p->npas > 2) return NULL;
+  if (neqdyn(p) != 5 && neqdyn(p) != 8) return NULL;
   gor_state_t* s = (gor_state_t*)calloc(1, sizeof(gor_state_t));
   s->p = *p;
   s->NX = p->nx + 2 * NG;

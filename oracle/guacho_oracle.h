@@ -26,8 +26,8 @@ extern "C" {
 /* Switch ids, equal to src/constants.f90:56-98. */
 enum {
   GOR_SOLVER_HLL = 1, GOR_SOLVER_HLLC = 2, GOR_SOLVER_HLLE = 3, GOR_SOLVER_HLLD = 4,
-  GOR_EOS_ADIABATIC = 1, GOR_EOS_SINGLE_SPECIE = 2,
-  GOR_COOL_NONE = 0, GOR_COOL_DMC = 3, GOR_COOL_CHI = 4,
+  GOR_EOS_ADIABATIC = 1, GOR_EOS_SINGLE_SPECIE = 2, GOR_EOS_H_RATE = 3,
+  GOR_COOL_NONE = 0, GOR_COOL_H = 1, GOR_COOL_DMC = 3, GOR_COOL_CHI = 4,
   GOR_BC_OUTFLOW = 1, GOR_BC_CLOSED = 2, GOR_BC_PERIODIC = 3, GOR_BC_OTHER = 4,
   GOR_LIMITER_NO_AVERAGE = -1, GOR_LIMITER_NO_LIMIT = 0, GOR_LIMITER_MINMOD = 1,
   GOR_LIMITER_VAN_LEER = 2, GOR_LIMITER_VAN_ALBADA = 3, GOR_LIMITER_UMIST = 4,
@@ -37,6 +37,7 @@ enum {
 #define GOR_MAX_SPHERES 8
 #define GOR_MAX_GRAV 4
 #define GOR_MAX_TAB 512
+#define GOR_MAX_NEQ 10  /* 8 dynamical equations + 2 passive scalars */
 
 /* Error bits (the reference prints and stops in these cases). */
 enum {
@@ -89,6 +90,10 @@ typedef struct {
    * scalings of parameters.f90:159-170 it converts with */
   int th_cond, tc_saturation;
   double rsc, rhosc, vsc2, bsc, mu;
+  /* passive scalars (npas of parameters.f90:131-135): the last npas of the
+   * neq equations, neqdyn = neq - npas; EOS_H_RATE reads the first one as
+   * the neutral hydrogen density (src/hydro_core.f90:106-111) */
+  int npas;
 } gor_params_t;
 
 typedef struct gor_state gor_state_t;

@@ -18,7 +18,7 @@ import numpy as np
 HERE = Path(__file__).resolve().parent
 LIB = HERE / "liboracle.so"
 SRC = HERE / "guacho_oracle.c"
-MAXSPH, MAXGRAV, MAXTAB = 8, 4, 512
+MAXSPH, MAXGRAV, MAXTAB, MAXNEQ = 8, 4, 512, 10
 
 
 def build(force: bool = False) -> Path:
@@ -61,6 +61,7 @@ class GorParams(C.Structure):
         ("th_cond", C.c_int), ("tc_saturation", C.c_int),
         ("rsc", C.c_double), ("rhosc", C.c_double), ("vsc2", C.c_double), ("bsc", C.c_double),
         ("mu", C.c_double),
+        ("npas", C.c_int),
     ]
 
 
@@ -96,6 +97,7 @@ def params_struct(p) -> GorParams:
         s.grav_GM[i], s.grav_x[i], s.grav_y[i], s.grav_z[i] = gm, x, y, z
     s.th_cond, s.tc_saturation = p.th_cond, int(p.tc_saturation)
     s.rsc, s.rhosc, s.vsc2, s.bsc, s.mu = p.rsc, p.rhosc, p.vsc2, p.bsc, p.mu
+    s.npas = p.npas
     return s
 
 
@@ -242,7 +244,7 @@ def riemann(params, pl, pr):
     ps = params_struct(params)
     pl = np.ascontiguousarray(pl, dtype=np.float64)
     pr = np.ascontiguousarray(pr, dtype=np.float64)
-    ff = np.zeros(8)
+    ff = np.zeros(MAXNEQ)
     err = C.c_int(0)
     lib().gor_riemann(C.byref(ps), _p(pl), _p(pr), _p(ff), C.byref(err))
     return ff[:params.neq], err.value
@@ -251,7 +253,7 @@ def riemann(params, pl, pr):
 def prim2f(params, prim):
     ps = params_struct(params)
     prim = np.ascontiguousarray(prim, dtype=np.float64)
-    ff = np.zeros(8)
+    ff = np.zeros(MAXNEQ)
     lib().gor_prim2f(C.byref(ps), _p(prim), _p(ff))
     return ff[:params.neq]
 
@@ -259,7 +261,7 @@ def prim2f(params, prim):
 def u2prim(params, uu):
     ps = params_struct(params)
     uu = np.ascontiguousarray(uu, dtype=np.float64)
-    pr = np.zeros(8)
+    pr = np.zeros(MAXNEQ)
     T = C.c_double()
     lib().gor_u2prim(C.byref(ps), _p(uu), _p(pr), C.byref(T))
     return pr[:params.neq], T.value
@@ -268,7 +270,7 @@ def u2prim(params, uu):
 def prim2u(params, prim):
     ps = params_struct(params)
     prim = np.ascontiguousarray(prim, dtype=np.float64)
-    uu = np.zeros(8)
+    uu = np.zeros(MAXNEQ)
     lib().gor_prim2u(C.byref(ps), _p(prim), _p(uu))
     return uu[:params.neq]
 

@@ -85,6 +85,20 @@ def test_conduction_params(gpu_lib):
     assert _check(p) == _abi.ERR_PARAM
 
 
+def test_passive_scalar_params(gpu_lib):
+    p, _ = problems.h_cooling_blob(8)
+    assert p.npas == 2 and p.neq == 7 and _check(p) == 0
+    assert _check(problems.h_cooling_blob(8, mhd=True)[0]) == 0
+    base = problems.orszag_tang(8, 8, 4)[0]
+    assert _check(base.replace(npas=2)) == 0
+    for bad in (dict(npas=1), dict(npas=3),                  # 0 or 2 passives
+                dict(eq_of_state=P.EOS_H_RATE),              # needs n_HI
+                dict(cooling=P.COOL_H)):                     # needs n_HI
+        assert _check(base.replace(**bad)) == _abi.ERR_PARAM, bad
+    p = problems.wind_cooling(16)[0].replace(npas=2)          # user spheres + passives
+    assert _check(p) == _abi.ERR_PARAM
+
+
 def test_hydro_with_flux_cd_rejected(gpu_lib):
     p = problems.wind_cooling(16)[0].replace(enable_flux_cd=True)
     assert _check(p) == _abi.ERR_PARAM
@@ -131,7 +145,8 @@ def test_switch_ids_match_reference_constants():
             "LIMITER_NO_AVERAGE": -1, "LIMITER_NO_LIMIT": 0, "LIMITER_MINMOD": 1,
             "LIMITER_VAN_LEER": 2, "LIMITER_VAN_ALBADA": 3, "LIMITER_UMIST": 4,
             "LIMITER_WOODWARD": 5, "LIMITER_SUPERBEE": 6,
-            "TC_OFF": 0, "TC_ISOTROPIC": 1, "TC_ANISOTROPIC": 2}
+            "TC_OFF": 0, "TC_ISOTROPIC": 1, "TC_ANISOTROPIC": 2,
+            "EOS_H_RATE": 3, "COOL_H": 1}
     for k, v in want.items():
         m = re.search(rf"#define GCH_{k} \(?(-?\d+)\)?", text)
         assert m and int(m.group(1)) == v, k
