@@ -280,6 +280,9 @@ int gch_create(const gch_params_t* p, void* stream, gch_domain_t** out) {
   d->cfl_fused = p->neq >= 8 && p->enable_flux_cd && p->eta == 0.0 && !d->prim_in &&
                  !p->bc_user && p->th_cond == GCH_TC_OFF && p->cooling == GCH_COOL_NONE &&
                  p->npas == 0;  // the epilogue recovers the 8 dynamical fields only
+#ifdef GCH_NO_FUSE
+  d->cfl_fused = false;
+#endif
   k.ngrav = p->user_source_terms ? p->ngrav : 0;
 
   // z planes per block: enough blocks to fill the 152 SMs several times
