@@ -277,12 +277,6 @@ int gch_create(const gch_params_t* p, void* stream, gch_domain_t** out) {
   k.ntab = p->ntab; k.tab_i0 = p->tab_i0;
   k.tab_inv_dlog = p->tab_inv_dlog; k.tab_tail = p->tab_tail; k.tab_Tmin = p->tab_Tmin;
   k.nsph = p->bc_user ? p->nsph : 0;
-  d->cfl_fused = p->neq >= 8 && p->enable_flux_cd && p->eta == 0.0 && !d->prim_in &&
-                 !p->bc_user && p->th_cond == GCH_TC_OFF && p->cooling == GCH_COOL_NONE &&
-                 p->npas == 0;  // the epilogue recovers the 8 dynamical fields only
-#ifdef GCH_NO_FUSE
-  d->cfl_fused = false;
-#endif
   k.ngrav = p->user_source_terms ? p->ngrav : 0;
 
   // z planes per block: enough blocks to fill the 152 SMs several times
@@ -493,14 +487,8 @@ int gch_advance_enqueue(gch_domain* d, int max_steps, double tmax, double dtprin
   k_set_ctrl<<<1, 1, 0, d->stream>>>(d->sc, iter, n_iter, time, tprint, dtprint, tmax,
                                      time <= tmax ? 1 : 0);
   int st = cuda_ok(cudaGetLastError());
-  if (d->cfl_fused && !d->cfl_ready) {
-    // the graph's get_timestep relies on the previous step's CFL min:
-    // form it once from the current u (outside the graph)
-    st |= engine(d).cfl(d);
-  }
   if (!d->graph) {
     // capture one device-resident iteration of src/main.f90:94-125
-    if (d->cfl_fused) d->cfl_ready = true;
     cudaGraph_t g = nullptr;
     st |= cuda_ok(cudaStreamBeginCapture(d->stream, cudaStreamCaptureModeThreadLocal));
     st |= engine(d).get_dt(d);
@@ -512,7 +500,6 @@ int gch_advance_enqueue(gch_domain* d, int max_steps, double tmax, double dtprin
     if (st) return st;
   }
   for (int n = 0; n < max_steps; ++n) st |= cuda_ok(cudaGraphLaunch(d->graph, d->stream));
-  d->cfl_ready = d->cfl_fused;  // the last replay's k_ct<2> left the min
   return st;
 }
 

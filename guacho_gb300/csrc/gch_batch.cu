@@ -64,7 +64,6 @@ struct gch_batch {
   int kz = 0;                                // 0 until the autotuner ran
   std::vector<int> tune_kz;                  // candidates and their times
   std::vector<float> tune_ms;
-  bool cfl_ready = false;
   cudaGraphExec_t graph = nullptr;
   StepScalars** sc_list = nullptr;           // device: the boxes' scalar blocks
   StepScalars* sc_all = nullptr;             // device gather buffer
@@ -126,8 +125,6 @@ int grouped_advance(gch_batch* b, int steps, int n_iter) {
   k_batch_begin<<<grid_of(n), 128, 0, b->stream>>>(b->sc_list, n, n_iter);
   st |= cuda_ok(cudaGetLastError());
   if (!b->kz) st |= autotune(b);
-  const bool fused = b->boxes[0]->cfl_fused;
-  if (fused && !b->cfl_ready) st |= b->gops->cfl(b->boxes.data(), n, b->kz, b->stream);
   if (!b->graph && !st) {
     cudaGraph_t g = nullptr;
     st |= cuda_ok(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
@@ -138,7 +135,6 @@ int grouped_advance(gch_batch* b, int steps, int n_iter) {
   }
   if (st) return st;
   for (int s = 0; s < steps; ++s) st |= cuda_ok(cudaGraphLaunch(b->graph, b->stream));
-  b->cfl_ready = fused;  // the last step's stage-2 CT left the CFL minima
   k_batch_gather<<<grid_of(n), 128, 0, b->stream>>>(b->sc_list, n, b->sc_all);
   st |= cuda_ok(cudaMemcpyAsync(b->sc_all_host, b->sc_all, n * sizeof(StepScalars),
                                 cudaMemcpyDeviceToHost, b->stream));
@@ -226,7 +222,6 @@ int gch_batch_upload(gch_batch_t* b, int box, const double* u) {
   st |= gch_boundaryI(b->boxes[box]);
   st |= gch_calcprim(b->boxes[box]);
   st |= cuda_ok(cudaStreamSynchronize(b->boxes[box]->stream));
-  b->cfl_ready = false;  // the CFL minima must be formed from the new state
   return st;
 }
 

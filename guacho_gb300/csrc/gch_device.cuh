@@ -464,7 +464,8 @@ __device__ __forceinline__ void hlld(const KParams& p, const T* pl, const T* pr,
 }
 
 // Paired FP32 arithmetic: the left and right states of an interface in the
-// two lanes of a float2, one FADD2/FMUL2/FFMA2 instruction for both.
+// two lanes of a float2, one paired FP32 operation (__fadd2_rn, __fmul2_rn,
+// __ffma2_rn) for both.
 __device__ __forceinline__ float2 f2(float a, float b) { return make_float2(a, b); }
 __device__ __forceinline__ float2 f2(float a) { return make_float2(a, a); }
 __device__ __forceinline__ float2 add2(float2 a, float2 b) { return __fadd2_rn(a, b); }

@@ -31,11 +31,6 @@ struct gch_domain {
   double* stage = nullptr;      // device staging buffer, host layout (FP64 AoS)
   size_t ncell_host = 0;        // NX*NY*NZ
   int kz = 8;                   // z planes per block of the stage kernels
-  // The next step's CFL reduction runs in the stage-2 CT epilogue when
-  // nothing modifies u after it (no viscosity, table cooling or user
-  // spheres); cfl_ready says the device min is current for get_timestep.
-  bool cfl_fused = false;
-  bool cfl_ready = false;
   int launches = 0;             // kernel launches of the last tstep
   // thermal conduction (th_cond != 0): rho, p, T and the three face fluxes
   // (6 fields, FP64), the device min of the conduction timescale and its
@@ -75,7 +70,6 @@ struct EngineOps {
   int (*download_u)(gch_domain*, double*);
   int (*download_prim)(gch_domain*, double*);
   int (*loopfin)(gch_domain*);        // device time-loop tail
-  int (*cfl)(gch_domain*);            // CFL min of the current u only
   int (*probe)(gch_domain*);          // stage-1 fluxes alone (autotuner)
 };
 
@@ -87,9 +81,7 @@ extern const EngineOps kEngineKahan;
 // boxes share solver, neq, limiter and flux-CD, have no table cooling,
 // resistivity or user spheres, and are advanced on one stream.
 struct GroupOps {
-  // CFL min of the current u of every box (k_cfl)
-  int (*cfl)(gch_domain* const* boxes, int n, int kz, cudaStream_t s);
-  // one device-resident iteration of every box: [k_cfl], k_dtfin, both
+  // one device-resident iteration of every box: k_cfl, k_dtfin, both
   // stages with their CT and ghost fills, k_loopfin
   int (*step)(gch_domain* const* boxes, int n, int kz, cudaStream_t s);
   // the stage-1 flux kernel alone (writes up and E, leaves u): the

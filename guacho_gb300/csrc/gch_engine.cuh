@@ -96,8 +96,8 @@ struct Engine {
   }
 
   // ---- get_timestep --------------------------------------------------------
-  // the CFL min over the interior into the device scalar block (k_cfl)
-  static int cfl(gch_domain* d) {
+  // the CFL min over the interior (k_cfl), then dt from it (k_dtfin)
+  static int get_dt(gch_domain* d) {
     const KParams& p = d->kp;
     dim3 cgrid = column_grid(p), block(32, 8);
     if (d->prim_in) {
@@ -109,28 +109,9 @@ struct Engine {
         k_cfl<Pol, decltype(N)::value, false><<<cgrid, block, 0, d->stream>>>(p, (const TU*)d->u, d->sc, kzc);
       });
     }
-    d->cfl_ready = true;
-    return cuda_status(cudaGetLastError());
-  }
-
-  static int get_dt(gch_domain* d) {
-    const KParams& p = d->kp;
-    dim3 cgrid = column_grid(p), block(32, 8);
-    if (d->cfl_fused && d->cfl_ready) {
-      // the min over cells was accumulated by the last step's k_ct<2>
-    } else if (d->prim_in) {
-      with_neq(p.neq, [&](auto N) {
-        k_cfl<Pol, decltype(N)::value, true><<<cgrid, block, 0, d->stream>>>(p, (const TS*)d->primit, d->sc, kzc);
-      });
-    } else {
-      with_neq(p.neq, [&](auto N) {
-        k_cfl<Pol, decltype(N)::value, false><<<cgrid, block, 0, d->stream>>>(p, (const TU*)d->u, d->sc, kzc);
-      });
-    }
-    if (!(d->cfl_fused && d->cfl_ready)) gch_mark(d, "k_cfl");
+    gch_mark(d, "k_cfl");
     k_dtfin<<<1, 1, 0, d->stream>>>(d->sc, p.cfl, p.dx, p.dy, p.dz);
     gch_mark(d, "k_dtfin");
-    d->cfl_ready = false;  // k_dtfin consumed the min
     return cuda_status(cudaGetLastError());
   }
 
@@ -147,7 +128,7 @@ struct Engine {
     ++d->launches;
     gch_mark(d, "k_flux_stage1");
     if (ct) {
-      k_ct<Pol, 1, false><<<column_grid(p), cblock, 0, d->stream>>>(
+      k_ct<Pol, 1><<<column_grid(p), cblock, 0, d->stream>>>(
           p, (const TU*)d->u, (TS*)d->up, (const TS*)d->E, (const TS*)d->s678, d->sc, kzc);
       ++d->launches;
       gch_mark(d, "k_ct_stage1");
@@ -160,12 +141,8 @@ struct Engine {
     ++d->launches;
     gch_mark(d, "k_flux_stage2");
     if (ct) {
-      if (d->cfl_fused)
-        k_ct<Pol, 2, true><<<column_grid(p), cblock, 0, d->stream>>>(
-            p, (const TU*)d->u, (TU*)dst2, (const TS*)d->E, (const TS*)d->s678, d->sc, kzc);
-      else
-        k_ct<Pol, 2, false><<<column_grid(p), cblock, 0, d->stream>>>(
-            p, (const TU*)d->u, (TU*)dst2, (const TS*)d->E, (const TS*)d->s678, d->sc, kzc);
+      k_ct<Pol, 2><<<column_grid(p), cblock, 0, d->stream>>>(
+          p, (const TU*)d->u, (TU*)dst2, (const TS*)d->E, (const TS*)d->s678, d->sc, kzc);
       ++d->launches;
       gch_mark(d, "k_ct_stage2");
     }
@@ -203,18 +180,15 @@ struct Engine {
       gch_mark(d, "k_calcprim");
     }
     st |= cuda_status(cudaGetLastError());
-    d->cfl_ready = d->cfl_fused;
     return st;
   }
 
   static int boundaryI(gch_domain* d) {
-    d->cfl_ready = false;
     ghost<TU>(d, (TU*)d->u, 1);
     return cuda_status(cudaGetLastError());
   }
 
   static int calcprim(gch_domain* d) {
-    d->cfl_ready = false;
     if (!d->prim_in) return GCH_OK;  // primitives are formed on the fly
     const KParams& p = d->kp;
     dim3 g((p.NX + 31) / 32, (p.NY + 7) / 8, p.NZ), b(32, 8);
@@ -227,7 +201,6 @@ struct Engine {
   // host layout <-> u: `aos` is the staging buffer or mapped host memory
   static constexpr int kLayoutGrid = 152 * 8;
   static int upload(gch_domain* d, const double* aos) {
-    d->cfl_ready = false;
     k_aos_to_soa<TU><<<kLayoutGrid, kLayoutCells, 0, d->stream>>>(d->kp, aos, (TU*)d->u, d->kp.neq);
     return cuda_status(cudaGetLastError());
   }
@@ -262,7 +235,7 @@ struct Engine {
 
   static constexpr EngineOps ops() {
     return EngineOps{&get_dt, &tstep, &boundaryI, &calcprim,
-                     &upload, &download_u, &download_prim, &loopfin, &cfl, &probe};
+                     &upload, &download_u, &download_prim, &loopfin, &probe};
   }
 };
 

@@ -105,7 +105,7 @@ struct GroupEngine {
     return (long long)x.gx * x.gy * ((p.nz + kzc - 1) / kzc);
   }
 
-  template <int STAGE, bool CFL>
+  template <int STAGE>
   static int ct(gch_domain* const* boxes, int n, cudaStream_t s) {
     return chunks(
         boxes, n,
@@ -117,7 +117,7 @@ struct GroupEngine {
           return column_setup(x, d->kp);
         },
         [&](GroupArgs& g, unsigned b) {
-          if (b) k_ct_grp<Pol, STAGE, CFL><<<b, dim3(32, 8), 0, s>>>(g);
+          if (b) k_ct_grp<Pol, STAGE><<<b, dim3(32, 8), 0, s>>>(g);
         });
   }
 
@@ -174,15 +174,14 @@ struct GroupEngine {
   static int step(gch_domain* const* boxes, int n, int kz, cudaStream_t s) {
     const KParams& p0 = boxes[0]->kp;
     const bool ctp = p0.neq >= 8 && p0.flux_cd;
-    const bool fused = boxes[0]->cfl_fused;
     int st = GCH_OK;
-    if (!fused) st |= cfl(boxes, n, kz, s);
+    st |= cfl(boxes, n, kz, s);
     st |= scalar_tail(boxes, n, false, s);
     st |= flux<1>(boxes, n, kz, s);
-    if (ctp) st |= ct<1, false>(boxes, n, s);
+    if (ctp) st |= ct<1>(boxes, n, s);
     st |= ghost<TS>(boxes, n, true, 2, s);
     st |= flux<2>(boxes, n, kz, s);
-    if (ctp) st |= fused ? ct<2, true>(boxes, n, s) : ct<2, false>(boxes, n, s);
+    if (ctp) st |= ct<2>(boxes, n, s);
     st |= ghost<TU>(boxes, n, false, 1, s);
     st |= scalar_tail(boxes, n, true, s);
     return st;
@@ -192,7 +191,7 @@ struct GroupEngine {
     return flux<1>(boxes, n, kz, s);
   }
 
-  static constexpr GroupOps ops() { return GroupOps{&cfl, &step, &probe}; }
+  static constexpr GroupOps ops() { return GroupOps{&step, &probe}; }
 };
 
 }  // namespace gch

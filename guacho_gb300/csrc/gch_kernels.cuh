@@ -430,19 +430,30 @@ k_flux(KParams p, const typename Src<Pol, NEQ, STAGE, PRIM_IN>::TIn* __restrict_
                                                    blockIdx.y, blockIdx.z);
 }
 // Products rounded on their own (never fused into a following sum), so the
-// CFL candidate rounds the same way in every kernel that inlines it: the
-// stage-2 CT epilogue (fused reduction) and k_cfl agree bit for bit.
+// CFL candidate rounds the same way in every kernel that inlines it (the
+// one-box and the grouped CFL reduction).
 __device__ __forceinline__ float mul_rn(float a, float b) { return __fmul_rn(a, b); }
 __device__ __forceinline__ double mul_rn(double a, double b) { return __dmul_rn(a, b); }
 
-// min(dx/(|vx|+cfx), dy/(|vy|+cfy), dz/(|vz|+cfz)) of one cell into dtp
+// The cell widths and gamma in the compute type, converted once per thread.
+template <class TC>
+struct CflConst {
+  TC h[3], g;
+  __device__ __forceinline__ explicit CflConst(const KParams& p)
+      : h{(TC)p.dx, (TC)p.dy, (TC)p.dz}, g((TC)p.gamma) {}
+};
+
+// min(dx/(|vx|+cfx), dy/(|vy|+cfy), dz/(|vz|+cfz)) of one cell into dtp.
+// The running min stays in the compute type: a float converts to double
+// exactly and in order, so the FP32 paths take the min of the same values
+// as a min over their FP64 images, with no FP64 instruction per cell.
 template <class TC, int NEQ>
-__device__ __forceinline__ void cfl_candidate(const KParams& p, const TC* pr, double& dtp,
-                                              int& bad) {
+__device__ __forceinline__ void cfl_candidate(const KParams& p, const CflConst<TC>& k,
+                                              const TC* pr, TC& dtp, int& bad) {
   TC cand[3];
   if (NEQ >= 8 && p.mhd) {
     // src/hydro_core.f90:568-581 cfast
-    const TC g = (TC)p.gamma;
+    const TC g = k.g;
     const TC bx = pr[5], by = pr[6], bz = pr[7];
     const TC b2 = mul_rn(bx, bx) + mul_rn(by, by) + mul_rn(bz, bz);
     const TC gp = mul_rn(g, pr[4]);
@@ -458,18 +469,18 @@ __device__ __forceinline__ void cfl_candidate(const KParams& p, const TC* pr, do
     const TC cx = tsqrt(mul_rn(TC(0.5), a + tsqrt(disc(bx))) / pr[0]);
     const TC cy = tsqrt(mul_rn(TC(0.5), a + tsqrt(disc(by))) / pr[0]);
     const TC cz = tsqrt(mul_rn(TC(0.5), a + tsqrt(disc(bz))) / pr[0]);
-    cand[0] = (TC)p.dx / (tabs(pr[1]) + cx);
-    cand[1] = (TC)p.dy / (tabs(pr[2]) + cy);
-    cand[2] = (TC)p.dz / (tabs(pr[3]) + cz);
+    cand[0] = k.h[0] / (tabs(pr[1]) + cx);
+    cand[1] = k.h[1] / (tabs(pr[2]) + cy);
+    cand[2] = k.h[2] / (tabs(pr[3]) + cz);
   } else {
     const TC c0 = csound(p, pr[4], pr[0]);
-    cand[0] = (TC)p.dx / (tabs(pr[1]) + c0);
-    cand[1] = (TC)p.dy / (tabs(pr[2]) + c0);
-    cand[2] = (TC)p.dz / (tabs(pr[3]) + c0);
+    cand[0] = k.h[0] / (tabs(pr[1]) + c0);
+    cand[1] = k.h[1] / (tabs(pr[2]) + c0);
+    cand[2] = k.h[2] / (tabs(pr[3]) + c0);
   }
 #pragma unroll
   for (int d = 0; d < 3; ++d) {
-    if (cand[d] == cand[d]) dtp = tmin_(dtp, (double)cand[d]);
+    if (cand[d] == cand[d]) dtp = tmin_(dtp, cand[d]);
     else bad = 1;
   }
 }
@@ -495,7 +506,7 @@ __device__ __forceinline__ void cfl_block_reduce(double dtp, int bad, StepScalar
 // ---------------------------------------------------------------------------
 // Constrained transport of B (src/flux_cd_module.f90:311-321) with the E
 // ghost layer of boundaryI_ef (:45-237) applied as an index map.
-template <class Pol, int STAGE, bool CFL>
+template <class Pol, int STAGE>
 __device__ __forceinline__ void
 ct_body(const KParams& p, const typename Pol::TU* u,
         typename std::conditional<STAGE == 1, typename Pol::TS, typename Pol::TU>::type* dst,
@@ -509,8 +520,8 @@ ct_body(const KParams& p, const typename Pol::TU* u,
   const int kb = bz * kz;
   const int ke = min(p.nz, kb + kz);
   const bool active = ci < p.nx && cj < p.ny;
-  if (!CFL && !active) return;
-  const int ax = min(ci, p.nx - 1) + NG, ay = min(cj, p.ny - 1) + NG;
+  if (!active) return;
+  const int ax = ci + NG, ay = cj + NG;
   const double dt = STAGE == 1 ? sc->dt / 2.0 : sc->dt;
   const TC hx = (TC)(0.5 * sc->dtd[STAGE - 1][0]), hy = (TC)(0.5 * sc->dtd[STAGE - 1][1]),
            hz = (TC)(0.5 * sc->dtd[STAGE - 1][2]);
@@ -531,8 +542,6 @@ ct_body(const KParams& p, const typename Pol::TU* u,
     return v;
   };
 
-  double dtp = 1e30;
-  int bad = 0;
   // E1 and E2 of this column at planes k-1 and k: the z neighbours march
   // with the column, so each plane loads only its k+1 values
   TC e1m = e_ghost(0, ax, ay, kb + NG - 1), e2m = e_ghost(1, ax, ay, kb + NG - 1);
@@ -569,13 +578,6 @@ ct_body(const KParams& p, const typename Pol::TU* u,
     const auto u6 = Ops<Pol>::ld(u[5 * p.fs + c]);
     const auto u7 = Ops<Pol>::ld(u[6 * p.fs + c]);
     const auto u8 = Ops<Pol>::ld(u[7 * p.fs + c]);
-    typename Ops<Pol>::R uu[8];
-    if constexpr (CFL && STAGE == 2) {
-      // u(1:5) of this cell (this kernel writes only B): loaded with the
-      // other inputs of the plane, ahead of the stores of B
-#pragma unroll
-      for (int q = 0; q < 5; ++q) uu[q] = Ops<Pol>::ld(dst[q * p.fs + c]);
-    }
     // src/flux_cd_module.f90:311-321
     auto b6 = Ops<Pol>::ct(u6, hy, e3ym, e3yp, hz, e2zm, e2zp, true);
     auto b7 = Ops<Pol>::ct(u7, hx, e3xm, e3xp, hz, e1zm, e1zp, false);
@@ -585,42 +587,21 @@ ct_body(const KParams& p, const typename Pol::TU* u,
       b7 = Ops<Pol>::add(b7, dt * (double)s678[p.fs + c]);
       b8 = Ops<Pol>::add(b8, dt * (double)s678[2 * p.fs + c]);
     }
-    if (active) {
-      dst[5 * p.fs + c] = store_as<TD>(b6);
-      dst[6 * p.fs + c] = store_as<TD>(b7);
-      dst[7 * p.fs + c] = store_as<TD>(b8);
-    }
-    if constexpr (CFL && STAGE == 2) {
-      // the next step's CFL candidate from the final state of this cell
-      // (same values and arithmetic as k_cfl on u)
-      if (active) {
-        uu[5] = store_as<typename Pol::TU>(b6);
-        uu[6] = store_as<typename Pol::TU>(b7);
-        uu[7] = store_as<typename Pol::TU>(b8);
-        TC pr[8];
-        unsigned pfl = 0;
-        Ops<Pol>::template prim_vals<8>(p, uu, pr, pfl);
-        cfl_candidate<TC, 8>(p, pr, dtp, bad);
-        if (pfl) atomicAdd(&sc->pfloor, (unsigned long long)pfl);
-      }
-    }
+    dst[5 * p.fs + c] = store_as<TD>(b6);
+    dst[6 * p.fs + c] = store_as<TD>(b7);
+    dst[7 * p.fs + c] = store_as<TD>(b8);
   }
-  if constexpr (CFL && STAGE == 2) cfl_block_reduce(dtp, bad, sc);
 }
 
 // block (32, 8); grid (ceil(nx/32), ceil(ny/8), ceil(nz/kz)).  Four blocks
-// per SM keep enough loads in flight for the plain CT update; the variant
-// with the fused CFL candidate (pressure recovery and three fast speeds per
-// cell) runs fastest with the registers of two blocks per SM (measured on
-// the 256^3 turbulence box: 0.54 ms against 0.58 ms with four, 0.60 ms with
-// three).
-template <class Pol, int STAGE, bool CFL>
-__global__ void __launch_bounds__(256, CFL ? 2 : 4)
+// per SM keep enough loads in flight for this bandwidth-bound update.
+template <class Pol, int STAGE>
+__global__ void __launch_bounds__(256, 4)
 k_ct(KParams p, const typename Pol::TU* u,
      typename std::conditional<STAGE == 1, typename Pol::TS, typename Pol::TU>::type* dst,
      const typename Pol::TS* __restrict__ E, const typename Pol::TS* __restrict__ s678,
      StepScalars* sc, int kz) {
-  ct_body<Pol, STAGE, CFL>(p, u, dst, E, s678, sc, kz, blockIdx.x, blockIdx.y, blockIdx.z);
+  ct_body<Pol, STAGE>(p, u, dst, E, s678, sc, kz, blockIdx.x, blockIdx.y, blockIdx.z);
 }
 
 // ---------------------------------------------------------------------------
@@ -747,7 +728,8 @@ cfl_body(const KParams& p,
   const int cj = by * 8 + threadIdx.y;
   const int kb = bz * kz;
   const int ke = min(p.nz, kb + kz);
-  double dtp = 1e30;
+  const CflConst<TC> kc(p);
+  TC dtp = TC(1e30);
   int bad = 0;
   if (ci < p.nx && cj < p.ny) {
     unsigned pfl = 0;
@@ -758,11 +740,12 @@ cfl_body(const KParams& p,
         Ops<Pol>::template load_stored_prim<NEQ>(p, src, c, pr);
       else
         Ops<Pol>::template load_prim<NEQ>(p, src, c, pr, pfl);
-      cfl_candidate<TC, NEQ>(p, pr, dtp, bad);
+      cfl_candidate<TC, NEQ>(p, kc, pr, dtp, bad);
     }
     if (pfl) atomicAdd(&sc->pfloor, (unsigned long long)pfl);
   }
-  cfl_block_reduce(dtp, bad, sc);
+  // the sentinel of a thread without cells is the FP64 1e30 on every path
+  cfl_block_reduce(dtp < TC(1e30) ? (double)dtp : 1e30, bad, sc);
 }
 
 // block (32, 8); grid (ceil(nx/32), ceil(ny/8), ceil(nz/kz))

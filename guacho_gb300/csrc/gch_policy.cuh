@@ -112,8 +112,8 @@ struct Ops<PolFP64> {
 // that feeds a sum here is rounded on its own (__fmul_rn, never contracted)
 // and the exact products use explicit fmaf.  That keeps the transformations
 // exact, and it makes the pressure recovery round the same way in every
-// kernel that inlines it (the dt of the fused and the separate CFL
-// reductions agree bit for bit).
+// kernel that inlines it (the one-box and the grouped CFL reductions agree
+// bit for bit).
 struct DF {
   float hi, lo;
 };
