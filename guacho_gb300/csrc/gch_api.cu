@@ -274,6 +274,7 @@ int gch_create(const gch_params_t* p, void* stream, gch_domain_t** out) {
   k.cv = p->cv; k.gamma = p->gamma; k.cfl = p->cfl; k.eta = p->eta;
   k.inv_cv = 1.0 / p->cv;
   k.Tempsc = p->Tempsc; k.Psc = p->Psc; k.tsc = p->tsc;
+  gch::set_f32_params(k);
   k.ntab = p->ntab; k.tab_i0 = p->tab_i0;
   k.tab_inv_dlog = p->tab_inv_dlog; k.tab_tail = p->tab_tail; k.tab_Tmin = p->tab_Tmin;
   k.nsph = p->bc_user ? p->nsph : 0;

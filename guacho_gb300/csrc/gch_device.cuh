@@ -115,6 +115,12 @@ struct KParams {
   double cv, gamma, cfl, eta;
   double inv_cv;              // 1/cv for the mixed-precision paths
   double Tempsc, Psc, tsc;
+  // cv, gamma, 1/cv, Tempsc and the cell widths rounded to FP32 once on the
+  // host (round to nearest, the same value a device conversion gives): the
+  // FP32 kernels read these from the parameter bank.  A conversion of the
+  // FP64 value at every use would run on the FP64 pipe, and the compiler
+  // re-forms such loop-invariant values per use under register pressure.
+  float f_cv, f_gamma, f_inv_cv, f_Tempsc, f_dx, f_dy, f_dz;
   // cooling table (device pointers)
   int ntab, tab_i0;
   double tab_inv_dlog, tab_tail, tab_Tmin;
@@ -181,10 +187,28 @@ __device__ __forceinline__ float tabs(float a) { return fabsf(a); }
 __device__ __forceinline__ double tdiv_pos(double a, double b) { return a / b; }
 __device__ __forceinline__ float tdiv_pos(float a, float b) { return __fdividef(a, b); }
 
+// The FP32 copies of the FP64 parameters (host, once per domain).
+inline void set_f32_params(KParams& k) {
+  k.f_cv = (float)k.cv;
+  k.f_gamma = (float)k.gamma;
+  k.f_inv_cv = (float)k.inv_cv;
+  k.f_Tempsc = (float)k.Tempsc;
+  k.f_dx = (float)k.dx;
+  k.f_dy = (float)k.dy;
+  k.f_dz = (float)k.dz;
+}
+
+// A parameter in the compute type T: the FP64 value, or its FP32 copy.
+template <class T>
+__device__ __forceinline__ T par(double d, float f) {
+  if constexpr (sizeof(T) == 4) return f;
+  else return d;
+}
+
 // src/hydro_core.f90:395-476  prim2f (x direction)
 template <class T, int NEQ>
 __device__ __forceinline__ void prim2f(const KParams& p, const T* prim, T* ff) {
-  const T cv = (T)p.cv;
+  const T cv = par<T>(p.cv, p.f_cv);
   if (NEQ >= 8 && p.mhd) {
     T etot = T(0.5) * (prim[0] * (prim[1] * prim[1] + prim[2] * prim[2] + prim[3] * prim[3])
                        + prim[5] * prim[5] + prim[6] * prim[6] + prim[7] * prim[7])
@@ -223,7 +247,7 @@ __device__ __forceinline__ void prim2u(const KParams& p, const T* prim, T* uu) {
   uu[2] = prim[0] * prim[2];
   uu[3] = prim[0] * prim[3];
   uu[4] = T(0.5) * prim[0] * (prim[1] * prim[1] + prim[2] * prim[2] + prim[3] * prim[3])
-          + (T)p.cv * prim[4];
+          + par<T>(p.cv, p.f_cv) * prim[4];
   if (NEQ >= 8) {
     if (p.mhd) uu[4] = uu[4] + T(0.5) * (prim[5] * prim[5] + prim[6] * prim[6] + prim[7] * prim[7]);
     uu[5] = prim[5];
@@ -237,7 +261,7 @@ __device__ __forceinline__ void prim2u(const KParams& p, const T* prim, T* uu) {
 // src/hydro_core.f90:591-604  cfastX
 template <class T>
 __device__ __forceinline__ T cfastX(const KParams& p, const T* prim) {
-  const T g = (T)p.gamma;
+  const T g = par<T>(p.gamma, p.f_gamma);
   T b2 = prim[5] * prim[5] + prim[6] * prim[6] + prim[7] * prim[7];
   T cs2va2 = (g * prim[4] + b2) / prim[0];
   T disc = cs2va2 * cs2va2 - T(4.0) * g * prim[4] * (prim[5] * prim[5]) / prim[0] / prim[0];
@@ -250,7 +274,7 @@ __device__ __forceinline__ T cfastX(const KParams& p, const T* prim) {
 // src/hydro_core.f90:544-553  csound
 template <class T>
 __device__ __forceinline__ T csound(const KParams& p, T pr, T d) {
-  return tsqrt((T)p.gamma * pr / d);
+  return tsqrt(par<T>(p.gamma, p.f_gamma) * pr / d);
 }
 
 // src/hydro_core.f90:735-796  average (slope limiter)
@@ -306,7 +330,7 @@ __device__ __forceinline__ T average_t(int lim, T a, T b) {
 // src/hlld.f90:48-319  prim2fhlld
 template <class T, int NEQ>
 __device__ __forceinline__ void hlld(const KParams& p, const T* pl, const T* pr, T* ff, int& err) {
-  const T cv = (T)p.cv;
+  const T cv = par<T>(p.cv, p.f_cv);
   T csl = cfastX(p, pl);
   T csr = cfastX(p, pr);
   T sr = tmax_(pl[1] + csl, pr[1] + csr);
@@ -515,7 +539,7 @@ __device__ __forceinline__ float2 muscl_pair(float ll, float l, float r, float r
 template <int NEQ>
 __device__ __forceinline__ void hlld_pair(const KParams& p, const float* pl, const float* pr,
                                           float* ff, int& err) {
-  const float cv = (float)p.cv, g = (float)p.gamma;
+  const float cv = p.f_cv, g = p.f_gamma;
   const float2 rho = f2(pl[0], pr[0]), vx = f2(pl[1], pr[1]);
   const float2 vy = f2(pl[2], pr[2]), vz = f2(pl[3], pr[3]), pg = f2(pl[4], pr[4]);
   const float2 bn = f2(pl[5], pr[5]), by = f2(pl[6], pr[6]), bz = f2(pl[7], pr[7]);
@@ -617,7 +641,7 @@ __device__ __forceinline__ void hlld_pair(const KParams& p, const float* pl, con
 // src/hllc.f90:44-140  prim2fhllc (hydro, or passive B when NEQ == 8)
 template <class T, int NEQ>
 __device__ __forceinline__ void hllc(const KParams& p, const T* pl, const T* pr, T* ff, int& err) {
-  const T cv = (T)p.cv;
+  const T cv = par<T>(p.cv, p.f_cv);
   T csl = csound(p, pl[4], pl[0]);
   T csr = csound(p, pr[4], pr[0]);
   T sr = tmax_(pl[1] + csl, pr[1] + csr);

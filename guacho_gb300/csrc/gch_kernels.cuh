@@ -440,7 +440,8 @@ template <class TC>
 struct CflConst {
   TC h[3], g;
   __device__ __forceinline__ explicit CflConst(const KParams& p)
-      : h{(TC)p.dx, (TC)p.dy, (TC)p.dz}, g((TC)p.gamma) {}
+      : h{par<TC>(p.dx, p.f_dx), par<TC>(p.dy, p.f_dy), par<TC>(p.dz, p.f_dz)},
+        g(par<TC>(p.gamma, p.f_gamma)) {}
 };
 
 // min(dx/(|vx|+cfx), dy/(|vy|+cfy), dz/(|vz|+cfz)) of one cell into dtp.

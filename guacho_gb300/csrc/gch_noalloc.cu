@@ -189,6 +189,7 @@ extern "C" int gch_get_timestep_noalloc(const gch_params_t* p, const double* u_d
   k.dx = p->dx; k.dy = p->dy; k.dz = p->dz;
   k.cv = p->cv; k.gamma = p->gamma; k.cfl = p->cfl;
   k.Tempsc = p->Tempsc;
+  gch::set_f32_params(k);
   cudaStream_t s = (cudaStream_t)stream;
   // the completion counter must start at zero (a call cut short earlier
   // could have left it set); clearing it is a memset, not an allocation

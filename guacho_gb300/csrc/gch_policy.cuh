@@ -155,16 +155,16 @@ __device__ __forceinline__ void prim_from_f32(const KParams& p, const float* uu,
   DF kb = fast_two_sum(q, __fmul_rn(rem, ir));
   if (NEQ >= 8 && p.mhd) kb = df_add(kb, df_sumsq(uu[5], uu[6], uu[7]));
   const DF d = two_sum(uu[4], __fmul_rn(-0.5f, kb.hi));
-  float pr = (d.hi + (d.lo - __fmul_rn(0.5f, kb.lo))) * (float)p.inv_cv;
+  float pr = (d.hi + (d.lo - __fmul_rn(0.5f, kb.lo))) * p.f_inv_cv;
   if (!(pr >= 1e-16f)) ++pfl;
   pr = tmax_(pr, 1e-16f);
   if (p.eos == GCH_EOS_SINGLE_SPECIE) {
-    const float t = tmax_(1.0f, (pr * ir) * (float)p.Tempsc);
-    pr = r * t / (float)p.Tempsc;
+    const float t = tmax_(1.0f, (pr * ir) * p.f_Tempsc);
+    pr = r * t / p.f_Tempsc;
   } else if (NEQ > kNeqDyn<NEQ> && p.eos == GCH_EOS_H_RATE) {
     const float dentot = tmax_(2.0f * r - uu[kNeqDyn<NEQ>], 1e-15f);
-    const float t = tmax_(1.0f, (pr / dentot) * (float)p.Tempsc);
-    pr = dentot * t / (float)p.Tempsc;
+    const float t = tmax_(1.0f, (pr / dentot) * p.f_Tempsc);
+    pr = dentot * t / p.f_Tempsc;
   }
   prim[0] = r;
   prim[1] = uu[1] * ir;
@@ -329,16 +329,16 @@ struct Ops<PolKahan> {
       if (NEQ >= 8 && p.mhd)
         kb = df_add(kb, df_add(df_add(df_sq(uu[5]), df_sq(uu[6])), df_sq(uu[7])));
       const DF d = two_sum(uu[4].x, __fmul_rn(-0.5f, kb.hi));
-      float pr = (d.hi + ((d.lo + uu[4].y) - __fmul_rn(0.5f, kb.lo))) * (float)p.inv_cv;
+      float pr = (d.hi + ((d.lo + uu[4].y) - __fmul_rn(0.5f, kb.lo))) * p.f_inv_cv;
       if (!(pr >= 1e-16f)) ++pfl;
       pr = tmax_(pr, 1e-16f);
       if (p.eos == GCH_EOS_SINGLE_SPECIE) {
-        const float t = tmax_(1.0f, (pr * ir) * (float)p.Tempsc);
-        pr = rh * t / (float)p.Tempsc;
+        const float t = tmax_(1.0f, (pr * ir) * p.f_Tempsc);
+        pr = rh * t / p.f_Tempsc;
       } else if (NEQ > kNeqDyn<NEQ> && p.eos == GCH_EOS_H_RATE) {
         const float dentot = tmax_(2.0f * rh - uu[kNeqDyn<NEQ>].x, 1e-15f);
-        const float t = tmax_(1.0f, (pr / dentot) * (float)p.Tempsc);
-        pr = dentot * t / (float)p.Tempsc;
+        const float t = tmax_(1.0f, (pr / dentot) * p.f_Tempsc);
+        pr = dentot * t / p.f_Tempsc;
       }
       prim[0] = rh;
       prim[1] = uu[1].x * ir;
