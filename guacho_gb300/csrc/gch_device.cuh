@@ -151,6 +151,10 @@ struct StepScalars {
   // dt/dx, dt/dy, dt/dz of stage 1 (dtm = dt/2) and stage 2 (dt), computed
   // once per step exactly as src/hydro_solver.f90:91-93 does
   double dtd[2][3];
+  // the same ratios and their halves rounded to FP32 (the FP32 kernels'
+  // operands, converted once per step instead of once per thread)
+  float dtdf[2][3];
+  float hdtdf[2][3];
 };
 
 // Fill the per-stage ratios from sc->dt (one thread).
@@ -163,6 +167,11 @@ __device__ __forceinline__ void set_stage_ratios(StepScalars* sc, double dx, dou
   sc->dtd[1][0] = sc->dt / dx;
   sc->dtd[1][1] = sc->dt / dy;
   sc->dtd[1][2] = sc->dt / dz;
+  for (int s = 0; s < 2; ++s)
+    for (int d = 0; d < 3; ++d) {
+      sc->dtdf[s][d] = (float)sc->dtd[s][d];
+      sc->hdtdf[s][d] = (float)(0.5 * sc->dtd[s][d]);
+    }
 }
 
 __host__ __device__ inline long long cell_index(const KParams& p, int ax, int ay, int az) {

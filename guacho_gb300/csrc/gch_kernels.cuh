@@ -133,8 +133,9 @@ flux_body(const KParams& p, const typename Src<Pol, NEQ, STAGE, PRIM_IN>::TIn* _
   const int lim = p.limiter;
 
   const double dt = STAGE == 1 ? sc->dt / 2.0 : sc->dt;  // dtm = dt_CFL/2.
-  const TC dtdx = (TC)sc->dtd[STAGE - 1][0], dtdy = (TC)sc->dtd[STAGE - 1][1],
-           dtdz = (TC)sc->dtd[STAGE - 1][2];
+  const TC dtdx = par<TC>(sc->dtd[STAGE - 1][0], sc->dtdf[STAGE - 1][0]);
+  const TC dtdy = par<TC>(sc->dtd[STAGE - 1][1], sc->dtdf[STAGE - 1][1]);
+  const TC dtdz = par<TC>(sc->dtd[STAGE - 1][2], sc->dtdf[STAGE - 1][2]);
 
   int err = 0;
   unsigned pfl = 0;
@@ -487,20 +488,25 @@ __device__ __forceinline__ void cfl_candidate(const KParams& p, const CflConst<T
 }
 
 // Block-wide min of dtp into sc->dtmin_bits; every thread of the block calls.
-__device__ __forceinline__ void cfl_block_reduce(double dtp, int bad, StepScalars* sc) {
+// The min is taken in the compute type T and converted to FP64 once per
+// block (exact and order-preserving for a float); T(1e30) is the sentinel of
+// a thread without cells and becomes the FP64 1e30 on every path.
+template <class T>
+__device__ __forceinline__ void cfl_block_reduce(T dtp, int bad, StepScalars* sc) {
   if (__any_sync(0xffffffffu, bad) && (threadIdx.x & 31) == 0) atomicOr(&sc->err, GCH_ERR_DT);
   for (int o = 16; o > 0; o >>= 1) dtp = tmin_(dtp, __shfl_xor_sync(0xffffffffu, dtp, o));
-  __shared__ double red[32];
+  __shared__ T red[32];
   const int t = threadIdx.y * blockDim.x + threadIdx.x;
   const int lane = t & 31, wid = t >> 5;
   if (lane == 0) red[wid] = dtp;
   __syncthreads();
   if (wid == 0) {
     const int nw = (blockDim.x * blockDim.y) >> 5;
-    double v = lane < nw ? red[lane] : 1e30;
+    T v = lane < nw ? red[lane] : T(1e30);
     for (int o = 16; o > 0; o >>= 1) v = tmin_(v, __shfl_xor_sync(0xffffffffu, v, o));
+    const double m = v < T(1e30) ? (double)v : 1e30;
     // positive doubles order like their bit patterns
-    if (lane == 0) atomicMin(&sc->dtmin_bits, (unsigned long long)__double_as_longlong(v));
+    if (lane == 0) atomicMin(&sc->dtmin_bits, (unsigned long long)__double_as_longlong(m));
   }
 }
 
@@ -524,8 +530,9 @@ ct_body(const KParams& p, const typename Pol::TU* u,
   if (!active) return;
   const int ax = ci + NG, ay = cj + NG;
   const double dt = STAGE == 1 ? sc->dt / 2.0 : sc->dt;
-  const TC hx = (TC)(0.5 * sc->dtd[STAGE - 1][0]), hy = (TC)(0.5 * sc->dtd[STAGE - 1][1]),
-           hz = (TC)(0.5 * sc->dtd[STAGE - 1][2]);
+  const TC hx = par<TC>(0.5 * sc->dtd[STAGE - 1][0], sc->hdtdf[STAGE - 1][0]);
+  const TC hy = par<TC>(0.5 * sc->dtd[STAGE - 1][1], sc->hdtdf[STAGE - 1][1]);
+  const TC hz = par<TC>(0.5 * sc->dtd[STAGE - 1][2], sc->hdtdf[STAGE - 1][2]);
   const long long sx = 1, sy = p.pitch, sz = (long long)p.pitch * p.NY;
   const bool inxy = ax > NG && ax < NG + p.nx - 1 && ay > NG && ay < NG + p.ny - 1;
 
@@ -745,8 +752,7 @@ cfl_body(const KParams& p,
     }
     if (pfl) atomicAdd(&sc->pfloor, (unsigned long long)pfl);
   }
-  // the sentinel of a thread without cells is the FP64 1e30 on every path
-  cfl_block_reduce(dtp < TC(1e30) ? (double)dtp : 1e30, bad, sc);
+  cfl_block_reduce<TC>(dtp, bad, sc);
 }
 
 // block (32, 8); grid (ceil(nx/32), ceil(ny/8), ceil(nz/kz))

@@ -246,7 +246,9 @@ int gch_advance(gch_domain_t* d, int max_steps, double tmax, double dtprint, int
  * accumulated error bits. */
 int gch_last_step_info(gch_domain_t* d, long long* pfloor_hits, int* err_bits);
 
-/* Number of kernel launches one gch_tstep issues (for launch accounting). */
+/* Kernel launches of one gch_get_timestep (k_cfl, k_dtfin) plus one
+ * gch_tstep of this domain (for launch accounting).  The device loop of
+ * gch_advance adds one loop-tail kernel per iteration. */
 int gch_launches_per_step(gch_domain_t* d);
 
 /* ---- z-march depth of the stage kernels (no reference counterpart) -------
