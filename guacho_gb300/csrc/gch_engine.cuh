@@ -78,15 +78,23 @@ struct Engine {
   template <class T>
   static void ghost(gch_domain* d, T* a, int layers) {
     const KParams& p = d->kp;
-    for (int axis = 0; axis < 3; ++axis) {
-      int N0, N1;
-      if (axis == 0) { N0 = p.NY; N1 = p.NZ; }
-      else if (axis == 1) { N0 = p.NX; N1 = p.NZ; }
-      else { N0 = p.NX; N1 = p.NY; }
-      dim3 grid((N0 + 127) / 128, N1, 2 * layers);
-      k_ghost<T><<<grid, 128, 0, d->stream>>>(p, a, p.neq, axis, layers, d->sc);
+    if (ghost_all_ok(p, layers)) {  // the whole shell in one launch
+      const long long n = ghost_all_count(p, layers);
+      const unsigned g = (unsigned)std::min<long long>((n + 255) / 256, 152 * 16);
+      k_ghost_all<T><<<g, 256, 0, d->stream>>>(p, a, p.neq, layers, d->sc);
       ++d->launches;
       gch_mark(d, "k_ghost");
+    } else {  // a side shorter than the fill: the axes one after the other
+      for (int axis = 0; axis < 3; ++axis) {
+        int N0, N1;
+        if (axis == 0) { N0 = p.NY; N1 = p.NZ; }
+        else if (axis == 1) { N0 = p.NX; N1 = p.NZ; }
+        else { N0 = p.NX; N1 = p.NY; }
+        dim3 grid((N0 + 127) / 128, N1, 2 * layers);
+        k_ghost<T><<<grid, 128, 0, d->stream>>>(p, a, p.neq, axis, layers, d->sc);
+        ++d->launches;
+        gch_mark(d, "k_ghost");
+      }
     }
     if (p.bc_user && p.nsph > 0) {
       k_user_bc<T><<<dim3(64, p.nsph), 256, 0, d->stream>>>(p, a, p.neq, d->sc);

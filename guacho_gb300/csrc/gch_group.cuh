@@ -73,6 +73,15 @@ __global__ void __launch_bounds__(256, 6) k_ct_grp(const __grid_constant__ Group
                            x.kz, l % x.gx, (l / x.gx) % x.gy, l / (x.gx * x.gy));
 }
 
+// a2 = the array to fill; i1 = layers; 256 cells of one box per block
+template <class T>
+__global__ void __launch_bounds__(256) k_ghost_all_grp(const __grid_constant__ GroupArgs g) {
+  const GroupBox& x = g.box[group_box(g, blockIdx.x)];
+  if (!x.sc->active) return;
+  const long long t = (long long)(blockIdx.x - x.blk0) * 256 + threadIdx.x;
+  if (t < ghost_all_count(x.p, g.i1)) ghost_all_cell<T>(x.p, (T*)x.a2, x.p.neq, g.i1, t);
+}
+
 // a2 = the array to fill; i0 = axis, i1 = layers
 template <class T>
 __global__ void __launch_bounds__(128) k_ghost_grp(const __grid_constant__ GroupArgs g) {

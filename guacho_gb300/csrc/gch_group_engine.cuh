@@ -123,7 +123,21 @@ struct GroupEngine {
 
   template <class T>
   static int ghost(gch_domain* const* boxes, int n, bool on_up, int layers, cudaStream_t s) {
-    int st = GCH_OK;
+    bool all = true;
+    for (int i = 0; i < n; ++i) all = all && ghost_all_ok(boxes[i]->kp, layers);
+    if (all) {  // the whole shell of every box in one launch
+      return chunks(
+          boxes, n,
+          [&](GroupBox& x, gch_domain* d) -> long long {
+            x.a2 = on_up ? d->up : d->u;
+            return (ghost_all_count(d->kp, layers) + 255) / 256;
+          },
+          [&](GroupArgs& g, unsigned b) {
+            g.i1 = layers;
+            if (b) k_ghost_all_grp<T><<<b, 256, 0, s>>>(g);
+          });
+    }
+    int st = GCH_OK;  // a box with a side shorter than the fill: axis by axis
     for (int axis = 0; axis < 3; ++axis) {
       st |= chunks(
           boxes, n,

@@ -5,10 +5,10 @@
 //                     faces of an x-y tile marching along z; hydro update of
 //                     up(1:5) and the cell-centred E of flux-CD, fused
 //   k_ct<1>           up(6:8) from E (src/flux_cd_module.f90:311-321)
-//   k_ghost x3        boundaryII on up (2 layers) [+ k_user_bc]
+//   k_ghost_all       boundaryII on up (2 layers) [+ k_user_bc]
 //   k_flux<STAGE 2>   up -> limited linear reconstruction + fluxes; u(1:5)
 //   k_ct<2>           u(6:8)
-//   [k_visc] [k_cool] k_ghost x3 (boundaryI, 1 layer) [+ k_user_bc]
+//   [k_visc] [k_cool] k_ghost_all (boundaryI, 1 layer) [+ k_user_bc]
 //   [k_prim_ghost]
 // and get_timestep is k_cfl (block min -> one atomic per block) + k_dtfin.
 //
@@ -644,6 +644,88 @@ __device__ __forceinline__ void ghost_body(const KParams& p, T* a, int neq, int 
     if (flip && q == axis + 1) v = neg(v);
     a[q * p.fs + di] = v;
   }
+}
+
+// ---------------------------------------------------------------------------
+// All ghost layers of one fill in one launch.  The x, y and z fills of
+// src/boundaries.f90 run one after the other and each copies whole planes,
+// the other axes' ghosts included, so every ghost cell ends up with the value
+// of one interior cell: per axis, a coordinate in a filled layer of a wall
+// with a rule maps to its source (periodic wrap or mirror), any other
+// coordinate stays, and each closed wall crossed negates its normal momentum
+// once.  When every side is at least `layers` cells long no source is a cell
+// that this launch writes, so the cells can be filled in any order.
+//
+// Cell t in [0, ghost_all_count) enumerates the z band (all x, y), then the
+// y band outside it (all x), then the x band outside both.
+__host__ __device__ inline long long ghost_all_count(const KParams& p, int L) {
+  const long long b = 2 * L;
+  return b * p.NX * p.NY + (p.NZ - b) * b * p.NX + (p.NZ - b) * (p.NY - b) * b;
+}
+__host__ __device__ inline bool ghost_all_ok(const KParams& p, int L) {
+  return p.nx >= L && p.ny >= L && p.nz >= L;
+}
+// layer b of the band: 0..L-1 below the interior, L..2L-1 above it
+__device__ __forceinline__ int ghost_band(int b, int L, int n) {
+  return b < L ? NG - 1 - b : NG + n + (b - L);
+}
+// the i-th coordinate outside the band
+__device__ __forceinline__ int ghost_rest(int i, int L, int n) {
+  return i < NG - L ? i : (i < NG - L + n ? i + L : i + 2 * L);
+}
+// source coordinate of c along one axis, or c itself
+__device__ __forceinline__ int ghost_map(int c, int n, int L, int blo, int bhi, bool& flip) {
+  flip = false;
+  const bool lo = c < NG && c >= NG - L, hi = c >= NG + n && c < NG + n + L;
+  if (!lo && !hi) return c;
+  if ((lo ? blo : bhi) == GCH_BC_OTHER) return c;
+  return ghost_src(c, n, blo, bhi, flip);
+}
+template <class T>
+__device__ __forceinline__ void ghost_all_cell(const KParams& p, T* a, int neq, int L,
+                                               long long t) {
+  const long long b = 2 * L;
+  const long long cz = b * p.NX * p.NY, cy = (p.NZ - b) * b * p.NX;
+  int ax, ay, az;
+  if (t < cz) {
+    ax = (int)(t % p.NX);
+    const long long r = t / p.NX;
+    ay = (int)(r % p.NY);
+    az = ghost_band((int)(r / p.NY), L, p.nz);
+  } else if (t < cz + cy) {
+    t -= cz;
+    ax = (int)(t % p.NX);
+    const long long r = t / p.NX;
+    ay = ghost_band((int)(r % b), L, p.ny);
+    az = ghost_rest((int)(r / b), L, p.nz);
+  } else {
+    t -= cz + cy;
+    ax = ghost_band((int)(t % b), L, p.nx);
+    const long long r = t / b;
+    ay = ghost_rest((int)(r % (p.NY - b)), L, p.ny);
+    az = ghost_rest((int)(r / (p.NY - b)), L, p.nz);
+  }
+  bool fx, fy, fz;
+  const int sx = ghost_map(ax, p.nx, L, p.bc[0], p.bc[1], fx);
+  const int sy = ghost_map(ay, p.ny, L, p.bc[2], p.bc[3], fy);
+  const int sz = ghost_map(az, p.nz, L, p.bc[4], p.bc[5], fz);
+  if (sx == ax && sy == ay && sz == az) return;  // only walls without a rule
+  const long long di = cell_index(p, ax, ay, az), si = cell_index(p, sx, sy, sz);
+  for (int q = 0; q < neq; ++q) {
+    T v = a[q * p.fs + si];
+    if ((fx && q == 1) || (fy && q == 2) || (fz && q == 3)) v = neg(v);
+    a[q * p.fs + di] = v;
+  }
+}
+
+// block 256; grid-stride over ghost_all_count cells
+template <class T>
+__global__ void __launch_bounds__(256) k_ghost_all(KParams p, T* a, int neq, int layers,
+                                                   const StepScalars* sc) {
+  if (!sc->active) return;
+  const long long n = ghost_all_count(p, layers);
+  for (long long t = blockIdx.x * 256LL + threadIdx.x; t < n; t += (long long)gridDim.x * 256)
+    ghost_all_cell<T>(p, a, neq, layers, t);
 }
 
 // block 128; grid (ceil(N0/128), N1, 2*layers) over the transverse extent

@@ -58,6 +58,24 @@ def test_grouped_batch_matches_single(gpu_lib, prec):
     b.close()
 
 
+@pytest.mark.parametrize("prec", [P.FP32_MIXED, P.FP32_KAHAN])
+def test_grouped_batch_ragged_boxes(gpu_lib, prec):
+    """Boxes whose sides are not multiples of the 32 x 8 tile or of any
+    z-march depth, grouped in one launch per kernel."""
+    from guacho_gb300.domain import Batch
+    dims = [(37, 19, 11), (13, 29, 7), (33, 9, 17), (5, 40, 3)]
+    boxes = [problems.orszag_tang(*d, precision=prec) for d in dims]
+    b = Batch([p for p, _ in boxes])
+    for i, (_, u) in enumerate(boxes):
+        b.upload(i, u)
+    b.advance(4)
+    assert b.tuning()["grouped"]
+    for i, (p, u) in enumerate(boxes):
+        ref, _ = _single(p, u, 4)
+        assert close(b.download(i), ref), f"box {dims[i]}"
+    b.close()
+
+
 def test_grouped_batch_more_boxes_than_one_launch(gpu_lib):
     """70 small boxes: two launches per kernel (64 + 6 boxes)."""
     from guacho_gb300.domain import Batch

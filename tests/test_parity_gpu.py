@@ -95,6 +95,14 @@ CASES = {
         12, riemann_solver=P.SOLVER_HLL, bc_left=P.BC_OUTFLOW, bc_right=P.BC_OUTFLOW),
     "pmhd_hllc": lambda: _pmhd_state(12),
     "wind_cooling_24": lambda: problems.wind_cooling(24),
+    # partial 32 x 8 tiles in x and y and a partial z chunk; walls on every
+    # side of partial tiles; the smallest box whose second ghost layer still
+    # maps to interior cells
+    "ot_ragged": lambda: problems.orszag_tang(37, 19, 11),
+    "ot_ragged_closed": lambda: problems.orszag_tang(
+        37, 19, 11, bc_left=P.BC_CLOSED, bc_right=P.BC_OUTFLOW, bc_bottom=P.BC_OUTFLOW,
+        bc_top=P.BC_CLOSED, bc_out=P.BC_CLOSED, bc_in=P.BC_OUTFLOW),
+    "ot_tiny": lambda: problems.orszag_tang(2, 3, 2),
 }
 for lim in range(-1, 7):
     CASES[f"ot_limiter_{lim}"] = (lambda l=lim: problems.orszag_tang(16, 16, 4,
@@ -202,7 +210,7 @@ def _prims(p, u):
 @pytest.mark.parametrize("name", ["ot_hlld_minmod", "blast_hlld_outflow", "turbulence_16",
                                   "hydro_hllc_periodic", "ot_hlle_vanleer", "ot_limiter_4",
                                   "hydro_hllc_closed", "ot_eta", "ot_eight_wave",
-                                  "wind_cooling_24"])
+                                  "wind_cooling_24", "ot_ragged", "ot_ragged_closed"])
 def test_fp32_l1(gpu_lib, name, prec):
     """FP32-mixed (FP64 u) and FP32 + Kahan pairs against the FP64 oracle."""
     p, u0 = CASES[name]()
