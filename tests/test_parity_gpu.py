@@ -103,6 +103,11 @@ CASES = {
         37, 19, 11, bc_left=P.BC_CLOSED, bc_right=P.BC_OUTFLOW, bc_bottom=P.BC_OUTFLOW,
         bc_top=P.BC_CLOSED, bc_out=P.BC_CLOSED, bc_in=P.BC_OUTFLOW),
     "ot_tiny": lambda: problems.orszag_tang(2, 3, 2),
+    # one-cell-thick boxes: the second ghost layer of that axis is filled
+    # axis by axis, as the reference's array copies leave it
+    "ot_2d_nz1": lambda: problems.orszag_tang(16, 16, 1),
+    "ot_thin_y": lambda: problems.orszag_tang(16, 1, 8),
+    "ot_thin_x": lambda: problems.orszag_tang(1, 12, 6),
 }
 for lim in range(-1, 7):
     CASES[f"ot_limiter_{lim}"] = (lambda l=lim: problems.orszag_tang(16, 16, 4,
