@@ -6,15 +6,18 @@ random-phase solenoidal velocity, E(k) ~ k^-2 on 2<=|k|<=8, RMS Mach 1;
 B = (0.1,0,0) + solenoidal perturbation of RMS 0.05), HLLD, van Leer,
 flux-CD, gamma = 5/3.  A step = get_timestep + tstep over the whole box.
 
-  value  : FP32-mixed zone-updates/s, state resident in HBM, CUDA-graph
-           device loop, timed with CUDA events (max over ranks)
-  e2e    : the same through the C ABI with the state in pinned HOST memory
-           (gch_step_host: H2D of u, get_timestep, tstep, D2H of u per step)
-  extra  : the plain FP64 path on the same box, the L1 error of FP32-mixed
-           against it, the live roofline of the dominant kernel, the CPU
-           oracle on a bounded sample, SM clocks sampled during the run.
+  value  : FP32 + Kahan-pair zone-updates/s, state resident in HBM,
+           CUDA-graph device loop, timed with CUDA events (max over ranks)
+  e2e    : the same through the C ABI with the state in page-locked HOST
+           memory (gch_step_host: u read over the host link, get_timestep,
+           tstep, u written back over the link, every step)
+  extra  : FP32 with FP64 u and the plain FP64 path on the same box, their
+           L1 distances, the batched boxes, the live roofline of the
+           dominant kernel, the CPU oracle on a bounded sample, SM clocks
+           sampled during the run.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+  python bench.py --configs      # the other configurations, one line each
 
 Under torchrun every rank advances its own replica box on its own GPU
 (the path does not shard: replicas only), timings are max-reduced.
@@ -480,6 +483,41 @@ def run_ncu_case(args) -> None:
                           "time": t, "info": d.step_info()}))
 
 
+def run_configs(args) -> None:
+    """The benchmark's other configurations, one JSON line per configuration
+    and precision (not the headline line): Orszag-Tang 128x128x4 (HLLD,
+    minmod, flux-CD, periodic), the low-beta blast 192^3 (outflow; pressure
+    floor hits reported) and the hydro wind + table cooling box 256^3 (HLLC,
+    user spheres re-imposed at every boundary call).  Device loop, CUDA
+    events, after `warmup` steps."""
+    from guacho_gb300 import build as gbuild
+    gbuild.build(verbose=False)
+    from guacho_gb300 import params as P
+    from guacho_gb300 import problems
+    from guacho_gb300.domain import Domain
+    precs = {"fp64": P.FP64, "fp32_mixed_fp64u": P.FP32_MIXED, "fp32_kahan": P.FP32_KAHAN}
+    cases = [
+        ("orszag_tang 128x128x4", lambda: problems.orszag_tang(128, 128, 4), 200, 200),
+        ("low-beta blast 192^3", lambda: problems.blast(192), 5, 50),
+        ("wind + table cooling 256^3 (hydro)", lambda: problems.wind_cooling(256), 5, 50),
+    ]
+    for name, make, steps64, steps32 in cases:
+        p0, u0 = make()
+        for pname, prec in precs.items():
+            steps = steps64 if prec == P.FP64 else steps32
+            with Domain(p0.replace(precision=prec)) as d:
+                d.init(u0)
+                d.advance_timed(args.warmup)
+                ms = d.advance_timed(steps)
+                pfloor, err = d.step_info()
+            cells = p0.nx * p0.ny * p0.nz
+            print(json.dumps({"config": name, "precision": pname,
+                              "value": cells * steps / (ms * 1e-3), "unit": UNIT,
+                              "ms_per_step": ms / steps, "steps": steps,
+                              "warmup": args.warmup, "pfloor_hits_last_step": pfloor,
+                              "err_bits": err}), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -500,9 +538,14 @@ def main():
     ap.add_argument("--ncu-case", action="store_true",
                     help="run a short host-driven step sequence for profiler captures")
     ap.add_argument("--precision", default="kahan", choices=["kahan", "mixed", "fp64"])
+    ap.add_argument("--configs", action="store_true",
+                    help="time the other benchmark configurations (one line each)")
     args = ap.parse_args()
     if args.ncu_case:
         run_ncu_case(args)
+        return
+    if args.configs:
+        run_configs(args)
         return
     ws, rank, local = _dist()
     if ws > 1 and args.impl == "ours":

@@ -274,9 +274,9 @@ int gch_create(const gch_params_t* p, void* stream, gch_domain_t** out) {
   k.cv = p->cv; k.gamma = p->gamma; k.cfl = p->cfl; k.eta = p->eta;
   k.inv_cv = 1.0 / p->cv;
   k.Tempsc = p->Tempsc; k.Psc = p->Psc; k.tsc = p->tsc;
-  gch::set_f32_params(k);
   k.ntab = p->ntab; k.tab_i0 = p->tab_i0;
   k.tab_inv_dlog = p->tab_inv_dlog; k.tab_tail = p->tab_tail; k.tab_Tmin = p->tab_Tmin;
+  gch::set_f32_params(k);
   k.nsph = p->bc_user ? p->nsph : 0;
   k.ngrav = p->user_source_terms ? p->ngrav : 0;
 
@@ -319,13 +319,23 @@ int gch_create(const gch_params_t* p, void* stream, gch_domain_t** out) {
     alloc((void**)&d->tc_min, sizeof(unsigned long long));
     if (e == cudaSuccess) e = cudaMallocHost((void**)&d->tc_min_host, sizeof(unsigned long long));
   }
-  if (e == cudaSuccess && d->prim_in) {  // the tabulated cooling curve
-    e = cudaMalloc((void**)&d->tab, 2 * p->ntab * sizeof(double));
-    if (e == cudaSuccess) e = cudaMemcpy(d->tab, p->tab_T, p->ntab * sizeof(double), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess && d->prim_in) {  // the tabulated cooling curve, FP64 and FP32 rows
+    const int nt = p->ntab;
+    e = cudaMalloc((void**)&d->tab, 2 * nt * (sizeof(double) + sizeof(float)));
+    if (e == cudaSuccess) e = cudaMemcpy(d->tab, p->tab_T, nt * sizeof(double), cudaMemcpyHostToDevice);
     if (e == cudaSuccess)
-      e = cudaMemcpy(d->tab + p->ntab, p->tab_L, p->ntab * sizeof(double), cudaMemcpyHostToDevice);
+      e = cudaMemcpy(d->tab + nt, p->tab_L, nt * sizeof(double), cudaMemcpyHostToDevice);
+    float f[2 * GCH_MAX_TABLE];
+    for (int i = 0; i < nt; ++i) {
+      f[i] = (float)p->tab_T[i];
+      f[nt + i] = (float)p->tab_L[i];
+    }
+    float* tf = reinterpret_cast<float*>(d->tab + 2 * nt);
+    if (e == cudaSuccess) e = cudaMemcpy(tf, f, 2 * nt * sizeof(float), cudaMemcpyHostToDevice);
     k.tabT = d->tab;
-    k.tabL = d->tab + p->ntab;
+    k.tabL = d->tab + nt;
+    k.tabTf = tf;
+    k.tabLf = tf + nt;
   }
   if (e == cudaSuccess && k.nsph > 0) {
     e = cudaMalloc((void**)&d->sph, k.nsph * sizeof(gch_sphere_t));

@@ -121,11 +121,14 @@ struct KParams {
   // FP64 value at every use would run on the FP64 pipe, and the compiler
   // re-forms such loop-invariant values per use under register pressure.
   float f_cv, f_gamma, f_inv_cv, f_Tempsc, f_dx, f_dy, f_dz;
+  float f_Psc, f_tab_Tmin, f_tab_tail, f_tab_inv_dlog;
   // cooling table (device pointers)
   int ntab, tab_i0;
   double tab_inv_dlog, tab_tail, tab_Tmin;
   const double* tabT;
   const double* tabL;
+  const float* tabTf;         // the same rows in FP32 (the FP32 paths)
+  const float* tabLf;
   // user spheres and point masses (device pointers)
   int nsph, ngrav;
   const gch_sphere_t* sph;
@@ -205,6 +208,10 @@ inline void set_f32_params(KParams& k) {
   k.f_dx = (float)k.dx;
   k.f_dy = (float)k.dy;
   k.f_dz = (float)k.dz;
+  k.f_Psc = (float)k.Psc;
+  k.f_tab_Tmin = (float)k.tab_Tmin;
+  k.f_tab_tail = (float)k.tab_tail;
+  k.f_tab_inv_dlog = (float)k.tab_inv_dlog;
 }
 
 // A parameter in the compute type T: the FP64 value, or its FP32 copy.

@@ -97,7 +97,8 @@ struct Engine {
       }
     }
     if (p.bc_user && p.nsph > 0) {
-      k_user_bc<T><<<dim3(64, p.nsph), 256, 0, d->stream>>>(p, a, p.neq, d->sc);
+      // grid-stride over each sphere's bounding box; 4 blocks per SM per sphere
+      k_user_bc<T><<<dim3(4 * 152, p.nsph), 256, 0, d->stream>>>(p, a, p.neq, d->sc);
       ++d->launches;
       gch_mark(d, "k_user_bc");
     }
@@ -179,10 +180,13 @@ struct Engine {
     }
     // boundaryI on u (+ user spheres), then primitives of the ghost shell
     ghost<TU>(d, (TU*)d->u, 1);
-    if (d->prim_in) {
-      dim3 g((p.NX + 31) / 32, (p.NY + 7) / 8, p.NZ);
+    if (d->prim_in) {  // primitives of the ghost shell (interior ones come from k_cool)
+      const long long ns = (long long)(p.nx + 2) * (p.ny + 2) * (p.nz + 2) -
+                           (long long)p.nx * p.ny * p.nz;
+      const unsigned g = (unsigned)std::min<long long>((ns + 255) / 256, 152 * 16);
       with_neq(p.neq, [&](auto N) {
-        k_calcprim<Pol, decltype(N)::value><<<g, cblock, 0, d->stream>>>(p, (const TU*)d->u, (TS*)d->primit, 1, d->sc);
+        k_calcprim_shell<Pol, decltype(N)::value><<<g, 256, 0, d->stream>>>(
+            p, (const TU*)d->u, (TS*)d->primit, d->sc);
       });
       ++d->launches;
       gch_mark(d, "k_calcprim");
@@ -201,7 +205,7 @@ struct Engine {
     const KParams& p = d->kp;
     dim3 g((p.NX + 31) / 32, (p.NY + 7) / 8, p.NZ), b(32, 8);
     with_neq(p.neq, [&](auto N) {
-      k_calcprim<Pol, decltype(N)::value><<<g, b, 0, d->stream>>>(p, (const TU*)d->u, (TS*)d->primit, 0, d->sc);
+      k_calcprim<Pol, decltype(N)::value><<<g, b, 0, d->stream>>>(p, (const TU*)d->u, (TS*)d->primit, d->sc);
     });
     return cuda_status(cudaGetLastError());
   }

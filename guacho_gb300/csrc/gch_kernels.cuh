@@ -750,10 +750,15 @@ __global__ void k_user_bc(KParams p, T* a, int neq, const StepScalars* sc) {
     lo = max(0, (int)floor(amin) - 1);
     hi = min(N, (int)ceil(amax) + 2);
   };
-  int xl, xh, yl, yh, zl, zh;
-  lo_hi(sp.xc, sp.radius, p.dx, p.nx, p.NX, xl, xh);
-  lo_hi(sp.yc, sp.radius, p.dy, p.ny, p.NY, yl, yh);
-  lo_hi(sp.zc, sp.radius, p.dz, p.nz, p.NZ, zl, zh);
+  // the box once per block (FP64 divides), shared with the block's threads
+  __shared__ int box[6];
+  if (threadIdx.x == 0) {
+    lo_hi(sp.xc, sp.radius, p.dx, p.nx, p.NX, box[0], box[1]);
+    lo_hi(sp.yc, sp.radius, p.dy, p.ny, p.NY, box[2], box[3]);
+    lo_hi(sp.zc, sp.radius, p.dz, p.nz, p.NZ, box[4], box[5]);
+  }
+  __syncthreads();
+  const int xl = box[0], xh = box[1], yl = box[2], yh = box[3], zl = box[4], zh = box[5];
   const long long wx = xh - xl, wy = yh - yl, wz = zh - zl;
   if (wx <= 0 || wy <= 0 || wz <= 0) return;
   const long long total = wx * wy * wz;
@@ -884,10 +889,55 @@ __device__ __forceinline__ void loopfin_body(StepScalars* sc) {
 }
 static __global__ void k_loopfin(StepScalars* sc) { loopfin_body(sc); }
 
+// Table cooling on the FP32 paths: the primitives from the path's own
+// conversion (FP64 or compensated pressure recovery) and the update of
+// src/cooling_dmc.f90:136-150 in FP32, from the FP32 rows of the table.  The
+// energy change is taken as Eth0 * expm1(-Ce dt tsc), which equals the
+// reference's -Eth0 + cv p exp(-Ce dt tsc) but keeps a loss below the FP32
+// rounding of exp(); it is added to the FP64 or compensated u(5).
+template <class Pol, int NEQ>
+__device__ __forceinline__ void cool_f32(const KParams& p, typename Pol::TU* u,
+                                         typename Pol::TS* primit, const StepScalars* sc,
+                                         long long c) {
+  float pr[NEQ];
+  unsigned pfl = 0;
+  Ops<Pol>::template load_prim<NEQ>(p, (const typename Pol::TU*)u, c, pr, pfl);
+  const float r = pr[0];
+  float T;
+  if (NEQ > kNeqDyn<NEQ> && p.eos == GCH_EOS_H_RATE)
+    T = (pr[4] / tmax_(2.0f * r - pr[kNeqDyn<NEQ>], 1e-15f)) * p.f_Tempsc;
+  else
+    T = (pr[4] / r) * p.f_Tempsc;
+  if (T > p.f_tab_Tmin) {
+    const float Eth0 = p.f_cv * pr[4];
+    float aloss;
+    if (T > 1e8f) {
+      aloss = p.f_tab_tail * sqrtf(T);
+    } else {
+      int if1 = (int)(log10f(T) * p.f_tab_inv_dlog) - p.tab_i0;
+      if1 = max(0, min(if1, p.ntab - 2));
+      const float T0 = p.tabTf[if1], c0 = p.tabLf[if1];
+      const float T1 = p.tabTf[if1 + 1], c1 = p.tabLf[if1 + 1];
+      aloss = (c1 - c0) * (T - T0) / (T1 - T0) + c0;
+    }
+    const float ce = (aloss * (r * r)) / (Eth0 * p.f_Psc);
+    const float em1 = expm1f(-ce * (float)(sc->dt * p.tsc));
+    const float dE = Eth0 * em1;
+    if constexpr (std::is_same<Pol, PolKahan>::value)
+      u[4 * p.fs + c] = Ops<PolKahan>::addf(u[4 * p.fs + c], dE);
+    else
+      u[4 * p.fs + c] = u[4 * p.fs + c] + (double)dE;
+    pr[4] = fmaf(pr[4], em1, pr[4]);
+  }
+#pragma unroll
+  for (int q = 0; q < NEQ; ++q) primit[q * p.fs + c] = pr[q];
+}
+
 // ---------------------------------------------------------------------------
-// Tabulated cooling (src/cooling_dmc.f90:115-156, src/cooling_chi.f90:114-154),
-// FP64 throughout (the reference keeps Lambda in real(8)).  Writes primit of
-// every interior cell and u(5) of the cooled ones.
+// Tabulated cooling (src/cooling_dmc.f90:115-156, src/cooling_chi.f90:114-154).
+// The FP64 path computes in FP64 throughout, as the reference (Lambda in
+// real(8)); the FP32 paths use cool_f32.  Writes primit of every interior
+// cell and u(5) of the cooled ones.
 template <class Pol, int NEQ>
 __global__ void k_cool(KParams p, typename Pol::TU* u, typename Pol::TS* primit,
                        StepScalars* sc) {
@@ -896,6 +946,10 @@ __global__ void k_cool(KParams p, typename Pol::TU* u, typename Pol::TS* primit,
   const int ck = blockIdx.z;
   if (ci >= p.nx || cj >= p.ny || !sc->active) return;
   const long long c = cell_index(p, ci + NG, cj + NG, ck + NG);
+  if constexpr (!std::is_same<Pol, PolFP64>::value) {
+    cool_f32<Pol, NEQ>(p, u, primit, sc, c);
+    return;
+  }
   double uu[NEQ], pp[NEQ];
 #pragma unroll
   for (int q = 0; q < NEQ; ++q) uu[q] = to_d(u[q * p.fs + c]);
@@ -1051,25 +1105,11 @@ __global__ void k_visc(KParams p, typename Pol::TU* u, const typename Pol::TU* w
   }
 }
 
-// calcprim over the one-cell ghost shell (src/hydro_core.f90:258-300) or over
-// the whole array; writes primit in the stored type.
+// u2prim of one cell into primit (FP64 arithmetic on every path, as the
+// reference's calcprim), stored in the stage type.
 template <class Pol, int NEQ>
-__global__ void k_calcprim(KParams p, const typename Pol::TU* u, typename Pol::TS* primit,
-                           int only_ghost, const StepScalars* sc) {
-  const int ax = blockIdx.x * blockDim.x + threadIdx.x;
-  const int ay = blockIdx.y * blockDim.y + threadIdx.y;
-  const int az = blockIdx.z;
-  if (ax >= p.NX || ay >= p.NY || !sc->active) return;
-  if (only_ghost) {
-    // the shell of the box [NG-1, NG+n] in each direction
-    const bool inx = ax >= NG - 1 && ax <= NG + p.nx, iny = ay >= NG - 1 && ay <= NG + p.ny,
-               inz = az >= NG - 1 && az <= NG + p.nz;
-    if (!(inx && iny && inz)) return;
-    const bool shell = ax == NG - 1 || ax == NG + p.nx || ay == NG - 1 || ay == NG + p.ny ||
-                       az == NG - 1 || az == NG + p.nz;
-    if (!shell) return;
-  }
-  const long long c = cell_index(p, ax, ay, az);
+__device__ __forceinline__ void calcprim_cell(const KParams& p, const typename Pol::TU* u,
+                                              typename Pol::TS* primit, long long c) {
   double uu[NEQ], pp[NEQ];
 #pragma unroll
   for (int q = 0; q < NEQ; ++q) uu[q] = to_d(u[q * p.fs + c]);
@@ -1077,6 +1117,52 @@ __global__ void k_calcprim(KParams p, const typename Pol::TU* u, typename Pol::T
   Ops<PolFP64>::u2prim<NEQ>(p, uu, pp, pfl);
 #pragma unroll
   for (int q = 0; q < NEQ; ++q) primit[q * p.fs + c] = (typename Pol::TS)pp[q];
+}
+
+// calcprim of the one-cell ghost shell only (src/hydro_core.f90:258-300 with
+// only_ghost): one thread per shell cell of [NG-1, NG+n]^3, the two z planes,
+// then the two y rows of every interior plane, then the two x cells of every
+// interior row; grid-stride.
+template <class Pol, int NEQ>
+__global__ void __launch_bounds__(256)
+k_calcprim_shell(KParams p, const typename Pol::TU* u, typename Pol::TS* primit,
+                 const StepScalars* sc) {
+  if (!sc->active) return;
+  const long long mx = p.nx + 2, my = p.ny + 2;
+  const long long cz = 2 * mx * my, cy = 2LL * p.nz * mx, cx = 2LL * p.nz * p.ny;
+  for (long long t = blockIdx.x * 256LL + threadIdx.x; t < cz + cy + cx;
+       t += (long long)gridDim.x * 256) {
+    int ax, ay, az;
+    if (t < cz) {
+      ax = NG - 1 + (int)(t % mx);
+      const long long r = t / mx;
+      ay = NG - 1 + (int)(r % my);
+      az = r / my == 0 ? NG - 1 : NG + p.nz;
+    } else if (t < cz + cy) {
+      const long long s = t - cz, r = s / mx;
+      ax = NG - 1 + (int)(s % mx);
+      ay = (r & 1) ? NG + p.ny : NG - 1;
+      az = NG + (int)(r >> 1);
+    } else {
+      const long long s = t - cz - cy, r = s >> 1;
+      ax = (s & 1) ? NG + p.nx : NG - 1;
+      ay = NG + (int)(r % p.ny);
+      az = NG + (int)(r / p.ny);
+    }
+    calcprim_cell<Pol, NEQ>(p, u, primit, cell_index(p, ax, ay, az));
+  }
+}
+
+// calcprim over the whole array (src/hydro_core.f90:245-320); writes primit in
+// the stored type.  block (32, 8); grid (ceil(NX/32), ceil(NY/8), NZ).
+template <class Pol, int NEQ>
+__global__ void k_calcprim(KParams p, const typename Pol::TU* u, typename Pol::TS* primit,
+                           const StepScalars* sc) {
+  const int ax = blockIdx.x * blockDim.x + threadIdx.x;
+  const int ay = blockIdx.y * blockDim.y + threadIdx.y;
+  const int az = blockIdx.z;
+  if (ax >= p.NX || ay >= p.NY || !sc->active) return;
+  calcprim_cell<Pol, NEQ>(p, u, primit, cell_index(p, ax, ay, az));
 }
 
 // Host layout (Fortran u(neq, x, y, z), FP64, no pitch) <-> device SoA.
