@@ -56,8 +56,13 @@ class Domain:
         assert u.shape == self.params.shape, (u.shape, self.params.shape)
         check("gch_upload", self._lib.gch_upload(self._h, ptr(u)))
 
-    def download(self, with_primit: bool = False):
-        u = np.empty(self.params.shape, dtype=np.float64)
+    def download(self, with_primit: bool = False, out: np.ndarray | None = None):
+        """u (and primit) in the host layout; `out`, if given, receives u (a
+        page-locked `out` is written directly over the host link)."""
+        if out is not None:
+            assert out.shape == self.params.shape and out.dtype == np.float64
+            assert out.flags.c_contiguous
+        u = out if out is not None else np.empty(self.params.shape, dtype=np.float64)
         pr = np.empty(self.params.shape, dtype=np.float64) if with_primit else None
         check("gch_download", self._lib.gch_download(self._h, ptr(u),
                                                       ptr(pr) if pr is not None else None))
