@@ -557,6 +557,16 @@ ct_body(const KParams& p, const typename Pol::TU* u,
   for (int k = kb; k < ke; ++k) {
     const int az = k + NG;
     const long long c = cell_index(p, ax, ay, az);
+    if (k + 1 < ke) {  // next plane's B and E into L2 (no registers held)
+      asm volatile("prefetch.global.L2 [%0];" ::"l"(u + 5 * p.fs + c + sz));
+      asm volatile("prefetch.global.L2 [%0];" ::"l"(u + 6 * p.fs + c + sz));
+      asm volatile("prefetch.global.L2 [%0];" ::"l"(u + 7 * p.fs + c + sz));
+      asm volatile("prefetch.global.L2 [%0];" ::"l"(E + 2 * p.fs + c + sz));
+      if (k + 2 < p.nz) {
+        asm volatile("prefetch.global.L2 [%0];" ::"l"(E + c + 2 * sz));
+        asm volatile("prefetch.global.L2 [%0];" ::"l"(E + p.fs + c + 2 * sz));
+      }
+    }
     // the face neighbours of E needed by the three components
     TC e1p, e2p;
     if (k + 1 < p.nz) {
