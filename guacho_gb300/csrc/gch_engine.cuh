@@ -34,7 +34,7 @@ struct Engine {
     using TIn = typename Src<Pol, NEQ, STAGE, PRIM_IN>::TIn;
     using TD = typename std::conditional<STAGE == 1, TS, TU>::type;
     using TC = typename Ops<Pol>::TC;
-    constexpr size_t smem = sizeof(FluxSmem<TC, NEQ, STAGE>);
+    constexpr size_t smem = FluxLayout<Pol, NEQ, STAGE, PRIM_IN>::kBytes;
     static bool attr = false;  // once per instantiation
     if (!attr) {
       cudaFuncSetAttribute(k_flux<Pol, SOLVER, NEQ, STAGE, PRIM_IN, LIM>,

@@ -49,7 +49,7 @@ struct GroupEngine {
   // ---- stage kernels ---------------------------------------------------------
   template <int SOLVER, int NEQ, int STAGE, int LIM>
   static void flux_lim(GroupArgs& g, unsigned blocks, cudaStream_t s) {
-    constexpr size_t smem = sizeof(FluxSmem<TC, NEQ, STAGE>);
+    constexpr size_t smem = FluxLayout<Pol, NEQ, STAGE, false>::kBytes;
     static bool attr = false;  // once per instantiation
     if (!attr) {
       cudaFuncSetAttribute(k_flux_grp<Pol, SOLVER, NEQ, STAGE, LIM>,

@@ -82,6 +82,57 @@ struct FluxSmem {
   TC Q[NQ][NEQ][TY][TX];
 };
 
+// Stored values on their way into the stage kernel, copied asynchronously
+// from global into shared memory (cp.async): the next plane's halo cell of
+// each halo thread and, where there is room, the next column value of each
+// thread.
+template <class TIn, int NEQ, int H>
+struct HaloBuf {
+  TIn halo[NEQ][2 * H * (TX + TY)];
+};
+template <class TIn, int NEQ>
+struct ColBuf {
+  TIn col[NEQ][TY][TX];
+};
+
+// The stage kernel's dynamic shared memory.  The FP32 first-order stage
+// stages its stored inputs with cp.async: no registers are held while they
+// are in flight, and the halo loads leave the start of a plane.  A block
+// stays within 64 KB, so that three blocks per SM leave L1 room for the
+// register spills and the halo reuse (the MHD stage with both buffers, at
+// 74 KB, ran 9% slower; hydro with both, and MHD with the halo buffer only,
+// run faster).  The limited stage and FP64 have no room at their occupancy.
+template <class Pol, int NEQ, int STAGE, bool PRIM_IN>
+struct FluxLayout {
+  using TC = typename Ops<Pol>::TC;
+  using TIn = typename Src<Pol, NEQ, STAGE, PRIM_IN>::TIn;
+  static constexpr int H = STAGE == 1 ? 1 : 2;
+  static constexpr size_t kMain = (sizeof(FluxSmem<TC, NEQ, STAGE>) + 15) / 16 * 16;
+  static constexpr size_t kHalo = (sizeof(HaloBuf<TIn, NEQ, H>) + 15) / 16 * 16;
+  static constexpr size_t kCol = sizeof(ColBuf<TIn, NEQ>);
+  static constexpr size_t kLimit = 64 * 1024;
+  static constexpr bool kFp32S1 = STAGE == 1 && sizeof(TC) == 4;
+  static constexpr bool kAsyncHalo = kFp32S1 && kMain + kHalo <= kLimit;
+  static constexpr bool kAsyncCol = kAsyncHalo && kMain + kHalo + kCol <= kLimit;
+  static constexpr size_t kBytes = kMain + (kAsyncHalo ? kHalo : 0) + (kAsyncCol ? kCol : 0);
+};
+
+// cp.async of one 4-, 8- or 16-byte value from global into shared memory,
+// and the waits of the issuing thread for its own copies.
+template <class T>
+__device__ __forceinline__ void cp_async(T* s, const T* g) {
+  static_assert(sizeof(T) == 4 || sizeof(T) == 8 || sizeof(T) == 16, "cp.async size");
+  const unsigned sa = (unsigned)__cvta_generic_to_shared(s);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], %2;" ::"r"(sa), "l"(g), "n"(sizeof(T))
+               : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() {
+  asm volatile("cp.async.commit_group;" ::: "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() {
+  asm volatile("cp.async.wait_group 0;" ::: "memory");
+}
+
 // ---------------------------------------------------------------------------
 // Stage kernel.  Block = TX x TY cells of one x-y tile; the block marches
 // over planes [kb, ke) of z.  Per plane k:
@@ -114,8 +165,12 @@ flux_body(const KParams& p, const typename Src<Pol, NEQ, STAGE, PRIM_IN>::TIn* _
   constexpr int H = STAGE == 1 ? 1 : 2;
   constexpr int NRING = 2 * H * (TX + TY);
   using SM = FluxSmem<TC, NEQ, STAGE>;
+  using LAY = FluxLayout<Pol, NEQ, STAGE, PRIM_IN>;
+  constexpr bool AHALO = LAY::kAsyncHalo, ACOL = LAY::kAsyncCol;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   SM& sm = *reinterpret_cast<SM*>(smem_raw);
+  auto& sbh = *reinterpret_cast<HaloBuf<typename S::TIn, NEQ, H>*>(smem_raw + LAY::kMain);
+  auto& sbc = *reinterpret_cast<ColBuf<typename S::TIn, NEQ>*>(smem_raw + LAY::kMain + LAY::kHalo);
   auto& sP = sm.P;    // primitive plane k with halo
   auto& sF = sm.F;    // x-face fluxes
   auto& sG = sm.G;    // y-face fluxes
@@ -183,11 +238,34 @@ flux_body(const KParams& p, const typename Src<Pol, NEQ, STAGE, PRIM_IN>::TIn* _
   // that precedes the update.  Their load latency overlaps the barrier wait
   // and the update instead of stalling the start of a plane.  (Fetching the
   // next halo cell as well costs more in register spills than it saves.)
+  // With AHALO (ACOL) the next plane's halo cell (the next column value)
+  // goes to shared memory by cp.async instead, from the plane before kb on;
+  // each thread reads back only what it copied, after its own wait.
   using TIn = typename S::TIn;
   TIn colr[NEQ];
-  S::fetch(p, src, gidx(axc, ayc, k0 + NG + H), colr);
+  auto fetch_col = [&](int az_) {
+    const long long cc = gidx(axc, ayc, az_);
+    if constexpr (ACOL) {
+#pragma unroll
+      for (int q = 0; q < NEQ; ++q) cp_async(&sbc.col[q][ty][tx], src + q * p.fs + cc);
+    } else {
+      S::fetch(p, src, cc, colr);
+    }
+  };
+  fetch_col(k0 + NG + H);
+  if constexpr (AHALO) cp_async_commit();
   auto prefetch_next = [&](int k) {
-    if (k + 1 < ke) S::fetch(p, src, gidx(axc, ayc, k + 1 + NG + H), colr);
+    if (k + 1 < ke) {
+      fetch_col(k + 1 + NG + H);
+      if constexpr (AHALO) {
+        if (has_halo && k + 1 >= kb) {
+          const long long hc = gidx(i0 + hx + NG, j0 + hy + NG, k + 1 + NG);
+#pragma unroll
+          for (int q = 0; q < NEQ; ++q) cp_async(&sbh.halo[q][tid], src + q * p.fs + hc);
+        }
+      }
+    }
+    if constexpr (AHALO) cp_async_commit();
   };
 
   for (int k = k0; k < ke; ++k) {
@@ -199,6 +277,11 @@ flux_body(const KParams& p, const typename Src<Pol, NEQ, STAGE, PRIM_IN>::TIn* _
     // 1. the column ring shifts (centre <- p(k), p(k+1) <- p(k+2)) and the
     //    next plane of the column is formed from the fetched values
     {
+      if constexpr (AHALO) cp_async_wait_all();  // this thread's copies
+      if constexpr (ACOL) {
+#pragma unroll
+        for (int q = 0; q < NEQ; ++q) colr[q] = sbc.col[q][ty][tx];
+      }
       TC nx_[NEQ];
       S::convert(p, colr, nx_, pfl);
 #pragma unroll
@@ -216,7 +299,14 @@ flux_body(const KParams& p, const typename Src<Pol, NEQ, STAGE, PRIM_IN>::TIn* _
       //  the halo of plane k
       if (has_halo) {
         TC pr[NEQ];
-        S::load(p, src, gidx(i0 + hx + NG, j0 + hy + NG, az), pr, pfl);
+        if constexpr (AHALO) {
+          TIn hv[NEQ];
+#pragma unroll
+          for (int q = 0; q < NEQ; ++q) hv[q] = sbh.halo[q][tid];
+          S::convert(p, hv, pr, pfl);
+        } else {
+          S::load(p, src, gidx(i0 + hx + NG, j0 + hy + NG, az), pr, pfl);
+        }
 #pragma unroll
         for (int q = 0; q < NEQ; ++q) sP[q][hy + H][hx + H] = pr[q];
       }
