@@ -50,6 +50,7 @@ UNITS = {
     # thermal conduction: FP64 device arithmetic and host-side super-step
     # scalars, neither contracted into multiply-adds
     "gch_tc.cu": ["-fmad=false", "-Xcompiler", "-ffp-contract=off"],
+    "gch_tc32.cu": ["-use_fast_math"],
 }
 
 

@@ -93,6 +93,8 @@ extern const GroupOps kGroupKahan;
 
 // Thermal conduction after a tstep of dt_CFL (gch_tc.cu): synchronises once.
 int tc_run(gch_domain* d, double dt_CFL);
+int tc_run_kahan(gch_domain* d, double dt_CFL);  // the FP32 paths (gch_tc32.cu)
+int tc_run_mixed(gch_domain* d, double dt_CFL);
 // The super-time-stepping scalars of src/thermal_cond.f90:625-681.
 double tc_superstep(int N, double snu);
 double tc_substep(int j, int N, double nu);
