@@ -1082,57 +1082,146 @@ __global__ void k_cool(KParams p, typename Pol::TU* u, typename Pol::TS* primit,
 // reference computes it in real(8)).  The first passive scalar is the
 // neutral hydrogen density.
 namespace coolh {
-__device__ __forceinline__ double alpha(double T) { return 2.55e-13 * pow(1.e4 / T, 0.79); }
-__device__ __forceinline__ double colf(double T) { return 5.83e-11 * sqrt(T) * exp(-157828. / T); }
-__device__ __forceinline__ double betah(double T) {
-  const double a = 157890. / T;
-  return 1.133e-24 / sqrt(a) * (-0.0713 + 0.5 * log(a) + 0.640 * pow(a, -0.33333));
+// T is double on the FP64 path (the reference's expressions) and float on
+// the FP32 paths
+template <class T>
+__device__ __forceinline__ T tpow(T x, T y) { return pow(x, y); }
+template <>
+__device__ __forceinline__ float tpow(float x, float y) { return powf(x, y); }
+template <class T>
+__device__ __forceinline__ T texp(T x) { return exp(x); }
+template <>
+__device__ __forceinline__ float texp(float x) { return expf(x); }
+template <class T>
+__device__ __forceinline__ T tlog(T x) { return log(x); }
+template <>
+__device__ __forceinline__ float tlog(float x) { return logf(x); }
+
+template <class T>
+__device__ __forceinline__ T alpha(T t) { return T(2.55e-13) * tpow(T(1.e4) / t, T(0.79)); }
+template <class T>
+__device__ __forceinline__ T colf(T t) {
+  return T(5.83e-11) * tsqrt(t) * texp(T(-157828.) / t);
+}
+template <class T>
+__device__ __forceinline__ T betah(T t) {
+  const T a = T(157890.) / t;
+  return T(1.133e-24) / tsqrt(a) * (T(-0.0713) + T(0.5) * tlog(a) + T(0.640) * tpow(a, T(-0.33333)));
 }
 // :155-242 ALOSS (X2 and DT enter only a quantity the reference does not use)
-__device__ __forceinline__ double aloss(double X1, double DEN, double DH0, double TE0) {
-  const double XION = 2.179e-11, XO = 1.e-3;
-  const double C0 = 0.5732, C1 = 1.8288e-5, C2 = -1.15822e-10, C3 = 9.4288e-16;
-  const double D0 = 0.5856, D1 = 1.55083e-5, D2 = -9.669e-12, D3 = 5.716e-19;
-  const double ENK = 118409., EN = 1.634E-11;
-  const double TE = tmax_(TE0, 10.);
-  const double DH = DEN;
-  const double DHP = (1. - X1) * DH;
-  const double DE = DHP + 1.E-4 * DH;
-  const double DOI = XO * DH0;
-  const double DOII = XO * DHP;
-  if (TE <= 1e4) return 0.;
-  double OMEGA = 0.0;
-  if (TE <= 55000.) OMEGA = C0 + TE * (C1 + TE * (C2 + TE * C3));
-  if (TE >= 72000.) OMEGA = D0 + TE * (D1 + TE * (D2 + TE * D3));
-  if (TE > 55000. && TE < 72000.) {
-    const double OMEGAL = C0 + TE * (C1 + TE * (C2 + TE * C3));
-    const double OMEGAH = D0 + TE * (D1 + TE * (D2 + TE * D3));
-    const double FRAC = (TE - 55000.) / 17000.;
-    OMEGA = (1. - FRAC) * OMEGAL + FRAC * OMEGAH;
+template <class T>
+__device__ __forceinline__ T aloss(T X1, T DEN, T DH0, T TE0) {
+  const T XION = 2.179e-11, XO = 1.e-3;
+  const T C0 = 0.5732, C1 = 1.8288e-5, C2 = -1.15822e-10, C3 = 9.4288e-16;
+  const T D0 = 0.5856, D1 = 1.55083e-5, D2 = -9.669e-12, D3 = 5.716e-19;
+  const T ENK = 118409., EN = 1.634E-11;
+  const T one = 1.;
+  const T TE = tmax_(TE0, T(10.));
+  const T DH = DEN;
+  const T DHP = (one - X1) * DH;
+  const T DE = DHP + T(1.E-4) * DH;
+  const T DOI = XO * DH0;
+  const T DOII = XO * DHP;
+  if (TE <= T(1e4)) return 0.;
+  T OMEGA = 0.0;
+  if (TE <= T(55000.)) OMEGA = C0 + TE * (C1 + TE * (C2 + TE * C3));
+  if (TE >= T(72000.)) OMEGA = D0 + TE * (D1 + TE * (D2 + TE * D3));
+  if (TE > T(55000.) && TE < T(72000.)) {
+    const T OMEGAL = C0 + TE * (C1 + TE * (C2 + TE * C3));
+    const T OMEGAH = D0 + TE * (D1 + TE * (D2 + TE * D3));
+    const T FRAC = (TE - T(55000.)) / T(17000.);
+    OMEGA = (one - FRAC) * OMEGAL + FRAC * OMEGAH;
   }
-  const double QLA = 8.6287E-6 / (2. * sqrt(TE)) * OMEGA * exp(-ENK / TE);
-  const double ECOLL = tmax_(DE * DH0 * QLA * EN, 0.);
-  const double CION = 5.834E-11 * sqrt(TE) * exp(-1.579E5 / TE);
-  const double EION = DE * DH0 * CION * XION;
-  const double EREC = tmax_(DE * DHP * (betah(TE)), 0.);
-  const double TM = 1. / TE;
-  const double T2 = TM * TM;
-  const double EOI = tmax_(DE * DOI * pow(10., 1381465 * T2 - 12328.69 * TM - 19.82621), 0.);
-  const double EOII = tmax_(DE * DOII * pow(10., -2061075. * T2 - 14596.24 * TM - 19.01402), 0.);
-  const double BETAF = 1.3 * 1.42E-27 * pow(TE, 0.5);
-  const double HIICOOL = DE * DHP * BETAF;
-  const double EQUIL =
-      (1.0455E-18 / pow(TE, 0.63)) * (1. - exp(-pow(TE * 1.E-5, 1.63))) * DE * DEN + HIICOOL;
-  double FR = 0.0;
-  if (TE >= 54770.) FR = 1.;
-  if (TE > 44770. && TE < 54770.) {
-    const double EX2 = exp(-2. * (TE - 49770.) / 500.);
-    const double TANH = (1. - EX2) / (1. + EX2);
-    FR = 0.5 * (1. + TANH);
+  const T QLA = T(8.6287E-6) / (T(2.) * tsqrt(TE)) * OMEGA * texp(-ENK / TE);
+  const T ECOLL = tmax_(DE * DH0 * QLA * EN, T(0.));
+  const T CION = T(5.834E-11) * tsqrt(TE) * texp(T(-1.579E5) / TE);
+  const T EION = DE * DH0 * CION * XION;
+  const T EREC = tmax_(DE * DHP * (betah(TE)), T(0.));
+  const T TM = one / TE;
+  const T T2 = TM * TM;
+  const T EOI =
+      tmax_(DE * DOI * tpow(T(10.), T(1381465) * T2 - T(12328.69) * TM - T(19.82621)), T(0.));
+  const T EOII =
+      tmax_(DE * DOII * tpow(T(10.), T(-2061075.) * T2 - T(14596.24) * TM - T(19.01402)), T(0.));
+  const T BETAF = T(1.3 * 1.42E-27) * tpow(TE, T(0.5));
+  const T HIICOOL = DE * DHP * BETAF;
+  const T EQUIL = (T(1.0455E-18) / tpow(TE, T(0.63))) *
+                      (one - texp(-tpow(TE * T(1.E-5), T(1.63)))) * DE * DEN +
+                  HIICOOL;
+  T FR = 0.0;
+  if (TE >= T(54770.)) FR = 1.;
+  if (TE > T(44770.) && TE < T(54770.)) {
+    const T EX2 = texp(T(-2.) * (TE - T(49770.)) / T(500.));
+    const T TANH = (one - EX2) / (one + EX2);
+    FR = T(0.5) * (one + TANH);
   }
-  return ECOLL + EION + (EREC + 7.033 * (EOI + EOII)) * (1. - FR) + EQUIL * FR;
+  return ECOLL + EION + (EREC + T(7.033) * (EOI + EOII)) * (one - FR) + EQUIL * FR;
 }
 }  // namespace coolh
+
+// COOL_H on the FP32 paths: the same update in FP32 from the path's own
+// primitives.  Two changes keep it accurate in FP32:
+//  - the discriminant of the ionisation quadratic, b^2 - 4ac, cancels to
+//    about 1e-8 of its terms; it equals (xi*rec + (1 + xi)*col)^2 exactly,
+//    and d is taken as that sum;
+//  - the new total energy differs from the stored one only by the thermal
+//    part, cv*((2 rho - n_HI') T' - (2 rho - n_HI) T)/Tempsc, which is added
+//    to the FP64 or compensated u(5).  Where the pressure floor or the 1 K
+//    clamp acted, the stored energy is not cv p + KE + B^2/2 and the
+//    reference's value is stored instead.
+template <class Pol, int NEQ>
+__device__ __forceinline__ void cool_h_f32(const KParams& p, typename Pol::TU* u,
+                                           const StepScalars* sc, long long c) {
+  constexpr int ND = kNeqDyn<NEQ>;
+  float pr[NEQ];
+  unsigned pfl = 0;
+  Ops<Pol>::template load_prim<NEQ>(p, (const typename Pol::TU*)u, c, pr, pfl);
+  const float rho = pr[0], nhi = pr[ND];
+  const float dent0 = p.eos == GCH_EOS_H_RATE ? tmax_(2.0f * rho - nhi, 1e-15f) : rho;
+  const float T = (pr[4] / dent0) * p.f_Tempsc;
+  const bool clamped = pfl != 0 || (p.eos != GCH_EOS_ADIABATIC && !(T > 1.001f));
+  const float dt = (float)(sc->dt * p.tsc);
+  const float xi = 1.e-4f, boltzm = 1.3807e-16f;
+  const float col = coolh::colf(T);
+  const float rec = coolh::alpha(T);
+  const float y0 = nhi / rho;
+  const float dh = rho;
+  const float a = rec + col;
+  const float b = -((2.f + xi) * rec + (1.f + xi) * col);
+  const float d = xi * rec + (1.f + xi) * col;
+  const float g0 = (2.f * a * y0 + b + d) / (2.f * a * y0 + b - d);
+  const float e = expf(-d * dh * dt);
+  float y1 = (-b - d * (1.f + g0 * e) / (1.f - g0 * e)) / (2.f * a);
+  y1 = tmin_(y1, 0.9999f);
+  y1 = tmax_(y1, 0.f);
+  const float al = coolh::aloss(y0, dh, nhi, T) / (dh * dh);
+  const float tprime = 10.f;
+  const float ce = (2.f * dh * al) / (3.f * boltzm * T);
+  float t1 = tprime + (T - tprime) * expf(-ce * dt);
+  t1 = tmax_(t1, 0.1f * T);
+  t1 = tmin_(t1, 10.f * T);
+  const float nhi1 = y1 * rho;
+  const float eth1 = p.f_cv * (2.f * rho - nhi1) * t1 / p.f_Tempsc;
+  if constexpr (std::is_same<Pol, PolKahan>::value) {
+    u[ND * p.fs + c] = make_float2(nhi1, 0.f);
+    if (clamped) {
+      float e5 = eth1 + 0.5f * rho * (pr[1] * pr[1] + pr[2] * pr[2] + pr[3] * pr[3]);
+      if (NEQ >= 8 && p.mhd) e5 = e5 + 0.5f * (pr[5] * pr[5] + pr[6] * pr[6] + pr[7] * pr[7]);
+      u[4 * p.fs + c] = make_float2(e5, 0.f);
+    } else {
+      u[4 * p.fs + c] = Ops<PolKahan>::addf(u[4 * p.fs + c], eth1 - p.f_cv * pr[4]);
+    }
+  } else {
+    u[ND * p.fs + c] = (double)nhi1;
+    if (clamped) {
+      float e5 = eth1 + 0.5f * rho * (pr[1] * pr[1] + pr[2] * pr[2] + pr[3] * pr[3]);
+      if (NEQ >= 8 && p.mhd) e5 = e5 + 0.5f * (pr[5] * pr[5] + pr[6] * pr[6] + pr[7] * pr[7]);
+      u[4 * p.fs + c] = (double)e5;
+    } else {
+      u[4 * p.fs + c] = u[4 * p.fs + c] + (double)(eth1 - p.f_cv * pr[4]);
+    }
+  }
+}
 
 template <class Pol, int NEQ>
 __global__ void k_cool_h(KParams p, typename Pol::TU* u, const StepScalars* sc) {
@@ -1143,6 +1232,10 @@ __global__ void k_cool_h(KParams p, typename Pol::TU* u, const StepScalars* sc) 
   const int ck = blockIdx.z;
   if (ci >= p.nx || cj >= p.ny || !sc->active) return;
   const long long c = cell_index(p, ci + NG, cj + NG, ck + NG);
+  if constexpr (!std::is_same<Pol, PolFP64>::value) {
+    cool_h_f32<Pol, NEQ>(p, u, sc, c);
+    return;
+  }
   // :259-371 atomic, without diffuse radiation (radphi = 1, tprime = 10 K)
   const double dt = sc->dt * p.tsc;
   const double xi = 1.e-4, boltzm = 1.3807e-16;
