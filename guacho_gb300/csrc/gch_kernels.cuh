@@ -1289,6 +1289,31 @@ __global__ void k_visc(KParams p, typename Pol::TU* u, const typename Pol::TU* w
     return inside ? to_d(w[q * p.fs + c]) : to_d(up[q * p.fs + c]);
   };
   const long long c = cell_index(p, ax, ay, az);
+  if constexpr (!std::is_same<Pol, PolFP64>::value) {
+    // FP32 paths: eta times the FP32 Laplacian, added to the cell's FP64 or
+    // compensated w (neighbours outside the interior are up's ghosts)
+    auto valf = [&](int q, int x, int y, int z) -> float {
+      const bool inside = x >= NG && x < NG + p.nx && y >= NG && y < NG + p.ny && z >= NG &&
+                          z < NG + p.nz;
+      const long long cc = cell_index(p, x, y, z);
+      if (!inside) return (float)up[q * p.fs + cc];
+      if constexpr (std::is_same<Pol, PolKahan>::value) return w[q * p.fs + cc].x;
+      else return (float)w[q * p.fs + cc];
+    };
+    const float eta = (float)p.eta;
+    for (int q = 0; q < NEQ; ++q) {
+      const auto wc = w[q * p.fs + c];
+      const float v = valf(q, ax, ay, az);
+      const float lap = valf(q, ax + 1, ay, az) + valf(q, ax - 1, ay, az) +
+                        valf(q, ax, ay + 1, az) + valf(q, ax, ay - 1, az) +
+                        valf(q, ax, ay, az + 1) + valf(q, ax, ay, az - 1) - 6.0f * v;
+      if constexpr (std::is_same<Pol, PolKahan>::value)
+        u[q * p.fs + c] = Ops<PolKahan>::addf(wc, eta * lap);
+      else
+        u[q * p.fs + c] = wc + (double)(eta * lap);
+    }
+    return;
+  }
   for (int q = 0; q < NEQ; ++q) {
     const double v = val(q, ax, ay, az);
     u[q * p.fs + c] = from_d<typename Pol::TU>(
