@@ -350,9 +350,14 @@ int gch_create(const gch_params_t* p, void* stream, gch_domain_t** out) {
       g[2 * k.ngrav + l] = p->grav_y[l];
       g[3 * k.ngrav + l] = p->grav_z[l];
     }
-    e = cudaMalloc((void**)&d->grav, 4 * k.ngrav * sizeof(double));
+    float gf[4 * GCH_MAX_GRAV];
+    for (int i = 0; i < 4 * k.ngrav; ++i) gf[i] = (float)g[i];
+    e = cudaMalloc((void**)&d->grav, 4 * k.ngrav * (sizeof(double) + sizeof(float)));
     if (e == cudaSuccess) e = cudaMemcpy(d->grav, g, 4 * k.ngrav * sizeof(double), cudaMemcpyHostToDevice);
+    float* gfd = reinterpret_cast<float*>(d->grav + 4 * k.ngrav);
+    if (e == cudaSuccess) e = cudaMemcpy(gfd, gf, 4 * k.ngrav * sizeof(float), cudaMemcpyHostToDevice);
     k.grav = d->grav;
+    k.gravf = gfd;
   }
   if (e == cudaSuccess) e = cudaMallocHost((void**)&d->sc_host, sizeof(StepScalars));
   if (e == cudaSuccess) {

@@ -133,6 +133,7 @@ struct KParams {
   int nsph, ngrav;
   const gch_sphere_t* sph;
   const double* grav;         // [4][ngrav]: GM, x, y, z
+  const float* gravf;         // the same in FP32 (the FP32 paths)
 };
 
 // Scalars shared by the kernels of one step, resident in device memory so a

@@ -28,6 +28,14 @@ __device__ __forceinline__ void raise_err(int* errp, int bits) {
   if (bits) atomicOr(errp, bits);
 }
 
+// u + dt * s for a source term s: FP64 on the FP64 and FP64-u paths; on the
+// pair path the FP32 product dt*s is added to the pair (no FP64 instruction)
+template <class Pol, class R, class T>
+__device__ __forceinline__ R add_source(R u, double dt, float dtf, T s) {
+  if constexpr (std::is_same<Pol, PolKahan>::value) return Ops<PolKahan>::addf(u, dtf * s);
+  else return Ops<Pol>::add(u, dt * (double)s);
+}
+
 // ---------------------------------------------------------------------------
 // Per-cell prim load from the stage source.
 template <class Pol, int NEQ, int STAGE, bool PRIM_IN>
@@ -188,6 +196,7 @@ flux_body(const KParams& p, const typename Src<Pol, NEQ, STAGE, PRIM_IN>::TIn* _
   const int lim = p.limiter;
 
   const double dt = STAGE == 1 ? sc->dt / 2.0 : sc->dt;  // dtm = dt_CFL/2.
+  const float dtf = (float)dt;
   const TC dtdx = par<TC>(sc->dtd[STAGE - 1][0], sc->dtdf[STAGE - 1][0]);
   const TC dtdy = par<TC>(sc->dtd[STAGE - 1][1], sc->dtdf[STAGE - 1][1]);
   const TC dtdz = par<TC>(sc->dtd[STAGE - 1][2], sc->dtdf[STAGE - 1][2]);
@@ -444,7 +453,25 @@ flux_body(const KParams& p, const typename Src<Pol, NEQ, STAGE, PRIM_IN>::TIn* _
 #pragma unroll
         for (int q = 0; q < NEQ; ++q) pcen[q] = sP[q][ty + H][tx + H];
         // src/sources.f90:190-220 with the cell's stage primitives
-        if (p.user_src) {
+        if (p.user_src && sizeof(TC) == 4) {
+          // EXO/user_mod.f90:158-206 point masses, FP32 paths: positions,
+          // the FP32 copy of the masses and r^3 as r^2 sqrt(r^2)
+          const float xc = ((float)(ci + 1 - p.nx / 2) - 0.5f) * p.f_dx;
+          const float yc = ((float)(cj + 1 - p.ny / 2) - 0.5f) * p.f_dy;
+          const float zc = ((float)(k + 1 - p.nz / 2) - 0.5f) * p.f_dz;
+          for (int l = 0; l < p.ngrav; ++l) {
+            const float x = xc - p.gravf[p.ngrav + l];
+            const float y = yc - p.gravf[2 * p.ngrav + l];
+            const float z = zc - p.gravf[3 * p.ngrav + l];
+            const float GM = p.gravf[l];
+            const float rad2 = x * x + y * y + z * z;
+            const float r15 = rad2 * sqrtf(rad2);
+            sv[1] = sv[1] - pcen[0] * GM * x / r15;
+            sv[2] = sv[2] - pcen[0] * GM * y / r15;
+            sv[3] = sv[3] - pcen[0] * GM * z / r15;
+            sv[4] = sv[4] - pcen[0] * GM * (pcen[1] * x + pcen[2] * y + pcen[3] * z) / r15;
+          }
+        } else if (p.user_src) {
           // EXO/user_mod.f90:158-206 point masses
           const double xc = ((double)(ci + 1 - p.nx / 2) - 0.5) * p.dx;
           const double yc = ((double)(cj + 1 - p.ny / 2) - 0.5) * p.dy;
@@ -465,9 +492,12 @@ flux_body(const KParams& p, const typename Src<Pol, NEQ, STAGE, PRIM_IN>::TIn* _
         if (NEQ >= 8 && p.eight_wave) {
           // src/sources.f90:124-175
           const TC bzp = sQ[0][7][ty][tx];
-          const TC divB = (sP[5][ty + H][tx + H + 1] - sP[5][ty + H][tx + H - 1]) / (TC)(2.0 * p.dx)
-                          + (sP[6][ty + H + 1][tx + H] - sP[6][ty + H - 1][tx + H]) / (TC)(2.0 * p.dy)
-                          + (bzp - bzm) / (TC)(2.0 * p.dz);
+          // 2 dx in the compute type (doubling is exact in either type)
+          const TC dx2 = TC(2) * par<TC>(p.dx, p.f_dx), dy2 = TC(2) * par<TC>(p.dy, p.f_dy),
+                   dz2 = TC(2) * par<TC>(p.dz, p.f_dz);
+          const TC divB = (sP[5][ty + H][tx + H + 1] - sP[5][ty + H][tx + H - 1]) / dx2
+                          + (sP[6][ty + H + 1][tx + H] - sP[6][ty + H - 1][tx + H]) / dy2
+                          + (bzp - bzm) / dz2;
           sv[1] = sv[1] - divB * pcen[5];
           sv[2] = sv[2] - divB * pcen[6];
           sv[3] = sv[3] - divB * pcen[7];
@@ -483,7 +513,7 @@ flux_body(const KParams& p, const typename Src<Pol, NEQ, STAGE, PRIM_IN>::TIn* _
           auto unew = Ops<Pol>::update(Ops<Pol>::ld(uq[q]), dtdx, dtdy, dtdz,
                                        sF[q][ty][tx], sF[q][ty][tx + 1], sG[q][ty][tx],
                                        sG[q][ty + 1][tx], sH[hp][q][ty][tx], sH[hn][q][ty][tx]);
-          if (src_terms) unew = Ops<Pol>::add(unew, dt * (double)sv[q]);
+          if (src_terms) unew = add_source<Pol>(unew, dt, dtf, sv[q]);
           dst[q * p.fs + c] = store_as<TD>(unew);
         }
       }
@@ -620,6 +650,7 @@ ct_body(const KParams& p, const typename Pol::TU* u,
   if (!active) return;
   const int ax = ci + NG, ay = cj + NG;
   const double dt = STAGE == 1 ? sc->dt / 2.0 : sc->dt;
+  const float dtf = (float)dt;
   const TC hx = par<TC>(0.5 * sc->dtd[STAGE - 1][0], sc->hdtdf[STAGE - 1][0]);
   const TC hy = par<TC>(0.5 * sc->dtd[STAGE - 1][1], sc->hdtdf[STAGE - 1][1]);
   const TC hz = par<TC>(0.5 * sc->dtd[STAGE - 1][2], sc->hdtdf[STAGE - 1][2]);
@@ -691,9 +722,9 @@ ct_body(const KParams& p, const typename Pol::TU* u,
     auto b7 = Ops<Pol>::ct(u7, hx, e3xm, e3xp, hz, e1zm, e1zp, false);
     auto b8 = Ops<Pol>::ct(u8, hx, e2xm, e2xp, hy, e1ym, e1yp, true);
     if (p.eight_wave) {
-      b6 = Ops<Pol>::add(b6, dt * (double)s678[c]);
-      b7 = Ops<Pol>::add(b7, dt * (double)s678[p.fs + c]);
-      b8 = Ops<Pol>::add(b8, dt * (double)s678[2 * p.fs + c]);
+      b6 = add_source<Pol>(b6, dt, dtf, s678[c]);
+      b7 = add_source<Pol>(b7, dt, dtf, s678[p.fs + c]);
+      b8 = add_source<Pol>(b8, dt, dtf, s678[2 * p.fs + c]);
     }
     dst[5 * p.fs + c] = store_as<TD>(b6);
     dst[6 * p.fs + c] = store_as<TD>(b7);
