@@ -88,13 +88,16 @@ extern "C" {
 /* ---- precision modes (no counterpart in the reference) ------------------ */
 /* Plain FP64 drop-in: every value and operation in FP64, no FMA contraction,
  * bitwise equal to the reference's x86-64 FP64 build where all operations
- * are IEEE-exact (everything but cooling's exp/log10). */
+ * are IEEE-exact (everything but the exp/log/pow of cooling and conduction). */
 #define GCH_FP64 0
 /* FP32 state, reconstruction and fluxes; u stored in FP64; FP64 for the
- * pressure recovery in u2prim, the u += dt*divF accumulation, dt and time. */
+ * pressure recovery in u2prim, the u += dt*divF accumulation, dt and time.
+ * Cooling, conduction, viscosity and sources compute in FP32 and add their
+ * change of u in FP64. */
 #define GCH_FP32_MIXED 1
 /* As GCH_FP32_MIXED but u stored as a compensated (hi, lo) FP32 pair and
- * accumulated with Kahan-style error-free sums instead of FP64. */
+ * accumulated with Kahan-style error-free sums instead of FP64; no FP64
+ * instruction per cell. */
 #define GCH_FP32_KAHAN 2
 
 /* ---- status bits --------------------------------------------------------- */
