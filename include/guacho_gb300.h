@@ -96,8 +96,8 @@ extern "C" {
  * change of u in FP64. */
 #define GCH_FP32_MIXED 1
 /* As GCH_FP32_MIXED but u stored as a compensated (hi, lo) FP32 pair and
- * accumulated with Kahan-style error-free sums instead of FP64; no FP64
- * instruction per cell. */
+ * accumulated with Kahan-style error-free sums instead of FP64; the stage
+ * kernels run no FP64 instruction per cell. */
 #define GCH_FP32_KAHAN 2
 
 /* ---- status bits --------------------------------------------------------- */
