@@ -118,6 +118,7 @@ def lib() -> C.CDLL:
         "gch_destroy": (I, [P]),
         "gch_upload": (I, [P, P]),
         "gch_download": (I, [P, P, P]),
+        "gch_set_background": (I, [P, P]),
         "gch_boundaryI": (I, [P]),
         "gch_calcprim": (I, [P]),
         "gch_get_timestep": (I, [P, I, I, D, D, DP, IP]),
@@ -151,7 +152,7 @@ def lib() -> C.CDLL:
 
 def exported_symbols() -> list[str]:
     return ["gch_params_default", "gch_params_check", "gch_create", "gch_destroy",
-            "gch_upload", "gch_download", "gch_boundaryI", "gch_calcprim",
+            "gch_upload", "gch_download", "gch_set_background", "gch_boundaryI", "gch_calcprim",
             "gch_get_timestep", "gch_tstep", "gch_tc_info", "gch_step_host", "gch_advance",
             "gch_last_step_info", "gch_launches_per_step", "gch_advance_timed",
             "gch_profile_step", "gch_get_kz", "gch_set_kz", "gch_autotune",

@@ -68,11 +68,24 @@ def bin_path(outputpath: str | os.PathLike, itprint: int, rank: int = 0,
     return Path(outputpath) / "BIN" / f"{base}{rank:03d}.{itprint:03d}.bin"
 
 
-def write_bin(path, u: np.ndarray, p: Params, scal=(1.0, 1.0, 1.0)) -> None:
+def write_bin(path, u: np.ndarray, p: Params, scal=(1.0, 1.0, 1.0),
+              prim0: np.ndarray | None = None) -> None:
     """u in the host layout (nz+4, ny+4, nx+4, neq) float64: its bytes are
-    the Fortran u(neq, nxmin:nxmax, ...) in column-major order."""
+    the Fortran u(neq, nxmin:nxmax, ...) in column-major order.  With the
+    split solver's background prim0 the file holds the total state, as
+    src/Out_BIN_Module.f90:144-158 writes it: rho + rho0, the momenta,
+    E + cv p0 + B0^2/2 and B + B0."""
     u = np.ascontiguousarray(u, dtype="<f8")
     assert u.shape == p.shape
+    if prim0 is not None:
+        q = np.asarray(prim0, dtype=np.float64)
+        assert q.shape == p.shape
+        u = u.copy()
+        u[..., 0] = u[..., 0] + q[..., 0]
+        u[..., 4] = (u[..., 4] + p.cv * q[..., 4]
+                     + 0.5 * (q[..., 5] * q[..., 5] + q[..., 6] * q[..., 6] + q[..., 7] * q[..., 7]))
+        for c in (5, 6, 7):
+            u[..., c] = u[..., c] + q[..., c]
     path = Path(path)
     path.parent.mkdir(parents=True, exist_ok=True)
     with open(path, "wb") as f:

@@ -51,6 +51,7 @@ UNITS = {
     # scalars, neither contracted into multiply-adds
     "gch_tc.cu": ["-fmad=false", "-Xcompiler", "-ffp-contract=off"],
     "gch_tc32.cu": ["-use_fast_math"],
+    "gch_split.cu": ["-fmad=false"],
 }
 
 

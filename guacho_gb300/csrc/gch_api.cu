@@ -163,6 +163,14 @@ int gch_params_check(const gch_params_t* p) {
     case GCH_SOLVER_HLL:
       if (p->mhd) return GCH_ERR_PARAM;   // hydro (or passive B) solvers
       break;
+    case GCH_SOLVER_HLLE_SPLIT_ALL:
+      // the split branches of the reference are written for MHD; built on
+      // the FP64 path, without cooling, conduction, passives, sources or
+      // user spheres
+      if (!p->mhd || p->npas != 0 || p->precision != GCH_FP64 || p->cooling != GCH_COOL_NONE ||
+          p->th_cond != GCH_TC_OFF || p->eight_wave || p->user_source_terms || p->bc_user)
+        return GCH_ERR_PARAM;
+      break;
     default:
       return GCH_ERR_PARAM;
   }
@@ -222,6 +230,8 @@ int gch_destroy(gch_domain_t* d) {
   cudaFree(d->E);
   cudaFree(d->s678);
   cudaFree(d->primit);
+  cudaFree(d->prim0);
+  cudaFree(d->split_f);
   cudaFree(d->tab);
   cudaFree(d->sph);
   cudaFree(d->grav);
@@ -314,6 +324,11 @@ int gch_create(const gch_params_t* p, void* stream, gch_domain_t** out) {
   d->ncell_host = (size_t)k.NX * k.NY * k.NZ;
   alloc((void**)&d->stage, d->ncell_host * k.neq * sizeof(double));
   alloc((void**)&d->sc, sizeof(StepScalars));
+  if (p->riemann_solver == GCH_SOLVER_HLLE_SPLIT_ALL) {
+    alloc((void**)&d->prim0, fs * k.neq * sizeof(double));
+    alloc(&d->primit, fs * k.neq * sizeof(double));
+    alloc((void**)&d->split_f, fs * 3 * k.neq * sizeof(double));
+  }
   if (p->th_cond != GCH_TC_OFF) {
     alloc((void**)&d->tcw, fs * 6 * sizeof(double));
     alloc((void**)&d->tc_min, sizeof(unsigned long long));
@@ -384,6 +399,15 @@ int gch_upload(gch_domain_t* d, const double* u) {
   int st = GCH_OK;
   const double* src = host_in(d, u, st);
   st |= engine(d).upload(d, src);
+  st |= cuda_ok(cudaStreamSynchronize(d->stream));
+  return st;
+}
+
+int gch_set_background(gch_domain_t* d, const double* primit0) {
+  if (!d || !primit0 || !d->prim0) return GCH_ERR_PARAM;
+  int st = GCH_OK;
+  const double* src = host_in(d, primit0, st);
+  st |= gch::split_set_background(d, src);
   st |= cuda_ok(cudaStreamSynchronize(d->stream));
   return st;
 }

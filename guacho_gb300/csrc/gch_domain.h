@@ -22,7 +22,9 @@ struct gch_domain {
   void* w = nullptr;            // neq fields, TU (stage-2 result when eta != 0)
   void* E = nullptr;            // 3 fields, TS
   void* s678 = nullptr;         // 3 fields, TS (eight-wave sources)
-  void* primit = nullptr;       // neq fields, TS (tabulated cooling)
+  void* primit = nullptr;       // neq fields, TS (tabulated cooling; FP64 with the split solver)
+  double* prim0 = nullptr;      // split solver: the background primit0, neq fields
+  double* split_f = nullptr;    // split solver: x, y, z face fluxes, 3 x neq fields
   double* tab = nullptr;        // [2][ntab]
   gch_sphere_t* sph = nullptr;
   double* grav = nullptr;       // [4][ngrav]
@@ -93,6 +95,12 @@ extern const GroupOps kGroupKahan;
 
 // Thermal conduction after a tstep of dt_CFL (gch_tc.cu): synchronises once.
 int tc_run(gch_domain* d, double dt_CFL);
+// the split solver SOLVER_HLLE_SPLIT_ALL on the FP64 path (gch_split.cu)
+int split_calcprim(gch_domain* d);
+int split_get_dt(gch_domain* d);
+int split_tstep(gch_domain* d);
+int split_set_background(gch_domain* d, const double* aos);
+int split_download_prim(gch_domain* d, double* aos);
 int tc_run_kahan(gch_domain* d, double dt_CFL);  // the FP32 paths (gch_tc32.cu)
 int tc_run_mixed(gch_domain* d, double dt_CFL);
 // The super-time-stepping scalars of src/thermal_cond.f90:625-681.

@@ -108,6 +108,8 @@ struct Engine {
   // the CFL min over the interior (k_cfl), then dt from it (k_dtfin)
   static int get_dt(gch_domain* d) {
     const KParams& p = d->kp;
+    if constexpr (std::is_same<Pol, PolFP64>::value)
+      if (p.solver == GCH_SOLVER_HLLE_SPLIT_ALL) return split_get_dt(d);
     dim3 cgrid = column_grid(p), block(32, 8);
     if (d->prim_in) {
       with_neq(p.neq, [&](auto N) {
@@ -127,6 +129,8 @@ struct Engine {
   // ---- tstep (src/hydro_solver.f90:134-229) ---------------------------------
   static int tstep(gch_domain* d) {
     const KParams& p = d->kp;
+    if constexpr (std::is_same<Pol, PolFP64>::value)
+      if (p.solver == GCH_SOLVER_HLLE_SPLIT_ALL) return split_tstep(d);
     int st = GCH_OK;
     d->launches = 0;
     const bool ct = p.neq >= 8 && p.flux_cd;
@@ -201,6 +205,8 @@ struct Engine {
   }
 
   static int calcprim(gch_domain* d) {
+    if constexpr (std::is_same<Pol, PolFP64>::value)
+      if (d->kp.solver == GCH_SOLVER_HLLE_SPLIT_ALL) return split_calcprim(d);
     if (!d->prim_in) return GCH_OK;  // primitives are formed on the fly
     const KParams& p = d->kp;
     dim3 g((p.NX + 31) / 32, (p.NY + 7) / 8, p.NZ), b(32, 8);
@@ -223,6 +229,8 @@ struct Engine {
   }
   static int download_prim(gch_domain* d, double* aos) {
     const KParams& p = d->kp;
+    if constexpr (std::is_same<Pol, PolFP64>::value)
+      if (p.solver == GCH_SOLVER_HLLE_SPLIT_ALL) return split_download_prim(d, aos);
     if (d->prim_in) {
       k_soa_to_aos<TS><<<kLayoutGrid, kLayoutCells, 0, d->stream>>>(p, (const TS*)d->primit, aos, p.neq);
     } else {

@@ -175,6 +175,8 @@ extern "C" int gch_get_timestep_noalloc(const gch_params_t* p, const double* u_d
   if (p->cooling != GCH_COOL_NONE) return GCH_ERR_PARAM;
   // the one-cell state of the kernel holds the 8 dynamical equations only
   if (p->npas != 0) return GCH_ERR_PARAM;
+  // the split solver's timestep needs the background state of a domain
+  if (p->riemann_solver == GCH_SOLVER_HLLE_SPLIT_ALL) return GCH_ERR_PARAM;
   const long long gx = (p->nx + 31) / 32, gy = (p->ny + 7) / 8, gz = (p->nz + 7) / 8;
   if (gx * gy * gz > kNoAllocMaxBlocks || gy > 65535 || gz > 65535) return GCH_ERR_TOO_LARGE;
   unsigned long long* scratch = nullptr;

@@ -15,6 +15,7 @@ import numpy as np
 
 from . import _abi
 from ._abi import check, ptr
+from . import params as P
 from .params import Params
 
 
@@ -67,6 +68,15 @@ class Domain:
         check("gch_download", self._lib.gch_download(self._h, ptr(u),
                                                       ptr(pr) if pr is not None else None))
         return (u, pr) if with_primit else u
+
+    def set_background(self, prim0: np.ndarray) -> None:
+        """The background primit0 of SOLVER_HLLE_SPLIT_ALL (layout of u);
+        call before init, as the reference's background is part of the
+        initial state."""
+        prim0 = np.ascontiguousarray(prim0, dtype=np.float64)
+        assert prim0.shape == self.params.shape, (prim0.shape, self.params.shape)
+        check("gch_set_background", self._lib.gch_set_background(self._h, ptr(prim0)))
+        self._prim0 = prim0.copy()  # for the BIN output of the total state
 
     # ---- reference entry points ----------------------------------------
     def boundaryI(self) -> None:
@@ -136,7 +146,9 @@ class Domain:
         write BIN/points000.<itprint>.bin (+ the div B dump when MHD)."""
         from . import binio
         u = self.download()
-        binio.write_bin(binio.bin_path(outputpath, itprint), u, self.params, scal)
+        split = self.params.riemann_solver == P.SOLVER_HLLE_SPLIT_ALL
+        prim0 = getattr(self, "_prim0", np.zeros(self.params.shape)) if split else None
+        binio.write_bin(binio.bin_path(outputpath, itprint), u, self.params, scal, prim0=prim0)
         if dump_divb and self.params.bfield:
             binio.write_divb(binio.bin_path(outputpath, itprint, base="divB-"), u,
                              self.params, scal)

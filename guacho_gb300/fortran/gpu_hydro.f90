@@ -69,6 +69,11 @@ module gpu_hydro
       type(c_ptr), value :: dom
       real(c_double), intent(out) :: u(*), primit(*)
     end function
+    integer(c_int) function gch_set_background(dom, primit0) bind(C, name="gch_set_background")
+      import :: c_int, c_ptr, c_double
+      type(c_ptr), value :: dom
+      real(c_double), intent(in) :: primit0(*)
+    end function
     integer(c_int) function gch_boundaryI(dom) bind(C, name="gch_boundaryI")
       import :: c_int, c_ptr
       type(c_ptr), value :: dom

@@ -12,6 +12,7 @@ from dataclasses import dataclass, field
 
 # src/constants.f90:56-98
 SOLVER_HLL, SOLVER_HLLC, SOLVER_HLLE, SOLVER_HLLD = 1, 2, 3, 4
+SOLVER_HLLE_SPLIT_ALL = 7  # src/constants.f90:62, fluctuations over a background
 EOS_ADIABATIC, EOS_SINGLE_SPECIE, EOS_H_RATE = 1, 2, 3
 COOL_NONE, COOL_H, COOL_DMC, COOL_CHI = 0, 1, 3, 4
 TC_OFF, TC_ISOTROPIC, TC_ANISOTROPIC = 0, 1, 2

@@ -57,6 +57,10 @@ extern "C" {
 #define GCH_SOLVER_HLLC 2
 #define GCH_SOLVER_HLLE 3
 #define GCH_SOLVER_HLLD 4
+/* HLLE with every variable split into a background and a fluctuation
+ * (src/hlle_split_all.f90); MHD on the FP64 path, background set with
+ * gch_set_background */
+#define GCH_SOLVER_HLLE_SPLIT_ALL 7
 
 #define GCH_EOS_ADIABATIC 1
 #define GCH_EOS_SINGLE_SPECIE 2
@@ -207,6 +211,13 @@ int gch_destroy(gch_domain_t* d);
  * gch_download also writes primit (same layout) when primit != NULL. */
 int gch_upload(gch_domain_t* d, const double* u);
 int gch_download(gch_domain_t* d, double* u, double* primit);
+
+/* The background state of GCH_SOLVER_HLLE_SPLIT_ALL, primit0 of
+ * src/globals.f90:42, in the layout of primit (u and primit then hold the
+ * fluctuation).  The reference allocates primit0 but never sets it; here it
+ * is zero until this call.  Call it before gch_calcprim, as the background is
+ * part of the initial state.  GCH_ERR_PARAM for the other solvers. */
+int gch_set_background(gch_domain_t* d, const double* primit0);
 
 /* src/boundaries.f90:44 boundaryI: one ghost layer of u, then the user
  * boundary spheres. */

@@ -40,6 +40,7 @@ struct gor_state {
   int NX, NY, NZ;     /* with ghosts */
   size_t ncell;
   double *u, *up, *primit, *f, *g, *h, *e;
+  double* primit0;    /* split solver background (src/globals.f90:42), else NULL */
   double* temp;       /* Temp (src/globals.f90), filled by calcprim */
   double time;
   int err;
@@ -483,6 +484,120 @@ static void prim2fhll_common(const gor_params_t* p, const double* pl, const doub
     ff[q] = (sr * fL[q] - sl * fR[q] + sl * sr * (uR[q] - uL[q])) / (sr - sl);
 }
 
+/* ---------------------------------------------------------------------- */
+/* The split solver (SOLVER_HLLE_SPLIT_ALL): primitives are fluctuations over
+ * a background state prim0, with the reference's expressions. */
+static inline int split_all(const gor_params_t* p) {
+  return p->riemann_solver == GOR_SOLVER_HLLE_SPLIT_ALL;
+}
+
+/* src/hydro_core.f90:143-229 u2primSplitAll (no density or pressure floor) */
+static void u2prim_split(const gor_params_t* p, const double* uu, const double* p0,
+                         double* prim, double* T) {
+  prim[0] = uu[0];
+  double r = prim[0] + p0[0];
+  prim[1] = uu[1] / r;
+  prim[2] = uu[2] / r;
+  prim[3] = uu[3] / r;
+  if (bfield(p) && (p->mhd || p->pmhd)) {
+    prim[5] = uu[5];
+    prim[6] = uu[6];
+    prim[7] = uu[7];
+  }
+  if (p->mhd) {
+    prim[4] = (uu[4] - 0.5 * r * (prim[1] * prim[1] + prim[2] * prim[2] + prim[3] * prim[3])
+               - 0.5 * (uu[5] * uu[5] + uu[6] * uu[6] + uu[7] * uu[7])
+               - p0[5] * uu[5] - p0[6] * uu[6] - p0[7] * uu[7]) / p->cv;
+  } else {
+    prim[4] = (uu[4] - 0.5 * r * (prim[1] * prim[1] + prim[2] * prim[2] + prim[3] * prim[3]))
+              / p->cv;
+  }
+  const int nd = neqdyn(p);
+  for (int q = nd; q < p->neq; ++q) prim[q] = uu[q];
+  double t = 0.0;
+  if (p->eq_of_state == GOR_EOS_ADIABATIC) t = ((prim[4] + p0[4]) / r) * p->Tempsc;
+  if (p->eq_of_state == GOR_EOS_SINGLE_SPECIE) {
+    r = dmax(r, 1e-15);
+    t = dmax(1.0, ((prim[4] + p0[4]) / r) * p->Tempsc);
+  }
+  if (p->eq_of_state == GOR_EOS_H_RATE && p->npas > 0) {
+    double dentot = (2.0 * r - prim[nd] - p0[nd]);
+    dentot = dmax(dentot, 1e-15);
+    t = dmax(1.0, ((prim[4] + p0[4]) / dentot) * p->Tempsc);
+  }
+  if (T) *T = t;
+}
+
+/* src/hydro_core.f90:331-383 prim2u with prim0 (split branch) */
+static void prim2u_split(const gor_params_t* p, const double* prim, const double* p0,
+                         double* uu) {
+  uu[0] = prim[0];
+  uu[1] = prim[1] * (prim[0] + p0[0]);
+  uu[2] = prim[2] * (prim[0] + p0[0]);
+  uu[3] = prim[3] * (prim[0] + p0[0]);
+  const double v2 = prim[1] * prim[1] + prim[2] * prim[2] + prim[3] * prim[3];
+  uu[4] = 0.5 * prim[0] * v2 + p->cv * prim[4];
+  if (bfield(p) && p->mhd)
+    uu[4] = uu[4] + 0.5 * (prim[5] * prim[5] + prim[6] * prim[6] + prim[7] * prim[7])
+            + 0.5 * p0[0] * v2 + p0[5] * prim[5] + p0[6] * prim[6] + p0[7] * prim[7];
+  if (bfield(p) && (p->mhd || p->pmhd)) {
+    uu[5] = prim[5];
+    uu[6] = prim[6];
+    uu[7] = prim[7];
+  }
+  for (int q = neqdyn(p); q < p->neq; ++q) uu[q] = prim[q];
+}
+
+/* src/hydro_core.f90:395-476 prim2f with prim0 (split branch, MHD) */
+static void prim2f_split(const gor_params_t* p, const double* prim, const double* p0,
+                         double* ff) {
+  const double rt = prim[0] + p0[0];
+  const double b6 = prim[5], b7 = prim[6], b8 = prim[7];
+  const double etot = 0.5 * (rt * (prim[1] * prim[1] + prim[2] * prim[2] + prim[3] * prim[3])
+                             + b6 * b6 + b7 * b7 + b8 * b8)
+                      + p->cv * prim[4] + p0[5] * b6 + p0[6] * b7 + p0[7] * b8;
+  ff[0] = rt * prim[1];
+  ff[1] = rt * prim[1] * prim[1] + prim[4] + 0.5 * (b7 * b7 + b8 * b8 - b6 * b6)
+          - p0[5] * b6 + p0[6] * b7 + p0[7] * b8;
+  ff[2] = rt * prim[1] * prim[2] - b6 * b7 - p0[6] * b6 - p0[5] * b7;
+  ff[3] = rt * prim[1] * prim[3] - b6 * b8 - p0[7] * b6 - p0[5] * b8;
+  const double t6 = b6 + p0[5], t7 = b7 + p0[6], t8 = b8 + p0[7];
+  ff[4] = prim[1] * (etot + prim[4] + 0.5 * (t6 * t6 + t7 * t7 + t8 * t8) + p->cv * p0[4]
+                     + p0[4] + 0.5 * (p0[5] * p0[5] + p0[6] * p0[6] + p0[7] * p0[7]))
+          - t6 * (prim[1] * t6 + prim[2] * t7 + prim[3] * t8);
+  ff[5] = 0.0;
+  ff[6] = prim[1] * (p0[6] + b7) - prim[2] * (p0[5] + b6);
+  ff[7] = prim[1] * (p0[7] + b8) - prim[3] * (p0[5] + b6);
+  for (int q = neqdyn(p); q < p->neq; ++q) ff[q] = prim[q] * prim[1];
+}
+
+/* src/hlle_split_all.f90:51-84 prim2fhlleSplitAll */
+static void prim2fhlle_split(const gor_params_t* p, const double* pl, const double* pr,
+                             const double* p0l, const double* p0r, double* ff) {
+  double tl[GOR_MAX_NEQ], tr[GOR_MAX_NEQ];
+  for (int q = 0; q < p->neq; ++q) {
+    tl[q] = pl[q] + p0l[q];
+    tr[q] = pr[q] + p0r[q];
+  }
+  const double csl = cfastX(p, tl), csr = cfastX(p, tr);
+  const double sr = dmax(pl[1] + p0l[1] + csl, pr[1] + p0r[1] + csr);
+  const double sl = dmin(pl[1] + p0l[1] - csl, pr[1] + p0r[1] - csr);
+  if (sl > 0) { prim2f_split(p, pl, p0l, ff); return; }
+  if (sr < 0) { prim2f_split(p, pr, p0r, ff); return; }
+  double fL[GOR_MAX_NEQ], fR[GOR_MAX_NEQ], uL[GOR_MAX_NEQ], uR[GOR_MAX_NEQ];
+  prim2f_split(p, pl, p0l, fL);
+  prim2f_split(p, pr, p0r, fR);
+  prim2u_split(p, pl, p0l, uL);
+  prim2u_split(p, pr, p0r, uR);
+  for (int q = 0; q < p->neq; ++q)
+    ff[q] = (sr * fL[q] - sl * fR[q] + sl * sr * (uR[q] - uL[q])) / (sr - sl);
+}
+
+void gor_riemann_split(const gor_params_t* p, const double* priml, const double* primr,
+                       const double* prim0l, const double* prim0r, double* ff) {
+  prim2fhlle_split(p, priml, primr, prim0l, prim0r, ff);
+}
+
 static void riemann(const gor_params_t* p, const double* pl, const double* pr, double* ff,
                     int* err) {
   switch (p->riemann_solver) {
@@ -497,8 +612,60 @@ static void riemann(const gor_params_t* p, const double* pl, const double* pr, d
 /* src/hlld.f90:331-432 (hlldfluxes) and its twins hllc.f90:152-253,
  * hlle.f90:95-196, hll.f90:93-194: fluxes at i+1/2, j+1/2, k+1/2 for
  * i,j,k in [0,n]. */
+/* src/hlle_split_all.f90:96-241 hllEfluxesSplitAll: the fluctuations and the
+ * background are read (and, in stage 2, limited) the same way, and solved
+ * together; the faces of i, j, k in [0, n]. */
+static void fluxes_split(gor_state_t* s, int choice) {
+  const gor_params_t* p = &s->p;
+  const int neq = p->neq, nx = p->nx, ny = p->ny, nz = p->nz;
+  const double* P = s->primit;
+  const double* P0 = s->primit0;
+#pragma omp parallel for schedule(static)
+  for (int k = 0; k <= nz; ++k) {
+    double pl[GOR_MAX_NEQ], pr[GOR_MAX_NEQ], pll[GOR_MAX_NEQ], prr[GOR_MAX_NEQ];
+    double ql[GOR_MAX_NEQ], qr[GOR_MAX_NEQ], qll[GOR_MAX_NEQ], qrr[GOR_MAX_NEQ];
+    double ff[GOR_MAX_NEQ];
+    for (int j = 0; j <= ny; ++j) {
+      for (int i = 0; i <= nx; ++i) {
+        for (int dir = 0; dir < 3; ++dir) {
+          const int di = dir == 0, dj = dir == 1, dk = dir == 2;
+          for (int q = 1; q <= neq; ++q) {
+            pl[q - 1] = AT(s, P, q, i, j, k);
+            pr[q - 1] = AT(s, P, q, i + di, j + dj, k + dk);
+            ql[q - 1] = AT(s, P0, q, i, j, k);
+            qr[q - 1] = AT(s, P0, q, i + di, j + dj, k + dk);
+            if (choice == 2) {
+              pll[q - 1] = AT(s, P, q, i - di, j - dj, k - dk);
+              prr[q - 1] = AT(s, P, q, i + 2 * di, j + 2 * dj, k + 2 * dk);
+              qll[q - 1] = AT(s, P0, q, i - di, j - dj, k - dk);
+              qrr[q - 1] = AT(s, P0, q, i + 2 * di, j + 2 * dj, k + 2 * dk);
+            }
+          }
+          void (*swap)(const gor_params_t*, double*) = dir == 1 ? swapy : swapz;
+          if (dir != 0) {
+            swap(p, pl); swap(p, pr); swap(p, ql); swap(p, qr);
+            if (choice == 2) { swap(p, pll); swap(p, prr); swap(p, qll); swap(p, qrr); }
+          }
+          if (choice == 2) {
+            limiter(p, pll, pl, pr, prr);
+            limiter(p, qll, ql, qr, qrr);
+          }
+          prim2fhlle_split(p, pl, pr, ql, qr, ff);
+          if (dir != 0) swap(p, ff);
+          double* out = dir == 0 ? s->f : (dir == 1 ? s->g : s->h);
+          for (int q = 1; q <= neq; ++q) AT(s, out, q, i, j, k) = ff[q - 1];
+        }
+      }
+    }
+  }
+}
+
 static void fluxes(gor_state_t* s, int choice) {
   const gor_params_t* p = &s->p;
+  if (split_all(p)) {
+    fluxes_split(s, choice);
+    return;
+  }
   const int neq = p->neq, nx = p->nx, ny = p->ny, nz = p->nz;
   int err = 0;
 #pragma omp parallel for schedule(static) reduction(| : err)
@@ -903,8 +1070,11 @@ static void boundaryII(gor_state_t* s) { boundary_fill(s, s->up, 2); }
 static void calcprim_arr(gor_state_t* s, const double* uarr, int only_ghost) {
   const gor_params_t* p = &s->p;
   const int neq = p->neq, nx = p->nx, ny = p->ny, nz = p->nz;
-#define CP(i, j, k) \
-  u2prim(p, &uarr[CID(s, i, j, k) * neq], &s->primit[CID(s, i, j, k) * neq], &s->temp[CID(s, i, j, k)])
+#define CP(i, j, k)                                                                          \
+  (split_all(p) ? u2prim_split(p, &uarr[CID(s, i, j, k) * neq], &s->primit0[CID(s, i, j, k) * neq], \
+                               &s->primit[CID(s, i, j, k) * neq], &s->temp[CID(s, i, j, k)])   \
+                : u2prim(p, &uarr[CID(s, i, j, k) * neq], &s->primit[CID(s, i, j, k) * neq],   \
+                         &s->temp[CID(s, i, j, k)]))
   if (only_ghost) {
     for (int j = 0; j <= ny + 1; ++j)
       for (int i = 0; i <= nx + 1; ++i) {
@@ -925,6 +1095,12 @@ static void calcprim_arr(gor_state_t* s, const double* uarr, int only_ghost) {
   }
 #undef CP
   const size_t n = s->ncell;
+  if (split_all(p)) {  /* src/hydro_core.f90:307-309 */
+#pragma omp parallel for schedule(static)
+    for (size_t c = 0; c < n; ++c)
+      u2prim_split(p, &uarr[c * neq], &s->primit0[c * neq], &s->primit[c * neq], &s->temp[c]);
+    return;
+  }
 #pragma omp parallel for schedule(static)
   for (size_t c = 0; c < n; ++c) u2prim(p, &uarr[c * neq], &s->primit[c * neq], &s->temp[c]);
 }
@@ -1090,7 +1266,13 @@ void gor_get_timestep(gor_state_t* s, int iter, int n_iter, double t, double tpr
         const double* pr = &s->primit[CID(s, i, j, k) * neq];
         if (p->mhd) {
           double cx, cy, cz;
-          cfast(p, pr[4], pr[0], pr[5], pr[6], pr[7], &cx, &cy, &cz);
+          if (split_all(p)) {  /* :650-655: the total state's fast speeds */
+            const double* p0 = &s->primit0[CID(s, i, j, k) * neq];
+            cfast(p, pr[4] + p0[4], pr[0] + p0[0], pr[5] + p0[5], pr[6] + p0[6], pr[7] + p0[7],
+                  &cx, &cy, &cz);
+          } else {
+            cfast(p, pr[4], pr[0], pr[5], pr[6], pr[7], &cx, &cy, &cz);
+          }
           dtp = dmin(dtp, p->dx / (fabs(pr[1]) + cx));
           dtp = dmin(dtp, p->dy / (fabs(pr[2]) + cy));
           dtp = dmin(dtp, p->dz / (fabs(pr[3]) + cz));
@@ -1404,7 +1586,9 @@ gor_state_t* gor_create(const gor_params_t* p) {
   s->h = (double*)calloc(nv, sizeof(double));
   s->e = (double*)calloc(s->ncell * 3, sizeof(double));
   s->temp = (double*)calloc(s->ncell, sizeof(double));
-  if (!s->u || !s->up || !s->primit || !s->f || !s->g || !s->h || !s->e || !s->temp) {
+  if (split_all(p)) s->primit0 = (double*)calloc(nv, sizeof(double));
+  if (!s->u || !s->up || !s->primit || !s->f || !s->g || !s->h || !s->e || !s->temp ||
+      (split_all(p) && !s->primit0)) {
     gor_destroy(s);
     return NULL;
   }
@@ -1414,7 +1598,7 @@ gor_state_t* gor_create(const gor_params_t* p) {
 void gor_destroy(gor_state_t* s) {
   if (!s) return;
   free(s->u); free(s->up); free(s->primit);
-  free(s->f); free(s->g); free(s->h); free(s->e); free(s->temp);
+  free(s->f); free(s->g); free(s->h); free(s->e); free(s->temp); free(s->primit0);
   free(s);
 }
 
@@ -1428,6 +1612,9 @@ int gor_nthreads(int n) {
 #endif
 }
 
+void gor_set_background(gor_state_t* s, const double* primit0) {
+  if (s->primit0) memcpy(s->primit0, primit0, s->ncell * s->p.neq * sizeof(double));
+}
 void gor_set_u(gor_state_t* s, const double* u) {
   memcpy(s->u, u, s->ncell * s->p.neq * sizeof(double));
 }

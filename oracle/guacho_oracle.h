@@ -26,6 +26,7 @@ extern "C" {
 /* Switch ids, equal to src/constants.f90:56-98. */
 enum {
   GOR_SOLVER_HLL = 1, GOR_SOLVER_HLLC = 2, GOR_SOLVER_HLLE = 3, GOR_SOLVER_HLLD = 4,
+  GOR_SOLVER_HLLE_SPLIT_ALL = 7,
   GOR_EOS_ADIABATIC = 1, GOR_EOS_SINGLE_SPECIE = 2, GOR_EOS_H_RATE = 3,
   GOR_COOL_NONE = 0, GOR_COOL_H = 1, GOR_COOL_DMC = 3, GOR_COOL_CHI = 4,
   GOR_BC_OUTFLOW = 1, GOR_BC_CLOSED = 2, GOR_BC_PERIODIC = 3, GOR_BC_OTHER = 4,
@@ -107,6 +108,10 @@ void gor_set_u(gor_state_t* s, const double* u);
 void gor_get_u(const gor_state_t* s, double* u);
 void gor_get_primit(const gor_state_t* s, double* primit);
 void gor_set_primit(gor_state_t* s, const double* primit);
+/* The background state primit0 of the split solver (src/globals.f90:42),
+ * same layout as primit.  The reference allocates but never sets it; here it
+ * is zero until set. */
+void gor_set_background(gor_state_t* s, const double* primit0);
 
 /* Reference entry points. */
 void gor_boundaryI(gor_state_t* s);                        /* src/boundaries.f90:44 */
@@ -121,6 +126,10 @@ int gor_error(const gor_state_t* s);
 /* Single-interface kernels (x-direction), for known-answer tests. */
 void gor_riemann(const gor_params_t* p, const double* priml, const double* primr,
                  double* ff, int* err);
+/* src/hlle_split_all.f90:51-84: fluctuations priml/primr over backgrounds
+ * prim0l/prim0r (x-direction) */
+void gor_riemann_split(const gor_params_t* p, const double* priml, const double* primr,
+                       const double* prim0l, const double* prim0r, double* ff);
 void gor_prim2f(const gor_params_t* p, const double* prim, double* ff);
 void gor_u2prim(const gor_params_t* p, const double* uu, double* prim, double* T);
 void gor_prim2u(const gor_params_t* p, const double* prim, double* uu);

@@ -116,6 +116,8 @@ def lib() -> C.CDLL:
             "gor_create": (P, [GP]), "gor_destroy": (None, [P]), "gor_nthreads": (I, [I]),
             "gor_set_u": (None, [P, P]), "gor_get_u": (None, [P, P]),
             "gor_get_primit": (None, [P, P]), "gor_set_primit": (None, [P, P]),
+            "gor_set_background": (None, [P, P]),
+            "gor_riemann_split": (None, [GP, P, P, P, P, P]),
             "gor_boundaryI": (None, [P]), "gor_calcprim": (None, [P, I]),
             "gor_get_timestep": (None, [P, I, I, D, D, DP, IP]),
             "gor_tstep": (None, [P, D]), "gor_time": (D, [P]), "gor_set_time": (None, [P, D]),
@@ -180,6 +182,12 @@ class Oracle:
         u = np.ascontiguousarray(u, dtype=np.float64)
         assert u.shape == self.params.shape
         self.L.gor_set_u(self.h, _p(u))
+
+    def set_background(self, prim0: np.ndarray):
+        """The split solver's background primit0 (same layout as u)."""
+        prim0 = np.ascontiguousarray(prim0, dtype=np.float64)
+        assert prim0.shape == self.params.shape
+        self.L.gor_set_background(self.h, _p(prim0))
 
     def download(self, with_primit: bool = False):
         u = np.empty(self.params.shape)
@@ -248,6 +256,17 @@ def riemann(params, pl, pr):
     err = C.c_int(0)
     lib().gor_riemann(C.byref(ps), _p(pl), _p(pr), _p(ff), C.byref(err))
     return ff[:params.neq], err.value
+
+
+def riemann_split(params, pl, pr, p0l, p0r):
+    """src/hlle_split_all.f90:51-84 for one x-interface."""
+    ps = params_struct(params)
+    a = [np.ascontiguousarray(np.pad(np.asarray(v, dtype=np.float64),
+                                     (0, MAXNEQ - len(v))), dtype=np.float64)
+         for v in (pl, pr, p0l, p0r)]
+    ff = np.zeros(MAXNEQ)
+    lib().gor_riemann_split(C.byref(ps), *[_p(v) for v in a], _p(ff))
+    return ff[:params.neq]
 
 
 def prim2f(params, prim):

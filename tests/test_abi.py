@@ -70,10 +70,19 @@ def test_params_check_accepts_configs(gpu_lib, make):
     dict(cooling=2),                               # COOL_BBC is not on this path
     dict(th_cond=3),
     dict(th_cond=P.TC_ISOTROPIC, rsc=0.0),          # conduction needs the cgs scalings
+    # the split solver: FP64 MHD without sources, cooling or spheres
+    dict(riemann_solver=P.SOLVER_HLLE_SPLIT_ALL, precision=P.FP32_KAHAN),
+    dict(riemann_solver=P.SOLVER_HLLE_SPLIT_ALL, eight_wave=True),
+    dict(riemann_solver=P.SOLVER_HLLE_SPLIT_ALL, mhd=False, pmhd=True),
 ])
 def test_params_check_rejects(gpu_lib, bad):
     p = problems.orszag_tang(16, 16, 4)[0].replace(**bad)
     assert _check(p) == _abi.ERR_PARAM
+
+
+def test_split_all_params(gpu_lib):
+    p = problems.orszag_tang(16, 16, 4, riemann_solver=P.SOLVER_HLLE_SPLIT_ALL)[0]
+    assert _check(p) == 0
 
 
 def test_conduction_params(gpu_lib):
