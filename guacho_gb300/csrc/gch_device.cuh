@@ -13,6 +13,7 @@
 #include <type_traits>
 
 #include "guacho_gb300.h"
+#include "gch_convert.h"
 
 namespace gch {
 
@@ -91,6 +92,9 @@ __host__ __device__ __forceinline__ float2 neg(float2 x) { return make_float2(-x
 // store an accumulator value (double or pair) in a stage array type
 template <class TD>
 __device__ __forceinline__ TD store_as(double v) { return from_d<TD>(v); }
+// FP64 u rounded to an FP32 stage state on the integer pipes (same bits)
+template <>
+__device__ __forceinline__ float store_as<float>(double v) { return d2f_rn(v); }
 template <class TD>
 __device__ __forceinline__ TD store_as(float2 v);
 template <>

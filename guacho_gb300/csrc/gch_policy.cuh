@@ -224,8 +224,9 @@ struct Ops<PolMixed> {
                                                    unsigned& pfl) {
     {
       const double r = tmax_(uu[0], 1e-15);
-      const float irf = 1.0f / (float)r;
-      double ir = (double)irf;
+      const float rf = d2f_rn(r);
+      const float irf = 1.0f / rf;
+      double ir = f2d(irf);
       ir = ir * fma(-r, ir, 2.0);
       const double m2 = fma(uu[3], uu[3], fma(uu[2], uu[2], uu[1] * uu[1]));
       double kb = m2 * ir;
@@ -241,19 +242,18 @@ struct Ops<PolMixed> {
         const double t = tmax_(1.0, (pr / dentot) * p.Tempsc);
         pr = dentot * t / p.Tempsc;
       }
-      const float rf = (float)r;
       prim[0] = rf;
-      prim[1] = (float)uu[1] * irf;
-      prim[2] = (float)uu[2] * irf;
-      prim[3] = (float)uu[3] * irf;
-      prim[4] = (float)pr;
+      prim[1] = d2f_rn(uu[1]) * irf;
+      prim[2] = d2f_rn(uu[2]) * irf;
+      prim[3] = d2f_rn(uu[3]) * irf;
+      prim[4] = d2f_rn(pr);
       if (NEQ >= 8) {
-        prim[5] = (float)uu[5];
-        prim[6] = (float)uu[6];
-        prim[7] = (float)uu[7];
+        prim[5] = d2f_rn(uu[5]);
+        prim[6] = d2f_rn(uu[6]);
+        prim[7] = d2f_rn(uu[7]);
       }
 #pragma unroll
-      for (int q = kNeqDyn<NEQ>; q < NEQ; ++q) prim[q] = (float)uu[q];
+      for (int q = kNeqDyn<NEQ>; q < NEQ; ++q) prim[q] = d2f_rn(uu[q]);
     }
   }
 
@@ -269,13 +269,13 @@ struct Ops<PolMixed> {
                                                   float fl, float fr, float gl, float gr,
                                                   float hl, float hr) {
     const float d = dtdx * (fr - fl) + dtdy * (gr - gl) + dtdz * (hr - hl);
-    return u - (double)d;
+    return u - f2d(d);
   }
 
   __device__ __forceinline__ static double ct(double u, float hdta, float a0, float a1,
                                               float hdtb, float b0, float b1, bool first_minus) {
     const float d = hdta * (a1 - a0) - hdtb * (b1 - b0);
-    return first_minus ? u - (double)d : u + (double)d;
+    return first_minus ? u - f2d(d) : u + f2d(d);
   }
 };
 
