@@ -558,7 +558,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--size", type=int, default=256)
     ap.add_argument("--fp64-steps", type=int, default=4)
-    ap.add_argument("--e2e-steps", type=int, default=10)
+    ap.add_argument("--e2e-steps", type=int, default=30)
     ap.add_argument("--loop-steps", type=int, default=50)
     ap.add_argument("--cpu-size", type=int, default=160)
     ap.add_argument("--cpu-steps", type=int, default=40)

@@ -14,6 +14,7 @@
 
 #include "guacho_gb300.h"
 #include "gch_convert.h"
+#include "gch_ddiv.h"
 
 namespace gch {
 
@@ -200,9 +201,17 @@ __device__ __forceinline__ double tabs(double a) { return fabs(a); }
 __device__ __forceinline__ float tabs(float a) { return fabsf(a); }
 // Quotient with a denominator known to lie in [2^-126, 2^126]: the FP32
 // paths use the hardware reciprocal (__fdividef, 2 ulp); FP64 divides
-// exactly as the reference does.
+// exactly as the reference does.  The slope limiters use this one: their 24
+// independent FP64 quotients per cell stay on the hardware division, since
+// inlining ddiv_rn there made the latency-bound FP64 stage-2 kernel 17%
+// slower (its code size and dependent integer chain), while ddiv_rn in HLLD,
+// the fast magnetosonic speed and u2prim makes the FP64 step 7-11% faster.
 __device__ __forceinline__ double tdiv_pos(double a, double b) { return a / b; }
 __device__ __forceinline__ float tdiv_pos(float a, float b) { return __fdividef(a, b); }
+// Any quotient: FP64 correctly rounded on the integer and FP32 pipes (the
+// same bits as a / b); FP32 as the unit's division.
+__device__ __forceinline__ double tdiv(double a, double b) { return ddiv_rn(a, b); }
+__device__ __forceinline__ float tdiv(float a, float b) { return a / b; }
 
 // The FP32 copies of the FP64 parameters (host, once per domain).
 inline void set_f32_params(KParams& k) {
@@ -284,8 +293,9 @@ template <class T>
 __device__ __forceinline__ T cfastX(const KParams& p, const T* prim) {
   const T g = par<T>(p.gamma, p.f_gamma);
   T b2 = prim[5] * prim[5] + prim[6] * prim[6] + prim[7] * prim[7];
-  T cs2va2 = (g * prim[4] + b2) / prim[0];
-  T disc = cs2va2 * cs2va2 - T(4.0) * g * prim[4] * (prim[5] * prim[5]) / prim[0] / prim[0];
+  T cs2va2 = tdiv(g * prim[4] + b2, prim[0]);
+  T disc = cs2va2 * cs2va2
+           - tdiv(tdiv(T(4.0) * g * prim[4] * (prim[5] * prim[5]), prim[0]), prim[0]);
   // >= 0 exactly; FP32 rounding can take it below zero where the sound
   // speed meets the normal Alfven speed (FP64 keeps the reference's value)
   if constexpr (sizeof(T) == 4) disc = tmax_(disc, T(0));
@@ -295,7 +305,7 @@ __device__ __forceinline__ T cfastX(const KParams& p, const T* prim) {
 // src/hydro_core.f90:544-553  csound
 template <class T>
 __device__ __forceinline__ T csound(const KParams& p, T pr, T d) {
-  return tsqrt(par<T>(p.gamma, p.f_gamma) * pr / d);
+  return tsqrt(tdiv(par<T>(p.gamma, p.f_gamma) * pr, d));
 }
 
 // src/hydro_core.f90:735-796  average (slope limiter)
@@ -367,16 +377,16 @@ __device__ __forceinline__ void hlld(const KParams& p, const T* pl, const T* pr,
   T srmur = sr - pr[1];
   T rholul = pl[0] * pl[1];
   T rhorur = pr[0] * pr[1];
-  T sM = (srmur * rhorur - slmul * rholul - pTR + pTL) / (srmur * pr[0] - slmul * pl[0]);
+  T sM = tdiv(srmur * rhorur - slmul * rholul - pTR + pTL, srmur * pr[0] - slmul * pl[0]);
   T srmsM = sr - sM;
   T slmsM = sl - sM;
-  T rhostl = pl[0] * slmul / slmsM;
-  T rhostr = pr[0] * srmur / srmsM;
-  T sstl = sM - tabs(bx) / tsqrt(rhostl);
-  T sstr = sM + tabs(bx) / tsqrt(rhostr);
-  T pst = (srmur * pr[0] * pTL - slmul * pl[0] * pTR
-           + pl[0] * pr[0] * srmur * slmul * (pr[1] - pl[1]))
-          / (srmur * pr[0] - slmul * pl[0]);
+  T rhostl = tdiv(pl[0] * slmul, slmsM);
+  T rhostr = tdiv(pr[0] * srmur, srmsM);
+  T sstl = sM - tdiv(tabs(bx), tsqrt(rhostl));
+  T sstr = sM + tdiv(tabs(bx), tsqrt(rhostr));
+  T pst = tdiv(srmur * pr[0] * pTL - slmul * pl[0] * pTR
+                   + pl[0] * pr[0] * srmur * slmul * (pr[1] - pl[1]),
+               srmur * pr[0] - slmul * pl[0]);
   T vstl, wstl, bystl, bzstl, vstr, wstr, bystr, bzstr;
 
   if (sstl >= T(0)) {  // UL* region
@@ -387,14 +397,14 @@ __device__ __forceinline__ void hlld(const KParams& p, const T* pl, const T* pr,
     if (denl == T(0)) {
       vstl = pl[2]; wstl = pl[3]; bystl = T(0); bzstl = T(0);
     } else {
-      vstl = pl[2] - bx * pl[6] * sMmul / denl;
-      wstl = pl[3] - bx * pl[7] * sMmul / denl;
-      bystl = pl[6] * (pl[0] * (slmul * slmul) - bx * bx) / denl;
-      bzstl = pl[7] * (pl[0] * (slmul * slmul) - bx * bx) / denl;
+      vstl = pl[2] - tdiv(bx * pl[6] * sMmul, denl);
+      wstl = pl[3] - tdiv(bx * pl[7] * sMmul, denl);
+      bystl = tdiv(pl[6] * (pl[0] * (slmul * slmul) - bx * bx), denl);
+      bzstl = tdiv(pl[7] * (pl[0] * (slmul * slmul) - bx * bx), denl);
     }
     T vdotbl = pl[1] * bx + pl[2] * pl[6] + pl[3] * pl[7];
     T vstdotbstl = sM * bx + vstl * bystl + wstl * bzstl;
-    T estl = (slmul * el - pTL * pl[1] + pst * sM + bx * (vdotbl - vstdotbstl)) / slmsM;
+    T estl = tdiv(slmul * el - pTL * pl[1] + pst * sM + bx * (vdotbl - vstdotbstl), slmsM);
     ff[0] = rhostl * sM;
     ff[1] = rhostl * (sM * sM) + pst - bx * bx;
     ff[2] = rhostl * sM * vstl - bx * bystl;
@@ -404,7 +414,7 @@ __device__ __forceinline__ void hlld(const KParams& p, const T* pl, const T* pr,
     ff[6] = bystl * sM - bx * vstl;
     ff[7] = bzstl * sM - bx * wstl;
 #pragma unroll
-    for (int q = 8; q < NEQ; ++q) ff[q] = sM * pl[q] * slmul / slmsM;  // :150-152
+    for (int q = 8; q < NEQ; ++q) ff[q] = tdiv(sM * pl[q] * slmul, slmsM);  // :150-152
     return;
   }
   if (sstr <= T(0)) {  // UR* region
@@ -417,14 +427,14 @@ __device__ __forceinline__ void hlld(const KParams& p, const T* pl, const T* pr,
       // (src/hlld.f90:167-171); mirror the L fallback
       vstr = pr[2]; wstr = pr[3]; bystr = T(0); bzstr = T(0);
     } else {
-      vstr = pr[2] - bx * pr[6] * sMmur / denr;
-      wstr = pr[3] - bx * pr[7] * sMmur / denr;
-      bystr = pr[6] * (pr[0] * (srmur * srmur) - bx * bx) / denr;
-      bzstr = pr[7] * (pr[0] * (srmur * srmur) - bx * bx) / denr;
+      vstr = pr[2] - tdiv(bx * pr[6] * sMmur, denr);
+      wstr = pr[3] - tdiv(bx * pr[7] * sMmur, denr);
+      bystr = tdiv(pr[6] * (pr[0] * (srmur * srmur) - bx * bx), denr);
+      bzstr = tdiv(pr[7] * (pr[0] * (srmur * srmur) - bx * bx), denr);
     }
     T vdotbr = pr[1] * bx + pr[2] * pr[6] + pr[3] * pr[7];
     T vstdotbstr = sM * bx + vstr * bystr + wstr * bzstr;
-    T estr = (srmur * er - pTR * pr[1] + pst * sM + bx * (vdotbr - vstdotbstr)) / srmsM;
+    T estr = tdiv(srmur * er - pTR * pr[1] + pst * sM + bx * (vdotbr - vstdotbstr), srmsM);
     ff[0] = rhostr * sM;
     ff[1] = rhostr * (sM * sM) + pst - bx * bx;
     ff[2] = rhostr * sM * vstr - bx * bystr;
@@ -434,7 +444,7 @@ __device__ __forceinline__ void hlld(const KParams& p, const T* pl, const T* pr,
     ff[6] = bystr * sM - bx * vstr;
     ff[7] = bzstr * sM - bx * wstr;
 #pragma unroll
-    for (int q = 8; q < NEQ; ++q) ff[q] = sM * pr[q] * srmur / srmsM;  // :198-200
+    for (int q = 8; q < NEQ; ++q) ff[q] = tdiv(sM * pr[q] * srmur, srmsM);  // :198-200
     return;
   }
   T sMmul = sM - pl[1];
@@ -444,33 +454,33 @@ __device__ __forceinline__ void hlld(const KParams& p, const T* pl, const T* pr,
   if (denl == T(0)) {
     vstl = pl[2]; wstl = pl[3]; bystl = T(0); bzstl = T(0);
   } else {
-    vstl = pl[2] - bx * pl[6] * sMmul / denl;
-    wstl = pl[3] - bx * pl[7] * sMmul / denl;
-    bystl = pl[6] * (pl[0] * (slmul * slmul) - bx * bx) / denl;
-    bzstl = pl[7] * (pl[0] * (slmul * slmul) - bx * bx) / denl;
+    vstl = pl[2] - tdiv(bx * pl[6] * sMmul, denl);
+    wstl = pl[3] - tdiv(bx * pl[7] * sMmul, denl);
+    bystl = tdiv(pl[6] * (pl[0] * (slmul * slmul) - bx * bx), denl);
+    bzstl = tdiv(pl[7] * (pl[0] * (slmul * slmul) - bx * bx), denl);
   }
   if (denr == T(0)) {
     vstr = pr[2]; wstr = pr[3]; bystr = T(0); bzstr = T(0);
   } else {
-    vstr = pr[2] - bx * pr[6] * sMmur / denr;
-    wstr = pr[3] - bx * pr[7] * sMmur / denr;
-    bystr = pr[6] * (pr[0] * (srmur * srmur) - bx * bx) / denr;
-    bzstr = pr[7] * (pr[0] * (srmur * srmur) - bx * bx) / denr;
+    vstr = pr[2] - tdiv(bx * pr[6] * sMmur, denr);
+    wstr = pr[3] - tdiv(bx * pr[7] * sMmur, denr);
+    bystr = tdiv(pr[6] * (pr[0] * (srmur * srmur) - bx * bx), denr);
+    bzstr = tdiv(pr[7] * (pr[0] * (srmur * srmur) - bx * bx), denr);
   }
   T sql = tsqrt(rhostl), sqr = tsqrt(rhostr);
   T dd = sql + sqr;
-  T vstst = (sql * vstl + sqr * vstr + (bystr - bystl) * signBx) / dd;
-  T wstst = (sql * wstl + sqr * wstr + (bzstr - bzstl) * signBx) / dd;
+  T vstst = tdiv(sql * vstl + sqr * vstr + (bystr - bystl) * signBx, dd);
+  T wstst = tdiv(sql * wstl + sqr * wstr + (bzstr - bzstl) * signBx, dd);
   T sqlr = tsqrt(rhostl * rhostr);
-  T bystst = (sql * bystr + sqr * bystl + sqlr * (vstr - vstl) * signBx) / dd;
-  T bzstst = (sql * bzstr + sqr * bzstl + sqlr * (wstr - wstl) * signBx) / dd;
+  T bystst = tdiv(sql * bystr + sqr * bystl + sqlr * (vstr - vstl) * signBx, dd);
+  T bzstst = tdiv(sql * bzstr + sqr * bzstl + sqlr * (wstr - wstl) * signBx, dd);
   T vststdotbstst = sM * bx + vstst * bystst + wstst * bzstst;
   if (sM >= T(0)) {  // UL** region
     T el = T(0.5) * pl[0] * (pl[1] * pl[1] + pl[2] * pl[2] + pl[3] * pl[3]) + cv * pl[4]
            + T(0.5) * (bx * bx + pl[6] * pl[6] + pl[7] * pl[7]);
     T vdotbl = pl[1] * bx + pl[2] * pl[6] + pl[3] * pl[7];
     T vstdotbstl = sM * bx + vstl * bystl + wstl * bzstl;
-    T estl = (slmul * el - pTL * pl[1] + pst * sM + bx * (vdotbl - vstdotbstl)) / slmsM;
+    T estl = tdiv(slmul * el - pTL * pl[1] + pst * sM + bx * (vdotbl - vstdotbstl), slmsM);
     T eststl = estl - sql * (vstdotbstl - vststdotbstst) * signBx;
     ff[0] = rhostl * sM;
     ff[1] = rhostl * (sM * sM) + pst - bx * bx;
@@ -481,7 +491,7 @@ __device__ __forceinline__ void hlld(const KParams& p, const T* pl, const T* pr,
     ff[6] = bystst * sM - bx * vstst;
     ff[7] = bzstst * sM - bx * wstst;
 #pragma unroll
-    for (int q = 8; q < NEQ; ++q) ff[q] = sM * pl[q] * slmul / slmsM;  // :277-279
+    for (int q = 8; q < NEQ; ++q) ff[q] = tdiv(sM * pl[q] * slmul, slmsM);  // :277-279
     return;
   }
   if (sM <= T(0)) {  // UR** region
@@ -489,7 +499,7 @@ __device__ __forceinline__ void hlld(const KParams& p, const T* pl, const T* pr,
            + T(0.5) * (bx * bx + pr[6] * pr[6] + pr[7] * pr[7]);
     T vdotbr = pr[1] * bx + pr[2] * pr[6] + pr[3] * pr[7];
     T vstdotbstr = sM * bx + vstr * bystr + wstr * bzstr;
-    T estr = (srmur * er - pTR * pr[1] + pst * sM + bx * (vdotbr - vstdotbstr)) / srmsM;
+    T estr = tdiv(srmur * er - pTR * pr[1] + pst * sM + bx * (vdotbr - vstdotbstr), srmsM);
     T eststr = estr + sqr * (vstdotbstr - vststdotbstst) * signBx;
     ff[0] = rhostr * sM;
     ff[1] = rhostr * (sM * sM) + pst - bx * bx;
@@ -500,7 +510,7 @@ __device__ __forceinline__ void hlld(const KParams& p, const T* pl, const T* pr,
     ff[6] = bystst * sM - bx * vstst;
     ff[7] = bzstst * sM - bx * wstst;
 #pragma unroll
-    for (int q = 8; q < NEQ; ++q) ff[q] = sM * pr[q] * srmur / srmsM;  // :308-310
+    for (int q = 8; q < NEQ; ++q) ff[q] = tdiv(sM * pr[q] * srmur, srmsM);  // :308-310
     return;
   }
   // src/hlld.f90:316-317 prints and stops here (sM not finite)

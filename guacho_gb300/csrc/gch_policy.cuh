@@ -46,15 +46,16 @@ struct Ops<PolFP64> {
                                                 unsigned& pfl, double* T = nullptr) {
     double r = tmax_(uu[0], 1e-15);
     prim[0] = r;
-    prim[1] = uu[1] / r;
-    prim[2] = uu[2] / r;
-    prim[3] = uu[3] / r;
+    prim[1] = tdiv(uu[1], r);
+    prim[2] = tdiv(uu[2], r);
+    prim[3] = tdiv(uu[3], r);
     if (NEQ >= 8 && p.mhd) {
-      prim[4] = (uu[4] - 0.5 * r * (prim[1] * prim[1] + prim[2] * prim[2] + prim[3] * prim[3])
-                 - 0.5 * (uu[5] * uu[5] + uu[6] * uu[6] + uu[7] * uu[7])) / p.cv;
+      prim[4] = tdiv(uu[4] - 0.5 * r * (prim[1] * prim[1] + prim[2] * prim[2] + prim[3] * prim[3])
+                         - 0.5 * (uu[5] * uu[5] + uu[6] * uu[6] + uu[7] * uu[7]),
+                     p.cv);
     } else {
-      prim[4] = (uu[4] - 0.5 * r * (prim[1] * prim[1] + prim[2] * prim[2] + prim[3] * prim[3]))
-                / p.cv;
+      prim[4] = tdiv(uu[4] - 0.5 * r * (prim[1] * prim[1] + prim[2] * prim[2] + prim[3] * prim[3]),
+                     p.cv);
     }
     if (!(prim[4] >= 1e-16)) ++pfl;
     prim[4] = tmax_(prim[4], 1e-16);

@@ -1,8 +1,10 @@
-// Host check of gch_convert.h: the integer-pipe FP64 <-> FP32 conversions
-// against the C casts, with the flush rule the header states (results and
-// FP32 inputs below 2^-126 in magnitude become signed zero).
+// Host check of gch_convert.h and gch_ddiv.h: the integer-pipe FP64 <-> FP32
+// conversions against the C casts, with the flush rule the header states
+// (results and FP32 inputs below 2^-126 in magnitude become signed zero),
+// and the integer-pipe FP64 division against the IEEE division.
 // Usage: convert_check <n_random>; prints "checked N bad B", exits 1 on a mismatch.
 #include "gch_convert.h"
+#include "gch_ddiv.h"
 
 #include <cfloat>
 #include <cmath>
@@ -37,6 +39,12 @@ int main(int argc, char** argv) {
     const bool ok = std::isnan(want) ? std::isnan(got) : bits_of(got) == bits_of(want);
     if (!ok && bad++ < 8) printf("f2d(%a) = %a, want %a\n", f, got, want);
   };
+  auto div = [&](double a, double b) {
+    ++checked;
+    const double got = gch::ddiv_rn(a, b), want = a / b;
+    const bool ok = std::isnan(want) ? std::isnan(got) : bits_of(got) == bits_of(want);
+    if (!ok && bad++ < 8) printf("ddiv_rn(%a, %a) = %a, want %a\n", a, b, got, want);
+  };
   std::mt19937_64 g(20260001);
   for (long i = 0; i < n; ++i) {
     // any bit pattern
@@ -61,6 +69,26 @@ int main(int argc, char** argv) {
     float f;
     memcpy(&f, &fb, 4);
     f2d(f);
+    // division: any bit patterns, operands of nearby magnitudes, and
+    // dividends one ulp either side of b times a 53-bit quotient, whose
+    // quotients sit next to a rounding boundary
+    const uint64_t ub = g(), vb = g();
+    double da, db;
+    memcpy(&da, &ub, 8);
+    memcpy(&db, &vb, 8);
+    div(da, db);
+    const double c = std::ldexp((double)(g() >> 11) * 0x1p-53 + 0.5, (int)(g() % 80) - 40);
+    div(y, c);
+    div(-c, y);
+    div(c, c);
+    div(3.0 * c, 3.0);
+    const uint64_t mb = (0x3FFull << 52) | (g() >> 12);
+    double q;
+    memcpy(&q, &mb, 8);
+    const double p = q * c;
+    div(p, c);
+    div(std::nextafter(p, 0.0), c);
+    div(std::nextafter(p, INFINITY), c);
   }
   const double special[] = {0.0, -0.0, INFINITY, -INFINITY, NAN, -NAN, DBL_MAX, -DBL_MAX,
                             FLT_MAX, -FLT_MAX, (double)FLT_MAX * (1 + 0x1p-25),
@@ -71,6 +99,8 @@ int main(int argc, char** argv) {
   const float fspecial[] = {0.0f, -0.0f, INFINITY, -INFINITY, NAN, FLT_MAX, FLT_MIN, -FLT_MIN,
                             0x1p-127f, 1.0f, -1.0f, 1e-15f};
   for (float s : fspecial) f2d(s);
+  for (double s : special)
+    for (double t : special) div(s, t);
   printf("checked %ld bad %ld\n", checked, bad);
   return bad ? 1 : 0;
 }

@@ -1,7 +1,9 @@
 """Integer-pipe FP64 <-> FP32 conversions used by the FP32 + FP64-u path
-(guacho_gb300/csrc/gch_convert.h): bit-identical to the C casts on random bit
-patterns, values around the FP32 range, exact rounding ties and the special
-values, compiled for the host with g++."""
+(guacho_gb300/csrc/gch_convert.h) and the integer-pipe FP64 division of the
+FP64 Riemann solvers (gch_ddiv.h): bit-identical to the C casts and to the
+IEEE division on random bit patterns, values around the FP32 range, exact
+rounding ties, quotients next to a rounding boundary and the special values,
+compiled for the host with g++."""
 import shutil
 import subprocess
 from pathlib import Path
@@ -11,12 +13,12 @@ import pytest
 ROOT = Path(__file__).resolve().parent.parent
 
 
-def test_conversions_match_c_casts(tmp_path):
+def test_conversions_and_division_match_ieee(tmp_path):
     cxx = shutil.which("g++")
     if cxx is None:
         pytest.skip("g++ not found")
     exe = tmp_path / "convert_check"
-    subprocess.run([cxx, "-O2", "-std=c++17", f"-I{ROOT / 'guacho_gb300' / 'csrc'}",
+    subprocess.run([cxx, "-O2", "-std=c++17", "-ffp-contract=off", f"-I{ROOT / 'guacho_gb300' / 'csrc'}",
                     str(ROOT / "tests" / "convert_check.cpp"), "-o", str(exe)], check=True)
     r = subprocess.run([str(exe), "2000000"], capture_output=True, text=True)
     assert r.returncode == 0, r.stdout + r.stderr
