@@ -205,7 +205,7 @@ __device__ __forceinline__ float tabs(float a) { return fabsf(a); }
 // independent FP64 quotients per cell stay on the hardware division, since
 // inlining ddiv_rn there made the latency-bound FP64 stage-2 kernel 17%
 // slower (its code size and dependent integer chain), while ddiv_rn in HLLD,
-// the fast magnetosonic speed and u2prim makes the FP64 step 7-11% faster.
+// HLLC, the wave speeds and u2prim makes the FP64 step 7-11% faster.
 __device__ __forceinline__ double tdiv_pos(double a, double b) { return a / b; }
 __device__ __forceinline__ float tdiv_pos(float a, float b) { return __fdividef(a, b); }
 // Any quotient: FP64 correctly rounded on the integer and FP32 pipes (the
@@ -683,23 +683,23 @@ __device__ __forceinline__ void hllc(const KParams& p, const T* pl, const T* pr,
   T srmur = sr - pr[1];
   T rholul = pl[0] * pl[1];
   T rhorur = pr[0] * pr[1];
-  T sst = (srmur * rhorur - slmul * rholul - pr[4] + pl[4]) / (srmur * pr[0] - slmul * pl[0]);
+  T sst = tdiv(srmur * rhorur - slmul * rholul - pr[4] + pl[4], srmur * pr[0] - slmul * pl[0]);
   T uu[NEQ], uuk[NEQ];
   if (sst >= T(0)) {
-    T rhost = pl[0] * (slmul) / (sl - sst);
+    T rhost = tdiv(pl[0] * (slmul), sl - sst);
     T ek = T(0.5) * pl[0] * (pl[1] * pl[1] + pl[2] * pl[2] + pl[3] * pl[3]) + cv * pl[4];
     uuk[0] = rhost;
     uuk[1] = rhost * sst;
     uuk[2] = rhost * pl[2];
     uuk[3] = rhost * pl[3];
-    uuk[4] = rhost * (ek / pl[0] + (sst - pl[1]) * (sst + pl[4] / (pl[0] * slmul)));
+    uuk[4] = rhost * (tdiv(ek, pl[0]) + (sst - pl[1]) * (sst + tdiv(pl[4], pl[0] * slmul)));
     if (NEQ >= 8) {
-      uuk[5] = rhost * pl[5] / pl[0];
-      uuk[6] = rhost * pl[6] / pl[0];
-      uuk[7] = rhost * pl[7] / pl[0];
+      uuk[5] = tdiv(rhost * pl[5], pl[0]);
+      uuk[6] = tdiv(rhost * pl[6], pl[0]);
+      uuk[7] = tdiv(rhost * pl[7], pl[0]);
     }
 #pragma unroll
-    for (int q = kNeqDyn<NEQ>; q < NEQ; ++q) uuk[q] = rhost * pl[q] / pl[0];  // :95-97
+    for (int q = kNeqDyn<NEQ>; q < NEQ; ++q) uuk[q] = tdiv(rhost * pl[q], pl[0]);  // :95-97
     prim2f<T, NEQ>(p, pl, ff);
     prim2u<T, NEQ>(p, pl, uu);
 #pragma unroll
@@ -707,20 +707,20 @@ __device__ __forceinline__ void hllc(const KParams& p, const T* pl, const T* pr,
     return;
   }
   if (sst <= T(0)) {
-    T rhost = pr[0] * (srmur) / (sr - sst);
+    T rhost = tdiv(pr[0] * (srmur), sr - sst);
     T ek = T(0.5) * pr[0] * (pr[1] * pr[1] + pr[2] * pr[2] + pr[3] * pr[3]) + cv * pr[4];
     uuk[0] = rhost;
     uuk[1] = rhost * sst;
     uuk[2] = rhost * pr[2];
     uuk[3] = rhost * pr[3];
-    uuk[4] = rhost * (ek / pr[0] + (sst - pr[1]) * (sst + pr[4] / (pr[0] * srmur)));
+    uuk[4] = rhost * (tdiv(ek, pr[0]) + (sst - pr[1]) * (sst + tdiv(pr[4], pr[0] * srmur)));
     if (NEQ >= 8) {
-      uuk[5] = rhost * pr[5] / pr[0];
-      uuk[6] = rhost * pr[6] / pr[0];
-      uuk[7] = rhost * pr[7] / pr[0];
+      uuk[5] = tdiv(rhost * pr[5], pr[0]);
+      uuk[6] = tdiv(rhost * pr[6], pr[0]);
+      uuk[7] = tdiv(rhost * pr[7], pr[0]);
     }
 #pragma unroll
-    for (int q = kNeqDyn<NEQ>; q < NEQ; ++q) uuk[q] = rhost * pr[q] / pr[0];  // :124-126
+    for (int q = kNeqDyn<NEQ>; q < NEQ; ++q) uuk[q] = tdiv(rhost * pr[q], pr[0]);  // :124-126
     prim2f<T, NEQ>(p, pr, ff);
     prim2u<T, NEQ>(p, pr, uu);
 #pragma unroll
