@@ -63,7 +63,8 @@ GCH_HD int32_t f2i_rn(float x) {
 GCH_HD void ddiv_digit(int64_t& R, int64_t& Q, int64_t Y, float rs, int s) {
   const float rf = (float)(int32_t)(R >> 24);   // |R| < 2^54: fits in 30 bits
   const int32_t q = f2i_rn(rf * rs);
-  R = (int64_t)(((uint64_t)R << s) - (uint64_t)((int64_t)q * Y));
+  // q Y reaches 2^74: the product is taken modulo 2^64 in unsigned arithmetic
+  R = (int64_t)(((uint64_t)R << s) - (uint64_t)(int64_t)q * (uint64_t)Y);
   Q = (int64_t)(((uint64_t)Q << s) + (uint64_t)(int64_t)q);
 }
 
