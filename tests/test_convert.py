@@ -23,3 +23,21 @@ def test_conversions_and_division_match_ieee(tmp_path):
     r = subprocess.run([str(exe), "2000000"], capture_output=True, text=True)
     assert r.returncode == 0, r.stdout + r.stderr
     assert "bad 0" in r.stdout
+
+
+def test_conversions_and_division_free_of_undefined_behaviour(tmp_path):
+    """The same check built with the undefined-behaviour sanitizer (signed
+    overflow, shifts out of range), where the host toolchain has it."""
+    cxx = shutil.which("g++")
+    if cxx is None:
+        pytest.skip("g++ not found")
+    exe = tmp_path / "convert_check_ubsan"
+    r = subprocess.run([cxx, "-O1", "-std=c++17", "-ffp-contract=off", "-fsanitize=undefined",
+                        "-fno-sanitize-recover=all", f"-I{ROOT / 'guacho_gb300' / 'csrc'}",
+                        str(ROOT / "tests" / "convert_check.cpp"), "-o", str(exe)],
+                       capture_output=True, text=True)
+    if r.returncode != 0:
+        pytest.skip("no undefined-behaviour sanitizer in this toolchain")
+    r = subprocess.run([str(exe), "200000"], capture_output=True, text=True)
+    assert r.returncode == 0, r.stdout + r.stderr
+    assert "bad 0" in r.stdout
