@@ -48,6 +48,14 @@ WORKLOAD = ("decaying MHD turbulence 256^3, periodic, HLLD + van Leer + flux-CD,
             "seeded random-phase solenoidal velocity (E(k)~k^-2, 2<=|k|<=8, Mach 1)")
 
 
+def bench_config(n: int, ws: int) -> dict:
+    """The workload description both arms print (the same box and problem)."""
+    return {"workload": WORKLOAD, "n": n,
+            "precision": "fp32 + Kahan-compensated pair accumulation (GCH_FP32_KAHAN)",
+            "parallelism": f"replicas x{ws}",
+            "l2": "state 1.1 GB FP64 u + 0.56 GB FP32 up >> 129 MB L2 (no flush)"}
+
+
 def _dist():
     ws = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -156,19 +164,69 @@ def step_bytes_per_zone(prec: int, neq: int = 8) -> int:
     return neq * (3 * tu + 2 * ts)
 
 
-def rel_l1(a, b):
-    import numpy as np
-    return float(np.abs(a - b).mean() / max(np.abs(b).mean(), 1e-300))
-
-
 def prim_fields(p, u):
+    """Interior primitives of a host-layout u (FP64), the reference's u2prim
+    without floors: rho, p, v and (MHD) B."""
     import numpy as np
     ui = u[2:-2, 2:-2, 2:-2]
     rho = ui[..., 0]
     v = ui[..., 1:4] / rho[..., None]
-    e = ui[..., 4] - 0.5 * rho * (v ** 2).sum(-1) - 0.5 * (ui[..., 5:8] ** 2).sum(-1)
-    return {"rho": rho, "p": e / p.cv, "vx": v[..., 0], "vy": v[..., 1], "vz": v[..., 2],
-            "Bx": ui[..., 5], "By": ui[..., 6], "Bz": ui[..., 7]}
+    e = ui[..., 4] - 0.5 * rho * (v ** 2).sum(-1)
+    out = {"rho": rho, "vx": v[..., 0], "vy": v[..., 1], "vz": v[..., 2]}
+    if p.neq >= 8:
+        if p.mhd:
+            e = e - 0.5 * (ui[..., 5:8] ** 2).sum(-1)
+        out.update(Bx=ui[..., 5], By=ui[..., 6], Bz=ui[..., 7])
+    out["p"] = e / p.cv
+    return out
+
+
+def field_errors(p, u, uref) -> dict:
+    """Per-field errors of u against uref over the interior: relative L1
+    mean|x - x_ref| / mean|x_ref|, absolute Linf max|x - x_ref| and Linf
+    relative to the field's scale max|x_ref|."""
+    import numpy as np
+    a, r = prim_fields(p, u), prim_fields(p, uref)
+    out = {}
+    for k in ("rho", "p", "vx", "vy", "vz", "Bx", "By", "Bz"):
+        if k not in r:
+            continue
+        d = np.abs(a[k] - r[k])
+        ref = np.abs(r[k])
+        out[k] = {"l1": float(d.mean() / max(ref.mean(), 1e-300)),
+                  "linf": float(d.max()), "linf_rel": float(d.max() / max(ref.max(), 1e-300))}
+    return out
+
+
+def max_divb(p, u) -> dict:
+    """max |div B| over the interior with the centred formula of the
+    reference's div B dump (src/Out_BIN_Module.f90:214-222), absolute and
+    relative to max|B|/dx."""
+    import numpy as np
+    from guacho_gb300 import binio
+    d = float(np.abs(binio.divb(u, p)).max())
+    ui = u[2:-2, 2:-2, 2:-2]
+    bmax = float(np.sqrt((ui[..., 5:8] ** 2).sum(-1)).max())
+    return {"abs": d, "rel": d * min(p.dx, p.dy, p.dz) / max(bmax, 1e-300)}
+
+
+def cpu_model() -> str:
+    """The host CPU's model name (lscpu, else /proc/cpuinfo)."""
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.strip().lower().startswith("model name"):
+                return line.split(":", 1)[1].strip()
+    except (OSError, subprocess.SubprocessError):
+        pass
+    try:
+        for line in Path("/proc/cpuinfo").read_text().splitlines():
+            if line.lower().startswith("model name"):
+                return line.split(":", 1)[1].strip()
+    except OSError:
+        pass
+    import platform
+    return platform.processor() or platform.machine()
 
 
 # ---------------------------------------------------------------------------
@@ -232,6 +290,106 @@ def batched_run(args, precision: int) -> dict:
     return res
 
 
+def c2_errors(n: int, steps: int, warm: int = 3) -> tuple:
+    """Decaying turbulence n^3 (HLLD, van Leer, flux-CD): `steps` steps from
+    the initial state on the plain FP64 path and on both FP32 paths, each
+    with its own dt; per-field L1/Linf of the FP32 states against the FP64
+    state at equal step count, and max |div B| of all three.  The FP64 run
+    is timed (CUDA events, device loop) over its last steps - warm steps;
+    returns (errors, FP64 ms over those steps, their count)."""
+    from guacho_gb300 import params as P
+    from guacho_gb300 import problems
+    from guacho_gb300.domain import Domain
+    p, u0 = problems.turbulence(n)
+    with Domain(p.replace(precision=P.FP64)) as d:
+        d.init(u0)
+        d.advance_timed(warm)
+        ms64 = d.advance_timed(steps - warm)
+        u64 = d.download()
+    res = {"workload": f"decaying MHD turbulence {n}^3 (HLLD, van Leer, flux-CD)",
+           "steps": steps, "compare": "equal step count, each precision with its own dt",
+           "fp64": {"max_divb": max_divb(p, u64)}}
+    for name, prec in (("fp32_kahan", P.FP32_KAHAN), ("fp32_mixed_fp64u", P.FP32_MIXED)):
+        with Domain(p.replace(precision=prec)) as d:
+            d.init(u0)
+            d.advance_timed(steps)
+            u = d.download()
+        res[name] = {"errors": field_errors(p, u, u64), "max_divb": max_divb(p, u)}
+        del u
+    return res, ms64, steps - warm
+
+
+def c3_errors(n: int, tmax: float) -> dict:
+    """Low-beta blast n^3 (outflow, HLLD, minmod, flux-CD) run to t = tmax in
+    FP64, FP32 with FP64 u and FP32 with Kahan pairs, host-driven steps
+    (get_timestep + tstep, the last dt clipped to land on tmax as the
+    reference clips to its output time): the pressure-floor hits of every
+    step (cells whose recovered pressure fell below the 1e-16 floor of
+    src/hydro_core.f90:78 when get_timestep formed the primitives of u),
+    per-field L1/Linf of the FP32 states against FP64 at t = tmax, and
+    max |div B|."""
+    from guacho_gb300 import params as P
+    from guacho_gb300 import problems
+    from guacho_gb300.domain import Domain
+    p, u0 = problems.blast(n)
+    res = {"workload": f"low-beta MHD blast {n}^3 (outflow, HLLD, minmod, flux-CD), "
+                       f"beta ~ 0.025 outside the sphere", "tmax": tmax,
+           "floor_count": "cells of u below the pressure floor at each step's get_timestep"}
+    ref = None
+    for name, prec in (("fp64", P.FP64), ("fp32_mixed_fp64u", P.FP32_MIXED),
+                       ("fp32_kahan", P.FP32_KAHAN)):
+        with Domain(p.replace(precision=prec)) as d:
+            d.init(u0)
+            t, it, floors, bits = 0.0, 1, [], 0
+            while it <= 100000:
+                dt, dump = d.get_timestep(it, 10, t, tmax)
+                d.tstep(dt)
+                t += dt
+                it += 1
+                pf, err = d.step_info()
+                floors.append(int(pf))
+                bits |= err
+                if dump or t >= tmax:
+                    break
+            u = d.download()
+        e = {"steps": it - 1, "time": t, "floor_hits_total": sum(floors),
+             "steps_with_floor_hits": sum(1 for x in floors if x),
+             "floor_hits_max_step": max(floors) if floors else 0,
+             "floor_hits_per_step": floors, "err_bits": bits, "max_divb": max_divb(p, u)}
+        if ref is None:
+            ref = u
+        else:
+            e["errors"] = field_errors(p, u, ref)
+        res[name] = e
+    return res
+
+
+def c5_errors(n: int, steps: int) -> dict:
+    """Hydro wind interaction with tabulated cooling n^3 (HLLC, outflow, two
+    spheres re-imposed at every boundary call): `steps` steps from the
+    initial state in FP64 and on both FP32 paths; per-field L1/Linf of the
+    FP32 states against FP64 at equal step count, and the FP64 step time."""
+    from guacho_gb300 import params as P
+    from guacho_gb300 import problems
+    from guacho_gb300.domain import Domain
+    p, u0 = problems.wind_cooling(n)
+    with Domain(p.replace(precision=P.FP64)) as d:
+        d.init(u0)
+        ms64 = d.advance_timed(steps)
+        u64 = d.download()
+    res = {"workload": f"hydro wind + table cooling {n}^3 (HLLC, outflow, 2 spheres)",
+           "steps": steps, "compare": "equal step count, each precision with its own dt",
+           "fp64_ms_per_step": ms64 / steps}
+    for name, prec in (("fp32_kahan", P.FP32_KAHAN), ("fp32_mixed_fp64u", P.FP32_MIXED)):
+        with Domain(p.replace(precision=prec)) as d:
+            d.init(u0)
+            ms = d.advance_timed(steps)
+            u = d.download()
+        res[name] = {"errors": field_errors(p, u, u64), "ms_per_step": ms / steps}
+        del u
+    return res
+
+
 def cpu_oracle_rate(n: int, steps: int, threads: int) -> dict:
     """The oracle (the C restatement of the reference's CPU algorithm) on an
     n^3 sample of the same turbulence problem, FP64, all threads."""
@@ -281,17 +439,17 @@ def run_reference(args, dist: Dist) -> None:
         it += 1
     el = time.perf_counter() - t0
     rate = n ** 3 * args.steps / el
-    sample = (f"{n}^3 sample of the same turbulence problem (same seed and spectrum), "
-              f"FP64, {args.steps} steps after {args.warmup} warm-up")
+    sample = (f"the same {n}^3 turbulence box (same seed and spectrum), FP64, {args.steps} "
+              f"steps after {args.warmup} warm-up, OpenMP over {threads} threads; the "
+              f"reference Fortran+MPI build cannot be compiled here (no Fortran compiler), so "
+              f"the C restatement of its algorithm (oracle/) runs instead")
     line = {"impl": "reference", "metric": METRIC, "value": rate, "unit": UNIT, "n_gpus": 1,
             "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": 1e3 * el / args.steps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": WORKLOAD, "reference_sample_n": n},
+            "config": bench_config(n, dist.ws),
             "cpu_baseline": {"value": rate, "unit": UNIT, "cores": threads, "kind": "port",
-                             "sample": sample + "; the reference Fortran+MPI build cannot "
-                                       "be compiled here (no Fortran compiler), so the C "
-                                       "restatement (oracle/) runs instead"},
+                             "cpu": cpu_model(), "sample": sample},
             "e2e": {"value": rate, "unit": UNIT, "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
@@ -336,8 +494,8 @@ def run_ours(args, dist: Dist) -> None:
             for _ in range(3):
                 for name, t in d.profile_step():
                     prof_v.setdefault(name, []).append(t)
-        variants[prec] = dict(ms=ms_v, clk=clk_v, prof=prof_v, u=d.download(),
-                              launches=d.launches_per_step(), steps=W + K + (3 if prof_v else 0))
+        variants[prec] = dict(ms=ms_v, clk=clk_v, prof=prof_v,
+                              launches=d.launches_per_step())
         d.close()
     ms = variants[headline]["ms"]
     clk = variants[headline]["clk"]
@@ -345,32 +503,14 @@ def run_ours(args, dist: Dist) -> None:
     launches = variants[headline]["launches"]
     value = dist.ws * n ** 3 * K / (ms * 1e-3)
 
-    # ---- plain FP64 on the same box (ratio, and the reference for L1) -------
-    p64 = p.replace(precision=P.FP64)
-    d64 = Domain(p64)
-    d64.init(u0)
-    d64.advance_timed(1)
-    k64 = max(2, args.fp64_steps)
-    ms64 = d64.advance_timed(k64)
-    done = 1 + k64
-    snaps = {}
-    for prec in sorted(variants, key=lambda q: variants[q]["steps"]):
-        need = variants[prec]["steps"] - done
-        if need > 0:
-            d64.advance_timed(need)
-            done += need
-        snaps[prec] = d64.download()
-    d64.close()
-    l1 = {}
-    for prec, v in variants.items():
-        fm, f64 = prim_fields(p, v["u"]), prim_fields(p, snaps[prec])
-        bmag = np.sqrt(f64["Bx"] ** 2 + f64["By"] ** 2 + f64["Bz"] ** 2).mean()
-        errs = {}
-        for k in ("rho", "p", "vx", "Bx", "By", "Bz"):
-            den = bmag if k.startswith("B") else np.abs(f64[k]).mean()
-            errs[k] = float(np.abs(fm[k] - f64[k]).mean() / den)
-        errs["steps"] = v["steps"]
-        l1[{P.FP32_KAHAN: "fp32_kahan", P.FP32_MIXED: "fp32_mixed_fp64u"}[prec]] = errs
+    # ---- plain FP64 on the same box, and the FP32 paths' errors against it ---
+    # (C2: every precision advanced the same number of steps from the initial
+    # state; the FP64 run's last steps are its timing)
+    c2, ms64, k64 = c2_errors(n, args.err_steps)
+    configs_err = {"C2": c2}
+    if not args.no_config_errors and dist.rank == 0:
+        configs_err["C3"] = c3_errors(args.blast_size, args.blast_tmax)
+        configs_err["C5"] = c5_errors(args.wind_size, args.wind_steps)
     pm = p.replace(precision=headline)
 
     # ---- e2e through the C ABI with host buffers ----------------------------
@@ -463,9 +603,10 @@ def run_ours(args, dist: Dist) -> None:
         threads = os.cpu_count() or 1
         r = cpu_oracle_rate(args.cpu_size, args.cpu_steps, threads)
         cpu = {"value": r["value"], "unit": UNIT, "cores": threads, "kind": "port",
-               "sample": f"oracle (C restatement of the reference CPU algorithm), "
-                         f"{r['n']}^3 sample of the same problem, {r['steps']} steps, FP64, "
-                         f"{r['seconds']:.1f} s"}
+               "cpu": cpu_model(),
+               "sample": f"oracle (C restatement of the reference CPU algorithm, OpenMP over "
+                         f"{threads} threads), {r['n']}^3 box of the same problem, "
+                         f"{r['steps']} steps after 1 warm-up, FP64, {r['seconds']:.1f} s"}
 
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": dist.ws, "steps": K,
@@ -473,15 +614,12 @@ def run_ours(args, dist: Dist) -> None:
         "vs_baseline": None,
         "dtype": "f32 (u as Kahan-compensated f32 pairs; double-float pressure recovery; f64 dt)",
         "data": "synthetic (seeded turbulence initial state, no dataset)",
-        "config": {"workload": WORKLOAD, "n": n,
-                   "precision": "fp32 + Kahan-compensated pair accumulation (GCH_FP32_KAHAN)",
-                   "parallelism": f"replicas x{dist.ws}",
-                   "l2": "state 1.1 GB FP64 u + 0.56 GB FP32 up >> 129 MB L2 (no flush)"},
+        "config": bench_config(n, dist.ws),
         "fp64_plain": {"value": dist.ws * n ** 3 * k64 / (ms64 * 1e-3),
                        "ms_per_step": ms64 / k64, "steps": k64},
         "fp32_mixed_fp64u": {"value": dist.ws * n ** 3 * K / (variants[P.FP32_MIXED]["ms"] * 1e-3),
                              "ms_per_step": variants[P.FP32_MIXED]["ms"] / K},
-        "l1_err_vs_fp64_gpu": l1,
+        "config_errors": configs_err,
         "batched": batched,
         "kernel_ms": {k: round(v, 4) for k, v in means.items()},
         "roofline": roof, "step_roofline": step_roof,
@@ -557,12 +695,19 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--size", type=int, default=256)
-    ap.add_argument("--fp64-steps", type=int, default=4)
+    ap.add_argument("--err-steps", type=int, default=200,
+                    help="steps of the turbulence error comparison (the FP64 timing too)")
+    ap.add_argument("--blast-size", type=int, default=192)
+    ap.add_argument("--blast-tmax", type=float, default=0.02)
+    ap.add_argument("--wind-size", type=int, default=256)
+    ap.add_argument("--wind-steps", type=int, default=500)
+    ap.add_argument("--no-config-errors", action="store_true",
+                    help="skip the blast and wind error runs")
     ap.add_argument("--e2e-steps", type=int, default=30)
     ap.add_argument("--loop-steps", type=int, default=50)
-    ap.add_argument("--cpu-size", type=int, default=160)
-    ap.add_argument("--cpu-steps", type=int, default=40)
-    ap.add_argument("--ref-size", type=int, default=128)
+    ap.add_argument("--cpu-size", type=int, default=256)
+    ap.add_argument("--cpu-steps", type=int, default=8)
+    ap.add_argument("--ref-size", type=int, default=256)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--batch-boxes", type=int, default=64)
     ap.add_argument("--batch-steps", type=int, default=100)

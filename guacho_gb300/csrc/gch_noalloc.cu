@@ -1,15 +1,17 @@
 // gch_noalloc.cu -- get_timestep for callers that cannot allocate device
 // memory.
 //
-// Some callers cannot call cudaMalloc at the moment they need a timestep:
-// a driver that records its whole time loop into a CUDA graph with stream
-// capture (an allocation is not a capturable operation), or a host code
-// that hands the GPU library a fixed, pre-sized memory budget and forbids
-// hidden allocations.  gch_get_timestep_noalloc serves them: the caller
-// passes the state and the output slots in device memory it owns, and the
-// only other memory the reduction needs -- one partial minimum per thread
-// block plus a completion counter -- lives in a fixed array compiled into
-// the library.
+// Some host codes cannot call cudaMalloc at the moment they need a
+// timestep.  A Fortran or C driver that hands the GPU library a fixed,
+// pre-sized memory budget (for example one sized at start-up by a job
+// scheduler's memory limit) forbids hidden allocations, because a late
+// allocation can fail or fragment memory in the middle of a run; a code that
+// owns every device buffer through its own pool allocator has no way to
+// return library-made buffers to that pool.  gch_get_timestep_noalloc serves
+// them: the caller passes the state and the output slots in device memory it
+// owns, and the only other memory the reduction needs -- one partial minimum
+// per thread block plus a completion counter -- lives in a fixed array
+// compiled into the library.
 //
 // Limits and sharing rules:
 //  - the array holds kNoAllocMaxBlocks partial minima (512 KiB); a box needs
@@ -17,12 +19,15 @@
 //    larger box is refused with GCH_ERR_TOO_LARGE before any launch;
 //  - every GPU that loads the library keeps the array until the process
 //    exits, whether or not this entry point is used;
-//  - all calls share the one array: calls that may overlap on the GPU
-//    (different streams without ordering between them) race and must not be
-//    issued; calls on one stream are ordered and safe;
-//  - the first call on a device looks up the array's device address
-//    (cudaGetSymbolAddress) with that device current; make that first call
-//    before any stream capture begins.  Later calls only launch.
+//  - all calls share the one array, and each call starts by clearing its
+//    completion counter: calls that may overlap on the GPU (different
+//    streams without ordering between them) race and must not be issued;
+//    calls on one stream are ordered and safe;
+//  - the first call on a device (and the first call after that device's
+//    context was destroyed and created again, e.g. by cudaDeviceReset) looks
+//    up the array's device address with cudaGetSymbolAddress, with that
+//    device current; make that first call before any stream capture begins.
+//    Later calls only clear the counter and launch.
 #include <cuda_runtime.h>
 
 #include <mutex>
@@ -41,18 +46,44 @@ static __device__ __align__(256) unsigned long long g_cfl_scratch[kNoAllocMaxBlo
 
 std::mutex g_setup_mutex;
 unsigned long long* g_scratch_ptr[kMaxDevices] = {};
+void* g_scratch_ctx[kMaxDevices] = {};  // the context the address belongs to
 
-// The device address of g_cfl_scratch on the current device (looked up once
-// per device).  In host code the symbol is only a stand-in, never a device
-// address.
+// cuCtxGetCurrent through the runtime's driver entry point (no link against
+// the driver library): the identity of the current context, so that an
+// address looked up in a context that has since been destroyed is not reused.
+using CtxGetCurrentFn = int (*)(void**);
+CtxGetCurrentFn ctx_get_current() {
+  static CtxGetCurrentFn fn = [] {
+    void* f = nullptr;
+    cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault, &q) !=
+            cudaSuccess ||
+        q != cudaDriverEntryPointSuccess)
+      f = nullptr;
+    return reinterpret_cast<CtxGetCurrentFn>(f);
+  }();
+  return fn;
+}
+
+// The device address of g_cfl_scratch on the current device, looked up once
+// per device and context.  In host code the symbol is only a stand-in, never
+// a device address.
 int scratch_for_current_device(unsigned long long** out) {
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) return GCH_ERR_CUDA;
+  CtxGetCurrentFn get = ctx_get_current();
+  if (!get) return GCH_ERR_CUDA;
   std::lock_guard<std::mutex> lock(g_setup_mutex);
-  if (!g_scratch_ptr[dev]) {
+  void* ctx = nullptr;
+  if (get(&ctx) != 0) return GCH_ERR_CUDA;
+  if (!ctx || !g_scratch_ptr[dev] || g_scratch_ctx[dev] != ctx) {
+    // the lookup also makes the device's primary context current if no
+    // runtime call on this thread has done so yet
     void* ptr = nullptr;
     if (cudaGetSymbolAddress(&ptr, g_cfl_scratch) != cudaSuccess || !ptr) return GCH_ERR_CUDA;
+    if (!ctx && (get(&ctx) != 0 || !ctx)) return GCH_ERR_CUDA;
     g_scratch_ptr[dev] = static_cast<unsigned long long*>(ptr);
+    g_scratch_ctx[dev] = ctx;
   }
   *out = g_scratch_ptr[dev];
   return GCH_OK;

@@ -141,3 +141,54 @@ def table_from_log(logT: list, logL: list, tail: float) -> dict:
     inv = 1.0 / dlog
     return dict(tab_T=[10.0 ** a for a in logT], tab_L=[10.0 ** b for b in logL],
                 tab_inv_dlog=round(inv, 9), tab_i0=int(round(logT[0] * inv)), tab_tail=tail)
+
+
+# The reference's two shipped cooling curves: 41 rows at 0.1 dex from
+# 10^4 K, read by src/cooling_dmc.f90:57-82 and src/cooling_chi.f90:56-80,
+# with their own tails above 10^8 K (cooling_dmc.f90:96, cooling_chi.f90:95).
+COOL_TABLE_ROWS = 41
+COOL_TABLE_TAIL = {COOL_DMC: 0.27e-26, COOL_CHI: 0.21e-26}
+
+
+def parse_cooling_rows(text: str, kind: int) -> tuple:
+    """Rows of a cooling table file in the reference's own format (list
+    directed `read(10,*) a, b`, Fortran exponents such as 4.0d0 allowed):
+    COOL_DMC rows are (log10 T, -log10 Lambda) and decode to
+    (10**a, 10**(-b)) (src/cooling_dmc.f90:71-75); COOL_CHI rows are raw
+    (T, Lambda) (src/cooling_chi.f90:69-73).  Returns (T, Lambda) lists."""
+    if kind not in COOL_TABLE_TAIL:
+        raise ValueError(f"cooling kind {kind} has no table")
+    T, L = [], []
+    for line in text.splitlines():
+        tok = line.replace("d", "e").replace("D", "e").split()
+        if len(tok) < 2:
+            continue
+        a, b = float(tok[0]), float(tok[1])
+        if kind == COOL_DMC:
+            T.append(10.0 ** a)
+            L.append(10.0 ** (-b))
+        else:
+            T.append(a)
+            L.append(b)
+        if len(T) == COOL_TABLE_ROWS:
+            break
+    if len(T) != COOL_TABLE_ROWS:
+        raise ValueError(f"a cooling table has {COOL_TABLE_ROWS} rows, found {len(T)}")
+    return T, L
+
+
+def cooling_table(T: list, L: list, kind: int) -> dict:
+    """Params fields for one of the reference's 41-row tables: row index
+    int(log10(T)*10) - 39 (1-based, src/cooling_dmc.f90:98), the tail of the
+    kind above 10^8 K, cooling above Tmin = 10^4 K."""
+    return dict(cooling=kind, tab_T=list(T), tab_L=list(L), tab_inv_dlog=10.0, tab_i0=40,
+                tab_tail=COOL_TABLE_TAIL[kind], tab_Tmin=1.0e4)
+
+
+def read_cooling_table(path, kind: int) -> dict:
+    """The reference's table file at `path` (src/DMClib/coolingDMC.tab for
+    COOL_DMC, src/CHIANTIlib/coolingCHIANTI.tab for COOL_CHI) as Params
+    fields, decoded the way the reference's reader decodes it."""
+    with open(path) as f:
+        T, L = parse_cooling_rows(f.read(), kind)
+    return cooling_table(T, L, kind)

@@ -288,20 +288,27 @@ int gch_advance_timed(gch_domain_t* d, int steps, int n_iter, float* ms);
 int gch_profile_step(gch_domain_t* d, int cap, float* ms, char* names, int name_len, int* n);
 
 /* get_timestep for callers that cannot allocate device memory.  No
- * counterpart in the reference: it exists for drivers that record their
- * time loop with CUDA stream capture (an allocation cannot be captured) and
- * for host codes that give the library a fixed memory budget and forbid
- * hidden allocations.  It allocates nothing: the caller passes u in device
- * memory in the reference layout u(neq, 1-2:nx+2, 1-2:ny+2, 1-2:nz+2)
- * (FP64, ghost cells filled) and device slots for the outputs dt and
- * dump_flag; the per-block partial minima go to a fixed array inside the
- * library (512 KiB on every GPU that loads it, kept until exit).  Same
- * result as gch_get_timestep in FP64 arithmetic.  Limits: boxes with
- * ceil(nx/32)*ceil(ny/8)*ceil(nz/8) > 65536 (beyond 512^3 cells) return
- * GCH_ERR_TOO_LARGE; table cooling and passive scalars return GCH_ERR_PARAM.
- * All calls share the fixed array: calls that can overlap on the GPU race,
- * so issue them on one stream.  The first call on a device looks up the array's address;
- * make it before any stream capture.  Asynchronous on `stream`. */
+ * counterpart in the reference.  It exists for host codes that give the
+ * library a fixed, pre-sized memory budget and forbid hidden allocations (a
+ * late cudaMalloc can fail or fragment memory in the middle of a run), and
+ * for codes that own every device buffer through their own pool allocator.
+ * It allocates nothing: the caller passes u in device memory in the
+ * reference layout u(neq, 1-2:nx+2, 1-2:ny+2, 1-2:nz+2) (FP64, ghost cells
+ * filled) and device slots for the outputs dt and dump_flag; the per-block
+ * partial minima go to a fixed array inside the library (512 KiB on every
+ * GPU that loads it, kept until exit).  Same result as gch_get_timestep in
+ * FP64 arithmetic.  Limits: boxes with ceil(nx/32)*ceil(ny/8)*ceil(nz/8) >
+ * 65536 (beyond 512^3 cells) return GCH_ERR_TOO_LARGE.  GCH_ERR_PARAM for
+ * what the one-kernel reduction does not cover: any cooling (table cooling
+ * takes dt from the stored primitives, COOL_H needs the passive n_HI),
+ * passive scalars (npas != 0), and the split solver
+ * GCH_SOLVER_HLLE_SPLIT_ALL (its fast speeds need the background state of a
+ * domain).  All calls share the fixed array and each call clears its
+ * completion counter first: calls that can overlap on the GPU race, so
+ * issue them on one stream.  The first call on a device, and the first call
+ * after that device's context was destroyed and created again (e.g. by
+ * cudaDeviceReset), looks up the array's address; make that first call
+ * before any stream capture.  Asynchronous on `stream`. */
 int gch_get_timestep_noalloc(const gch_params_t* p, const double* u_dev, int current_iter,
                              int n_iter, double current_time, double tprint, double* dt_dev,
                              int* dump_dev, void* stream);

@@ -2,8 +2,9 @@
 guacho_gb300.binio, and what the reference's own Python reader
 (py/guacho_utils.py: read_header, readbin3d_block, u2prim) reads back from it.
 
-Run in the build container, where the reference sources are present:
-    python tests/golden/make_bin_golden.py /root/reference
+Run where the reference sources are present, giving the root of the
+reference checkout (the directory that holds py/guacho_utils.py):
+    python tests/golden/make_bin_golden.py <reference-root>
 The GPU-free test tests/test_binio.py compares against the stored arrays; it
 never imports the reference."""
 import importlib.util
@@ -51,4 +52,6 @@ def main(ref_root: str) -> None:
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    if len(sys.argv) != 2:
+        raise SystemExit("usage: make_bin_golden.py <reference-root>")
+    main(sys.argv[1])

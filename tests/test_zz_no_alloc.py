@@ -1,10 +1,11 @@
-"""gch_get_timestep_noalloc: the CFL timestep for callers that cannot
-allocate device memory (a time loop recorded with stream capture, or a host
-code that forbids hidden allocations).  The caller owns the state and the
-output slots; the library's only other memory is a fixed array compiled
-into it.  Checked through the C ABI against gch_get_timestep on the same
-state, on two calls in a row (the shared array must not carry anything from
-one call into the next).
+"""gch_get_timestep_noalloc: the CFL timestep for host codes that cannot
+allocate device memory (a driver with a fixed, pre-sized memory budget that
+forbids hidden allocations, or one that owns every device buffer through its
+own pool).  The caller owns the state and the output slots; the library's
+only other memory is a fixed array compiled into it.  Checked through the C
+ABI against gch_get_timestep on the same state, on two calls in a row (the
+shared array must not carry anything from one call into the next), and on a
+call whose step reaches the next output time (dt clipped, dump flag set).
 
 This file is named so that pytest collects it last."""
 import ctypes as C
@@ -89,3 +90,39 @@ def test_noalloc_rejects_oversized_box(gpu_lib):
     st = _noalloc(gpu_lib, p, u.data_ptr(), 1, 10, 0.0, 1.0, out_dt.data_ptr(),
                   out_dump.data_ptr())
     assert st == _abi.ERR_TOO_LARGE
+
+
+def test_noalloc_clips_to_output_time(gpu_lib):
+    """current_time + dt >= tprint: dt is clipped to tprint - current_time
+    and the dump flag is set (src/hydro_core.f90:691-694), as in
+    gch_get_timestep on the same state."""
+    import torch
+    from guacho_gb300.domain import Domain
+    p, u0 = problems.turbulence(24, seed=12)
+    p = p.replace(precision=P.FP64)
+    t = 0.125
+    with Domain(p) as d:
+        d.init(u0)
+        u = d.download()
+        dt_free, dump_free = d.get_timestep(20, 10, t, 1e30)
+        assert not dump_free
+        tprint = t + 0.5 * dt_free
+        dt_ref, dump_ref = d.get_timestep(20, 10, t, tprint)
+    assert dump_ref and dt_ref == tprint - t
+    dev = torch.device("cuda", 0)
+    out_dt = torch.zeros(1, dtype=torch.float64, device=dev)
+    out_dump = torch.zeros(1, dtype=torch.int32, device=dev)
+    u_dev = torch.from_numpy(u).to(dev)
+    torch.cuda.synchronize()
+    for _ in range(2):
+        st = _noalloc(gpu_lib, p, u_dev.data_ptr(), 20, 10, t, tprint, out_dt.data_ptr(),
+                      out_dump.data_ptr())
+        torch.cuda.synchronize()
+        assert st == 0
+        assert float(out_dt.item()) == dt_ref
+        assert bool(out_dump.item()) is True
+    # the same state without the clip gives the free dt again
+    st = _noalloc(gpu_lib, p, u_dev.data_ptr(), 20, 10, t, 1e30, out_dt.data_ptr(),
+                  out_dump.data_ptr())
+    torch.cuda.synchronize()
+    assert st == 0 and float(out_dt.item()) == dt_free and not bool(out_dump.item())
