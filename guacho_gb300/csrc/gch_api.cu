@@ -8,11 +8,55 @@
 #include <cmath>
 #include <new>
 
+#include <cuda.h>
+#include <cudaTypedefs.h>
+
 #include "gch_domain.h"
 
 using gch::EngineOps;
 using gch::KParams;
 using gch::StepScalars;
+
+namespace gch {
+
+// cuTensorMapEncodeTiled through the runtime's driver entry point (no link
+// against the driver library), looked up once.
+static PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = [] {
+    void* f = nullptr;
+    cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &f, 12000, cudaEnableDefault,
+                                         &q) != cudaSuccess ||
+        q != cudaDriverEntryPointSuccess)
+      f = nullptr;
+    return reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(f);
+  }();
+  return fn;
+}
+
+int encode_stage_map(unsigned char* map, const void* base, int es, const KParams& k, int box_x,
+                     int box_rows) {
+  static_assert(sizeof(CUtensorMap) == kTmaMapBytes, "tensor map size");
+  PFN_cuTensorMapEncodeTiled_v12000 enc = tensor_map_encoder();
+  if (!enc || (es != 4 && es != 8) || box_x * es % 16 != 0) return GCH_ERR_CUDA;
+  // dims fastest first: x (the NX cells of a row with ghosts; the row
+  // padding is never copied), field, y, z; strides in bytes of field, row,
+  // plane (multiples of 16: rows are padded to 4 elements)
+  const cuuint64_t dims[4] = {(cuuint64_t)k.NX, (cuuint64_t)k.neq, (cuuint64_t)k.NY,
+                              (cuuint64_t)k.NZ};
+  const cuuint64_t strides[3] = {(cuuint64_t)k.fs * es, (cuuint64_t)k.pitch * es,
+                                 (cuuint64_t)k.pitch * k.NY * es};
+  const cuuint32_t box[4] = {(cuuint32_t)box_x, (cuuint32_t)k.neq, (cuuint32_t)box_rows, 1};
+  const cuuint32_t estr[4] = {1, 1, 1, 1};
+  CUtensorMap* m = reinterpret_cast<CUtensorMap*>(map);
+  const CUresult r = enc(m, es == 8 ? CU_TENSOR_MAP_DATA_TYPE_UINT64 : CU_TENSOR_MAP_DATA_TYPE_FLOAT32,
+                         4, const_cast<void*>(base), dims, strides, box, estr,
+                         CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                         CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  return r == CUDA_SUCCESS ? GCH_OK : GCH_ERR_CUDA;
+}
+
+}  // namespace gch
 
 namespace {
 
@@ -236,6 +280,7 @@ int gch_destroy(gch_domain_t* d) {
   cudaFree(d->sph);
   cudaFree(d->grav);
   cudaFree(d->sc);
+  cudaFree(d->tmaps);
   cudaFree(d->stage);
   cudaFree(d->tcw);
   cudaFree(d->tc_min);
@@ -373,6 +418,27 @@ int gch_create(const gch_params_t* p, void* stream, gch_domain_t** out) {
     if (e == cudaSuccess) e = cudaMemcpy(gfd, gf, 4 * k.ngrav * sizeof(float), cudaMemcpyHostToDevice);
     k.grav = d->grav;
     k.gravf = gfd;
+  }
+  if (e == cudaSuccess && d->mode != GCH_FP64 && p->riemann_solver != GCH_SOLVER_HLLE_SPLIT_ALL) {
+    // TMA tensor maps of the FP32 stage kernels' sources: stage 1 reads u
+    // (8-byte FP64 or pair values) or, with table cooling, primit (FP32);
+    // stage 2 reads up (FP32)
+    e = cudaMalloc((void**)&d->tmaps, gch::kTmaCount * gch::kTmaMapBytes);
+    if (e == cudaSuccess) {
+      unsigned char maps[gch::kTmaCount * gch::kTmaMapBytes];
+      const void* s1 = d->prim_in ? d->primit : d->u;
+      const int es1 = d->prim_in ? (int)d->ts_size : (int)d->tu_size;
+      int r = gch::encode_stage_map(maps + gch::kTmaS1Rows * gch::kTmaMapBytes, s1, es1, k, 36, 1);
+      r |= gch::encode_stage_map(maps + gch::kTmaS1Sides * gch::kTmaMapBytes, s1, es1, k,
+                                 16 / es1, gch::TY);
+      r |= gch::encode_stage_map(maps + gch::kTmaS2Rows * gch::kTmaMapBytes, d->up,
+                                 (int)d->ts_size, k, 36, 1);
+      r |= gch::encode_stage_map(maps + gch::kTmaS2Sides * gch::kTmaMapBytes, d->up,
+                                 (int)d->ts_size, k, 16 / (int)d->ts_size, gch::TY);
+      if (r != GCH_OK) e = cudaErrorInvalidValue;
+      if (e == cudaSuccess) e = cudaMemcpy(d->tmaps, maps, sizeof(maps), cudaMemcpyHostToDevice);
+      k.tmaps = d->tmaps;
+    }
   }
   if (e == cudaSuccess) e = cudaMallocHost((void**)&d->sc_host, sizeof(StepScalars));
   if (e == cudaSuccess) {

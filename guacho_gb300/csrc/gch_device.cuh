@@ -139,6 +139,9 @@ struct KParams {
   const gch_sphere_t* sph;
   const double* grav;         // [4][ngrav]: GM, x, y, z
   const float* gravf;         // the same in FP32 (the FP32 paths)
+  // TMA tensor maps of the stage sources (FP32 paths; device memory,
+  // kTmaCount maps of 128 bytes, see gch_tma.cuh), null on the FP64 path
+  const unsigned char* tmaps;
 };
 
 // Scalars shared by the kernels of one step, resident in device memory so a

@@ -6,6 +6,7 @@
 #include <cuda_runtime.h>
 
 #include "gch_device.cuh"
+#include "gch_tma.cuh"
 #include "guacho_gb300.h"
 
 struct gch_domain {
@@ -28,6 +29,7 @@ struct gch_domain {
   double* tab = nullptr;        // [2][ntab]
   gch_sphere_t* sph = nullptr;
   double* grav = nullptr;       // [4][ngrav]
+  unsigned char* tmaps = nullptr;       // TMA tensor maps of the stage sources (FP32 paths)
   gch::StepScalars* sc = nullptr;       // device
   gch::StepScalars* sc_host = nullptr;  // pinned mirror
   double* stage = nullptr;      // device staging buffer, host layout (FP64 AoS)
@@ -92,6 +94,13 @@ struct GroupOps {
 };
 extern const GroupOps kGroupMixed;
 extern const GroupOps kGroupKahan;
+
+// Encode the 4-D TMA tensor map (x, field, y, z) of a stage source array
+// (es-byte elements, the domain's padded layout) with a box of `box_x`
+// cells x every field x `box_rows` rows x 1 plane into `map` (128 bytes);
+// GCH_OK or GCH_ERR_CUDA (gch_api.cu).
+int encode_stage_map(unsigned char* map, const void* base, int es, const KParams& k, int box_x,
+                     int box_rows);
 
 // Thermal conduction after a tstep of dt_CFL (gch_tc.cu): synchronises once.
 int tc_run(gch_domain* d, double dt_CFL);

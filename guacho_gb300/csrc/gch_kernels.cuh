@@ -20,6 +20,7 @@
 #include <type_traits>
 
 #include "gch_policy.cuh"
+#include "gch_tma.cuh"
 
 namespace gch {
 
@@ -78,51 +79,92 @@ template <class TC, int LIM>
 constexpr bool kPairedMuscl = sizeof(TC) == 4 &&
                               (LIM == GCH_LIMITER_VAN_LEER || LIM == GCH_LIMITER_MINMOD);
 
-// Shared memory of the stage kernel (dynamic: up to 72 KB in FP32).
-template <class TC, int NEQ, int STAGE>
+// Shared memory of the stage kernel (dynamic: up to 72 KB in FP32).  The
+// staged primitive plane P has two layouts:
+//  - field-major [q][y][x] (the FP64 path, staged by per-thread loads);
+//  - row-major [y][q][x] with a 128-byte multiple row stride (the FP32
+//    paths): a TMA box of one halo row of every field lands in one row of P,
+//    and each row starts 128-byte aligned as a TMA destination must.
+template <class TC, int NEQ, int STAGE, bool TMA>
 struct FluxSmem {
   static constexpr int H = STAGE == 1 ? 1 : 2;
   static constexpr int NQ = STAGE == 1 ? 1 : 3;
-  TC P[NEQ][TY + 2 * H][TX + 2 * H];
+  static constexpr int PW = TX + 2 * H;                       // staged row width
+  static constexpr int PH = TY + 2 * H;                       // staged rows
+  static constexpr int RS = (NEQ * PW * (int)sizeof(TC) + 127) / 128 * 128 / (int)sizeof(TC);
+  static constexpr int kP = TMA ? PH * RS : NEQ * PH * PW;
+  __device__ __forceinline__ static int pidx(int q, int y, int x) {
+    if constexpr (TMA) return y * RS + q * PW + x;
+    else return (q * PH + y) * PW + x;
+  }
+  TC P[kP];
   TC F[NEQ][TY][TX + 1];
   TC G[NEQ][TY + 1][TX];
   TC Hz[2][NEQ][TY][TX];
   TC Q[NQ][NEQ][TY][TX];
 };
 
-// Stored values on their way into the stage kernel, copied asynchronously
-// from global into shared memory (cp.async): the next plane's halo cell of
-// each halo thread and, where there is room, the next column value of each
-// thread.
+// Stored values on their way into the stage kernel's shared memory.
+//  TmaRows / TmaSides: the halo ring of a plane copied by TMA (FP32 paths).
+//  Rows: the whole halo row(s) below and above the tile, 36 cells wide (the
+//  box starts at the tile's x origin, 16-byte aligned), every field; the
+//  second stage lands its rows in P directly, the first stage (whose stored
+//  type differs from the compute type) in TmaRows.  Sides: the H columns left
+//  and right of the tile in a box 16 bytes wide, every field, TY rows.
+//  ColBuf: the next column value of each thread, copied by cp.async where
+//  there is room.
 template <class TIn, int NEQ, int H>
-struct HaloBuf {
-  TIn halo[NEQ][2 * H * (TX + TY)];
+struct TmaRows {
+  static constexpr int kRow = (NEQ * (TX + 4) * (int)sizeof(TIn) + 127) / 128 * 128;
+  unsigned char raw[2 * H][kRow];
+  __device__ __forceinline__ TIn& at(int strip_row, int q, int x) {
+    return reinterpret_cast<TIn*>(raw[strip_row])[q * (TX + 4) + x];
+  }
+};
+template <class TIn, int NEQ>
+struct TmaSides {
+  static constexpr int SW = 16 / (int)sizeof(TIn);  // cells per 16-byte box row
+  static constexpr int kSide = (TY * NEQ * 16 + 127) / 128 * 128;
+  unsigned char raw[2][kSide];
+  __device__ __forceinline__ TIn& at(int side, int y, int q, int c) {
+    return reinterpret_cast<TIn*>(raw[side])[(y * NEQ + q) * SW + c];
+  }
 };
 template <class TIn, int NEQ>
 struct ColBuf {
   TIn col[NEQ][TY][TX];
 };
 
-// The stage kernel's dynamic shared memory.  The FP32 first-order stage
-// stages its stored inputs with cp.async: no registers are held while they
-// are in flight, and the halo loads leave the start of a plane.  A block
-// stays within 64 KB, so that three blocks per SM leave L1 room for the
-// register spills and the halo reuse (the MHD stage with both buffers, at
-// 74 KB, ran 9% slower; hydro with both, and MHD with the halo buffer only,
-// run faster).  The limited stage and FP64 have no room at their occupancy.
+// The stage kernel's dynamic shared memory.  The FP32 paths stage the halo
+// ring of every plane by TMA (the copies of plane k+1 are in flight while
+// plane k is worked on: the first stage's raw rows and both stages' side
+// columns have their own buffer; the second stage's rows land in P once the
+// faces of the previous plane are done).  A block stays within 75 KB so that
+// three blocks fit on an SM; the first stage also copies the next column
+// value of each thread with cp.async where the block stays within 64 KB
+// (hydro), which leaves L1 room for the halo reuse.
 template <class Pol, int NEQ, int STAGE, bool PRIM_IN>
 struct FluxLayout {
   using TC = typename Ops<Pol>::TC;
   using TIn = typename Src<Pol, NEQ, STAGE, PRIM_IN>::TIn;
   static constexpr int H = STAGE == 1 ? 1 : 2;
-  static constexpr size_t kMain = (sizeof(FluxSmem<TC, NEQ, STAGE>) + 15) / 16 * 16;
-  static constexpr size_t kHalo = (sizeof(HaloBuf<TIn, NEQ, H>) + 15) / 16 * 16;
+  static constexpr bool kTma = sizeof(TC) == 4;
+  using SM = FluxSmem<TC, NEQ, STAGE, kTma>;
+  static constexpr size_t kMain = (sizeof(SM) + 127) / 128 * 128;
+  static constexpr size_t kRows = (kTma && STAGE == 1) ? sizeof(TmaRows<TIn, NEQ, H>) : 0;
+  static constexpr size_t kSides = kTma ? sizeof(TmaSides<TIn, NEQ>) : 0;
+  static constexpr size_t kBar = kTma ? 128 : 0;  // mbarrier + abort flag
   static constexpr size_t kCol = sizeof(ColBuf<TIn, NEQ>);
   static constexpr size_t kLimit = 64 * 1024;
-  static constexpr bool kFp32S1 = STAGE == 1 && sizeof(TC) == 4;
-  static constexpr bool kAsyncHalo = kFp32S1 && kMain + kHalo <= kLimit;
-  static constexpr bool kAsyncCol = kAsyncHalo && kMain + kHalo + kCol <= kLimit;
-  static constexpr size_t kBytes = kMain + (kAsyncHalo ? kHalo : 0) + (kAsyncCol ? kCol : 0);
+  static constexpr bool kAsyncCol =
+      STAGE == 1 && sizeof(TC) == 4 && kMain + kRows + kSides + kBar + kCol <= kLimit;
+  static constexpr size_t kBytes = kMain + kRows + kSides + kBar + (kAsyncCol ? kCol : 0);
+  // bytes of one plane's halo copies (full boxes, out-of-range cells filled)
+  static constexpr unsigned kTmaBytes =
+      (unsigned)(2 * H * NEQ * (TX + 4) * sizeof(TIn) + 2 * TY * NEQ * 16);
+  // (with passive scalars, NEQ = 10, the second stage holds two blocks per SM
+  // with or without the TMA buffers)
+  static_assert(!kTma || NEQ > 8 || kBytes <= 75 * 1024, "three blocks per SM");
 };
 
 // cp.async of one 4-, 8- or 16-byte value from global into shared memory,
@@ -169,17 +211,24 @@ flux_body(const KParams& p, const typename Src<Pol, NEQ, STAGE, PRIM_IN>::TIn* _
   using TC = typename Ops<Pol>::TC;
   using TD = typename std::conditional<STAGE == 1, typename Pol::TS, typename Pol::TU>::type;
   using S = Src<Pol, NEQ, STAGE, PRIM_IN>;
+  using TIn = typename S::TIn;
   if (!sc->active) return;
   constexpr int H = STAGE == 1 ? 1 : 2;
   constexpr int NRING = 2 * H * (TX + TY);
-  using SM = FluxSmem<TC, NEQ, STAGE>;
   using LAY = FluxLayout<Pol, NEQ, STAGE, PRIM_IN>;
-  constexpr bool AHALO = LAY::kAsyncHalo, ACOL = LAY::kAsyncCol;
-  extern __shared__ __align__(16) unsigned char smem_raw[];
+  using SM = typename LAY::SM;
+  constexpr bool TMA = LAY::kTma, ACOL = LAY::kAsyncCol;
+  extern __shared__ __align__(128) unsigned char smem_raw[];
   SM& sm = *reinterpret_cast<SM*>(smem_raw);
-  auto& sbh = *reinterpret_cast<HaloBuf<typename S::TIn, NEQ, H>*>(smem_raw + LAY::kMain);
-  auto& sbc = *reinterpret_cast<ColBuf<typename S::TIn, NEQ>*>(smem_raw + LAY::kMain + LAY::kHalo);
-  auto& sP = sm.P;    // primitive plane k with halo
+  auto& trows = *reinterpret_cast<TmaRows<TIn, NEQ, H>*>(smem_raw + LAY::kMain);
+  auto& tsides = *reinterpret_cast<TmaSides<TIn, NEQ>*>(smem_raw + LAY::kMain + LAY::kRows);
+  uint64_t* tbar = reinterpret_cast<uint64_t*>(smem_raw + LAY::kMain + LAY::kRows + LAY::kSides);
+  int* tabort = reinterpret_cast<int*>(tbar + 1);
+  auto& sbc = *reinterpret_cast<ColBuf<TIn, NEQ>*>(smem_raw + LAY::kMain + LAY::kRows +
+                                                   LAY::kSides + LAY::kBar);
+  // primitive plane k with halo: component q of the cell (x, y) of the
+  // staged plane, x and y counted from the halo's corner
+  auto sP = [&](int q, int y, int x) -> TC& { return sm.P[SM::pidx(q, y, x)]; };
   auto& sF = sm.F;    // x-face fluxes
   auto& sG = sm.G;    // y-face fluxes
   auto& sH = sm.Hz;   // z-face fluxes, slot (face+1/2)&1
@@ -241,40 +290,103 @@ flux_body(const KParams& p, const typename Src<Pol, NEQ, STAGE, PRIM_IN>::TIn* _
     hx = col < H ? col - H : TX + (col - H);
   }
 
+  // TMA staging of the halo ring (FP32 paths).  Warp 0 issues the copies of
+  // a plane: 2H rows of 36 cells (x from the tile origin i0, every field) and
+  // the left and right column boxes (16 bytes wide, TY rows); they complete
+  // on the mbarrier *tbar, whose phase flips once per plane.  Stage 1 copies
+  // into its raw buffers, which are free once the plane's halo is
+  // converted, so the copies of plane k+1 are issued right after plane k is
+  // staged.  Stage 2 copies its rows into P itself, free once the faces of
+  // the plane before are solved (or, when the update reads P's halo rows
+  // for the eight-wave div B, once that update is done).
+  // the right column box starts at the last 16-byte boundary at or before
+  // the tile's first right-halo cell
+  constexpr int XR = NG + TX + H - 1 - ((NG + TX + H - 1) % TmaSides<TIn, NEQ>::SW);
+  auto early2 = [&]() { return !(NEQ >= 8 && p.eight_wave); };
+  auto tma_issue = [&](int kk) {
+    if constexpr (TMA) {
+      if (tid < 32) {
+        const unsigned char* maps = p.tmaps + (STAGE == 1 ? kTmaS1Rows : kTmaS2Rows) * kTmaMapBytes;
+        if (tid == 0) mbar_arrive_expect_tx(tbar, LAY::kTmaBytes);
+        __syncwarp();
+        const int az = kk + NG;
+        if (tid < 2 * H) {  // halo row `tid` (0..H-1 below, H..2H-1 above)
+          const int ay = tid < H ? j0 + NG - H + tid : j0 + NG + TY + (tid - H);
+          void* dst;
+          if constexpr (STAGE == 1) dst = trows.raw[tid];
+          else dst = &sm.P[SM::pidx(0, tid < H ? tid : TY + tid, 0)];
+          tma_load_4d(dst, maps, tbar, i0, 0, ay, az);
+        } else if (tid < 2 * H + 2) {  // left / right columns
+          const int sd = tid - 2 * H;
+          tma_load_4d(tsides.raw[sd], maps + kTmaMapBytes, tbar, sd == 0 ? i0 : i0 + XR, 0, j0 + NG,
+                      az);
+        }
+      }
+    }
+  };
+  if constexpr (TMA) {
+    if (tid == 0) {
+      // a TMA destination must be 128-byte aligned: refuse to copy otherwise
+      *tabort = (smem_addr(smem_raw) & 127u) != 0;
+      if (!*tabort) {
+        mbar_init(tbar, 1);
+        mbar_init_fence();
+      }
+    }
+    __syncthreads();
+    if (*tabort) {
+      if (tid == 0) atomicOr(&sc->err, GCH_ERR_TIMEOUT);
+      return;
+    }
+    if (kb < ke) tma_issue(kb);
+  }
+  // the halo cell of this thread from the TMA copies, converted; stage 2 row
+  // cells are converted in place in P
+  auto halo_from_tma = [&]() {
+    TIn hv[NEQ];
+    const int c = hx + 2;  // column in a 36-wide row box (box origin i0 = tile x - 2)
+    if (hy < 0 || hy >= TY) {
+      const int r = hy < 0 ? hy + H : H + (hy - TY);  // strip row 0..2H-1
+      if constexpr (STAGE == 1) {
+#pragma unroll
+        for (int q = 0; q < NEQ; ++q) hv[q] = trows.at(r, q, c);
+      } else {
+#pragma unroll
+        for (int q = 0; q < NEQ; ++q) hv[q] = sP(q, hy + H, hx + H);
+      }
+    } else {
+      const int sd = hx < 0 ? 0 : 1;
+      const int cc = hx < 0 ? hx + 2 : NG + hx - XR;
+#pragma unroll
+      for (int q = 0; q < NEQ; ++q) hv[q] = tsides.at(sd, hy, q, cc);
+    }
+    TC pr[NEQ];
+    S::convert(p, hv, pr, pfl);
+#pragma unroll
+    for (int q = 0; q < NEQ; ++q) sP(q, hy + H, hx + H) = pr[q];
+  };
+
   // Stored values are fetched into registers before they are needed: the
   // next column value after the faces of a plane are solved (converted at
   // the start of the next iteration), and this plane's u before the barrier
   // that precedes the update.  Their load latency overlaps the barrier wait
-  // and the update instead of stalling the start of a plane.  (Fetching the
-  // next halo cell as well costs more in register spills than it saves.)
-  // With AHALO (ACOL) the next plane's halo cell (the next column value)
-  // goes to shared memory by cp.async instead, from the plane before kb on;
-  // each thread reads back only what it copied, after its own wait.
-  using TIn = typename S::TIn;
+  // and the update instead of stalling the start of a plane.  With ACOL the
+  // next column value goes to shared memory by cp.async instead; each thread
+  // reads back only what it copied, after its own wait.
   TIn colr[NEQ];
   auto fetch_col = [&](int az_) {
     const long long cc = gidx(axc, ayc, az_);
     if constexpr (ACOL) {
 #pragma unroll
       for (int q = 0; q < NEQ; ++q) cp_async(&sbc.col[q][ty][tx], src + q * p.fs + cc);
+      cp_async_commit();
     } else {
       S::fetch(p, src, cc, colr);
     }
   };
   fetch_col(k0 + NG + H);
-  if constexpr (AHALO) cp_async_commit();
   auto prefetch_next = [&](int k) {
-    if (k + 1 < ke) {
-      fetch_col(k + 1 + NG + H);
-      if constexpr (AHALO) {
-        if (has_halo && k + 1 >= kb) {
-          const long long hc = gidx(i0 + hx + NG, j0 + hy + NG, k + 1 + NG);
-#pragma unroll
-          for (int q = 0; q < NEQ; ++q) cp_async(&sbh.halo[q][tid], src + q * p.fs + hc);
-        }
-      }
-    }
-    if constexpr (AHALO) cp_async_commit();
+    if (k + 1 < ke) fetch_col(k + 1 + NG + H);
   };
 
   for (int k = k0; k < ke; ++k) {
@@ -282,12 +394,17 @@ flux_body(const KParams& p, const typename Src<Pol, NEQ, STAGE, PRIM_IN>::TIn* _
     const bool zface = k >= kb - 1;
     const bool zwork = STAGE == 1 ? zface : k >= kb - 2;
     const int az = k + NG;
-    if (plane) __syncthreads();  // readers of the previous plane are done
+    if (plane) {
+      if constexpr (TMA && STAGE == 2) fence_proxy_async_smem();
+      __syncthreads();  // readers of the previous plane are done
+      if constexpr (TMA && STAGE == 2)
+        if (!early2() && k > kb) tma_issue(k);
+    }
     // 1. the column ring shifts (centre <- p(k), p(k+1) <- p(k+2)) and the
     //    next plane of the column is formed from the fetched values
     {
-      if constexpr (AHALO) cp_async_wait_all();  // this thread's copies
       if constexpr (ACOL) {
+        cp_async_wait_all();  // this thread's copies
 #pragma unroll
         for (int q = 0; q < NEQ; ++q) colr[q] = sbc.col[q][ty][tx];
       }
@@ -295,7 +412,7 @@ flux_body(const KParams& p, const typename Src<Pol, NEQ, STAGE, PRIM_IN>::TIn* _
       S::convert(p, colr, nx_, pfl);
 #pragma unroll
       for (int q = 0; q < NEQ; ++q) {
-        sP[q][ty + H][tx + H] = sQ[0][q][ty][tx];
+        sP(q, ty + H, tx + H) = sQ[0][q][ty][tx];
         if (STAGE == 1) {
           sQ[0][q][ty][tx] = nx_[q];
         } else {
@@ -306,20 +423,32 @@ flux_body(const KParams& p, const typename Src<Pol, NEQ, STAGE, PRIM_IN>::TIn* _
     }
     if (plane) {
       //  the halo of plane k
-      if (has_halo) {
-        TC pr[NEQ];
-        if constexpr (AHALO) {
-          TIn hv[NEQ];
-#pragma unroll
-          for (int q = 0; q < NEQ; ++q) hv[q] = sbh.halo[q][tid];
-          S::convert(p, hv, pr, pfl);
-        } else {
-          S::load(p, src, gidx(i0 + hx + NG, j0 + hy + NG, az), pr, pfl);
+      if constexpr (TMA) {
+        const unsigned parity = (unsigned)(k - kb) & 1u;  // one phase per plane
+        if (has_halo) {
+          if (mbar_wait(tbar, parity)) halo_from_tma();
+          else *tabort = 1;
         }
+        fence_proxy_async_smem();  // the raw buffers are read: the next copy may overwrite
+        __syncthreads();
+        if (*tabort) {  // a copy did not arrive: report, drain, leave together
+          if (tid == 0) {
+            atomicOr(&sc->err, GCH_ERR_TIMEOUT);
+            mbar_wait(tbar, parity);
+          }
+          return;
+        }
+        if constexpr (STAGE == 1)
+          if (k + 1 < ke) tma_issue(k + 1);
+      } else {
+        if (has_halo) {
+          TC pr[NEQ];
+          S::load(p, src, gidx(i0 + hx + NG, j0 + hy + NG, az), pr, pfl);
 #pragma unroll
-        for (int q = 0; q < NEQ; ++q) sP[q][hy + H][hx + H] = pr[q];
+          for (int q = 0; q < NEQ; ++q) sP(q, hy + H, hx + H) = pr[q];
+        }
+        __syncthreads();
       }
-      __syncthreads();
     }
 
     // 2. all faces through one Riemann call site
@@ -348,7 +477,7 @@ flux_body(const KParams& p, const typename Src<Pol, NEQ, STAGE, PRIM_IN>::TIn* _
         if (STAGE == 1) {
 #pragma unroll
           for (int q = 0; q < NEQ; ++q) {
-            l[q] = sP[perm<2, NEQ>(q)][ty + H][tx + H];
+            l[q] = sP(perm<2, NEQ>(q), ty + H, tx + H);
             r[q] = sQ[0][perm<2, NEQ>(q)][ty][tx];
           }
         } else {
@@ -359,7 +488,7 @@ flux_body(const KParams& p, const typename Src<Pol, NEQ, STAGE, PRIM_IN>::TIn* _
           for (int q = 0; q < NEQ; ++q) {
             const int s = perm<2, NEQ>(q);
             const TC al = sQ[2][s][ty][tx], rr = sQ[1][s][ty][tx];
-            l[q] = sP[s][ty + H][tx + H];
+            l[q] = sP(s, ty + H, tx + H);
             r[q] = sQ[0][s][ty][tx];
             const TC dm = r[q] - l[q], dr = rr - r[q];
             const TC ar = average_t<LIM>(lim, dm, dr);
@@ -373,10 +502,10 @@ flux_body(const KParams& p, const typename Src<Pol, NEQ, STAGE, PRIM_IN>::TIn* _
         const int cy = fy + H, cl = fx - 1 + H;
 #pragma unroll
         for (int q = 0; q < NEQ; ++q) {
-          l[q] = sP[q][cy][cl];
-          r[q] = sP[q][cy][cl + 1];
+          l[q] = sP(q, cy, cl);
+          r[q] = sP(q, cy, cl + 1);
           if (STAGE == 2) {
-            const TC ll = sP[q][cy][cl - 1], rr = sP[q][cy][cl + 2];
+            const TC ll = sP(q, cy, cl - 1), rr = sP(q, cy, cl + 2);
             if constexpr (kPairedMuscl<TC, LIM>) {
               const float2 o = muscl_pair<LIM>(ll, l[q], r[q], rr);
               l[q] = o.x;
@@ -394,10 +523,10 @@ flux_body(const KParams& p, const typename Src<Pol, NEQ, STAGE, PRIM_IN>::TIn* _
 #pragma unroll
         for (int q = 0; q < NEQ; ++q) {
           const int s = perm<1, NEQ>(q);
-          l[q] = sP[s][cl][cx];
-          r[q] = sP[s][cl + 1][cx];
+          l[q] = sP(s, cl, cx);
+          r[q] = sP(s, cl + 1, cx);
           if (STAGE == 2) {
-            const TC ll = sP[s][cl - 1][cx], rr = sP[s][cl + 2][cx];
+            const TC ll = sP(s, cl - 1, cx), rr = sP(s, cl + 2, cx);
             if constexpr (kPairedMuscl<TC, LIM>) {
               const float2 o = muscl_pair<LIM>(ll, l[q], r[q], rr);
               l[q] = o.x;
@@ -424,7 +553,7 @@ flux_body(const KParams& p, const typename Src<Pol, NEQ, STAGE, PRIM_IN>::TIn* _
       }
     }
     if (!plane) {  // column-private work only: no barrier
-      if (NEQ >= 8) bzm = sP[7][ty + H][tx + H];
+      if (NEQ >= 8) bzm = sP(7, ty + H, tx + H);
       prefetch_next(k);
       continue;
     }
@@ -438,7 +567,10 @@ flux_body(const KParams& p, const typename Src<Pol, NEQ, STAGE, PRIM_IN>::TIn* _
       for (int q = 0; q < NEQ; ++q)
         if (upd(q)) uq[q] = u[q * p.fs + c];
     }
+    if constexpr (TMA && STAGE == 2) fence_proxy_async_smem();  // P read by the faces
     __syncthreads();
+    if constexpr (TMA && STAGE == 2)
+      if (early2() && k + 1 < ke) tma_issue(k + 1);  // P's halo rows are free now
     prefetch_next(k);
 
     // 3. cell update and E
@@ -451,7 +583,7 @@ flux_body(const KParams& p, const typename Src<Pol, NEQ, STAGE, PRIM_IN>::TIn* _
       if (src_terms) {
         TC pcen[NEQ];
 #pragma unroll
-        for (int q = 0; q < NEQ; ++q) pcen[q] = sP[q][ty + H][tx + H];
+        for (int q = 0; q < NEQ; ++q) pcen[q] = sP(q, ty + H, tx + H);
         // src/sources.f90:190-220 with the cell's stage primitives
         if (p.user_src && sizeof(TC) == 4) {
           // EXO/user_mod.f90:158-206 point masses, FP32 paths: positions,
@@ -495,8 +627,8 @@ flux_body(const KParams& p, const typename Src<Pol, NEQ, STAGE, PRIM_IN>::TIn* _
           // 2 dx in the compute type (doubling is exact in either type)
           const TC dx2 = TC(2) * par<TC>(p.dx, p.f_dx), dy2 = TC(2) * par<TC>(p.dy, p.f_dy),
                    dz2 = TC(2) * par<TC>(p.dz, p.f_dz);
-          const TC divB = (sP[5][ty + H][tx + H + 1] - sP[5][ty + H][tx + H - 1]) / dx2
-                          + (sP[6][ty + H + 1][tx + H] - sP[6][ty + H - 1][tx + H]) / dy2
+          const TC divB = (sP(5, ty + H, tx + H + 1) - sP(5, ty + H, tx + H - 1)) / dx2
+                          + (sP(6, ty + H + 1, tx + H) - sP(6, ty + H - 1, tx + H)) / dy2
                           + (bzp - bzm) / dz2;
           sv[1] = sv[1] - divB * pcen[5];
           sv[2] = sv[2] - divB * pcen[6];
@@ -535,7 +667,7 @@ flux_body(const KParams& p, const typename Src<Pol, NEQ, STAGE, PRIM_IN>::TIn* _
         }
       }
     }
-    if (NEQ >= 8) bzm = sP[7][ty + H][tx + H];
+    if (NEQ >= 8) bzm = sP(7, ty + H, tx + H);
   }
   raise_err(&sc->err, err);
 }
