@@ -230,6 +230,17 @@ def cpu_model() -> str:
 
 
 # ---------------------------------------------------------------------------
+def _tuning_record(t: dict) -> dict:
+    """The autotuner's choice and search for the JSON line: the stage
+    kernels' z-march depth and launch form (blocks_per_sm: resident blocks
+    per SM of the persistent work-queue grid, 0 = one block per work item),
+    and the stage-1 time of every pair tried."""
+    return {"grouped": t["grouped"], "kz": t["kz"], "blocks_per_sm": t["blocks_per_sm"],
+            "tile": "32x8 cells", "stage1_ms": [
+                {"kz": k, "blocks_per_sm": b, "ms": round(ms, 4)}
+                for (k, b), ms in sorted(t["grid"].items())]}
+
+
 def batched_run(args, precision: int) -> dict:
     """The batched configuration: nbox boxes of sizes drawn from
     {32,48,64,96}^3, each an Orszag-Tang box (B0 x U[0.5,2]) or a blast
@@ -269,7 +280,7 @@ def batched_run(args, precision: int) -> dict:
            "step_ms_p99": 1e3 * float(np.percentile(times, 99)),
            "timing": (f"host wall clock around one advance of {n_run} steps; p50/p99 over "
                       f"{n_single} synchronous single-step advances"),
-           "tuning": b.tuning()}
+           "tuning": _tuning_record(b.tuning())}
     # per-box error against FP64 boxes advanced the same number of steps
     b64 = Batch([p.replace(precision=P.FP64) for p, _ in boxes])
     for i, (_, u) in enumerate(boxes):

@@ -140,6 +140,7 @@ def lib() -> C.CDLL:
         "gch_batch_advance": (I, [P, I, I]),
         "gch_batch_time": (I, [P, DP, IP]),
         "gch_batch_tuning": (I, [P, IP, IP, I, IP, C.POINTER(C.c_float), IP]),
+        "gch_batch_tuning_grid": (I, [P, IP, IP, IP, I, IP, IP, C.POINTER(C.c_float), IP]),
         "gch_get_timestep_noalloc": (I, [C.POINTER(Params_t), P, I, I, D, D, P, P, P]),
     }
     for name, (res, args) in sig.items():
@@ -158,7 +159,7 @@ def exported_symbols() -> list[str]:
             "gch_profile_step", "gch_get_kz", "gch_set_kz", "gch_autotune",
             "gch_batch_create",
             "gch_batch_destroy", "gch_batch_upload", "gch_batch_download",
-            "gch_batch_advance", "gch_batch_time", "gch_batch_tuning",
+            "gch_batch_advance", "gch_batch_time", "gch_batch_tuning", "gch_batch_tuning_grid",
             "gch_get_timestep_noalloc"]
 
 

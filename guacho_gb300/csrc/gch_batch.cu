@@ -3,12 +3,17 @@
 //
 // Grouped mode (FP32 policies; no cooling, conduction, resistivity, passive
 // scalars or user spheres): one step of all boxes is one CUDA graph of grouped launches,
-// one launch per kernel of the step for up to 64 boxes (gch_group.cuh).
-// The z-march depth of the stage kernels is chosen by timing the stage-1
-// flux kernel over the whole batch for each candidate depth (the autotuner
-// runs once, before the first step; that kernel only writes the stage
-// arrays up and E, so timing it leaves the state untouched).  The loop state
-// of every box is gathered into one array and read back with one copy.
+// one launch per kernel of the step for up to 64 boxes (gch_group.cuh).  The
+// two stage kernels work (box, tile, z chunk) items, either one block per
+// item or as a persistent grid whose blocks pull items from a device
+// counter.  The autotuner picks the z-march depth of an item and the launch
+// form (one block per item, or 1, 2 or 3 resident blocks per SM) by timing
+// the stage-1 flux kernel over the whole batch for every pair (it runs once, before the first step; that kernel only
+// writes the stage arrays up and E, so timing it leaves the state
+// untouched).  The tile of a work item stays 32 x 8 cells: the stage
+// kernel's shared-memory layout and its TMA boxes are built for it.  The
+// loop state of every box is gathered into one array and read back with one
+// copy.
 //
 // Otherwise (FP64, or physics the grouped step does not carry) every box
 // runs its own captured step graph on its own stream.
@@ -62,8 +67,11 @@ struct gch_batch {
   cudaStream_t stream = nullptr;
   bool own_stream = false;
   int kz = 0;                                // 0 until the autotuner ran
+  int bps = 0;                               // stage kernels: persistent blocks per SM (0: one per item)
   std::vector<int> tune_kz;                  // candidates and their times
+  std::vector<int> tune_bps;
   std::vector<float> tune_ms;
+  int* queue = nullptr;                      // device work counter of the stage kernels
   cudaGraphExec_t graph = nullptr;
   StepScalars** sc_list = nullptr;           // device: the boxes' scalar blocks
   StepScalars* sc_all = nullptr;             // device gather buffer
@@ -80,8 +88,8 @@ bool groupable(const gch_params_t& p) {
 
 int grid_of(int n) { return (n + 127) / 128; }
 
-// Time the stage-1 flux kernel of all boxes for each candidate z-march
-// depth and keep the fastest.
+// Time the stage-1 flux kernel of all boxes for each candidate pair of
+// z-march depth and resident blocks per SM, and keep the fastest.
 int autotune(gch_batch* b) {
   const int n = (int)b->boxes.size();
   int nzmax = 1;
@@ -90,25 +98,32 @@ int autotune(gch_batch* b) {
   int st = cuda_ok(cudaEventCreate(&e0));
   st |= cuda_ok(cudaEventCreate(&e1));
   b->tune_kz.clear();
+  b->tune_bps.clear();
   b->tune_ms.clear();
   float best = 0.f;
-  int best_kz = std::min(8, nzmax);
+  int best_kz = std::min(8, nzmax), best_bps = 3;
   for (int kz : {2, 4, 8, 16, 32}) {
     if (kz > nzmax && kz != 2) break;
-    st |= b->gops->probe(b->boxes.data(), n, kz, b->stream);  // warm-up
-    st |= cuda_ok(cudaEventRecord(e0, b->stream));
-    for (int r = 0; r < 3; ++r) st |= b->gops->probe(b->boxes.data(), n, kz, b->stream);
-    st |= cuda_ok(cudaEventRecord(e1, b->stream));
-    st |= cuda_ok(cudaEventSynchronize(e1));
-    float ms = 0.f;
-    st |= cuda_ok(cudaEventElapsedTime(&ms, e0, e1));
-    if (st) break;
-    b->tune_kz.push_back(kz);
-    b->tune_ms.push_back(ms / 3);
-    if (b->tune_kz.size() == 1 || ms < best) {
-      best = ms;
-      best_kz = kz;
+    for (int bps : {0, 1, 2, 3}) {
+      st |= b->gops->probe(b->boxes.data(), n, kz, bps, b->queue, b->stream);  // warm-up
+      st |= cuda_ok(cudaEventRecord(e0, b->stream));
+      for (int r = 0; r < 3; ++r)
+        st |= b->gops->probe(b->boxes.data(), n, kz, bps, b->queue, b->stream);
+      st |= cuda_ok(cudaEventRecord(e1, b->stream));
+      st |= cuda_ok(cudaEventSynchronize(e1));
+      float ms = 0.f;
+      st |= cuda_ok(cudaEventElapsedTime(&ms, e0, e1));
+      if (st) break;
+      b->tune_kz.push_back(kz);
+      b->tune_bps.push_back(bps);
+      b->tune_ms.push_back(ms / 3);
+      if (b->tune_kz.size() == 1 || ms < best) {
+        best = ms;
+        best_kz = kz;
+        best_bps = bps;
+      }
     }
+    if (st) break;
   }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
@@ -116,6 +131,7 @@ int autotune(gch_batch* b) {
   k_batch_clear_info<<<grid_of(n), 128, 0, b->stream>>>(b->sc_list, n);
   st |= cuda_ok(cudaGetLastError());
   b->kz = best_kz;
+  b->bps = best_bps;
   return st;
 }
 
@@ -128,7 +144,7 @@ int grouped_advance(gch_batch* b, int steps, int n_iter) {
   if (!b->graph && !st) {
     cudaGraph_t g = nullptr;
     st |= cuda_ok(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
-    st |= b->gops->step(b->boxes.data(), n, b->kz, b->stream);
+    st |= b->gops->step(b->boxes.data(), n, b->kz, b->bps, b->queue, b->stream);
     st |= cuda_ok(cudaStreamEndCapture(b->stream, &g));
     if (st == GCH_OK) st |= cuda_ok(cudaGraphInstantiate(&b->graph, g, 0));
     if (g) cudaGraphDestroy(g);
@@ -157,6 +173,7 @@ int gch_batch_destroy(gch_batch_t* b) {
   if (b->graph) cudaGraphExecDestroy(b->graph);
   cudaFree(b->sc_list);
   cudaFree(b->sc_all);
+  cudaFree(b->queue);
   if (b->sc_all_host) cudaFreeHost(b->sc_all_host);
   if (b->stream && b->own_stream) cudaStreamDestroy(b->stream);
   for (gch_domain* d : b->boxes) gch_destroy(d);
@@ -204,6 +221,7 @@ int gch_batch_create(int n, const gch_params_t* params, void* stream, gch_batch_
     if (e == cudaSuccess) e = cudaMalloc((void**)&b->sc_list, n * sizeof(StepScalars*));
     if (e == cudaSuccess) e = cudaMalloc((void**)&b->sc_all, n * sizeof(StepScalars));
     if (e == cudaSuccess) e = cudaMallocHost((void**)&b->sc_all_host, n * sizeof(StepScalars));
+    if (e == cudaSuccess) e = cudaMalloc((void**)&b->queue, sizeof(int));
     if (e == cudaSuccess)
       e = cudaMemcpy(b->sc_list, sc.data(), n * sizeof(StepScalars*), cudaMemcpyHostToDevice);
     if (e != cudaSuccess) {
@@ -259,9 +277,28 @@ int gch_batch_tuning(gch_batch_t* b, int* grouped, int* kz, int cap, int* cand_k
   if (!b) return GCH_ERR_PARAM;
   if (grouped) *grouped = b->gops != nullptr;
   if (kz) *kz = b->gops ? b->kz : -1;
+  // the candidates timed with the chosen blocks per SM
+  int m = 0;
+  for (size_t i = 0; i < b->tune_kz.size() && m < cap; ++i) {
+    if (b->tune_bps[i] != b->bps) continue;
+    if (cand_kz) cand_kz[m] = b->tune_kz[i];
+    if (cand_ms) cand_ms[m] = b->tune_ms[i];
+    ++m;
+  }
+  if (ncand) *ncand = m;
+  return GCH_OK;
+}
+
+int gch_batch_tuning_grid(gch_batch_t* b, int* grouped, int* kz, int* bps, int cap,
+                          int* cand_kz, int* cand_bps, float* cand_ms, int* ncand) {
+  if (!b) return GCH_ERR_PARAM;
+  if (grouped) *grouped = b->gops != nullptr;
+  if (kz) *kz = b->gops ? b->kz : -1;
+  if (bps) *bps = b->gops ? b->bps : -1;
   const int m = std::min(cap, (int)b->tune_kz.size());
   for (int i = 0; i < m; ++i) {
     if (cand_kz) cand_kz[i] = b->tune_kz[i];
+    if (cand_bps) cand_bps[i] = b->tune_bps[i];
     if (cand_ms) cand_ms[i] = b->tune_ms[i];
   }
   if (ncand) *ncand = m;

@@ -86,11 +86,13 @@ extern const EngineOps kEngineKahan;
 // resistivity or user spheres, and are advanced on one stream.
 struct GroupOps {
   // one device-resident iteration of every box: k_cfl, k_dtfin, both
-  // stages with their CT and ghost fills, k_loopfin
-  int (*step)(gch_domain* const* boxes, int n, int kz, cudaStream_t s);
+  // stages with their CT and ghost fills, k_loopfin.  The stage kernels are
+  // persistent: `bps` blocks per SM pull (box, tile, z chunk) work items of
+  // `kz` planes from the device counter `queue` (cleared before each launch)
+  int (*step)(gch_domain* const* boxes, int n, int kz, int bps, int* queue, cudaStream_t s);
   // the stage-1 flux kernel alone (writes up and E, leaves u): the
   // autotuner's timing probe
-  int (*probe)(gch_domain* const* boxes, int n, int kz, cudaStream_t s);
+  int (*probe)(gch_domain* const* boxes, int n, int kz, int bps, int* queue, cudaStream_t s);
 };
 extern const GroupOps kGroupMixed;
 extern const GroupOps kGroupKahan;

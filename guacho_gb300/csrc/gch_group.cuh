@@ -47,16 +47,47 @@ __device__ __forceinline__ int group_box(const GroupArgs& g, int blk) {
   return lo;
 }
 
-// a0 = stage source, a1 = u, a2 = stage destination, a3 = E, a4 = s678
+// The stage kernel of many boxes (a0 = stage source, a1 = u, a2 = stage
+// destination, a3 = E, a4 = s678).  Work item b -- one (box, tile, z chunk),
+// numbered box by box from the box's blk0 on as the blocks of a one-box
+// grid -- is worked by one block.  Two launch forms:
+//  - k_flux_grp: one block per work item (the hardware hands out blocks);
+//  - k_flux_pst: a persistent grid of a few blocks per SM, each block taking
+//    the next item from the device counter `queue` (zero at launch) until
+//    all `total` items are done.  The block fetches its following item while
+//    it works the current one, so the counter's latency stays hidden.
+//    Blocks never wait on one another: a grid larger than what the SMs hold
+//    at once only starts its last blocks later.
 template <class Pol, int SOLVER, int NEQ, int STAGE, int LIM>
-__global__ void __launch_bounds__(NT, Pol::kMinBlocks) k_flux_grp(const __grid_constant__ GroupArgs g) {
+__device__ __forceinline__ void flux_item(const GroupArgs& g, int item) {
   using TIn = typename Src<Pol, NEQ, STAGE, false>::TIn;
   using TD = typename std::conditional<STAGE == 1, typename Pol::TS, typename Pol::TU>::type;
-  const GroupBox& x = g.box[group_box(g, blockIdx.x)];
-  const int l = blockIdx.x - x.blk0;
+  const GroupBox& x = g.box[group_box(g, item)];
+  const int l = item - x.blk0;
   flux_body<Pol, SOLVER, NEQ, STAGE, false, LIM>(
       x.p, (const TIn*)x.a0, (const typename Pol::TU*)x.a1, (TD*)x.a2, (typename Pol::TS*)x.a3,
       (typename Pol::TS*)x.a4, x.sc, x.kz, l % x.gx, (l / x.gx) % x.gy, l / (x.gx * x.gy));
+}
+template <class Pol, int SOLVER, int NEQ, int STAGE, int LIM>
+__global__ void __launch_bounds__(NT, Pol::kMinBlocks) k_flux_grp(const __grid_constant__ GroupArgs g) {
+  flux_item<Pol, SOLVER, NEQ, STAGE, LIM>(g, blockIdx.x);
+}
+template <class Pol, int SOLVER, int NEQ, int STAGE, int LIM>
+__global__ void __launch_bounds__(NT, Pol::kMinBlocks)
+    k_flux_pst(const __grid_constant__ GroupArgs g, int* queue, int total) {
+  __shared__ int s_item[2];
+  const bool lead = threadIdx.x == 0 && threadIdx.y == 0;
+  if (lead) s_item[0] = atomicAdd(queue, 1);
+  __syncthreads();
+  for (int slot = 0;; slot ^= 1) {
+    const int item = s_item[slot];
+    if (item >= total) break;
+    int next = 0;
+    if (lead) next = atomicAdd(queue, 1);  // its result is needed only after the item
+    flux_item<Pol, SOLVER, NEQ, STAGE, LIM>(g, item);
+    if (lead) s_item[slot ^ 1] = next;
+    __syncthreads();  // the item is finished with shared memory; the next index is set
+  }
 }
 
 // a1 = u, a2 = destination of B, a3 = E, a4 = s678

@@ -47,26 +47,51 @@ struct GroupEngine {
   }
 
   // ---- stage kernels ---------------------------------------------------------
+  // `blocks` work items: with bps = 0 one block per item, otherwise a
+  // persistent grid of min(blocks, bps x SMs) blocks pulling them from
+  // `queue`, which is cleared on the stream first.
+  static int sm_count() {
+    static int n = [] {
+      int dev = 0, v = 0;
+      if (cudaGetDevice(&dev) != cudaSuccess ||
+          cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+        v = 152;
+      return v > 0 ? v : 152;
+    }();
+    return n;
+  }
   template <int SOLVER, int NEQ, int STAGE, int LIM>
-  static void flux_lim(GroupArgs& g, unsigned blocks, cudaStream_t s) {
+  static void flux_lim(GroupArgs& g, unsigned blocks, int bps, int* queue, cudaStream_t s) {
     constexpr size_t smem = FluxLayout<Pol, NEQ, STAGE, false>::kBytes;
     static bool attr = false;  // once per instantiation
     if (!attr) {
       cudaFuncSetAttribute(k_flux_grp<Pol, SOLVER, NEQ, STAGE, LIM>,
                            cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      cudaFuncSetAttribute(k_flux_pst<Pol, SOLVER, NEQ, STAGE, LIM>,
+                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
       attr = true;
     }
-    if (blocks) k_flux_grp<Pol, SOLVER, NEQ, STAGE, LIM><<<blocks, dim3(TX, TY), smem, s>>>(g);
+    if (!blocks) return;
+    if (bps <= 0) {
+      k_flux_grp<Pol, SOLVER, NEQ, STAGE, LIM><<<blocks, dim3(TX, TY), smem, s>>>(g);
+      return;
+    }
+    const unsigned grid = std::min<unsigned>(blocks, (unsigned)(bps * sm_count()));
+    cudaMemsetAsync(queue, 0, sizeof(int), s);
+    k_flux_pst<Pol, SOLVER, NEQ, STAGE, LIM><<<grid, dim3(TX, TY), smem, s>>>(g, queue, (int)blocks);
   }
   template <int SOLVER, int NEQ, int STAGE>
-  static void flux_solver(GroupArgs& g, unsigned blocks, cudaStream_t s, int lim) {
-    if constexpr (STAGE == 1) flux_lim<SOLVER, NEQ, STAGE, kLimRuntime>(g, blocks, s);
-    else if (lim == GCH_LIMITER_MINMOD) flux_lim<SOLVER, NEQ, STAGE, GCH_LIMITER_MINMOD>(g, blocks, s);
-    else if (lim == GCH_LIMITER_VAN_LEER) flux_lim<SOLVER, NEQ, STAGE, GCH_LIMITER_VAN_LEER>(g, blocks, s);
-    else flux_lim<SOLVER, NEQ, STAGE, kLimRuntime>(g, blocks, s);
+  static void flux_solver(GroupArgs& g, unsigned blocks, int bps, int* queue, cudaStream_t s,
+                          int lim) {
+    if constexpr (STAGE == 1) flux_lim<SOLVER, NEQ, STAGE, kLimRuntime>(g, blocks, bps, queue, s);
+    else if (lim == GCH_LIMITER_MINMOD)
+      flux_lim<SOLVER, NEQ, STAGE, GCH_LIMITER_MINMOD>(g, blocks, bps, queue, s);
+    else if (lim == GCH_LIMITER_VAN_LEER)
+      flux_lim<SOLVER, NEQ, STAGE, GCH_LIMITER_VAN_LEER>(g, blocks, bps, queue, s);
+    else flux_lim<SOLVER, NEQ, STAGE, kLimRuntime>(g, blocks, bps, queue, s);
   }
   template <int STAGE>
-  static int flux(gch_domain* const* boxes, int n, int kz, cudaStream_t s) {
+  static int flux(gch_domain* const* boxes, int n, int kz, int bps, int* queue, cudaStream_t s) {
     const KParams& p0 = boxes[0]->kp;
     const int sv = p0.solver, neq = p0.neq, lim = p0.limiter;
     auto setup = [&](GroupBox& x, gch_domain* d) -> long long {
@@ -82,18 +107,16 @@ struct GroupEngine {
       return (long long)x.gx * x.gy * ((p.nz + x.kz - 1) / x.kz);
     };
     auto go = [&](auto launch) { return chunks(boxes, n, setup, launch); };
-    if (sv == GCH_SOLVER_HLLD && neq == 8)
-      return go([&](GroupArgs& g, unsigned b) { flux_solver<GCH_SOLVER_HLLD, 8, STAGE>(g, b, s, lim); });
-    if (sv == GCH_SOLVER_HLLC && neq == 5)
-      return go([&](GroupArgs& g, unsigned b) { flux_solver<GCH_SOLVER_HLLC, 5, STAGE>(g, b, s, lim); });
-    if (sv == GCH_SOLVER_HLLC && neq == 8)
-      return go([&](GroupArgs& g, unsigned b) { flux_solver<GCH_SOLVER_HLLC, 8, STAGE>(g, b, s, lim); });
-    if (sv == GCH_SOLVER_HLLE && neq == 8)
-      return go([&](GroupArgs& g, unsigned b) { flux_solver<GCH_SOLVER_HLLE, 8, STAGE>(g, b, s, lim); });
-    if (sv == GCH_SOLVER_HLL && neq == 5)
-      return go([&](GroupArgs& g, unsigned b) { flux_solver<GCH_SOLVER_HLL, 5, STAGE>(g, b, s, lim); });
-    if (sv == GCH_SOLVER_HLL && neq == 8)
-      return go([&](GroupArgs& g, unsigned b) { flux_solver<GCH_SOLVER_HLL, 8, STAGE>(g, b, s, lim); });
+#define GCH_GRP_FLUX(SV, NQ)                                                                  \
+    if (sv == SV && neq == NQ)                                                                \
+      return go([&](GroupArgs& g, unsigned b) { flux_solver<SV, NQ, STAGE>(g, b, bps, queue, s, lim); });
+    GCH_GRP_FLUX(GCH_SOLVER_HLLD, 8)
+    GCH_GRP_FLUX(GCH_SOLVER_HLLC, 5)
+    GCH_GRP_FLUX(GCH_SOLVER_HLLC, 8)
+    GCH_GRP_FLUX(GCH_SOLVER_HLLE, 8)
+    GCH_GRP_FLUX(GCH_SOLVER_HLL, 5)
+    GCH_GRP_FLUX(GCH_SOLVER_HLL, 8)
+#undef GCH_GRP_FLUX
     return GCH_ERR_PARAM;
   }
 
@@ -185,24 +208,25 @@ struct GroupEngine {
 
   // get_timestep + tstep + the loop tail of every box (Engine<Pol>::get_dt,
   // tstep and loopfin with resistivity, table cooling and spheres absent)
-  static int step(gch_domain* const* boxes, int n, int kz, cudaStream_t s) {
+  static int step(gch_domain* const* boxes, int n, int kz, int bps, int* queue, cudaStream_t s) {
     const KParams& p0 = boxes[0]->kp;
     const bool ctp = p0.neq >= 8 && p0.flux_cd;
     int st = GCH_OK;
     st |= cfl(boxes, n, kz, s);
     st |= scalar_tail(boxes, n, false, s);
-    st |= flux<1>(boxes, n, kz, s);
+    st |= flux<1>(boxes, n, kz, bps, queue, s);
     if (ctp) st |= ct<1>(boxes, n, s);
     st |= ghost<TS>(boxes, n, true, 2, s);
-    st |= flux<2>(boxes, n, kz, s);
+    st |= flux<2>(boxes, n, kz, bps, queue, s);
     if (ctp) st |= ct<2>(boxes, n, s);
     st |= ghost<TU>(boxes, n, false, 1, s);
     st |= scalar_tail(boxes, n, true, s);
     return st;
   }
 
-  static int probe(gch_domain* const* boxes, int n, int kz, cudaStream_t s) {
-    return flux<1>(boxes, n, kz, s);
+  static int probe(gch_domain* const* boxes, int n, int kz, int bps, int* queue,
+                   cudaStream_t s) {
+    return flux<1>(boxes, n, kz, bps, queue, s);
   }
 
   static constexpr GroupOps ops() { return GroupOps{&step, &probe}; }

@@ -264,12 +264,18 @@ class Batch:
         return list(t), list(it)
 
     def tuning(self) -> dict:
-        """Grouped mode, the z-march depth chosen by the autotuner and the
-        measured stage-1 time of each candidate depth."""
-        g, kz, n = C.c_int(), C.c_int(), C.c_int()
-        ck = (C.c_int * 16)()
-        cm = (C.c_float * 16)()
-        check("gch_batch_tuning", self._lib.gch_batch_tuning(self._h, C.byref(g), C.byref(kz),
-                                                              16, ck, cm, C.byref(n)))
-        return {"grouped": bool(g.value), "kz": kz.value,
-                "candidates": {int(ck[i]): float(cm[i]) for i in range(n.value)}}
+        """Grouped mode, the z-march depth and launch form chosen by the
+        autotuner (blocks_per_sm: resident blocks per SM of the persistent
+        stage kernels, 0 for one block per work item), and the measured
+        stage-1 time of every candidate pair ({(kz, blocks_per_sm): ms});
+        kz-only candidates at the chosen launch form under "candidates"."""
+        g, kz, bps, n = C.c_int(), C.c_int(), C.c_int(), C.c_int()
+        cap = 64
+        ck, cb = (C.c_int * cap)(), (C.c_int * cap)()
+        cm = (C.c_float * cap)()
+        check("gch_batch_tuning_grid", self._lib.gch_batch_tuning_grid(
+            self._h, C.byref(g), C.byref(kz), C.byref(bps), cap, ck, cb, cm, C.byref(n)))
+        grid = {(int(ck[i]), int(cb[i])): float(cm[i]) for i in range(n.value)}
+        return {"grouped": bool(g.value), "kz": kz.value, "blocks_per_sm": bps.value,
+                "candidates": {k: v for (k, b), v in grid.items() if b == bps.value},
+                "grid": grid}

@@ -321,10 +321,12 @@ typedef struct gch_batch gch_batch_t;
  * sizes, spacings, boundary kinds and problem data may differ.
  *
  * FP32 boxes without cooling, thermal conduction, resistivity, passive
- * scalars or user spheres are advanced in grouped mode on `stream` (0 = a stream of the
- * batch's own): one launch
- * per kernel of the step covers up to 64 boxes, one CUDA graph holds the
- * step, and the z-march depth is chosen by timing before the first step.
+ * scalars or user spheres are advanced in grouped mode on `stream` (0 = a
+ * stream of the batch's own): one launch per kernel of the step covers up to
+ * 64 boxes, the two stage kernels work (box, tile, z chunk) items either
+ * one block per item or as a persistent grid whose blocks pull items from
+ * a device counter, one CUDA graph holds the step, and the z-march depth of
+ * an item and the launch form are chosen by timing before the first step.
  * Other batches run each box's own step graph on its own stream.  No
  * reference counterpart: the reference advances one domain per process. */
 int gch_batch_create(int n, const gch_params_t* params, void* stream, gch_batch_t** out);
@@ -338,10 +340,17 @@ int gch_batch_advance(gch_batch_t* b, int steps, int n_iter);
 int gch_batch_time(gch_batch_t* b, double* times, int* iters);
 /* How the batch runs: grouped (1/0), the z-march depth the autotuner chose
  * (-1 when not grouped, 0 before the first advance) and up to `cap`
- * candidate depths with their measured stage-1 times in ms (ncand of them).
- * Any output pointer may be NULL. */
+ * candidate depths with their measured stage-1 times in ms (ncand of them)
+ * at the chosen resident blocks per SM.  Any output pointer may be NULL. */
 int gch_batch_tuning(gch_batch_t* b, int* grouped, int* kz, int cap, int* cand_kz,
                      float* cand_ms, int* ncand);
+/* The autotuner's whole search: grouped (1/0), the chosen z-march depth and
+ * launch form of the stage kernels (bps = resident blocks per SM of the
+ * persistent grid, 0 = one block per work item; both -1 when not grouped),
+ * and up to `cap` timed candidates (depth, bps, stage-1 ms).  Any output
+ * pointer may be NULL. */
+int gch_batch_tuning_grid(gch_batch_t* b, int* grouped, int* kz, int* bps, int cap,
+                          int* cand_kz, int* cand_bps, float* cand_ms, int* ncand);
 
 #ifdef __cplusplus
 }

@@ -1,8 +1,10 @@
 """Batched boxes through the C ABI (gch_batch_*).
 
 FP32 batches without cooling, resistivity or user spheres run in grouped
-mode: one launch per kernel of the step covers up to 64 boxes, and the
-z-march depth comes from the autotuner.  A box of a grouped batch must
+mode: one launch per kernel of the step covers up to 64 boxes, the stage
+kernels are persistent launches whose blocks pull (box, tile, z chunk) work
+items from a device counter (or one block per item), and the z-march depth
+and launch form come from the autotuner.  A box of a grouped batch must
 compute what the same box computes alone (the grouped kernels run the
 one-box kernel bodies), whatever depth the tuner picked and however the
 boxes are chunked.  The FP32 units are compiled with multiply-add
@@ -50,6 +52,12 @@ def test_grouped_batch_matches_single(gpu_lib, prec):
     b.advance(2)  # device-resident loop state carries over between calls
     tun = b.tuning()
     assert tun["grouped"] and tun["kz"] in tun["candidates"]
+    # the autotuner searched depth x resident blocks per SM of the
+    # persistent stage kernels and kept the fastest pair
+    assert tun["blocks_per_sm"] in (0, 1, 2, 3)
+    assert {b_ for _, b_ in tun["grid"]} == {0, 1, 2, 3}
+    best = min(tun["grid"], key=tun["grid"].get)
+    assert best == (tun["kz"], tun["blocks_per_sm"])
     times, iters = b.times()
     for i, (p, u) in enumerate(boxes):
         ref, t = _single(p, u, 5)
@@ -120,7 +128,8 @@ def test_fp64_batch_runs_per_box(gpu_lib):
     for i, (_, u) in enumerate(boxes):
         b.upload(i, u)
     b.advance(2)
-    assert b.tuning() == {"grouped": False, "kz": -1, "candidates": {}}
+    assert b.tuning() == {"grouped": False, "kz": -1, "blocks_per_sm": -1, "candidates": {},
+                          "grid": {}}
     for i, (p, u) in enumerate(boxes):
         ref, _ = _single(p, u, 2)
         assert np.array_equal(b.download(i), ref)
