@@ -151,6 +151,33 @@ def peaks() -> dict:
 STAGE2_KAHAN_TRAFFIC_PER_CELL = (1281077760 + 842317056) / 256 ** 3
 
 
+# The plain FP64 path is bound by the FP64 pipe, not by HBM.  ncu on the
+# 64^3 turbulence box (smsp/sm__inst_executed_pipe_fp64.sum per launch over
+# the 262,144 cells; sm__inst_executed_pipe_fp64.avg.pct_of_peak_sustained_active
+# with sm__cycles_elapsed.avg gives the pipe's peak issue rate):
+#   FP64-pipe warp instructions per zone-update of a whole step
+#   k_flux stage 1 44.83 + stage 2 78.03 + k_cfl 4.62 + k_ct 0.91 + 0.90
+FP64_PIPE_WARP_INST_PER_ZONE = 44.83 + 78.03 + 4.62 + 0.91 + 0.90
+#   peak: 0.0530 FP64-pipe warp instructions per SM cycle (stage 2: 20,456,302
+#   instructions over 152 SMs x 4,283,477 cycles at 59.27% of peak)
+FP64_PIPE_PEAK_PER_SM_CYCLE = 20456302 / (152 * 4283477.11) / 0.5927
+N_SM = 152
+
+
+def fp64_pipe_record(zone_updates_per_s: float, sm_mhz) -> dict:
+    """FP64-pipe utilisation of the plain FP64 step: the ncu instruction
+    count per zone-update times the live zone-update rate, over the pipe's
+    peak issue rate at the SM clock sampled during the run."""
+    mhz = sm_mhz or 2070.0
+    achieved = FP64_PIPE_WARP_INST_PER_ZONE * zone_updates_per_s / (N_SM * mhz * 1e6)
+    return {"bound": "fp64 pipe", "warp_inst_per_zone_update": FP64_PIPE_WARP_INST_PER_ZONE,
+            "achieved_per_sm_cycle": achieved, "peak_per_sm_cycle": FP64_PIPE_PEAK_PER_SM_CYCLE,
+            "frac": achieved / FP64_PIPE_PEAK_PER_SM_CYCLE, "sm_mhz": mhz,
+            "source": "FP64-pipe instruction counts per zone-update and the pipe's peak "
+                      "issue rate from ncu on the 64^3 turbulence box; zone-update rate and "
+                      "SM clock from this run"}
+
+
 def kernel_bytes_per_cell(prec: int, neq: int = 8) -> int:
     tu = 8  # FP64 u, or a (hi, lo) FP32 pair
     ts = 8 if prec == 0 else 4
@@ -598,6 +625,7 @@ def run_ours(args, dist: Dist) -> None:
                 "unit": "GB/s", "frac": ach / pk["hbm_gbs"], "traffic": traffic,
                 "bytes_per_cell": bpc, "launch_ms": means[dom],
                 "share_of_step": sum(prof[dom]) / total, "peak_source": pk["source"]}
+    mixed_value = dist.ws * n ** 3 * K / (variants[P.FP32_MIXED]["ms"] * 1e-3)
     sbz = step_bytes_per_zone(headline)
     step_gbs = value / dist.ws * sbz / 1e9
     step_roof = {"bytes_per_zone_update": sbz, "achieved": step_gbs, "peak": pk["hbm_gbs"],
@@ -627,9 +655,17 @@ def run_ours(args, dist: Dist) -> None:
         "data": "synthetic (seeded turbulence initial state, no dataset)",
         "config": bench_config(n, dist.ws),
         "fp64_plain": {"value": dist.ws * n ** 3 * k64 / (ms64 * 1e-3),
-                       "ms_per_step": ms64 / k64, "steps": k64},
-        "fp32_mixed_fp64u": {"value": dist.ws * n ** 3 * K / (variants[P.FP32_MIXED]["ms"] * 1e-3),
-                             "ms_per_step": variants[P.FP32_MIXED]["ms"] / K},
+                       "ms_per_step": ms64 / k64, "steps": k64,
+                       "roofline": fp64_pipe_record(n ** 3 * k64 / (ms64 * 1e-3),
+                                                    clk.get("sm_mhz"))},
+        "fp32_mixed_fp64u": {"value": mixed_value, "ms_per_step": variants[P.FP32_MIXED]["ms"] / K,
+                             "step_roofline": {
+                                 "bytes_per_zone_update": step_bytes_per_zone(P.FP32_MIXED),
+                                 "achieved": mixed_value / dist.ws
+                                             * step_bytes_per_zone(P.FP32_MIXED) / 1e9,
+                                 "peak": pk["hbm_gbs"], "unit": "GB/s",
+                                 "frac": mixed_value / dist.ws * step_bytes_per_zone(P.FP32_MIXED)
+                                         / 1e9 / pk["hbm_gbs"]}},
         "config_errors": configs_err,
         "batched": batched,
         "kernel_ms": {k: round(v, 4) for k, v in means.items()},
