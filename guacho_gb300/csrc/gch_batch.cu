@@ -1,8 +1,9 @@
 // gch_batch.cu -- many independent boxes of uneven size, each with its own
 // CFL dt, advanced together.
 //
-// Grouped mode (FP32 policies; no cooling, conduction, resistivity, passive
-// scalars or user spheres): one step of all boxes is one CUDA graph of grouped launches,
+// Grouped mode (FP32 policies; no COOL_H, conduction, resistivity or
+// passive scalars; table cooling and user spheres are carried): one step of
+// all boxes is one CUDA graph of grouped launches,
 // one launch per kernel of the step for up to 64 boxes (gch_group.cuh).  The
 // two stage kernels work (box, tile, z chunk) items, either one block per
 // item or as a persistent grid whose blocks pull items from a device
@@ -80,10 +81,12 @@ struct gch_batch {
 
 namespace {
 
+// FP32 boxes without resistivity, COOL_H, thermal conduction or passive
+// scalars; table cooling and user spheres run grouped too
 bool groupable(const gch_params_t& p) {
-  const bool prim_in = p.cooling == GCH_COOL_DMC || p.cooling == GCH_COOL_CHI;
-  return p.precision != GCH_FP64 && !prim_in && p.eta == 0.0 && !p.bc_user &&
-         p.th_cond == GCH_TC_OFF && p.cooling == GCH_COOL_NONE && p.npas == 0;
+  const bool table = p.cooling == GCH_COOL_DMC || p.cooling == GCH_COOL_CHI;
+  return p.precision != GCH_FP64 && p.eta == 0.0 && p.th_cond == GCH_TC_OFF &&
+         (p.cooling == GCH_COOL_NONE || table) && p.npas == 0;
 }
 
 int grid_of(int n) { return (n + 127) / 128; }

@@ -47,7 +47,8 @@ __device__ __forceinline__ int group_box(const GroupArgs& g, int blk) {
   return lo;
 }
 
-// The stage kernel of many boxes (a0 = stage source, a1 = u, a2 = stage
+// The stage kernel of many boxes (a0 = stage source: u, or primit with
+// table cooling, in stage 1 and up in stage 2; a1 = u, a2 = stage
 // destination, a3 = E, a4 = s678).  Work item b -- one (box, tile, z chunk),
 // numbered box by box from the box's blk0 on as the blocks of a one-box
 // grid -- is worked by one block.  Two launch forms:
@@ -58,21 +59,21 @@ __device__ __forceinline__ int group_box(const GroupArgs& g, int blk) {
 //    it works the current one, so the counter's latency stays hidden.
 //    Blocks never wait on one another: a grid larger than what the SMs hold
 //    at once only starts its last blocks later.
-template <class Pol, int SOLVER, int NEQ, int STAGE, int LIM>
+template <class Pol, int SOLVER, int NEQ, int STAGE, int LIM, bool PRIM_IN>
 __device__ __forceinline__ void flux_item(const GroupArgs& g, int item) {
-  using TIn = typename Src<Pol, NEQ, STAGE, false>::TIn;
+  using TIn = typename Src<Pol, NEQ, STAGE, PRIM_IN>::TIn;
   using TD = typename std::conditional<STAGE == 1, typename Pol::TS, typename Pol::TU>::type;
   const GroupBox& x = g.box[group_box(g, item)];
   const int l = item - x.blk0;
-  flux_body<Pol, SOLVER, NEQ, STAGE, false, LIM>(
+  flux_body<Pol, SOLVER, NEQ, STAGE, PRIM_IN, LIM>(
       x.p, (const TIn*)x.a0, (const typename Pol::TU*)x.a1, (TD*)x.a2, (typename Pol::TS*)x.a3,
       (typename Pol::TS*)x.a4, x.sc, x.kz, l % x.gx, (l / x.gx) % x.gy, l / (x.gx * x.gy));
 }
-template <class Pol, int SOLVER, int NEQ, int STAGE, int LIM>
+template <class Pol, int SOLVER, int NEQ, int STAGE, int LIM, bool PRIM_IN>
 __global__ void __launch_bounds__(NT, Pol::kMinBlocks) k_flux_grp(const __grid_constant__ GroupArgs g) {
-  flux_item<Pol, SOLVER, NEQ, STAGE, LIM>(g, blockIdx.x);
+  flux_item<Pol, SOLVER, NEQ, STAGE, LIM, PRIM_IN>(g, blockIdx.x);
 }
-template <class Pol, int SOLVER, int NEQ, int STAGE, int LIM>
+template <class Pol, int SOLVER, int NEQ, int STAGE, int LIM, bool PRIM_IN>
 __global__ void __launch_bounds__(NT, Pol::kMinBlocks)
     k_flux_pst(const __grid_constant__ GroupArgs g, int* queue, int total) {
   __shared__ int s_item[2];
@@ -84,7 +85,7 @@ __global__ void __launch_bounds__(NT, Pol::kMinBlocks)
     if (item >= total) break;
     int next = 0;
     if (lead) next = atomicAdd(queue, 1);  // its result is needed only after the item
-    flux_item<Pol, SOLVER, NEQ, STAGE, LIM>(g, item);
+    flux_item<Pol, SOLVER, NEQ, STAGE, LIM, PRIM_IN>(g, item);
     if (lead) s_item[slot ^ 1] = next;
     __syncthreads();  // the item is finished with shared memory; the next index is set
   }
@@ -122,13 +123,43 @@ __global__ void __launch_bounds__(128) k_ghost_grp(const __grid_constant__ Group
                 l / (x.gx * x.gy));
 }
 
-// a1 = u
-template <class Pol, int NEQ>
+// a1 = u, or primit with table cooling (PRIM_IN)
+template <class Pol, int NEQ, bool PRIM_IN>
 __global__ void __launch_bounds__(256) k_cfl_grp(const __grid_constant__ GroupArgs g) {
+  using TSrc = typename std::conditional<PRIM_IN, typename Pol::TS, typename Pol::TU>::type;
   const GroupBox& x = g.box[group_box(g, blockIdx.x)];
   const int l = blockIdx.x - x.blk0;
-  cfl_body<Pol, NEQ, false>(x.p, (const typename Pol::TU*)x.a1, x.sc, x.kz, l % x.gx,
-                            (l / x.gx) % x.gy, l / (x.gx * x.gy));
+  cfl_body<Pol, NEQ, PRIM_IN>(x.p, (const TSrc*)x.a1, x.sc, x.kz, l % x.gx, (l / x.gx) % x.gy,
+                              l / (x.gx * x.gy));
+}
+
+// The user boundary spheres of the boxes that have them: a2 = the array to
+// fill, i0 = blocks per sphere; a box's blocks are its spheres x i0
+template <class T>
+__global__ void __launch_bounds__(256) k_user_bc_grp(const __grid_constant__ GroupArgs g) {
+  const GroupBox& x = g.box[group_box(g, blockIdx.x)];
+  const int l = blockIdx.x - x.blk0;
+  user_bc_body<T>(x.p, (T*)x.a2, x.p.neq, x.sc, l / g.i0, l % g.i0, g.i0);
+}
+
+// Table cooling: a1 = u, a2 = primit; block (32, 8), one block per 32 x 8
+// tile of each interior plane
+template <class Pol, int NEQ>
+__global__ void __launch_bounds__(256) k_cool_grp(const __grid_constant__ GroupArgs g) {
+  const GroupBox& x = g.box[group_box(g, blockIdx.x)];
+  const int l = blockIdx.x - x.blk0;
+  cool_body<Pol, NEQ>(x.p, (typename Pol::TU*)x.a1, (typename Pol::TS*)x.a2, x.sc,
+                      (l % x.gx) * 32 + threadIdx.x, ((l / x.gx) % x.gy) * 8 + threadIdx.y,
+                      l / (x.gx * x.gy));
+}
+
+// calcprim of the ghost shell after boundaryI: a1 = u, a2 = primit,
+// i0 = blocks per box (grid-stride over the box's shell)
+template <class Pol, int NEQ>
+__global__ void __launch_bounds__(256) k_calcprim_shell_grp(const __grid_constant__ GroupArgs g) {
+  const GroupBox& x = g.box[group_box(g, blockIdx.x)];
+  calcprim_shell_body<Pol, NEQ>(x.p, (const typename Pol::TU*)x.a1, (typename Pol::TS*)x.a2,
+                                x.sc, blockIdx.x - x.blk0, g.i0);
 }
 
 // one thread per box

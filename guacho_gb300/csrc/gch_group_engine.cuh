@@ -60,43 +60,52 @@ struct GroupEngine {
     }();
     return n;
   }
-  template <int SOLVER, int NEQ, int STAGE, int LIM>
+  template <int SOLVER, int NEQ, int STAGE, int LIM, bool PRIM_IN>
   static void flux_lim(GroupArgs& g, unsigned blocks, int bps, int* queue, cudaStream_t s) {
-    constexpr size_t smem = FluxLayout<Pol, NEQ, STAGE, false>::kBytes;
+    constexpr size_t smem = FluxLayout<Pol, NEQ, STAGE, PRIM_IN>::kBytes;
     static bool attr = false;  // once per instantiation
     if (!attr) {
-      cudaFuncSetAttribute(k_flux_grp<Pol, SOLVER, NEQ, STAGE, LIM>,
+      cudaFuncSetAttribute(k_flux_grp<Pol, SOLVER, NEQ, STAGE, LIM, PRIM_IN>,
                            cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-      cudaFuncSetAttribute(k_flux_pst<Pol, SOLVER, NEQ, STAGE, LIM>,
+      cudaFuncSetAttribute(k_flux_pst<Pol, SOLVER, NEQ, STAGE, LIM, PRIM_IN>,
                            cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
       attr = true;
     }
     if (!blocks) return;
     if (bps <= 0) {
-      k_flux_grp<Pol, SOLVER, NEQ, STAGE, LIM><<<blocks, dim3(TX, TY), smem, s>>>(g);
+      k_flux_grp<Pol, SOLVER, NEQ, STAGE, LIM, PRIM_IN><<<blocks, dim3(TX, TY), smem, s>>>(g);
       return;
     }
     const unsigned grid = std::min<unsigned>(blocks, (unsigned)(bps * sm_count()));
     cudaMemsetAsync(queue, 0, sizeof(int), s);
-    k_flux_pst<Pol, SOLVER, NEQ, STAGE, LIM><<<grid, dim3(TX, TY), smem, s>>>(g, queue, (int)blocks);
+    k_flux_pst<Pol, SOLVER, NEQ, STAGE, LIM, PRIM_IN><<<grid, dim3(TX, TY), smem, s>>>(
+        g, queue, (int)blocks);
   }
+  // stage 1 reads u, or primit with table cooling (prim_in); stage 2 reads
+  // up and specialises minmod and van Leer
   template <int SOLVER, int NEQ, int STAGE>
   static void flux_solver(GroupArgs& g, unsigned blocks, int bps, int* queue, cudaStream_t s,
-                          int lim) {
-    if constexpr (STAGE == 1) flux_lim<SOLVER, NEQ, STAGE, kLimRuntime>(g, blocks, bps, queue, s);
-    else if (lim == GCH_LIMITER_MINMOD)
-      flux_lim<SOLVER, NEQ, STAGE, GCH_LIMITER_MINMOD>(g, blocks, bps, queue, s);
-    else if (lim == GCH_LIMITER_VAN_LEER)
-      flux_lim<SOLVER, NEQ, STAGE, GCH_LIMITER_VAN_LEER>(g, blocks, bps, queue, s);
-    else flux_lim<SOLVER, NEQ, STAGE, kLimRuntime>(g, blocks, bps, queue, s);
+                          int lim, bool prim_in) {
+    if constexpr (STAGE == 1) {
+      if (prim_in) flux_lim<SOLVER, NEQ, STAGE, kLimRuntime, true>(g, blocks, bps, queue, s);
+      else flux_lim<SOLVER, NEQ, STAGE, kLimRuntime, false>(g, blocks, bps, queue, s);
+    } else if (lim == GCH_LIMITER_MINMOD) {
+      flux_lim<SOLVER, NEQ, STAGE, GCH_LIMITER_MINMOD, false>(g, blocks, bps, queue, s);
+    } else if (lim == GCH_LIMITER_VAN_LEER) {
+      flux_lim<SOLVER, NEQ, STAGE, GCH_LIMITER_VAN_LEER, false>(g, blocks, bps, queue, s);
+    } else {
+      flux_lim<SOLVER, NEQ, STAGE, kLimRuntime, false>(g, blocks, bps, queue, s);
+    }
   }
   template <int STAGE>
   static int flux(gch_domain* const* boxes, int n, int kz, int bps, int* queue, cudaStream_t s) {
     const KParams& p0 = boxes[0]->kp;
     const int sv = p0.solver, neq = p0.neq, lim = p0.limiter;
+    const bool prim_in = boxes[0]->prim_in;
     auto setup = [&](GroupBox& x, gch_domain* d) -> long long {
       const KParams& p = d->kp;
-      x.a0 = STAGE == 1 ? d->u : d->up;  // u, or up for the second half step
+      // stage source: u (or primit) for the first half step, up for the second
+      x.a0 = STAGE == 1 ? (prim_in ? d->primit : d->u) : d->up;
       x.a1 = d->u;
       x.a2 = STAGE == 1 ? d->up : d->u;
       x.a3 = d->E;
@@ -107,9 +116,11 @@ struct GroupEngine {
       return (long long)x.gx * x.gy * ((p.nz + x.kz - 1) / x.kz);
     };
     auto go = [&](auto launch) { return chunks(boxes, n, setup, launch); };
-#define GCH_GRP_FLUX(SV, NQ)                                                                  \
-    if (sv == SV && neq == NQ)                                                                \
-      return go([&](GroupArgs& g, unsigned b) { flux_solver<SV, NQ, STAGE>(g, b, bps, queue, s, lim); });
+#define GCH_GRP_FLUX(SV, NQ)                                                               \
+    if (sv == SV && neq == NQ)                                                             \
+      return go([&](GroupArgs& g, unsigned b) {                                            \
+        flux_solver<SV, NQ, STAGE>(g, b, bps, queue, s, lim, prim_in);                     \
+      });
     GCH_GRP_FLUX(GCH_SOLVER_HLLD, 8)
     GCH_GRP_FLUX(GCH_SOLVER_HLLC, 5)
     GCH_GRP_FLUX(GCH_SOLVER_HLLC, 8)
@@ -144,8 +155,35 @@ struct GroupEngine {
         });
   }
 
+  // the user spheres of the boxes that have them, after a ghost fill
+  // (Engine<Pol>::ghost): blocks per sphere as the one-box launch's 4 x 152
+  // split over the boxes, at least 8
+  template <class T>
+  static int user_bc(gch_domain* const* boxes, int n, bool on_up, cudaStream_t s) {
+    bool any = false;
+    for (int i = 0; i < n; ++i) any = any || (boxes[i]->kp.bc_user && boxes[i]->kp.nsph > 0);
+    if (!any) return GCH_OK;
+    const int per = std::max(8, 4 * 152 / n);
+    return chunks(
+        boxes, n,
+        [&](GroupBox& x, gch_domain* d) -> long long {
+          const KParams& p = d->kp;
+          x.a2 = on_up ? d->up : d->u;
+          return (p.bc_user && p.nsph > 0) ? (long long)p.nsph * per : 0;
+        },
+        [&](GroupArgs& g, unsigned b) {
+          g.i0 = per;
+          if (b) k_user_bc_grp<T><<<b, 256, 0, s>>>(g);
+        });
+  }
+
   template <class T>
   static int ghost(gch_domain* const* boxes, int n, bool on_up, int layers, cudaStream_t s) {
+    return ghost_fill<T>(boxes, n, on_up, layers, s) | user_bc<T>(boxes, n, on_up, s);
+  }
+
+  template <class T>
+  static int ghost_fill(gch_domain* const* boxes, int n, bool on_up, int layers, cudaStream_t s) {
     bool all = true;
     for (int i = 0; i < n; ++i) all = all && ghost_all_ok(boxes[i]->kp, layers);
     if (all) {  // the whole shell of every box in one launch
@@ -182,18 +220,63 @@ struct GroupEngine {
     return st;
   }
 
+  // get_timestep's CFL pass: from u, or from primit with table cooling (the
+  // reference takes dt from the stored, cooled primitives)
   static int cfl(gch_domain* const* boxes, int n, int, cudaStream_t s) {
     const int neq = boxes[0]->kp.neq;
+    const bool prim_in = boxes[0]->prim_in;
     return chunks(
         boxes, n,
         [&](GroupBox& x, gch_domain* d) {
-          x.a1 = d->u;
+          x.a1 = prim_in ? d->primit : d->u;
           return column_setup(x, d->kp);
         },
         [&](GroupArgs& g, unsigned b) {
           if (!b) return;
-          if (neq == 8) k_cfl_grp<Pol, 8><<<b, dim3(32, 8), 0, s>>>(g);
-          else k_cfl_grp<Pol, 5><<<b, dim3(32, 8), 0, s>>>(g);
+          if (neq == 8 && prim_in) k_cfl_grp<Pol, 8, true><<<b, dim3(32, 8), 0, s>>>(g);
+          else if (neq == 8) k_cfl_grp<Pol, 8, false><<<b, dim3(32, 8), 0, s>>>(g);
+          else if (prim_in) k_cfl_grp<Pol, 5, true><<<b, dim3(32, 8), 0, s>>>(g);
+          else k_cfl_grp<Pol, 5, false><<<b, dim3(32, 8), 0, s>>>(g);
+        });
+  }
+
+  // table cooling of every box (updates u(5) and primit), one block per
+  // 32 x 8 tile of every interior plane
+  static int cool(gch_domain* const* boxes, int n, cudaStream_t s) {
+    const int neq = boxes[0]->kp.neq;
+    return chunks(
+        boxes, n,
+        [&](GroupBox& x, gch_domain* d) -> long long {
+          const KParams& p = d->kp;
+          x.a1 = d->u;
+          x.a2 = d->primit;
+          x.gx = (p.nx + 31) / 32;
+          x.gy = (p.ny + 7) / 8;
+          return (long long)x.gx * x.gy * p.nz;
+        },
+        [&](GroupArgs& g, unsigned b) {
+          if (!b) return;
+          if (neq == 8) k_cool_grp<Pol, 8><<<b, dim3(32, 8), 0, s>>>(g);
+          else k_cool_grp<Pol, 5><<<b, dim3(32, 8), 0, s>>>(g);
+        });
+  }
+
+  // primitives of every box's ghost shell after boundaryI (table cooling)
+  static int calcprim_shell(gch_domain* const* boxes, int n, cudaStream_t s) {
+    const int neq = boxes[0]->kp.neq;
+    const int per = std::max(4, 152 * 16 / n);
+    return chunks(
+        boxes, n,
+        [&](GroupBox& x, gch_domain* d) -> long long {
+          x.a1 = d->u;
+          x.a2 = d->primit;
+          return per;
+        },
+        [&](GroupArgs& g, unsigned b) {
+          if (!b) return;
+          g.i0 = per;
+          if (neq == 8) k_calcprim_shell_grp<Pol, 8><<<b, 256, 0, s>>>(g);
+          else k_calcprim_shell_grp<Pol, 5><<<b, 256, 0, s>>>(g);
         });
   }
 
@@ -207,10 +290,14 @@ struct GroupEngine {
   }
 
   // get_timestep + tstep + the loop tail of every box (Engine<Pol>::get_dt,
-  // tstep and loopfin with resistivity, table cooling and spheres absent)
+  // tstep and loopfin without resistivity, COOL_H or conduction): the
+  // stage-1 fluxes from primit and the cooling with the ghost-shell
+  // primitives after boundaryI when the boxes cool by table, the user
+  // spheres of each box after each ghost fill
   static int step(gch_domain* const* boxes, int n, int kz, int bps, int* queue, cudaStream_t s) {
     const KParams& p0 = boxes[0]->kp;
     const bool ctp = p0.neq >= 8 && p0.flux_cd;
+    const bool prim_in = boxes[0]->prim_in;
     int st = GCH_OK;
     st |= cfl(boxes, n, kz, s);
     st |= scalar_tail(boxes, n, false, s);
@@ -219,7 +306,9 @@ struct GroupEngine {
     st |= ghost<TS>(boxes, n, true, 2, s);
     st |= flux<2>(boxes, n, kz, bps, queue, s);
     if (ctp) st |= ct<2>(boxes, n, s);
+    if (prim_in) st |= cool(boxes, n, s);
     st |= ghost<TU>(boxes, n, false, 1, s);
+    if (prim_in) st |= calcprim_shell(boxes, n, s);
     st |= scalar_tail(boxes, n, true, s);
     return st;
   }

@@ -1000,10 +1000,11 @@ __global__ void k_ghost(KParams p, T* a, int neq, int axis, int layers, const St
 // User boundary spheres (EXO/exoplanet.f90:125-266 pattern) over the box
 // [lo, hi) of array coordinates of sphere `m`; the first sphere containing a
 // cell wins.
+// Body for block `blk` of the `nblk` blocks given to sphere `m`.
 template <class T>
-__global__ void k_user_bc(KParams p, T* a, int neq, const StepScalars* sc) {
+__device__ __forceinline__ void user_bc_body(const KParams& p, T* a, int neq,
+                                             const StepScalars* sc, int m, int blk, int nblk) {
   if (!sc->active) return;
-  const int m = blockIdx.y;
   const gch_sphere_t sp = p.sph[m];
   // bounding box of the sphere in array coordinates, clipped to the array
   auto lo_hi = [&](double c, double r, double d, int n, int N, int& lo, int& hi) {
@@ -1025,8 +1026,8 @@ __global__ void k_user_bc(KParams p, T* a, int neq, const StepScalars* sc) {
   const long long wx = xh - xl, wy = yh - yl, wz = zh - zl;
   if (wx <= 0 || wy <= 0 || wz <= 0) return;
   const long long total = wx * wy * wz;
-  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < total;
-       t += (long long)gridDim.x * blockDim.x) {
+  for (long long t = blk * (long long)blockDim.x + threadIdx.x; t < total;
+       t += (long long)nblk * blockDim.x) {
     const int ax = xl + (int)(t % wx);
     const int ay = yl + (int)((t / wx) % wy);
     const int az = zl + (int)(t / (wx * wy));
@@ -1069,6 +1070,11 @@ __global__ void k_user_bc(KParams p, T* a, int neq, const StepScalars* sc) {
     if (p.mhd) e = e + 0.5 * b2;
     a[4 * p.fs + c] = from_d<T>(e);
   }
+}
+// grid (blocks per sphere, nsph)
+template <class T>
+__global__ void k_user_bc(KParams p, T* a, int neq, const StepScalars* sc) {
+  user_bc_body<T>(p, a, neq, sc, blockIdx.y, blockIdx.x, gridDim.x);
 }
 
 // ---------------------------------------------------------------------------
@@ -1202,11 +1208,9 @@ __device__ __forceinline__ void cool_f32(const KParams& p, typename Pol::TU* u,
 // real(8)); the FP32 paths use cool_f32.  Writes primit of every interior
 // cell and u(5) of the cooled ones.
 template <class Pol, int NEQ>
-__global__ void k_cool(KParams p, typename Pol::TU* u, typename Pol::TS* primit,
-                       StepScalars* sc) {
-  const int ci = blockIdx.x * blockDim.x + threadIdx.x;
-  const int cj = blockIdx.y * blockDim.y + threadIdx.y;
-  const int ck = blockIdx.z;
+__device__ __forceinline__ void cool_body(const KParams& p, typename Pol::TU* u,
+                                          typename Pol::TS* primit, StepScalars* sc, int ci,
+                                          int cj, int ck) {
   if (ci >= p.nx || cj >= p.ny || !sc->active) return;
   const long long c = cell_index(p, ci + NG, cj + NG, ck + NG);
   if constexpr (!std::is_same<Pol, PolFP64>::value) {
@@ -1238,6 +1242,13 @@ __global__ void k_cool(KParams p, typename Pol::TU* u, typename Pol::TS* primit,
   }
 #pragma unroll
   for (int q = 0; q < NEQ; ++q) primit[q * p.fs + c] = (typename Pol::TS)pp[q];
+}
+// block (32, 8); grid (ceil(nx/32), ceil(ny/8), nz)
+template <class Pol, int NEQ>
+__global__ void k_cool(KParams p, typename Pol::TU* u, typename Pol::TS* primit,
+                       StepScalars* sc) {
+  cool_body<Pol, NEQ>(p, u, primit, sc, blockIdx.x * blockDim.x + threadIdx.x,
+                      blockIdx.y * blockDim.y + threadIdx.y, blockIdx.z);
 }
 
 // COOL_H (src/cooling_h.f90): non-equilibrium ionisation of hydrogen and
@@ -1505,14 +1516,14 @@ __device__ __forceinline__ void calcprim_cell(const KParams& p, const typename P
 // then the two y rows of every interior plane, then the two x cells of every
 // interior row; grid-stride.
 template <class Pol, int NEQ>
-__global__ void __launch_bounds__(256)
-k_calcprim_shell(KParams p, const typename Pol::TU* u, typename Pol::TS* primit,
-                 const StepScalars* sc) {
+__device__ __forceinline__ void calcprim_shell_body(const KParams& p, const typename Pol::TU* u,
+                                                    typename Pol::TS* primit,
+                                                    const StepScalars* sc, int blk, int nblk) {
   if (!sc->active) return;
   const long long mx = p.nx + 2, my = p.ny + 2;
   const long long cz = 2 * mx * my, cy = 2LL * p.nz * mx, cx = 2LL * p.nz * p.ny;
-  for (long long t = blockIdx.x * 256LL + threadIdx.x; t < cz + cy + cx;
-       t += (long long)gridDim.x * 256) {
+  for (long long t = blk * 256LL + threadIdx.x; t < cz + cy + cx;
+       t += (long long)nblk * 256) {
     int ax, ay, az;
     if (t < cz) {
       ax = NG - 1 + (int)(t % mx);
@@ -1532,6 +1543,12 @@ k_calcprim_shell(KParams p, const typename Pol::TU* u, typename Pol::TS* primit,
     }
     calcprim_cell<Pol, NEQ>(p, u, primit, cell_index(p, ax, ay, az));
   }
+}
+template <class Pol, int NEQ>
+__global__ void __launch_bounds__(256)
+k_calcprim_shell(KParams p, const typename Pol::TU* u, typename Pol::TS* primit,
+                 const StepScalars* sc) {
+  calcprim_shell_body<Pol, NEQ>(p, u, primit, sc, blockIdx.x, gridDim.x);
 }
 
 // calcprim over the whole array (src/hydro_core.f90:245-320); writes primit in

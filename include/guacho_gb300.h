@@ -320,8 +320,9 @@ typedef struct gch_batch gch_batch_t;
  * together.  All boxes must share precision, neq and the physics switches;
  * sizes, spacings, boundary kinds and problem data may differ.
  *
- * FP32 boxes without cooling, thermal conduction, resistivity, passive
- * scalars or user spheres are advanced in grouped mode on `stream` (0 = a
+ * FP32 boxes without COOL_H, thermal conduction, resistivity or passive
+ * scalars (table cooling and user spheres included) are advanced in
+ * grouped mode on `stream` (0 = a
  * stream of the batch's own): one launch per kernel of the step covers up to
  * 64 boxes, the two stage kernels work (box, tile, z chunk) items either
  * one block per item or as a persistent grid whose blocks pull items from

@@ -1,7 +1,7 @@
 """Batched boxes through the C ABI (gch_batch_*).
 
-FP32 batches without cooling, resistivity or user spheres run in grouped
-mode: one launch per kernel of the step covers up to 64 boxes, the stage
+FP32 batches without COOL_H, conduction, resistivity or passive scalars run
+in grouped mode (table cooling and user spheres included): one launch per kernel of the step covers up to 64 boxes, the stage
 kernels are persistent launches whose blocks pull (box, tile, z chunk) work
 items from a device counter (or one block per item), and the z-march depth
 and launch form come from the autotuner.  A box of a grouped batch must
@@ -13,6 +13,8 @@ and the one-box instantiation of a body, so FP32 boxes are compared to the
 single-domain run within a few FP32 roundings (`close`); an indexing or
 chunking error shows up as an O(1) difference.  FP64 boxes (per-box mode,
 no contraction) are compared bitwise."""
+import dataclasses
+
 import numpy as np
 import pytest
 
@@ -81,6 +83,33 @@ def test_grouped_batch_ragged_boxes(gpu_lib, prec):
     for i, (p, u) in enumerate(boxes):
         ref, _ = _single(p, u, 4)
         assert close(b.download(i), ref), f"box {dims[i]}"
+    b.close()
+
+
+@pytest.mark.parametrize("prec", [P.FP32_MIXED, P.FP32_KAHAN])
+def test_grouped_batch_wind_cooling(gpu_lib, prec):
+    """Boxes of the hydro wind problem (HLLC, outflow, table cooling, two
+    user spheres re-imposed at every boundary call) grouped: the stage-1
+    fluxes and the CFL pass read the stored primitives, cooling and the
+    ghost-shell primitives run after the stage-2 update, the spheres after
+    every ghost fill -- each box as it runs alone.  The boxes differ in size,
+    star density and wind speed."""
+    from guacho_gb300.domain import Batch
+    boxes = []
+    for n, dens, vscale in ((16, 1.0, 1.0), (20, 2.0, 0.5), (24, 0.5, 1.5)):
+        p, u = problems.wind_cooling(n, precision=prec)
+        star = p.spheres[0]
+        sph = [dataclasses.replace(star, dens=dens, vwind=star.vwind * vscale), p.spheres[1]]
+        boxes.append((p.replace(spheres=sph), u))
+    b = Batch([p for p, _ in boxes])
+    for i, (_, u) in enumerate(boxes):
+        b.upload(i, u)
+    b.advance(3)
+    b.advance(2)
+    assert b.tuning()["grouped"]
+    for i, (p, u) in enumerate(boxes):
+        ref, _ = _single(p, u, 5)
+        assert close(b.download(i), ref), f"box {i}"
     b.close()
 
 
