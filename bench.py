@@ -706,20 +706,24 @@ def run_configs(args) -> None:
     minmod, flux-CD, periodic), the low-beta blast 192^3 (outflow; pressure
     floor hits reported) and the hydro wind + table cooling box 256^3 (HLLC,
     user spheres re-imposed at every boundary call).  Device loop, CUDA
-    events, after `warmup` steps."""
+    events, after `warmup` steps.  Then one line per configuration with the
+    CPU oracle (all host threads) on the same box, a bounded number of steps
+    after one warm-up step."""
     from guacho_gb300 import build as gbuild
     gbuild.build(verbose=False)
     from guacho_gb300 import params as P
     from guacho_gb300 import problems
     from guacho_gb300.domain import Domain
+    from oracle.oracle import Oracle, build as obuild
     precs = {"fp64": P.FP64, "fp32_mixed_fp64u": P.FP32_MIXED, "fp32_kahan": P.FP32_KAHAN}
-    # every precision runs the same steps, so the floor counts compare
+    # every precision runs the same steps, so the floor counts compare;
+    # (name, problem, GPU steps, CPU oracle steps)
     cases = [
-        ("orszag_tang 128x128x4", lambda: problems.orszag_tang(128, 128, 4), 200),
-        ("low-beta blast 192^3", lambda: problems.blast(192), 50),
-        ("wind + table cooling 256^3 (hydro)", lambda: problems.wind_cooling(256), 50),
+        ("orszag_tang 128x128x4", lambda: problems.orszag_tang(128, 128, 4), 200, 40),
+        ("low-beta blast 192^3", lambda: problems.blast(192), 50, 5),
+        ("wind + table cooling 256^3 (hydro)", lambda: problems.wind_cooling(256), 50, 4),
     ]
-    for name, make, steps in cases:
+    for name, make, steps, _ in cases:
         p0, u0 = make()
         for pname, prec in precs.items():
             with Domain(p0.replace(precision=prec)) as d:
@@ -733,6 +737,29 @@ def run_configs(args) -> None:
                               "ms_per_step": ms / steps, "steps": steps,
                               "warmup": args.warmup, "pfloor_hits_last_step": pfloor,
                               "err_bits": err}), flush=True)
+    obuild()
+    threads = os.cpu_count() or 1
+    for name, make, _, csteps in cases:
+        p0, u0 = make()
+        o = Oracle(p0, threads=threads)
+        o.init(u0)
+        t, it = 0.0, 1
+        dt, _ = o.get_timestep(it, 10, t, 1e30)  # warm-up step
+        o.tstep(dt)
+        t += dt
+        it += 1
+        t0 = time.perf_counter()
+        for _ in range(csteps):
+            dt, _ = o.get_timestep(it, 10, t, 1e30)
+            o.tstep(dt)
+            t += dt
+            it += 1
+        el = time.perf_counter() - t0
+        cells = p0.nx * p0.ny * p0.nz
+        print(json.dumps({"config": name, "impl": "cpu oracle (FP64 C restatement)",
+                          "value": cells * csteps / el, "unit": UNIT,
+                          "ms_per_step": 1e3 * el / csteps, "steps": csteps,
+                          "cores": threads, "cpu": cpu_model()}), flush=True)
 
 
 def main():
