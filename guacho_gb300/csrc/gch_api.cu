@@ -308,6 +308,11 @@ int gch_create(const gch_params_t* p, void* stream, gch_domain_t** out) {
   d->hp = *p;
   d->mode = p->precision;
   d->prim_in = p->cooling == GCH_COOL_DMC || p->cooling == GCH_COOL_CHI;
+  // FP32 with FP64 u: get_timestep stores the primitives it recovers (in
+  // FP64 arithmetic) for the first stage, which otherwise recovers them
+  // again in one FP64-bound burst per plane.  (On the pair path the store
+  // costs more than the first stage saves.)
+  d->prim_pre = !d->prim_in && p->precision == GCH_FP32_MIXED;
   d->tu_size = 8;
   d->ts_size = d->mode == GCH_FP64 ? 8 : 4;
 
@@ -365,7 +370,7 @@ int gch_create(const gch_params_t* p, void* stream, gch_domain_t** out) {
   if (p->eta != 0.0) alloc(&d->w, fs * k.neq * d->tu_size);
   if (k.neq >= 8 && p->enable_flux_cd) alloc(&d->E, fs * 3 * d->ts_size);
   if (p->eight_wave) alloc(&d->s678, fs * 3 * d->ts_size);
-  if (d->prim_in) alloc(&d->primit, fs * k.neq * d->ts_size);
+  if (d->prim_in || d->prim_pre) alloc(&d->primit, fs * k.neq * d->ts_size);
   d->ncell_host = (size_t)k.NX * k.NY * k.NZ;
   alloc((void**)&d->stage, d->ncell_host * k.neq * sizeof(double));
   alloc((void**)&d->sc, sizeof(StepScalars));
@@ -420,21 +425,28 @@ int gch_create(const gch_params_t* p, void* stream, gch_domain_t** out) {
     k.gravf = gfd;
   }
   if (e == cudaSuccess && d->mode != GCH_FP64 && p->riemann_solver != GCH_SOLVER_HLLE_SPLIT_ALL) {
-    // TMA tensor maps of the FP32 stage kernels' sources: stage 1 reads u
-    // (8-byte FP64 or pair values) or, with table cooling, primit (FP32);
-    // stage 2 reads up (FP32)
+    // TMA tensor maps of the FP32 stage kernels' sources: stage 1 from u
+    // (8-byte FP64 or pair values) and, when the domain keeps them (table
+    // cooling, or the primitives get_timestep stores), from primit (FP32);
+    // stage 2 from up (FP32).  Maps of an array the domain does not have
+    // stay zero and are never used.
     e = cudaMalloc((void**)&d->tmaps, gch::kTmaCount * gch::kTmaMapBytes);
     if (e == cudaSuccess) {
-      unsigned char maps[gch::kTmaCount * gch::kTmaMapBytes];
-      const void* s1 = d->prim_in ? d->primit : d->u;
-      const int es1 = d->prim_in ? (int)d->ts_size : (int)d->tu_size;
-      int r = gch::encode_stage_map(maps + gch::kTmaS1Rows * gch::kTmaMapBytes, s1, es1, k, 36, 1);
-      r |= gch::encode_stage_map(maps + gch::kTmaS1Sides * gch::kTmaMapBytes, s1, es1, k,
-                                 16 / es1, gch::TY);
-      r |= gch::encode_stage_map(maps + gch::kTmaS2Rows * gch::kTmaMapBytes, d->up,
-                                 (int)d->ts_size, k, 36, 1);
-      r |= gch::encode_stage_map(maps + gch::kTmaS2Sides * gch::kTmaMapBytes, d->up,
-                                 (int)d->ts_size, k, 16 / (int)d->ts_size, gch::TY);
+      alignas(64) unsigned char maps[gch::kTmaCount * gch::kTmaMapBytes];
+      memset(maps, 0, sizeof(maps));
+      const int esu = (int)d->tu_size, ess = (int)d->ts_size;
+      int r = gch::encode_stage_map(maps + gch::kTmaS1Rows * gch::kTmaMapBytes, d->u, esu, k, 36, 1);
+      r |= gch::encode_stage_map(maps + gch::kTmaS1Sides * gch::kTmaMapBytes, d->u, esu, k,
+                                 16 / esu, gch::TY);
+      if (d->primit) {
+        r |= gch::encode_stage_map(maps + gch::kTmaS1PRows * gch::kTmaMapBytes, d->primit, ess, k,
+                                   36, 1);
+        r |= gch::encode_stage_map(maps + gch::kTmaS1PSides * gch::kTmaMapBytes, d->primit, ess,
+                                   k, 16 / ess, gch::TY);
+      }
+      r |= gch::encode_stage_map(maps + gch::kTmaS2Rows * gch::kTmaMapBytes, d->up, ess, k, 36, 1);
+      r |= gch::encode_stage_map(maps + gch::kTmaS2Sides * gch::kTmaMapBytes, d->up, ess, k,
+                                 16 / ess, gch::TY);
       if (r != GCH_OK) e = cudaErrorInvalidValue;
       if (e == cudaSuccess) e = cudaMemcpy(d->tmaps, maps, sizeof(maps), cudaMemcpyHostToDevice);
       k.tmaps = d->tmaps;

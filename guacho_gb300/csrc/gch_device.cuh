@@ -158,7 +158,10 @@ struct StepScalars {
   int dump;                   // dump flag of the last get_timestep
   int err;                    // GCH_ERR_* bits raised on the device
   int active;                 // loop condition of the device time loop
-  int pad;
+  // 1 while primit holds the primitives of the current u (interior and the
+  // one-cell ghost shell), stored by get_timestep's CFL pass; cleared
+  // when u changes (the end of tstep, an upload, a boundary fill)
+  int prim_fresh;
   unsigned long long pfloor;  // pressure-floor hits (u2prim)
   // dt/dx, dt/dy, dt/dz of stage 1 (dtm = dt/2) and stage 2 (dt), computed
   // once per step exactly as src/hydro_solver.f90:91-93 does

@@ -16,6 +16,9 @@ struct gch_domain {
   bool own_stream = false;      // created here (destroyed with the domain)
   int mode = GCH_FP64;
   bool prim_in = false;         // tabulated cooling keeps a primit array
+  // FP32 paths otherwise: get_timestep's CFL pass stores the primitives of u
+  // in primit for the first stage of the same step (StepScalars::prim_fresh)
+  bool prim_pre = false;
   size_t tu_size = 8, ts_size = 8;
   // device arrays
   void* u = nullptr;            // neq fields, TU

@@ -104,6 +104,13 @@ struct Engine {
     }
   }
 
+  // grid-stride launches over the one-cell ghost shell
+  static unsigned shell_grid(const KParams& p) {
+    const long long ns = (long long)(p.nx + 2) * (p.ny + 2) * (p.nz + 2) -
+                         (long long)p.nx * p.ny * p.nz;
+    return (unsigned)std::min<long long>((ns + 255) / 256, 152 * 16);
+  }
+
   // ---- get_timestep --------------------------------------------------------
   // the CFL min over the interior (k_cfl), then dt from it (k_dtfin)
   static int get_dt(gch_domain* d) {
@@ -117,10 +124,18 @@ struct Engine {
       });
     } else {
       with_neq(p.neq, [&](auto N) {
-        k_cfl<Pol, decltype(N)::value, false><<<cgrid, block, 0, d->stream>>>(p, (const TU*)d->u, d->sc, kzc);
+        k_cfl<Pol, decltype(N)::value, false><<<cgrid, block, 0, d->stream>>>(
+            p, (const TU*)d->u, d->sc, kzc, d->prim_pre ? (TS*)d->primit : nullptr);
       });
     }
     gch_mark(d, "k_cfl");
+    if (d->prim_pre) {  // the ghost shell's primitives too; then they are fresh
+      with_neq(p.neq, [&](auto N) {
+        k_prim_shell_own<Pol, decltype(N)::value><<<shell_grid(p), 256, 0, d->stream>>>(
+            p, (const TU*)d->u, (TS*)d->primit, d->sc);
+      });
+      gch_mark(d, "k_prim_shell");
+    }
     k_dtfin<<<1, 1, 0, d->stream>>>(d->sc, p.cfl, p.dx, p.dy, p.dz);
     gch_mark(d, "k_dtfin");
     return cuda_status(cudaGetLastError());
@@ -135,8 +150,17 @@ struct Engine {
     d->launches = 0;
     const bool ct = p.neq >= 8 && p.flux_cd;
     const dim3 cgrid = cell_grid(p), cblock(32, 8);
-    // 1st half step: first-order fluxes, up = u - dtm*divF
-    if (d->prim_in) st |= flux<1, true>(d, d->primit, d->up);
+    // 1st half step: first-order fluxes, up = u - dtm*divF (from the stored
+    // primitives with table cooling, or those get_timestep stored for this u)
+    if (d->prim_pre) {
+      with_neq(p.neq, [&](auto N) {
+        k_prim_refresh<Pol, decltype(N)::value><<<152 * 4, 256, 0, d->stream>>>(
+            p, (const TU*)d->u, (TS*)d->primit, d->sc);
+      });
+      ++d->launches;
+      gch_mark(d, "k_prim_refresh");
+    }
+    if (d->prim_in || d->prim_pre) st |= flux<1, true>(d, d->primit, d->up);
     else st |= flux<1, false>(d, d->u, d->up);
     ++d->launches;
     gch_mark(d, "k_flux_stage1");
@@ -184,6 +208,7 @@ struct Engine {
     }
     // boundaryI on u (+ user spheres), then primitives of the ghost shell
     ghost<TU>(d, (TU*)d->u, 1);
+    if (d->prim_pre) clear_prim_fresh(d);  // u has changed
     if (d->prim_in) {  // primitives of the ghost shell (interior ones come from k_cool)
       const long long ns = (long long)(p.nx + 2) * (p.ny + 2) * (p.nz + 2) -
                            (long long)p.nx * p.ny * p.nz;
@@ -199,8 +224,13 @@ struct Engine {
     return st;
   }
 
+  static void clear_prim_fresh(gch_domain* d) {
+    cudaMemsetAsync(&d->sc->prim_fresh, 0, sizeof(int), d->stream);
+  }
+
   static int boundaryI(gch_domain* d) {
     ghost<TU>(d, (TU*)d->u, 1);
+    if (d->prim_pre) clear_prim_fresh(d);
     return cuda_status(cudaGetLastError());
   }
 
@@ -219,6 +249,7 @@ struct Engine {
   // host layout <-> u: `aos` is the staging buffer or mapped host memory
   static constexpr int kLayoutGrid = 152 * 8;
   static int upload(gch_domain* d, const double* aos) {
+    if (d->prim_pre) clear_prim_fresh(d);
     k_aos_to_soa<TU><<<kLayoutGrid, kLayoutCells, 0, d->stream>>>(d->kp, aos, (TU*)d->u, d->kp.neq);
     return cuda_status(cudaGetLastError());
   }
@@ -249,7 +280,8 @@ struct Engine {
   // the stage-1 flux kernel alone: it writes the stage arrays up and E and
   // leaves u and primit unchanged (the autotuner times it)
   static int probe(gch_domain* d) {
-    int st = d->prim_in ? flux<1, true>(d, d->primit, d->up) : flux<1, false>(d, d->u, d->up);
+    int st = (d->prim_in || d->prim_pre) ? flux<1, true>(d, d->primit, d->up)
+                                         : flux<1, false>(d, d->u, d->up);
     return st | cuda_status(cudaGetLastError());
   }
 

@@ -306,7 +306,11 @@ flux_body(const KParams& p, const typename Src<Pol, NEQ, STAGE, PRIM_IN>::TIn* _
   auto tma_issue = [&](int kk) {
     if constexpr (TMA) {
       if (tid < 32) {
-        const unsigned char* maps = p.tmaps + (STAGE == 1 ? kTmaS1Rows : kTmaS2Rows) * kTmaMapBytes;
+        constexpr int kRowsMap = STAGE == 2 ? kTmaS2Rows : (PRIM_IN ? kTmaS1PRows : kTmaS1Rows);
+        static_assert(kRowsMap + 1 == (STAGE == 2 ? kTmaS2Sides
+                                                  : (PRIM_IN ? kTmaS1PSides : kTmaS1Sides)),
+                      "a source's side map follows its row map");
+        const unsigned char* maps = p.tmaps + kRowsMap * kTmaMapBytes;
         if (tid == 0) mbar_arrive_expect_tx(tbar, LAY::kTmaBytes);
         __syncwarp();
         const int az = kk + NG;
@@ -1083,11 +1087,14 @@ __global__ void k_user_bc(KParams p, T* a, int neq, const StepScalars* sc) {
 // CFL reduction (src/hydro_core.f90:644-675): per-cell candidate, warp
 // shuffle min, one atomicMin per block on the bits of the positive double.
 
+// With `store` (u as the source) every interior cell's primitives are also
+// written to `store` in the stage type: the first stage of the same step
+// then reads them instead of recovering them again.
 template <class Pol, int NEQ, bool PRIM_IN>
 __device__ __forceinline__ void
 cfl_body(const KParams& p,
          const typename std::conditional<PRIM_IN, typename Pol::TS, typename Pol::TU>::type* src,
-         StepScalars* sc, int kz, int bx, int by, int bz) {
+         StepScalars* sc, int kz, int bx, int by, int bz, typename Pol::TS* store = nullptr) {
   using TC = typename Ops<Pol>::TC;
   if (!sc->active) return;
   const int ci = bx * 32 + threadIdx.x;
@@ -1106,6 +1113,10 @@ cfl_body(const KParams& p,
         Ops<Pol>::template load_stored_prim<NEQ>(p, src, c, pr);
       else
         Ops<Pol>::template load_prim<NEQ>(p, src, c, pr, pfl);
+      if (!PRIM_IN && store) {
+#pragma unroll
+        for (int q = 0; q < NEQ; ++q) store[q * p.fs + c] = (typename Pol::TS)pr[q];
+      }
       cfl_candidate<TC, NEQ>(p, kc, pr, dtp, bad);
     }
     if (pfl) atomicAdd(&sc->pfloor, (unsigned long long)pfl);
@@ -1117,8 +1128,8 @@ cfl_body(const KParams& p,
 template <class Pol, int NEQ, bool PRIM_IN>
 __global__ void __launch_bounds__(256)
 k_cfl(KParams p, const typename std::conditional<PRIM_IN, typename Pol::TS, typename Pol::TU>::type* src,
-      StepScalars* sc, int kz) {
-  cfl_body<Pol, NEQ, PRIM_IN>(p, src, sc, kz, blockIdx.x, blockIdx.y, blockIdx.z);
+      StepScalars* sc, int kz, typename Pol::TS* store = nullptr) {
+  cfl_body<Pol, NEQ, PRIM_IN>(p, src, sc, kz, blockIdx.x, blockIdx.y, blockIdx.z, store);
 }
 
 // get_timestep's scalar tail (src/hydro_core.f90:677-694) and the bookkeeping
@@ -1517,7 +1528,21 @@ __device__ __forceinline__ void calcprim_cell(const KParams& p, const typename P
 // only_ghost): one thread per shell cell of [NG-1, NG+n]^3, the two z planes,
 // then the two y rows of every interior plane, then the two x cells of every
 // interior row; grid-stride.
+// The primitives of one cell with the policy's own recovery (the arithmetic
+// of the stage kernels' conversion), stored in the stage type.
 template <class Pol, int NEQ>
+__device__ __forceinline__ void own_prim_cell(const KParams& p, const typename Pol::TU* u,
+                                              typename Pol::TS* primit, long long c) {
+  typename Ops<Pol>::TC pr[NEQ];
+  unsigned pfl = 0;
+  Ops<Pol>::template load_prim<NEQ>(p, u, c, pr, pfl);
+#pragma unroll
+  for (int q = 0; q < NEQ; ++q) primit[q * p.fs + c] = (typename Pol::TS)pr[q];
+}
+
+// OWN: the policy's own recovery (stored primitives of the first stage),
+// else the reference's calcprim (table cooling)
+template <class Pol, int NEQ, bool OWN = false>
 __device__ __forceinline__ void calcprim_shell_body(const KParams& p, const typename Pol::TU* u,
                                                     typename Pol::TS* primit,
                                                     const StepScalars* sc, int blk, int nblk) {
@@ -1543,7 +1568,8 @@ __device__ __forceinline__ void calcprim_shell_body(const KParams& p, const type
       ay = NG + (int)(r % p.ny);
       az = NG + (int)(r / p.ny);
     }
-    calcprim_cell<Pol, NEQ>(p, u, primit, cell_index(p, ax, ay, az));
+    if constexpr (OWN) own_prim_cell<Pol, NEQ>(p, u, primit, cell_index(p, ax, ay, az));
+    else calcprim_cell<Pol, NEQ>(p, u, primit, cell_index(p, ax, ay, az));
   }
 }
 template <class Pol, int NEQ>
@@ -1551,6 +1577,35 @@ __global__ void __launch_bounds__(256)
 k_calcprim_shell(KParams p, const typename Pol::TU* u, typename Pol::TS* primit,
                  const StepScalars* sc) {
   calcprim_shell_body<Pol, NEQ>(p, u, primit, sc, blockIdx.x, gridDim.x);
+}
+
+// The shell part of get_timestep's stored primitives (after the CFL pass
+// stored the interior ones); marks them fresh for the next tstep.
+template <class Pol, int NEQ>
+__global__ void __launch_bounds__(256)
+k_prim_shell_own(KParams p, const typename Pol::TU* u, typename Pol::TS* primit,
+                 StepScalars* sc) {
+  calcprim_shell_body<Pol, NEQ, true>(p, u, primit, sc, blockIdx.x, gridDim.x);
+  if (blockIdx.x == 0 && threadIdx.x == 0 && sc->active) sc->prim_fresh = 1;
+}
+
+// At the start of tstep: the stored primitives of the interior and the
+// one-cell ghost shell, unless get_timestep stored them for this u already
+// (a tstep without get_timestep, or after an upload or boundary fill).
+// Grid-stride over the (nx+2)(ny+2)(nz+2) cells, a few blocks per SM: when
+// the primitives are fresh every block returns at once.
+template <class Pol, int NEQ>
+__global__ void __launch_bounds__(256)
+k_prim_refresh(KParams p, const typename Pol::TU* u, typename Pol::TS* primit,
+               const StepScalars* sc) {
+  if (sc->prim_fresh || !sc->active) return;
+  const long long mx = p.nx + 2, my = p.ny + 2, n = mx * my * (p.nz + 2);
+  for (long long t = blockIdx.x * 256LL + threadIdx.x; t < n; t += (long long)gridDim.x * 256) {
+    const int ax = NG - 1 + (int)(t % mx);
+    const int ay = NG - 1 + (int)((t / mx) % my);
+    const int az = NG - 1 + (int)(t / (mx * my));
+    own_prim_cell<Pol, NEQ>(p, u, primit, cell_index(p, ax, ay, az));
+  }
 }
 
 // calcprim over the whole array (src/hydro_core.f90:245-320); writes primit in

@@ -128,7 +128,7 @@ __device__ __forceinline__ DF fast_two_sum(float a, float b) {  // |a| >= |b|
   return {s, b - (s - a)};
 }
 __device__ __forceinline__ DF two_prod(float a, float b) {
-  const float p = a * b;
+  const float p = __fmul_rn(a, b);  // rounded on its own: never fused into a later sum
   return {p, fmaf(a, b, -p)};
 }
 __device__ __forceinline__ DF df_add(DF x, DF y) {
@@ -151,7 +151,7 @@ __device__ __forceinline__ void prim_from_f32(const KParams& p, const float* uu,
   float ir = 1.0f / r;
   ir = ir * fmaf(-r, ir, 2.0f);
   const DF m2 = df_sumsq(uu[1], uu[2], uu[3]);
-  const float q = m2.hi * ir;
+  const float q = __fmul_rn(m2.hi, ir);
   const float rem = fmaf(-q, r, m2.hi) + m2.lo;
   DF kb = fast_two_sum(q, __fmul_rn(rem, ir));
   if (NEQ >= 8 && p.mhd) kb = df_add(kb, df_sumsq(uu[5], uu[6], uu[7]));
@@ -324,7 +324,7 @@ struct Ops<PolKahan> {
       ir = ir * fmaf(-rh, ir, 2.0f);
       // m.m / rho as a pair quotient of pair operands
       const DF m2 = df_add(df_add(df_sq(uu[1]), df_sq(uu[2])), df_sq(uu[3]));
-      const float q = m2.hi * ir;
+      const float q = __fmul_rn(m2.hi, ir);
       const float rem = (fmaf(-q, rh, m2.hi) - __fmul_rn(q, rl)) + m2.lo;
       DF kb = fast_two_sum(q, __fmul_rn(rem, ir));
       if (NEQ >= 8 && p.mhd)

@@ -83,12 +83,18 @@ __device__ __forceinline__ void tma_load_4d(void* dst, const void* tmap, uint64_
 // host with cuTensorMapEncodeTiled when the domain is created).  Each is a
 // 4-D map over (x, field, y, z) of a padded structure-of-arrays array: dims
 // (NX, neq, NY, NZ), strides (field, row, plane).
+// The first stage reads u (8-byte values) or the stored primitives (FP32,
+// when the domain keeps them); each source has its own pair of maps, chosen
+// by the kernel's source type, so a map always matches the element size the
+// kernel's box coordinates assume.
 enum TmaMap : int {
-  kTmaS1Rows = 0,   // stage-1 source: one halo row, 36 x neq
-  kTmaS1Sides = 1,  // stage-1 source: 16 bytes wide x neq x TY rows
-  kTmaS2Rows = 2,   // stage-2 source (up): one halo row, 36 x neq
-  kTmaS2Sides = 3,  // stage-2 source: 16 bytes wide x neq x TY rows
-  kTmaCount = 4
+  kTmaS1Rows = 0,    // stage-1 source u: one halo row, 36 x neq
+  kTmaS1Sides = 1,   // stage-1 source u: 16 bytes wide x neq x TY rows
+  kTmaS2Rows = 2,    // stage-2 source (up): one halo row, 36 x neq
+  kTmaS2Sides = 3,   // stage-2 source: 16 bytes wide x neq x TY rows
+  kTmaS1PRows = 4,   // stage-1 source primit: one halo row, 36 x neq
+  kTmaS1PSides = 5,  // stage-1 source primit: 16 bytes wide x neq x TY rows
+  kTmaCount = 6
 };
 constexpr int kTmaMapBytes = 128;  // sizeof(CUtensorMap)
 
