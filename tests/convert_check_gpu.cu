@@ -1,0 +1,121 @@
+// Device check of gch_convert.h and gch_ddiv.h: the integer-pipe FP64 <-> FP32
+// conversions and the integer-pipe FP64 division, run in a kernel on the
+// same cases as the host check (convert_cases.h), against the device's own
+// IEEE operations in the same kernel: __ddiv_rn(a, b) for the division,
+// __double2float_rn(x) for FP64 -> FP32 and the exact FP32 -> FP64
+// conversion, with the flush rule gch_convert.h states (results and FP32
+// inputs below 2^-126 in magnitude become signed zero).  The device
+// quotients are also compared with the host's IEEE division.
+// Usage: convert_check_gpu <n_random>; prints "checked N bad B", exits 1 on a
+// mismatch and 2 on a CUDA error.
+#include <cuda_runtime.h>
+
+#include <cstdio>
+#include <cstdlib>
+#include <vector>
+
+#include "convert_cases.h"
+#include "gch_convert.h"
+#include "gch_ddiv.h"
+
+__global__ void k_convert(const double* x, float* d2f_got, float* d2f_want, long nx,
+                          const float* f, double* f2d_got, double* f2d_want, long nf,
+                          const double* a, const double* b, double* div_got, double* div_want,
+                          long nd) {
+  const long stride = (long)gridDim.x * blockDim.x;
+  for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < nx; i += stride) {
+    const double v = x[i];
+    d2f_got[i] = gch::d2f_rn(v);
+    d2f_want[i] = fabs(v) < 0x1p-126 ? copysignf(0.0f, (float)v) : __double2float_rn(v);
+  }
+  for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < nf; i += stride) {
+    const float v = f[i];
+    f2d_got[i] = gch::f2d(v);
+    f2d_want[i] = ((__float_as_uint(v) >> 23) & 0xFFu) == 0 ? copysign(0.0, (double)v) : (double)v;
+  }
+  for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < nd; i += stride) {
+    div_got[i] = gch::ddiv_rn(a[i], b[i]);
+    div_want[i] = __ddiv_rn(a[i], b[i]);
+  }
+}
+
+#define CK(call)                                                                       \
+  do {                                                                                 \
+    cudaError_t e_ = (call);                                                           \
+    if (e_ != cudaSuccess) {                                                           \
+      printf("CUDA error %s at %s:%d\n", cudaGetErrorString(e_), __FILE__, __LINE__); \
+      return 2;                                                                        \
+    }                                                                                  \
+  } while (0)
+
+template <class T>
+static T* to_device(const std::vector<T>& h) {
+  T* d = nullptr;
+  if (cudaMalloc(&d, h.size() * sizeof(T) + 16) != cudaSuccess) return nullptr;
+  if (cudaMemcpy(d, h.data(), h.size() * sizeof(T), cudaMemcpyHostToDevice) != cudaSuccess)
+    return nullptr;
+  return d;
+}
+template <class T>
+static T* device_array(size_t n) {
+  T* d = nullptr;
+  if (cudaMalloc(&d, n * sizeof(T) + 16) != cudaSuccess) return nullptr;
+  return d;
+}
+template <class T>
+static bool same_bits(T got, T want) {
+  return std::isnan(want) ? std::isnan(got) : gch::bits_of(got) == gch::bits_of(want);
+}
+
+int main(int argc, char** argv) {
+  const long n = argc > 1 ? atol(argv[1]) : 200000;
+  std::vector<double> xs, as, bs;
+  std::vector<float> fs;
+  convert_cases(
+      n, [&](double x) { xs.push_back(x); }, [&](float v) { fs.push_back(v); },
+      [&](double a, double b) {
+        as.push_back(a);
+        bs.push_back(b);
+      });
+  const long nx = (long)xs.size(), nf = (long)fs.size(), nd = (long)as.size();
+
+  double *dx = to_device(xs), *da = to_device(as), *db = to_device(bs);
+  float* df = to_device(fs);
+  float *d2f_got = device_array<float>(nx), *d2f_want = device_array<float>(nx);
+  double *f2d_got = device_array<double>(nf), *f2d_want = device_array<double>(nf);
+  double *div_got = device_array<double>(nd), *div_want = device_array<double>(nd);
+  if (!dx || !da || !db || !df || !d2f_got || !d2f_want || !f2d_got || !f2d_want || !div_got ||
+      !div_want) {
+    printf("CUDA error: allocation or copy failed\n");
+    return 2;
+  }
+  k_convert<<<4 * 152, 256>>>(dx, d2f_got, d2f_want, nx, df, f2d_got, f2d_want, nf, da, db,
+                              div_got, div_want, nd);
+  CK(cudaGetLastError());
+  CK(cudaDeviceSynchronize());
+
+  std::vector<float> hg(nx), hw(nx);
+  std::vector<double> fg(nf), fw(nf), qg(nd), qw(nd);
+  CK(cudaMemcpy(hg.data(), d2f_got, nx * sizeof(float), cudaMemcpyDeviceToHost));
+  CK(cudaMemcpy(hw.data(), d2f_want, nx * sizeof(float), cudaMemcpyDeviceToHost));
+  CK(cudaMemcpy(fg.data(), f2d_got, nf * sizeof(double), cudaMemcpyDeviceToHost));
+  CK(cudaMemcpy(fw.data(), f2d_want, nf * sizeof(double), cudaMemcpyDeviceToHost));
+  CK(cudaMemcpy(qg.data(), div_got, nd * sizeof(double), cudaMemcpyDeviceToHost));
+  CK(cudaMemcpy(qw.data(), div_want, nd * sizeof(double), cudaMemcpyDeviceToHost));
+
+  long checked = 0, bad = 0;
+  for (long i = 0; i < nx; ++i, ++checked)
+    if (!same_bits(hg[i], hw[i]) && bad++ < 8)
+      printf("device d2f_rn(%a) = %a, device conversion %a\n", xs[i], hg[i], hw[i]);
+  for (long i = 0; i < nf; ++i, ++checked)
+    if (!same_bits(fg[i], fw[i]) && bad++ < 8)
+      printf("device f2d(%a) = %a, device conversion %a\n", fs[i], fg[i], fw[i]);
+  for (long i = 0; i < nd; ++i, ++checked) {
+    const double host = as[i] / bs[i];
+    if ((!same_bits(qg[i], qw[i]) || !same_bits(qg[i], host)) && bad++ < 8)
+      printf("device ddiv_rn(%a, %a) = %a, device division %a, host %a\n", as[i], bs[i], qg[i],
+             qw[i], host);
+  }
+  printf("checked %ld bad %ld\n", checked, bad);
+  return bad ? 1 : 0;
+}
