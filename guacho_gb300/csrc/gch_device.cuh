@@ -15,6 +15,7 @@
 #include "guacho_gb300.h"
 #include "gch_convert.h"
 #include "gch_ddiv.h"
+#include "gch_dsqrt.h"
 
 namespace gch {
 
@@ -201,6 +202,10 @@ template <class T>
 __device__ __forceinline__ T tmin_(T a, T b) { return a < b ? a : b; }
 __device__ __forceinline__ double tcopysign(double a, double b) { return copysign(a, b); }
 __device__ __forceinline__ float tcopysign(float a, float b) { return copysignf(a, b); }
+// The FP64 stage kernels keep the hardware square root: the integer-pipe one
+// (dsqrt_rn, same bits) made each of them about 7% slower at 256^3, its long
+// dependent integer chain costing more than the FP64-pipe time it frees at
+// one block per SM.  get_timestep's pass takes it (cfl_sqrt).
 __device__ __forceinline__ double tsqrt(double a) { return sqrt(a); }
 __device__ __forceinline__ float tsqrt(float a) { return sqrtf(a); }
 __device__ __forceinline__ double tabs(double a) { return fabs(a); }

@@ -692,6 +692,15 @@ k_flux(KParams p, const typename Src<Pol, NEQ, STAGE, PRIM_IN>::TIn* __restrict_
 __device__ __forceinline__ float mul_rn(float a, float b) { return __fmul_rn(a, b); }
 __device__ __forceinline__ double mul_rn(double a, double b) { return __dmul_rn(a, b); }
 
+// get_timestep's square roots and quotients.  In FP64 they run on the integer
+// and FP32 pipes, correctly rounded (the same bits as sqrt and /): the CFL
+// pass is bound by the FP64 pipe and has the issue slots to spare.  FP32 as
+// the unit's operations.
+__device__ __forceinline__ double cfl_sqrt(double a) { return dsqrt_rn(a); }
+__device__ __forceinline__ float cfl_sqrt(float a) { return sqrtf(a); }
+__device__ __forceinline__ double cfl_div(double a, double b) { return ddiv_rn(a, b); }
+__device__ __forceinline__ float cfl_div(float a, float b) { return a / b; }
+
 // The cell widths and gamma in the compute type, converted once per thread.
 template <class TC>
 struct CflConst {
@@ -724,17 +733,18 @@ __device__ __forceinline__ void cfl_candidate(const KParams& p, const CflConst<T
       const TC d = a2 - mul_rn(mul_rn(g4, bn), bn);
       return sizeof(TC) == 4 ? tmax_(d, TC(0)) : d;
     };
-    const TC cx = tsqrt(mul_rn(TC(0.5), a + tsqrt(disc(bx))) / pr[0]);
-    const TC cy = tsqrt(mul_rn(TC(0.5), a + tsqrt(disc(by))) / pr[0]);
-    const TC cz = tsqrt(mul_rn(TC(0.5), a + tsqrt(disc(bz))) / pr[0]);
-    cand[0] = k.h[0] / (tabs(pr[1]) + cx);
-    cand[1] = k.h[1] / (tabs(pr[2]) + cy);
-    cand[2] = k.h[2] / (tabs(pr[3]) + cz);
+    const TC cx = cfl_sqrt(cfl_div(mul_rn(TC(0.5), a + cfl_sqrt(disc(bx))), pr[0]));
+    const TC cy = cfl_sqrt(cfl_div(mul_rn(TC(0.5), a + cfl_sqrt(disc(by))), pr[0]));
+    const TC cz = cfl_sqrt(cfl_div(mul_rn(TC(0.5), a + cfl_sqrt(disc(bz))), pr[0]));
+    cand[0] = cfl_div(k.h[0], tabs(pr[1]) + cx);
+    cand[1] = cfl_div(k.h[1], tabs(pr[2]) + cy);
+    cand[2] = cfl_div(k.h[2], tabs(pr[3]) + cz);
   } else {
-    const TC c0 = csound(p, pr[4], pr[0]);
-    cand[0] = k.h[0] / (tabs(pr[1]) + c0);
-    cand[1] = k.h[1] / (tabs(pr[2]) + c0);
-    cand[2] = k.h[2] / (tabs(pr[3]) + c0);
+    // src/hydro_core.f90:544-553 csound
+    const TC c0 = cfl_sqrt(tdiv(k.g * pr[4], pr[0]));
+    cand[0] = cfl_div(k.h[0], tabs(pr[1]) + c0);
+    cand[1] = cfl_div(k.h[1], tabs(pr[2]) + c0);
+    cand[2] = cfl_div(k.h[2], tabs(pr[3]) + c0);
   }
 #pragma unroll
   for (int d = 0; d < 3; ++d) {

@@ -2,7 +2,9 @@
 // random bit patterns, values around the FP32 range, exact rounding ties of
 // the 29 bits FP64 -> FP32 drops and their neighbours, operands of nearby
 // magnitudes, dividends one ulp either side of b times a 53-bit quotient
-// (quotients next to a rounding boundary), and the special values.  The
+// (quotients next to a rounding boundary), radicands within two ulps of the
+// square of a 53-bit root and of the square of a midpoint between two roots
+// (roots next to a rounding boundary), and the special values.  The
 // host check (convert_check.cpp) and the device check (convert_check_gpu.cu)
 // feed the same cases to their callbacks, seeded alike.
 #pragma once
@@ -14,8 +16,8 @@
 #include <cmath>
 #include <random>
 
-template <class D2F, class F2D, class DIV>
-void convert_cases(long n, D2F&& d2f, F2D&& f2d, DIV&& div) {
+template <class D2F, class F2D, class DIV, class SQ>
+void convert_cases(long n, D2F&& d2f, F2D&& f2d, DIV&& div, SQ&& sq) {
   std::mt19937_64 g(20260001);
   for (long i = 0; i < n; ++i) {
     // any bit pattern
@@ -60,6 +62,22 @@ void convert_cases(long n, D2F&& d2f, F2D&& f2d, DIV&& div) {
     div(p, c);
     div(std::nextafter(p, 0.0), c);
     div(std::nextafter(p, INFINITY), c);
+    // square roots: any positive or negative bit pattern, and radicands next
+    // to r^2 and to (r + half an ulp)^2 for a 53-bit r of any magnitude
+    sq(da);
+    sq(std::fabs(da));
+    const double r = std::ldexp(q, (int)(g() % 1000) - 500);
+    const double mid = r + std::ldexp(0.5, std::ilogb(r) - 52);
+    for (double s0 : {r * r, mid * mid}) {
+      double lo = s0, hi = s0;
+      sq(s0);
+      for (int k = 0; k < 2; ++k) {
+        lo = std::nextafter(lo, 0.0);
+        hi = std::nextafter(hi, INFINITY);
+        sq(lo);
+        sq(hi);
+      }
+    }
   }
   const double special[] = {0.0, -0.0, INFINITY, -INFINITY, NAN, -NAN, DBL_MAX, -DBL_MAX,
                             FLT_MAX, -FLT_MAX, (double)FLT_MAX * (1 + 0x1p-25),
@@ -72,4 +90,8 @@ void convert_cases(long n, D2F&& d2f, F2D&& f2d, DIV&& div) {
   for (float s : fspecial) f2d(s);
   for (double s : special)
     for (double t : special) div(s, t);
+  for (double s : special) sq(s);
+  const double sspecial[] = {0x1p-1022, 0x1.0000000000001p-1022, 0x1.fffffffffffffp1023,
+                             0x1p-1074, 4.0, 2.0, 0x1.fffffffffffffp-1, 0x1.0000000000001p0};
+  for (double s : sspecial) sq(s);
 }

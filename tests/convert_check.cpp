@@ -1,10 +1,12 @@
-// Host check of gch_convert.h and gch_ddiv.h: the integer-pipe FP64 <-> FP32
-// conversions against the C casts, with the flush rule the header states
-// (results and FP32 inputs below 2^-126 in magnitude become signed zero),
-// and the integer-pipe FP64 division against the IEEE division.
+// Host check of gch_convert.h, gch_ddiv.h and gch_dsqrt.h: the integer-pipe
+// FP64 <-> FP32 conversions against the C casts, with the flush rule the
+// header states (results and FP32 inputs below 2^-126 in magnitude become
+// signed zero), and the integer-pipe FP64 division and square root against
+// the IEEE division and square root.
 // Usage: convert_check <n_random>; prints "checked N bad B", exits 1 on a mismatch.
 #include "gch_convert.h"
 #include "gch_ddiv.h"
+#include "gch_dsqrt.h"
 #include "convert_cases.h"
 
 #include <cfloat>
@@ -46,7 +48,13 @@ int main(int argc, char** argv) {
     const bool ok = std::isnan(want) ? std::isnan(got) : bits_of(got) == bits_of(want);
     if (!ok && bad++ < 8) printf("ddiv_rn(%a, %a) = %a, want %a\n", a, b, got, want);
   };
-  convert_cases(n, d2f, f2d, div);
+  auto sq = [&](double a) {
+    ++checked;
+    const double got = gch::dsqrt_rn(a), want = std::sqrt(a);
+    const bool ok = std::isnan(want) ? std::isnan(got) : bits_of(got) == bits_of(want);
+    if (!ok && bad++ < 8) printf("dsqrt_rn(%a) = %a, want %a\n", a, got, want);
+  };
+  convert_cases(n, d2f, f2d, div, sq);
   printf("checked %ld bad %ld\n", checked, bad);
   return bad ? 1 : 0;
 }
