@@ -12,7 +12,7 @@ import numpy as np
 
 from .params import Params
 
-ABI_VERSION = 2
+ABI_VERSION = 3
 MAX_SPHERES, MAX_GRAV, MAX_TABLE = 8, 4, 512
 
 ERR_PARAM, ERR_CUDA, ERR_HLLD, ERR_HLLC = 0x1, 0x2, 0x4, 0x8
@@ -28,7 +28,8 @@ LIB_PATH = Path(__file__).resolve().parent / "lib" / "libguacho_gb300.so"
 class Sphere_t(C.Structure):
     _fields_ = [("xc", C.c_double), ("yc", C.c_double), ("zc", C.c_double),
                 ("radius", C.c_double), ("dens", C.c_double), ("vwind", C.c_double),
-                ("vorb", C.c_double * 3), ("tfac", C.c_double), ("bdip", C.c_double)]
+                ("vorb", C.c_double * 3), ("tfac", C.c_double), ("bdip", C.c_double),
+                ("orbit_r", C.c_double), ("orbit_omega", C.c_double), ("orbit_phase", C.c_double)]
 
 
 class Params_t(C.Structure):
@@ -86,6 +87,7 @@ def to_struct(p: Params) -> Params_t:
         d = s.sph[i]
         d.xc, d.yc, d.zc, d.radius = sp.xc, sp.yc, sp.zc, sp.radius
         d.dens, d.vwind, d.tfac, d.bdip = sp.dens, sp.vwind, sp.tfac, sp.bdip
+        d.orbit_r, d.orbit_omega, d.orbit_phase = sp.orbit_r, sp.orbit_omega, sp.orbit_phase
         for a in range(3):
             d.vorb[a] = sp.vorb[a]
     s.ngrav = len(p.grav)

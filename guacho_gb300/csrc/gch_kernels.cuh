@@ -1013,6 +1013,23 @@ __global__ void k_ghost(KParams p, T* a, int neq, int axis, int layers, const St
   ghost_body<T>(p, a, neq, axis, layers, sc, blockIdx.x, blockIdx.y, blockIdx.z);
 }
 
+// A sphere at time t: as given, or moved along its circular orbit in the
+// x-z plane (EXO/exoplanet.f90:143-148: XP = Rorb cos(omegap t + phi),
+// ZP = Rorb sin(omegap t + phi), and the orbital velocity).
+__device__ __forceinline__ gch_sphere_t sphere_at(const gch_sphere_t& s0, double t) {
+  gch_sphere_t s = s0;
+  if (s.orbit_omega != 0.0) {
+    double sn, cs;
+    sincos(__dadd_rn(__dmul_rn(s.orbit_omega, t), s.orbit_phase), &sn, &cs);
+    s.xc = __dmul_rn(s.orbit_r, cs);
+    s.zc = __dmul_rn(s.orbit_r, sn);
+    s.vorb[0] = __dmul_rn(__dmul_rn(-s.orbit_omega, s.orbit_r), sn);
+    s.vorb[1] = 0.0;
+    s.vorb[2] = __dmul_rn(__dmul_rn(s.orbit_omega, s.orbit_r), cs);
+  }
+  return s;
+}
+
 // User boundary spheres (EXO/exoplanet.f90:125-266 pattern) over the box
 // [lo, hi) of array coordinates of sphere `m`; the first sphere containing a
 // cell wins.
@@ -1021,7 +1038,8 @@ template <class T>
 __device__ __forceinline__ void user_bc_body(const KParams& p, T* a, int neq,
                                              const StepScalars* sc, int m, int blk, int nblk) {
   if (!sc->active) return;
-  const gch_sphere_t sp = p.sph[m];
+  const double t = sc->time;
+  const gch_sphere_t sp = sphere_at(p.sph[m], t);
   // bounding box of the sphere in array coordinates, clipped to the array
   auto lo_hi = [&](double c, double r, double d, int n, int N, int& lo, int& hi) {
     // cell centre of array coordinate a: ((a-NG+1 - n/2) + 0.5)*d
@@ -1052,7 +1070,7 @@ __device__ __forceinline__ void user_bc_body(const KParams& p, T* a, int neq,
     const double z = cell_pos(az, p.nz, p.dz);
     bool earlier = false;
     for (int e = 0; e < m; ++e) {
-      const gch_sphere_t& q = p.sph[e];
+      const gch_sphere_t q = sphere_at(p.sph[e], t);
       const double xs = x - q.xc, ys = y - q.yc, zs = z - q.zc;
       if (sqrt(xs * xs + ys * ys + zs * zs) <= q.radius) { earlier = true; break; }
     }

@@ -18,6 +18,7 @@ module gpu_hydro
     real(c_double) :: xc, yc, zc, radius, dens, vwind
     real(c_double) :: vorb(3)
     real(c_double) :: tfac, bdip
+    real(c_double) :: orbit_r, orbit_omega, orbit_phase
   end type gch_sphere_t
 
   type, bind(C) :: gch_params_t

@@ -27,7 +27,11 @@ NGHOST = 2
 
 @dataclass
 class Sphere:
-    """A wind sphere re-imposed by the user boundary hook (EXO pattern)."""
+    """A wind sphere re-imposed by the user boundary hook (EXO pattern).
+    With orbit_omega != 0 it moves on a circular orbit in the x-z plane
+    (EXO/exoplanet.f90:143-148): centre (orbit_r cos th, yc, orbit_r sin th)
+    and velocity orbit_omega*orbit_r*(-sin th, 0, cos th) at
+    th = orbit_omega*t + orbit_phase, t the step's start time."""
     xc: float = 0.0
     yc: float = 0.0
     zc: float = 0.0
@@ -37,6 +41,9 @@ class Sphere:
     vorb: tuple = (0.0, 0.0, 0.0)
     tfac: float = 1.0
     bdip: float = 0.0
+    orbit_r: float = 0.0
+    orbit_omega: float = 0.0
+    orbit_phase: float = 0.0
 
 
 @dataclass

@@ -15,6 +15,7 @@ inputs are deterministic for a given seed.
 from __future__ import annotations
 
 import math
+from dataclasses import replace
 
 import numpy as np
 
@@ -175,6 +176,7 @@ def blast(n=192, precision=FP64, p_in=10.0, p_out=0.1, radius=0.1, cfl=0.4, b_sc
 
 # ---------------------------------------------------------------------------
 AMH, RG, KB = 1.66e-24, 8.3145e7, 1.38e-16   # src/constants.f90:33-35
+GGRAV, MSUN = 6.67259e-8, 1.99e33             # src/constants.f90:36,39
 
 
 def synthetic_cooling_table(n=101, peak=5.3):
@@ -186,14 +188,18 @@ def synthetic_cooling_table(n=101, peak=5.3):
     return logT, logL
 
 
-def wind_cooling(n=256, precision=FP64, xphys=3.0e13, nsc=1.0e5, cfl=0.4, **kw) -> tuple:
+def wind_cooling(n=256, precision=FP64, xphys=3.0e13, nsc=1.0e5, cfl=0.4, orbit=True,
+                 **kw) -> tuple:
     """Hydro wind interaction with optically-thin cooling (EXO pattern).
     Star sphere r = 0.1 at the centre (rho = 1, T = 1e6 K, v_r = 200 km/s),
-    planet sphere r = 0.02 at x offset 0.3 (rho = 100, T = 1e4 K,
+    planet sphere r = 0.02 at distance 0.3 (rho = 100, T = 1e4 K,
     v_r = 10 km/s), both re-imposed in every boundary call; HLLC, outflow;
     tabulated cooling (101 rows, COOL_DMC-style implicit update).
-    Scalings as EXO/parameters.f90:162-170 with T0 = 1e4 K, density scale
-    nsc * amh (code rho = 1 is nsc particles per cm^3)."""
+    With `orbit` the planet moves on its circular Keplerian orbit about a
+    1.1 solar-mass star in the x-z plane, starting 25 degrees below the x
+    axis (EXO/exoplanet.f90:83-84,106-111,143-148); otherwise it stays at
+    x = 0.3.  Scalings as EXO/parameters.f90:162-170 with T0 = 1e4 K,
+    density scale nsc * amh (code rho = 1 is nsc particles per cm^3)."""
     cv = 1.5
     gamma = (cv + 1.0) / cv
     T0 = 1.0e4
@@ -210,6 +216,12 @@ def wind_cooling(n=256, precision=FP64, xphys=3.0e13, nsc=1.0e5, cfl=0.4, **kw) 
                   tfac=1.0e6 / Tempsc)
     planet = Sphere(xc=0.3, yc=0.0, zc=0.0, radius=0.02, dens=100.0, vwind=1.0e6 / vsc,
                     tfac=1.0e4 / Tempsc)
+    if orbit:
+        # omega = sqrt(G M / r^3) at r = 0.3 xphys, in units of 1/tsc
+        rorb = 0.3
+        omega = math.sqrt(GGRAV * 1.1 * MSUN / (rorb * xphys) ** 3) * tsc
+        planet = replace(planet, orbit_r=rorb, orbit_omega=omega,
+                         orbit_phase=-25.0 * math.pi / 180.0)
     bc = dict(bc_left=BC_OUTFLOW, bc_right=BC_OUTFLOW, bc_bottom=BC_OUTFLOW,
               bc_top=BC_OUTFLOW, bc_out=BC_OUTFLOW, bc_in=BC_OUTFLOW)
     p = Params(nx=n, ny=n, nz=n, precision=precision, mhd=False, pmhd=False,

@@ -50,7 +50,7 @@
 extern "C" {
 #endif
 
-#define GCH_ABI_VERSION 2
+#define GCH_ABI_VERSION 3
 
 /* ---- switch ids: identical values to src/constants.f90:56-98 ----------- */
 #define GCH_SOLVER_HLL 1
@@ -125,7 +125,14 @@ extern "C" {
  * impose_user_bc (EXO/user_mod.f90:131-144).  Cells whose centre lies within
  * `radius` of (xc, yc, zc) (measured from the grid centre) are set to
  * rho = dens, v = vorb + vwind * r_hat, E = 1/2 rho v^2 + cv*dens*tfac
- * (+ the dipole field of strength bdip and its energy when MHD). */
+ * (+ the dipole field of strength bdip and its energy when MHD).
+ * With orbit_omega != 0 the sphere moves on the planet's circular orbit in
+ * the x-z plane (EXO/exoplanet.f90:143-148): at the time t of the boundary
+ * call (the step's start time, as the reference's global `time` inside
+ * tstep; 0 before the first step), with th = orbit_omega*t + orbit_phase,
+ * the centre is (orbit_r cos th, yc, orbit_r sin th) and vorb is the orbital
+ * velocity orbit_omega*orbit_r*(-sin th, 0, cos th); xc, zc and vorb are
+ * then unused. */
 typedef struct {
   double xc, yc, zc;
   double radius;
@@ -134,6 +141,7 @@ typedef struct {
   double vorb[3];
   double tfac;
   double bdip;
+  double orbit_r, orbit_omega, orbit_phase;
 } gch_sphere_t;
 
 /* The parameter surface of parameters.f90 (OT/parameters.f90:48-177), as

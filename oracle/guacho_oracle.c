@@ -1020,10 +1020,24 @@ static void boundary_fill(gor_state_t* s, double* a, int layers) {
 }
 
 /* EXO/exoplanet.f90:125-266  impose_exo, generalised to a list of spheres
- * (the first sphere that contains a cell wins, as the if/else-if chain). */
+ * (the first sphere that contains a cell wins, as the if/else-if chain).
+ * An orbiting sphere's centre and velocity at the state's time follow
+ * EXO/exoplanet.f90:143-148. */
 static void impose_user_bc(gor_state_t* s, double* a) {
   const gor_params_t* p = &s->p;
   const int neq = p->neq, nx = p->nx, ny = p->ny, nz = p->nz;
+  gor_sphere_t now[GOR_MAX_SPHERES];
+  for (int m = 0; m < p->nsph; ++m) {
+    now[m] = p->sph[m];
+    if (now[m].orbit_omega != 0.0) {
+      const double th = now[m].orbit_omega * s->time + now[m].orbit_phase;
+      now[m].xc = now[m].orbit_r * cos(th);
+      now[m].zc = now[m].orbit_r * sin(th);
+      now[m].vorb[0] = -now[m].orbit_omega * now[m].orbit_r * sin(th);
+      now[m].vorb[1] = 0.0;
+      now[m].vorb[2] = now[m].orbit_omega * now[m].orbit_r * cos(th);
+    }
+  }
   for (int k = 1 - NG; k <= nz + NG; ++k)
     for (int j = 1 - NG; j <= ny + NG; ++j)
       for (int i = 1 - NG; i <= nx + NG; ++i) {
@@ -1031,7 +1045,7 @@ static void impose_user_bc(gor_state_t* s, double* a) {
         double y = ((double)(j - ny / 2) + 0.5) * p->dy;
         double z = ((double)(k - nz / 2) + 0.5) * p->dz;
         for (int m = 0; m < p->nsph; ++m) {
-          const gor_sphere_t* sp = &p->sph[m];
+          const gor_sphere_t* sp = &now[m];
           double xs = x - sp->xc, ys = y - sp->yc, zs = z - sp->zc;
           double rads = sqrt(xs * xs + ys * ys + zs * zs);
           if (rads <= sp->radius) {
@@ -1257,6 +1271,7 @@ static void coolingh(gor_state_t* s, double dt_CFL) {
 void gor_get_timestep(gor_state_t* s, int iter, int n_iter, double t, double tprint,
                       double* dt, int* dump) {
   const gor_params_t* p = &s->p;
+  s->time = t;  /* the step's time, read by the user boundary hook inside tstep */
   const int neq = p->neq, nx = p->nx, ny = p->ny, nz = p->nz;
   double dtp = 1e30;
 #pragma omp parallel for schedule(static) reduction(min : dtp)

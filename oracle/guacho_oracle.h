@@ -49,7 +49,9 @@ enum {
 
 /* One wind sphere re-imposed by the user boundary hook (EXO pattern,
  * EXO/exoplanet.f90:125-266): cells with r <= radius get rho = dens,
- * v = vorb + vwind * r_hat, E = 1/2 rho v^2 + cv*dens*tfac (+ 1/2 B^2). */
+ * v = vorb + vwind * r_hat, E = 1/2 rho v^2 + cv*dens*tfac (+ 1/2 B^2).
+ * With orbit_omega != 0 the centre and vorb follow the planet's orbit in the
+ * x-z plane at the state's time (EXO/exoplanet.f90:143-148). */
 typedef struct {
   double xc, yc, zc;      /* centre, measured from the grid centre */
   double radius;
@@ -58,6 +60,7 @@ typedef struct {
   double vorb[3];
   double tfac;            /* the "1.9999*Tsw" / "1.8*Tpw" factor, code units */
   double bdip;            /* dipole strength ("bsw"/"bpw"), MHD only */
+  double orbit_r, orbit_omega, orbit_phase;  /* "Rorb", "omegap", "phi" */
 } gor_sphere_t;
 
 typedef struct {

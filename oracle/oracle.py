@@ -37,7 +37,8 @@ def build(force: bool = False) -> Path:
 class Sph(C.Structure):
     _fields_ = [("xc", C.c_double), ("yc", C.c_double), ("zc", C.c_double),
                 ("radius", C.c_double), ("dens", C.c_double), ("vwind", C.c_double),
-                ("vorb", C.c_double * 3), ("tfac", C.c_double), ("bdip", C.c_double)]
+                ("vorb", C.c_double * 3), ("tfac", C.c_double), ("bdip", C.c_double),
+                ("orbit_r", C.c_double), ("orbit_omega", C.c_double), ("orbit_phase", C.c_double)]
 
 
 class GorParams(C.Structure):
@@ -90,6 +91,7 @@ def params_struct(p) -> GorParams:
         d.xc, d.yc, d.zc, d.radius, d.dens, d.vwind = (sp.xc, sp.yc, sp.zc, sp.radius, sp.dens,
                                                        sp.vwind)
         d.tfac, d.bdip = sp.tfac, sp.bdip
+        d.orbit_r, d.orbit_omega, d.orbit_phase = sp.orbit_r, sp.orbit_omega, sp.orbit_phase
         for a in range(3):
             d.vorb[a] = sp.vorb[a]
     s.ngrav = len(p.grav)
@@ -203,6 +205,10 @@ class Oracle:
         self.upload(u0)
         self.L.gor_boundaryI(self.h)
         self.L.gor_calcprim(self.h, 0)
+
+    def boundaryI(self):
+        """src/boundaries.f90 boundaryI on u (user spheres at the state's time)."""
+        self.L.gor_boundaryI(self.h)
 
     def get_timestep(self, it, n_iter, t, tprint):
         dt = C.c_double()
