@@ -127,6 +127,7 @@ def lib() -> C.CDLL:
         "gch_tstep": (I, [P, D]),
         "gch_tc_info": (I, [P, IP, DP]),
         "gch_step_host": (I, [P, P, I, I, D, D, DP, IP]),
+        "gch_step_host_overlaps": (I, [P]),
         "gch_advance": (I, [P, I, D, D, I, DP, IP, DP, IP]),
         "gch_last_step_info": (I, [P, C.POINTER(C.c_longlong), IP]),
         "gch_launches_per_step": (I, [P]),
@@ -156,7 +157,8 @@ def lib() -> C.CDLL:
 def exported_symbols() -> list[str]:
     return ["gch_params_default", "gch_params_check", "gch_create", "gch_destroy",
             "gch_upload", "gch_download", "gch_set_background", "gch_boundaryI", "gch_calcprim",
-            "gch_get_timestep", "gch_tstep", "gch_tc_info", "gch_step_host", "gch_advance",
+            "gch_get_timestep", "gch_tstep", "gch_tc_info", "gch_step_host",
+            "gch_step_host_overlaps", "gch_advance",
             "gch_last_step_info", "gch_launches_per_step", "gch_advance_timed",
             "gch_profile_step", "gch_get_kz", "gch_set_kz", "gch_autotune",
             "gch_batch_create",

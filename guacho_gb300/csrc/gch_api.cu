@@ -133,6 +133,18 @@ int host_out_finish(gch_domain* d, double* h, const double* view) {
                                  cudaMemcpyDeviceToHost, d->stream));
 }
 
+}  // namespace
+
+bool gch::pipe_ok(const gch_domain* d) {
+  const gch::KParams& k = d->kp;
+  if (d->prim_in || d->hp.cooling == GCH_COOL_H || k.eta != 0.0 || d->hp.th_cond != GCH_TC_OFF)
+    return false;
+  if ((k.bc_user && k.nsph > 0) || k.solver == GCH_SOLVER_HLLE_SPLIT_ALL) return false;
+  // every side at least one cell: the whole-shell fill of one layer
+  return k.nx >= 1 && k.ny >= 1 && (k.nz + d->kz - 1) / d->kz >= 3;
+}
+
+namespace {
 int fetch_scalars(gch_domain* d) {
   int st = cuda_ok(cudaMemcpyAsync(d->sc_host, d->sc, sizeof(StepScalars), cudaMemcpyDeviceToHost,
                                    d->stream));
@@ -266,6 +278,9 @@ int gch_params_check(const gch_params_t* p) {
 int gch_destroy(gch_domain_t* d) {
   if (!d) return GCH_OK;
   if (d->graph) cudaGraphExecDestroy(d->graph);
+  for (int i = 0; i < gch_domain::kPipeEv; ++i)
+    if (d->pipe_ev[i]) cudaEventDestroy(d->pipe_ev[i]);
+  if (d->cstream) cudaStreamDestroy(d->cstream);
   for (int i = 0; i < 64; ++i)
     if (d->prof_ev[i]) cudaEventDestroy(d->prof_ev[i]);
   cudaFree(d->u);
@@ -547,6 +562,8 @@ int gch_tc_info(gch_domain_t* d, int* nsteps, double* dt_cond) {
   return GCH_OK;
 }
 
+int gch_step_host_overlaps(const gch_domain_t* d) { return d && gch::pipe_ok(d) ? 1 : 0; }
+
 int gch_step_host(gch_domain_t* d, double* u, int current_iter, int n_iter, double current_time,
                   double tprint, double* dt, int* dump_flag) {
   if (!d || !u || !dt || !dump_flag) return GCH_ERR_PARAM;
@@ -556,14 +573,19 @@ int gch_step_host(gch_domain_t* d, double* u, int current_iter, int n_iter, doub
   if (d->prim_in) st |= engine(d).calcprim(d);
   k_set_ctrl<<<1, 1, 0, d->stream>>>(d->sc, current_iter, n_iter, current_time, tprint, 0.0, 0.0, 1);
   st |= engine(d).get_dt(d);
-  st |= engine(d).tstep(d);
-  if (d->hp.th_cond != GCH_TC_OFF && st == GCH_OK) {
-    st |= fetch_scalars(d);  // the conduction substeps need dt on the host
-    st |= gch::tc_run(d, d->sc_host->dt);
+  if (gch::pipe_ok(d)) {
+    // the download of u overlaps the second stage
+    st |= engine(d).tstep_dl(d, u);
+  } else {
+    st |= engine(d).tstep(d);
+    if (d->hp.th_cond != GCH_TC_OFF && st == GCH_OK) {
+      st |= fetch_scalars(d);  // the conduction substeps need dt on the host
+      st |= gch::tc_run(d, d->sc_host->dt);
+    }
+    double* dst = host_out(d, u);
+    st |= engine(d).download_u(d, dst);
+    st |= host_out_finish(d, u, dst);
   }
-  double* dst = host_out(d, u);
-  st |= engine(d).download_u(d, dst);
-  st |= host_out_finish(d, u, dst);
   st |= fetch_scalars(d);
   *dt = d->sc_host->dt;
   if (d->sc_host->dump) *dump_flag = 1;

@@ -38,6 +38,14 @@ struct gch_domain {
   double* stage = nullptr;      // device staging buffer, host layout (FP64 AoS)
   size_t ncell_host = 0;        // NX*NY*NZ
   int kz = 8;                   // z planes per block of the stage kernels
+  // the z chunks [zc0, zc0 + zcn) of kz planes that the next stage launch
+  // covers (all of them when zcn == 0): a slab of the pipelined second stage
+  int zc0 = 0, zcn = 0;
+  // gch_step_host's download behind the second stage: the copy stream and
+  // one event per copied slab plus one for the last copy
+  cudaStream_t cstream = nullptr;
+  static constexpr int kPipeEv = 24;
+  cudaEvent_t pipe_ev[kPipeEv] = {};
   int launches = 0;             // kernel launches of the last tstep
   // thermal conduction (th_cond != 0): rho, p, T and the three face fluxes
   // (6 fields, FP64), the device min of the conduction timescale and its
@@ -78,7 +86,16 @@ struct EngineOps {
   int (*download_prim)(gch_domain*, double*);
   int (*loopfin)(gch_domain*);        // device time-loop tail
   int (*probe)(gch_domain*);          // stage-1 fluxes alone (autotuner)
+  // tstep, then u copied into the host array `host` (reference layout)
+  // slab by slab behind the second stage; only for domains pipe_ok accepts
+  int (*tstep_dl)(gch_domain*, double* host);
 };
+
+// Whether gch_step_host can overlap the download of u with the second
+// stage: the boundary fill of u is the plain shell fill (no user spheres,
+// table cooling, COOL_H, resistivity, conduction or split solver) and the
+// box has at least three z chunks.
+bool pipe_ok(const gch_domain* d);
 
 extern const EngineOps kEngineFP64;
 extern const EngineOps kEngineMixed;

@@ -29,7 +29,8 @@ struct Engine {
   template <int SOLVER, int NEQ, int STAGE, bool PRIM_IN, int LIM>
   static void flux_launch_lim(gch_domain* d, const void* src, void* dst) {
     const KParams& p = d->kp;
-    dim3 grid((p.nx + TX - 1) / TX, (p.ny + TY - 1) / TY, (p.nz + d->kz - 1) / d->kz);
+    dim3 grid((p.nx + TX - 1) / TX, (p.ny + TY - 1) / TY,
+              d->zcn > 0 ? d->zcn : (p.nz + d->kz - 1) / d->kz);
     dim3 block(TX, TY);
     using TIn = typename Src<Pol, NEQ, STAGE, PRIM_IN>::TIn;
     using TD = typename std::conditional<STAGE == 1, TS, TU>::type;
@@ -42,7 +43,8 @@ struct Engine {
       attr = true;
     }
     k_flux<Pol, SOLVER, NEQ, STAGE, PRIM_IN, LIM><<<grid, block, smem, d->stream>>>(
-        p, (const TIn*)src, (const TU*)d->u, (TD*)dst, (TS*)d->E, (TS*)d->s678, d->sc, d->kz);
+        p, (const TIn*)src, (const TU*)d->u, (TD*)dst, (TS*)d->E, (TS*)d->s678, d->sc, d->kz,
+        d->zc0);
   }
 
   // stage 1 has no limiter; stage 2 specialises minmod and van Leer
@@ -146,10 +148,16 @@ struct Engine {
     const KParams& p = d->kp;
     if constexpr (std::is_same<Pol, PolFP64>::value)
       if (p.solver == GCH_SOLVER_HLLE_SPLIT_ALL) return split_tstep(d);
-    int st = GCH_OK;
     d->launches = 0;
+    return stage1(d) | stage2(d);
+  }
+
+  // the first half step and boundaryII on up
+  static int stage1(gch_domain* d) {
+    const KParams& p = d->kp;
+    int st = GCH_OK;
     const bool ct = p.neq >= 8 && p.flux_cd;
-    const dim3 cgrid = cell_grid(p), cblock(32, 8);
+    const dim3 cblock(32, 8);
     // 1st half step: first-order fluxes, up = u - dtm*divF (from the stored
     // primitives with table cooling, or those get_timestep stored for this u)
     if (d->prim_pre) {
@@ -172,6 +180,15 @@ struct Engine {
     }
     // boundaryII on up (+ user spheres)
     ghost<TS>(d, (TS*)d->up, 2);
+    return st | cuda_status(cudaGetLastError());
+  }
+
+  // the second half step, the sources after it and boundaryI on u
+  static int stage2(gch_domain* d) {
+    const KParams& p = d->kp;
+    int st = GCH_OK;
+    const bool ct = p.neq >= 8 && p.flux_cd;
+    const dim3 cgrid = cell_grid(p), cblock(32, 8);
     // 2nd half step: limited reconstruction, u(+w) = u - dt*divF
     void* dst2 = p.eta != 0.0 ? d->w : d->u;
     st |= flux<2, false>(d, d->up, dst2);
@@ -221,6 +238,97 @@ struct Engine {
       gch_mark(d, "k_calcprim");
     }
     st |= cuda_status(cudaGetLastError());
+    return st;
+  }
+
+  // ---- tstep + download, the download behind the second stage ------------
+  // The second stage, its CT and the ring of x/y ghost cells run slab by
+  // slab of z chunks; each finished slab of u is transposed into the staging
+  // buffer (host layout) and copied to `host` on the copy stream while the
+  // next slabs compute.  The last chunk's fluxes go first: its E is the z
+  // neighbour of the first slab's CT under periodic walls.  Each slab's CT
+  // waits for the fluxes of the slab after it (its E at the slab's top
+  // plane).  The z ghost planes follow the whole-shell fill at the end (it
+  // writes the rings again with the same values).  The kernels' per-plane
+  // results do not depend on where a chunk or slab begins, so u ends the
+  // same, bit for bit, as with tstep and a download.
+  static int tstep_dl(gch_domain* d, double* host) {
+    const KParams& p = d->kp;
+    d->launches = 0;
+    int st = stage1(d);
+    if (!d->cstream) {
+      st |= cuda_status(cudaStreamCreateWithFlags(&d->cstream, cudaStreamNonBlocking));
+      for (int i = 0; i < gch_domain::kPipeEv && st == GCH_OK; ++i)
+        st |= cuda_status(cudaEventCreateWithFlags(&d->pipe_ev[i], cudaEventDisableTiming));
+      if (st) return st;
+    }
+    const bool ct = p.neq >= 8 && p.flux_cd;
+    const int kz = d->kz, C = (p.nz + kz - 1) / kz;
+    const int m = std::max(1, (C - 1 + 7) / 8);  // chunks per slab: about 8 slabs
+    const long long plane = (long long)p.NX * p.NY;
+    long long cut[gch_domain::kPipeEv][2];
+    int np = 0;
+    auto flux2 = [&](int c0, int nc) {
+      d->zc0 = c0;
+      d->zcn = nc;
+      st |= flux<2, false>(d, d->up, d->u);
+      d->zc0 = d->zcn = 0;
+      ++d->launches;
+      gch_mark(d, "k_flux_stage2");
+    };
+    // planes [az0, az1) of u (array coordinates) into the staging buffer
+    auto layout_out = [&](int az0, int az1) {
+      cut[np][0] = az0 * plane;
+      cut[np][1] = az1 * plane;
+      k_soa_to_aos<TU><<<kLayoutGrid, kLayoutCells, 0, d->stream>>>(
+          p, (const TU*)d->u, d->stage, p.neq, cut[np][0], cut[np][1]);
+      ++d->launches;
+      gch_mark(d, "k_soa_to_aos");
+      cudaEventRecord(d->pipe_ev[np++], d->stream);
+    };
+    auto finish = [&](int c0, int nc) {
+      const int z0 = c0 * kz, z1 = std::min(p.nz, (c0 + nc) * kz);
+      if (ct) {
+        const dim3 g((p.nx + 31) / 32, (p.ny + 7) / 8, nc);
+        k_ct<Pol, 2><<<g, dim3(32, 8), 0, d->stream>>>(p, (const TU*)d->u, (TU*)d->u,
+                                                       (const TS*)d->E, (const TS*)d->s678,
+                                                       d->sc, kz, c0);
+        ++d->launches;
+        gch_mark(d, "k_ct_stage2");
+      }
+      const long long n = (2LL * p.NX + 2LL * (p.NY - 2)) * (z1 - z0);
+      const unsigned g = (unsigned)std::min<long long>((n + 255) / 256, 152 * 16);
+      k_ghost_ring<TU><<<g, 256, 0, d->stream>>>(p, (TU*)d->u, p.neq, 1, NG + z0, NG + z1, d->sc);
+      ++d->launches;
+      gch_mark(d, "k_ghost_ring");
+      layout_out(NG + z0, NG + z1);
+    };
+    flux2(C - 1, 1);
+    int prev = -1, prevn = 0;
+    for (int c = 0; c < C - 1; c += m) {
+      const int nc = std::min(m, C - 1 - c);
+      flux2(c, nc);
+      if (prev >= 0) finish(prev, prevn);
+      prev = c;
+      prevn = nc;
+    }
+    finish(prev, prevn);
+    finish(C - 1, 1);
+    ghost<TU>(d, (TU*)d->u, 1);  // the z ghost planes (and the rings again)
+    if (d->prim_pre) clear_prim_fresh(d);
+    layout_out(0, NG);
+    layout_out(NG + p.nz, p.NZ);
+    st |= cuda_status(cudaGetLastError());
+    // the copies, queued after every launch (a copy into pageable memory
+    // returns only when it is done)
+    for (int i = 0; i < np && st == GCH_OK; ++i) {
+      st |= cuda_status(cudaStreamWaitEvent(d->cstream, d->pipe_ev[i], 0));
+      st |= cuda_status(cudaMemcpyAsync(host + cut[i][0] * p.neq, d->stage + cut[i][0] * p.neq,
+                                        (cut[i][1] - cut[i][0]) * p.neq * sizeof(double),
+                                        cudaMemcpyDeviceToHost, d->cstream));
+    }
+    st |= cuda_status(cudaEventRecord(d->pipe_ev[gch_domain::kPipeEv - 1], d->cstream));
+    st |= cuda_status(cudaStreamWaitEvent(d->stream, d->pipe_ev[gch_domain::kPipeEv - 1], 0));
     return st;
   }
 
@@ -286,8 +394,8 @@ struct Engine {
   }
 
   static constexpr EngineOps ops() {
-    return EngineOps{&get_dt, &tstep, &boundaryI, &calcprim,
-                     &upload, &download_u, &download_prim, &loopfin, &probe};
+    return EngineOps{&get_dt,   &tstep,      &boundaryI, &calcprim, &upload,
+                     &download_u, &download_prim, &loopfin, &probe,  &tstep_dl};
   }
 };
 

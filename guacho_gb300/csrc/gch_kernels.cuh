@@ -676,15 +676,17 @@ flux_body(const KParams& p, const typename Src<Pol, NEQ, STAGE, PRIM_IN>::TIn* _
   raise_err(&sc->err, err);
 }
 
+// grid (ceil(nx/TX), ceil(ny/TY), z chunks); block z works chunk bz0 + z
+// (kz planes each), so a launch can cover a slab of chunks
 template <class Pol, int SOLVER, int NEQ, int STAGE, bool PRIM_IN, int LIM>
 __global__ void __launch_bounds__(NT, Pol::kMinBlocks)
 k_flux(KParams p, const typename Src<Pol, NEQ, STAGE, PRIM_IN>::TIn* __restrict__ src,
        const typename Pol::TU* u,
        typename std::conditional<STAGE == 1, typename Pol::TS, typename Pol::TU>::type* dst,
        typename Pol::TS* __restrict__ E, typename Pol::TS* __restrict__ s678,
-       StepScalars* sc, int kz) {
+       StepScalars* sc, int kz, int bz0 = 0) {
   flux_body<Pol, SOLVER, NEQ, STAGE, PRIM_IN, LIM>(p, src, u, dst, E, s678, sc, kz, blockIdx.x,
-                                                   blockIdx.y, blockIdx.z);
+                                                   blockIdx.y, blockIdx.z + bz0);
 }
 // Products rounded on their own (never fused into a following sum), so the
 // CFL candidate rounds the same way in every kernel that inlines it (the
@@ -878,8 +880,8 @@ ct_body(const KParams& p, const typename Pol::TU* u,
   }
 }
 
-// block (32, 8); grid (ceil(nx/32), ceil(ny/8), ceil(nz/kz)).  Enough blocks
-// per SM to keep loads in flight for this bandwidth-bound update: four for
+// block (32, 8); grid (ceil(nx/32), ceil(ny/8), z chunks of kz planes from
+// chunk bz0).  Enough blocks per SM to keep loads in flight for this bandwidth-bound update: four for
 // stage 1, six for stage 2 (measured on the 256^3 turbulence box: stage 2
 // 0.202 -> 0.184 ms with six; stage 1 0.180 -> 0.184 ms, so it keeps four).
 template <class Pol, int STAGE>
@@ -887,8 +889,8 @@ __global__ void __launch_bounds__(256, STAGE == 2 ? 6 : 4)
 k_ct(KParams p, const typename Pol::TU* u,
      typename std::conditional<STAGE == 1, typename Pol::TS, typename Pol::TU>::type* dst,
      const typename Pol::TS* __restrict__ E, const typename Pol::TS* __restrict__ s678,
-     StepScalars* sc, int kz) {
-  ct_body<Pol, STAGE>(p, u, dst, E, s678, sc, kz, blockIdx.x, blockIdx.y, blockIdx.z);
+     StepScalars* sc, int kz, int bz0 = 0) {
+  ct_body<Pol, STAGE>(p, u, dst, E, s678, sc, kz, blockIdx.x, blockIdx.y, blockIdx.z + bz0);
 }
 
 // ---------------------------------------------------------------------------
@@ -960,6 +962,22 @@ __device__ __forceinline__ int ghost_map(int c, int n, int L, int blo, int bhi, 
   if ((lo ? blo : bhi) == GCH_BC_OTHER) return c;
   return ghost_src(c, n, blo, bhi, flip);
 }
+// the ghost cell (ax, ay, az) from its interior source
+template <class T>
+__device__ __forceinline__ void ghost_fill_at(const KParams& p, T* a, int neq, int L, int ax,
+                                              int ay, int az) {
+  bool fx, fy, fz;
+  const int sx = ghost_map(ax, p.nx, L, p.bc[0], p.bc[1], fx);
+  const int sy = ghost_map(ay, p.ny, L, p.bc[2], p.bc[3], fy);
+  const int sz = ghost_map(az, p.nz, L, p.bc[4], p.bc[5], fz);
+  if (sx == ax && sy == ay && sz == az) return;  // only walls without a rule
+  const long long di = cell_index(p, ax, ay, az), si = cell_index(p, sx, sy, sz);
+  for (int q = 0; q < neq; ++q) {
+    T v = a[q * p.fs + si];
+    if ((fx && q == 1) || (fy && q == 2) || (fz && q == 3)) v = neg(v);
+    a[q * p.fs + di] = v;
+  }
+}
 template <class T>
 __device__ __forceinline__ void ghost_all_cell(const KParams& p, T* a, int neq, int L,
                                                long long t) {
@@ -984,17 +1002,7 @@ __device__ __forceinline__ void ghost_all_cell(const KParams& p, T* a, int neq, 
     ay = ghost_rest((int)(r % (p.NY - b)), L, p.ny);
     az = ghost_rest((int)(r / (p.NY - b)), L, p.nz);
   }
-  bool fx, fy, fz;
-  const int sx = ghost_map(ax, p.nx, L, p.bc[0], p.bc[1], fx);
-  const int sy = ghost_map(ay, p.ny, L, p.bc[2], p.bc[3], fy);
-  const int sz = ghost_map(az, p.nz, L, p.bc[4], p.bc[5], fz);
-  if (sx == ax && sy == ay && sz == az) return;  // only walls without a rule
-  const long long di = cell_index(p, ax, ay, az), si = cell_index(p, sx, sy, sz);
-  for (int q = 0; q < neq; ++q) {
-    T v = a[q * p.fs + si];
-    if ((fx && q == 1) || (fy && q == 2) || (fz && q == 3)) v = neg(v);
-    a[q * p.fs + di] = v;
-  }
+  ghost_fill_at<T>(p, a, neq, L, ax, ay, az);
 }
 
 // block 256; grid-stride over ghost_all_count cells
@@ -1005,6 +1013,34 @@ __global__ void __launch_bounds__(256) k_ghost_all(KParams p, T* a, int neq, int
   const long long n = ghost_all_count(p, layers);
   for (long long t = blockIdx.x * 256LL + threadIdx.x; t < n; t += (long long)gridDim.x * 256)
     ghost_all_cell<T>(p, a, neq, layers, t);
+}
+
+// The x and y ghost cells of the interior planes az in [az0, az1) (array
+// coordinates), the cells of those planes that the whole-shell fill writes:
+// per plane the y band over every x, then the x band over the other rows.
+// Their sources lie in the same plane, so a slab of planes can be filled as
+// soon as its interior cells are final.  block 256; grid-stride.
+template <class T>
+__global__ void __launch_bounds__(256) k_ghost_ring(KParams p, T* a, int neq, int L, int az0,
+                                                    int az1, const StepScalars* sc) {
+  if (!sc->active) return;
+  const long long b = 2 * L;
+  const long long per = b * p.NX + (p.NY - b) * b;
+  const long long n = per * (az1 - az0);
+  for (long long t = blockIdx.x * 256LL + threadIdx.x; t < n; t += (long long)gridDim.x * 256) {
+    const int az = az0 + (int)(t / per);
+    long long r = t % per;
+    int ax, ay;
+    if (r < b * p.NX) {
+      ax = (int)(r % p.NX);
+      ay = ghost_band((int)(r / p.NX), L, p.ny);
+    } else {
+      r -= b * p.NX;
+      ax = ghost_band((int)(r % b), L, p.nx);
+      ay = ghost_rest((int)(r / b), L, p.ny);
+    }
+    ghost_fill_at<T>(p, a, neq, L, ax, ay, az);
+  }
 }
 
 // block 128; grid (ceil(N0/128), N1, 2*layers) over the transverse extent
@@ -1689,12 +1725,14 @@ k_aos_to_soa(KParams p, const double* __restrict__ aos, T* __restrict__ soa, int
   }
 }
 
+// cells [cb, ce) of the host layout only when ce > 0 (a slab of planes)
 template <class T>
 __global__ void __launch_bounds__(kLayoutCells)
-k_soa_to_aos(KParams p, const T* __restrict__ soa, double* __restrict__ aos, int neq) {
+k_soa_to_aos(KParams p, const T* __restrict__ soa, double* __restrict__ aos, int neq,
+             long long cb = 0, long long ce = 0) {
   __shared__ double buf[kLayoutCells * kLayoutPad];
-  const long long n = (long long)p.NX * p.NY * p.NZ;
-  for (long long c0 = (long long)blockIdx.x * kLayoutCells; c0 < n;
+  const long long n = ce > 0 ? ce : (long long)p.NX * p.NY * p.NZ;
+  for (long long c0 = cb + (long long)blockIdx.x * kLayoutCells; c0 < n;
        c0 += (long long)gridDim.x * kLayoutCells) {
     const int m = (int)min((long long)kLayoutCells, n - c0);
     if (threadIdx.x < m) {

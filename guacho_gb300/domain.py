@@ -182,6 +182,10 @@ class Domain:
     def launches_per_step(self) -> int:
         return self._lib.gch_launches_per_step(self._h)
 
+    def step_host_overlaps(self) -> bool:
+        """Whether step_host copies u back behind the second half step."""
+        return bool(self._lib.gch_step_host_overlaps(self._h))
+
     @property
     def kz(self) -> int:
         """z planes per block of the stage kernels."""
