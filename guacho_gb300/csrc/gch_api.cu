@@ -137,9 +137,16 @@ int host_out_finish(gch_domain* d, double* h, const double* view) {
 
 bool gch::pipe_ok(const gch_domain* d) {
   const gch::KParams& k = d->kp;
+  // the plain FP64 step is bound by its arithmetic (about 140 ms at 256^3
+  // against 11 ms of copies), and its one-block-per-SM stage kernels lose
+  // more to the partial waves of slab launches than the overlap saves
+  // (measured: 172 ms per step overlapped)
+  if (d->mode == GCH_FP64) return false;
   if (d->prim_in || d->hp.cooling == GCH_COOL_H || k.eta != 0.0 || d->hp.th_cond != GCH_TC_OFF)
     return false;
   if ((k.bc_user && k.nsph > 0) || k.solver == GCH_SOLVER_HLLE_SPLIT_ALL) return false;
+  // the deferred first stage: no source terms, no passive scalars
+  if (k.user_src || k.eight_wave || (k.neq != 5 && k.neq != 8)) return false;
   // every side at least one cell: the whole-shell fill of one layer
   return k.nx >= 1 && k.ny >= 1 && (k.nz + d->kz - 1) / d->kz >= 3;
 }
@@ -297,6 +304,7 @@ int gch_destroy(gch_domain_t* d) {
   cudaFree(d->sc);
   cudaFree(d->tmaps);
   cudaFree(d->stage);
+  cudaFree(d->dif);
   cudaFree(d->tcw);
   cudaFree(d->tc_min);
   if (d->tc_min_host) cudaFreeHost(d->tc_min_host);
@@ -568,15 +576,18 @@ int gch_step_host(gch_domain_t* d, double* u, int current_iter, int n_iter, doub
                   double tprint, double* dt, int* dump_flag) {
   if (!d || !u || !dt || !dump_flag) return GCH_ERR_PARAM;
   int st = GCH_OK;
-  const double* src = host_in(d, u, st);
-  st |= engine(d).upload(d, src);
-  if (d->prim_in) st |= engine(d).calcprim(d);
-  k_set_ctrl<<<1, 1, 0, d->stream>>>(d->sc, current_iter, n_iter, current_time, tprint, 0.0, 0.0, 1);
-  st |= engine(d).get_dt(d);
   if (gch::pipe_ok(d)) {
-    // the download of u overlaps the second stage
-    st |= engine(d).tstep_dl(d, u);
+    // the copies of u in and out overlap the step
+    k_set_ctrl<<<1, 1, 0, d->stream>>>(d->sc, current_iter, n_iter, current_time, tprint, 0.0,
+                                       0.0, 1);
+    st |= engine(d).step_host(d, u);
   } else {
+    const double* src = host_in(d, u, st);
+    st |= engine(d).upload(d, src);
+    if (d->prim_in) st |= engine(d).calcprim(d);
+    k_set_ctrl<<<1, 1, 0, d->stream>>>(d->sc, current_iter, n_iter, current_time, tprint, 0.0,
+                                       0.0, 1);
+    st |= engine(d).get_dt(d);
     st |= engine(d).tstep(d);
     if (d->hp.th_cond != GCH_TC_OFF && st == GCH_OK) {
       st |= fetch_scalars(d);  // the conduction substeps need dt on the host

@@ -41,6 +41,11 @@ struct gch_domain {
   // the z chunks [zc0, zc0 + zcn) of kz planes that the next stage launch
   // covers (all of them when zcn == 0): a slab of the pipelined second stage
   int zc0 = 0, zcn = 0;
+  // the next first-stage launch defers its update: it writes the flux
+  // differences to `dif` (3 x neq fields of the stage type, allocated on
+  // first use) for k_s1_apply
+  bool defer = false;
+  void* dif = nullptr;
   // gch_step_host's download behind the second stage: the copy stream and
   // one event per copied slab plus one for the last copy
   cudaStream_t cstream = nullptr;
@@ -86,9 +91,10 @@ struct EngineOps {
   int (*download_prim)(gch_domain*, double*);
   int (*loopfin)(gch_domain*);        // device time-loop tail
   int (*probe)(gch_domain*);          // stage-1 fluxes alone (autotuner)
-  // tstep, then u copied into the host array `host` (reference layout)
-  // slab by slab behind the second stage; only for domains pipe_ok accepts
-  int (*tstep_dl)(gch_domain*, double* host);
+  // gch_step_host's upload, get_timestep and tstep with the copies in and
+  // out of the host array `host` (reference layout) overlapped with the
+  // step; only for domains pipe_ok accepts (the step's controls are set)
+  int (*step_host)(gch_domain*, double* host);
 };
 
 // Whether gch_step_host can overlap the download of u with the second

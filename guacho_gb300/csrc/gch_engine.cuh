@@ -36,6 +36,20 @@ struct Engine {
     using TD = typename std::conditional<STAGE == 1, TS, TU>::type;
     using TC = typename Ops<Pol>::TC;
     constexpr size_t smem = FluxLayout<Pol, NEQ, STAGE, PRIM_IN>::kBytes;
+    if constexpr (STAGE == 1 && !PRIM_IN && (NEQ == 5 || NEQ == 8)) {
+      if (d->defer) {  // the flux differences into dif, no update
+        static bool attr_d = false;
+        if (!attr_d) {
+          cudaFuncSetAttribute(k_flux<Pol, SOLVER, NEQ, STAGE, PRIM_IN, LIM, true>,
+                               cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+          attr_d = true;
+        }
+        k_flux<Pol, SOLVER, NEQ, STAGE, PRIM_IN, LIM, true><<<grid, block, smem, d->stream>>>(
+            p, (const TIn*)src, (const TU*)d->u, (TD*)d->dif, (TS*)d->E, (TS*)d->s678, d->sc,
+            d->kz, d->zc0);
+        return;
+      }
+    }
     static bool attr = false;  // once per instantiation
     if (!attr) {
       cudaFuncSetAttribute(k_flux<Pol, SOLVER, NEQ, STAGE, PRIM_IN, LIM>,
@@ -241,30 +255,140 @@ struct Engine {
     return st;
   }
 
-  // ---- tstep + download, the download behind the second stage ------------
-  // The second stage, its CT and the ring of x/y ghost cells run slab by
-  // slab of z chunks; each finished slab of u is transposed into the staging
-  // buffer (host layout) and copied to `host` on the copy stream while the
-  // next slabs compute.  The last chunk's fluxes go first: its E is the z
-  // neighbour of the first slab's CT under periodic walls.  Each slab's CT
-  // waits for the fluxes of the slab after it (its E at the slab's top
-  // plane).  The z ghost planes follow the whole-shell fill at the end (it
-  // writes the rings again with the same values).  The kernels' per-plane
-  // results do not depend on where a chunk or slab begins, so u ends the
-  // same, bit for bit, as with tstep and a download.
-  static int tstep_dl(gch_domain* d, double* host) {
+  // ---- gch_step_host with the copies overlapped ----------------------------
+  // Upload: the host array goes up in slabs of z chunks (copy-engine copies
+  // into the staging buffer on the copy stream); each slab is transposed into
+  // u as it lands, its CFL candidates are reduced, and the first stage's
+  // fluxes of the slab below it (which needs one plane of this one) run
+  // deferred: they do not depend on dt, so they write their flux differences
+  // and k_s1_apply finishes the update once k_dtfin has dt.  Download: the
+  // second stage, its CT and the x/y ghost ring run slab by slab; each
+  // finished slab is transposed into the staging buffer and copied to the
+  // host while the next slabs compute.  The last chunk's second-stage
+  // fluxes go first: under periodic walls its E is the z neighbour of the
+  // first slab's CT.  Each slab's CT follows the fluxes of the slab after it
+  // (its E at the slab's top plane).  The z ghost planes follow the
+  // whole-shell fill at the end (it writes the rings again with the same
+  // values).  The kernels' per-plane results do not depend on where a chunk
+  // or slab begins, and the deferred update rounds as the fused one, so the
+  // host array ends bit for bit as with upload, get_timestep, tstep and
+  // download in turn.
+  static constexpr int kUpEv = 0, kDownEv = 10;  // event slots of the two phases
+  // Slabs of z chunks covering chunks [c0, c0 + n): two single-chunk slabs at
+  // the end where the pipeline waits on them (`small_first`: the start), the
+  // rest in at most 8 slabs of equal depth; at most 10 slabs.  out[i] =
+  // {first chunk, chunks}; returns the count.
+  static int slab_plan(int c0, int n, bool small_first, int (*out)[2]) {
+    int ns = 0;
+    if (n <= 4) {
+      for (int i = 0; i < n; ++i) out[ns][0] = c0 + i, out[ns++][1] = 1;
+      return ns;
+    }
+    const int r = n - 2, m = (r + 7) / 8;
+    int c = c0;
+    if (small_first)
+      for (int i = 0; i < 2; ++i) out[ns][0] = c++, out[ns++][1] = 1;
+    for (int left = r; left > 0; left -= m) {
+      out[ns][0] = c;
+      out[ns++][1] = std::min(m, left);
+      c += std::min(m, left);
+    }
+    if (!small_first)
+      for (int i = 0; i < 2; ++i) out[ns][0] = c++, out[ns++][1] = 1;
+    return ns;
+  }
+  static int step_host(gch_domain* d, double* host) {
     const KParams& p = d->kp;
+    int st = GCH_OK;
     d->launches = 0;
-    int st = stage1(d);
     if (!d->cstream) {
       st |= cuda_status(cudaStreamCreateWithFlags(&d->cstream, cudaStreamNonBlocking));
       for (int i = 0; i < gch_domain::kPipeEv && st == GCH_OK; ++i)
         st |= cuda_status(cudaEventCreateWithFlags(&d->pipe_ev[i], cudaEventDisableTiming));
       if (st) return st;
     }
+    if (!d->dif) {
+      st |= cuda_status(cudaMalloc(&d->dif, (size_t)3 * p.neq * p.fs * sizeof(TS)));
+      if (st) return st;
+    }
+    if (d->prim_pre) clear_prim_fresh(d);  // the first stage recovers from u here
+    const int kz = d->kz, C = (p.nz + kz - 1) / kz;
+    const long long plane = (long long)p.NX * p.NY;
+    const size_t rowb = (size_t)p.neq * sizeof(double);
+    const dim3 cblock(32, 8);
+    int ne = kUpEv;
+    // array planes [az0, az1) from the host into u
+    auto up_slab = [&](int az0, int az1) {
+      const long long c0 = az0 * plane, c1 = az1 * plane;
+      st |= cuda_status(cudaMemcpyAsync(d->stage + c0 * p.neq, host + c0 * p.neq,
+                                        (size_t)(c1 - c0) * rowb, cudaMemcpyHostToDevice,
+                                        d->cstream));
+      st |= cuda_status(cudaEventRecord(d->pipe_ev[ne], d->cstream));
+      st |= cuda_status(cudaStreamWaitEvent(d->stream, d->pipe_ev[ne++], 0));
+      k_aos_to_soa<TU><<<kLayoutGrid, kLayoutCells, 0, d->stream>>>(p, d->stage, (TU*)d->u,
+                                                                     p.neq, c0, c1);
+      ++d->launches;
+      gch_mark(d, "k_aos_to_soa");
+    };
+    auto cfl_slab = [&](int c0, int nc) {
+      const dim3 g((p.nx + 31) / 32, (p.ny + 7) / 8, nc);
+      with_neq(p.neq, [&](auto N) {
+        k_cfl<Pol, decltype(N)::value, false><<<g, cblock, 0, d->stream>>>(
+            p, (const TU*)d->u, d->sc, kz, nullptr, c0);
+      });
+      ++d->launches;
+      gch_mark(d, "k_cfl");
+    };
+    auto flux1_deferred = [&](int c0, int nc) {
+      d->zc0 = c0;
+      d->zcn = nc;
+      d->defer = true;
+      st |= flux<1, false>(d, d->u, d->up);
+      d->defer = false;
+      d->zc0 = d->zcn = 0;
+      ++d->launches;
+      gch_mark(d, "k_flux_stage1");
+    };
+    // the last slabs are single chunks: only their fluxes remain once the
+    // last copy has landed
+    int plan[10][2];
+    const int ns = slab_plan(0, C, false, plan);
+    for (int i = 0; i < ns; ++i) {
+      const int c = plan[i][0], nc = plan[i][1];
+      const int az0 = c == 0 ? 0 : NG + c * kz;
+      const int az1 = c + nc == C ? p.NZ : NG + std::min(p.nz, (c + nc) * kz);
+      up_slab(az0, az1);
+      cfl_slab(c, nc);
+      if (i > 0) flux1_deferred(plan[i - 1][0], plan[i - 1][1]);
+    }
+    flux1_deferred(plan[ns - 1][0], plan[ns - 1][1]);
+    k_dtfin<<<1, 1, 0, d->stream>>>(d->sc, p.cfl, p.dx, p.dy, p.dz);
+    ++d->launches;
+    gch_mark(d, "k_dtfin");
+    // the first stage's update, its CT and boundaryII on up
+    with_neq(p.neq, [&](auto N) {
+      constexpr int n = decltype(N)::value;
+      if constexpr (n == 5 || n == 8)
+        k_s1_apply<Pol, n><<<cell_grid(p), cblock, 0, d->stream>>>(p, (const TU*)d->u, (TS*)d->up,
+                                                                    (const TS*)d->dif, d->sc);
+    });
+    ++d->launches;
+    gch_mark(d, "k_s1_apply");
+    if (p.neq >= 8 && p.flux_cd) {
+      k_ct<Pol, 1><<<column_grid(p), cblock, 0, d->stream>>>(
+          p, (const TU*)d->u, (TS*)d->up, (const TS*)d->E, (const TS*)d->s678, d->sc, kzc);
+      ++d->launches;
+      gch_mark(d, "k_ct_stage1");
+    }
+    ghost<TS>(d, (TS*)d->up, 2);
+    return st | stage2_dl(d, host);
+  }
+
+  static int stage2_dl(gch_domain* d, double* host) {
+    const KParams& p = d->kp;
+    int st = GCH_OK;
     const bool ct = p.neq >= 8 && p.flux_cd;
     const int kz = d->kz, C = (p.nz + kz - 1) / kz;
-    const int m = std::max(1, (C - 1 + 7) / 8);  // chunks per slab: about 8 slabs
     const long long plane = (long long)p.NX * p.NY;
     long long cut[gch_domain::kPipeEv][2];
     int np = 0;
@@ -284,7 +408,7 @@ struct Engine {
           p, (const TU*)d->u, d->stage, p.neq, cut[np][0], cut[np][1]);
       ++d->launches;
       gch_mark(d, "k_soa_to_aos");
-      cudaEventRecord(d->pipe_ev[np++], d->stream);
+      cudaEventRecord(d->pipe_ev[kDownEv + np++], d->stream);
     };
     auto finish = [&](int c0, int nc) {
       const int z0 = c0 * kz, z1 = std::min(p.nz, (c0 + nc) * kz);
@@ -303,16 +427,15 @@ struct Engine {
       gch_mark(d, "k_ghost_ring");
       layout_out(NG + z0, NG + z1);
     };
+    // the first slabs are single chunks: the first copy starts early
+    int plan[10][2];
+    const int ns = slab_plan(0, C - 1, true, plan);
     flux2(C - 1, 1);
-    int prev = -1, prevn = 0;
-    for (int c = 0; c < C - 1; c += m) {
-      const int nc = std::min(m, C - 1 - c);
-      flux2(c, nc);
-      if (prev >= 0) finish(prev, prevn);
-      prev = c;
-      prevn = nc;
+    for (int i = 0; i < ns; ++i) {
+      flux2(plan[i][0], plan[i][1]);
+      if (i > 0) finish(plan[i - 1][0], plan[i - 1][1]);
     }
-    finish(prev, prevn);
+    finish(plan[ns - 1][0], plan[ns - 1][1]);
     finish(C - 1, 1);
     ghost<TU>(d, (TU*)d->u, 1);  // the z ghost planes (and the rings again)
     if (d->prim_pre) clear_prim_fresh(d);
@@ -322,7 +445,7 @@ struct Engine {
     // the copies, queued after every launch (a copy into pageable memory
     // returns only when it is done)
     for (int i = 0; i < np && st == GCH_OK; ++i) {
-      st |= cuda_status(cudaStreamWaitEvent(d->cstream, d->pipe_ev[i], 0));
+      st |= cuda_status(cudaStreamWaitEvent(d->cstream, d->pipe_ev[kDownEv + i], 0));
       st |= cuda_status(cudaMemcpyAsync(host + cut[i][0] * p.neq, d->stage + cut[i][0] * p.neq,
                                         (cut[i][1] - cut[i][0]) * p.neq * sizeof(double),
                                         cudaMemcpyDeviceToHost, d->cstream));
@@ -395,7 +518,7 @@ struct Engine {
 
   static constexpr EngineOps ops() {
     return EngineOps{&get_dt,   &tstep,      &boundaryI, &calcprim, &upload,
-                     &download_u, &download_prim, &loopfin, &probe,  &tstep_dl};
+                     &download_u, &download_prim, &loopfin, &probe,  &step_host};
   }
 };
 

@@ -201,7 +201,11 @@ __device__ __forceinline__ void cp_async_wait_all() {
 // The body takes the block's tile coordinates (bx, by) and z chunk (bz) as
 // arguments: the one-box kernel passes blockIdx, the grouped kernel of many
 // boxes passes the coordinates decoded from its linear block index.
-template <class Pol, int SOLVER, int NEQ, int STAGE, bool PRIM_IN, int LIM>
+// DEFER (first stage only): instead of the update, write the three flux
+// differences (fr - fl, gr - gl, hr - hl) of every updated field q to fields
+// 3q, 3q+1, 3q+2 of `dst`: the fluxes do not depend on dt, so they can be
+// computed before get_timestep has it (k_s1_apply finishes the update).
+template <class Pol, int SOLVER, int NEQ, int STAGE, bool PRIM_IN, int LIM, bool DEFER = false>
 __device__ __forceinline__ void
 flux_body(const KParams& p, const typename Src<Pol, NEQ, STAGE, PRIM_IN>::TIn* __restrict__ src,
           const typename Pol::TU* u,
@@ -566,7 +570,7 @@ flux_body(const KParams& p, const typename Src<Pol, NEQ, STAGE, PRIM_IN>::TIn* _
     auto upd = [&](int q) { return !ct || q < 5 || q >= 8; };
     const long long c = cell_index(p, axc, ayc, az);
     typename Pol::TU uq[NEQ];
-    if (active) {
+    if (active && !DEFER) {
 #pragma unroll
       for (int q = 0; q < NEQ; ++q)
         if (upd(q)) uq[q] = u[q * p.fs + c];
@@ -583,7 +587,8 @@ flux_body(const KParams& p, const typename Src<Pol, NEQ, STAGE, PRIM_IN>::TIn* _
       TC sv[NEQ];
 #pragma unroll
       for (int q = 0; q < NEQ; ++q) sv[q] = TC(0);
-      const bool src_terms = p.user_src || (NEQ >= 8 && p.eight_wave);
+      // (a deferred first stage runs only without source terms)
+      const bool src_terms = !DEFER && (p.user_src || (NEQ >= 8 && p.eight_wave));
       if (src_terms) {
         TC pcen[NEQ];
 #pragma unroll
@@ -645,7 +650,13 @@ flux_body(const KParams& p, const typename Src<Pol, NEQ, STAGE, PRIM_IN>::TIn* _
       }
 #pragma unroll
       for (int q = 0; q < NEQ; ++q) {
-        if (upd(q)) {
+        if constexpr (DEFER) {
+          if (upd(q)) {
+            dst[(3 * q) * p.fs + c] = sF[q][ty][tx + 1] - sF[q][ty][tx];
+            dst[(3 * q + 1) * p.fs + c] = sG[q][ty + 1][tx] - sG[q][ty][tx];
+            dst[(3 * q + 2) * p.fs + c] = sH[hn][q][ty][tx] - sH[hp][q][ty][tx];
+          }
+        } else if (upd(q)) {
           auto unew = Ops<Pol>::update(Ops<Pol>::ld(uq[q]), dtdx, dtdy, dtdz,
                                        sF[q][ty][tx], sF[q][ty][tx + 1], sG[q][ty][tx],
                                        sG[q][ty + 1][tx], sH[hp][q][ty][tx], sH[hn][q][ty][tx]);
@@ -678,15 +689,45 @@ flux_body(const KParams& p, const typename Src<Pol, NEQ, STAGE, PRIM_IN>::TIn* _
 
 // grid (ceil(nx/TX), ceil(ny/TY), z chunks); block z works chunk bz0 + z
 // (kz planes each), so a launch can cover a slab of chunks
-template <class Pol, int SOLVER, int NEQ, int STAGE, bool PRIM_IN, int LIM>
+template <class Pol, int SOLVER, int NEQ, int STAGE, bool PRIM_IN, int LIM, bool DEFER = false>
 __global__ void __launch_bounds__(NT, Pol::kMinBlocks)
 k_flux(KParams p, const typename Src<Pol, NEQ, STAGE, PRIM_IN>::TIn* __restrict__ src,
        const typename Pol::TU* u,
        typename std::conditional<STAGE == 1, typename Pol::TS, typename Pol::TU>::type* dst,
        typename Pol::TS* __restrict__ E, typename Pol::TS* __restrict__ s678,
        StepScalars* sc, int kz, int bz0 = 0) {
-  flux_body<Pol, SOLVER, NEQ, STAGE, PRIM_IN, LIM>(p, src, u, dst, E, s678, sc, kz, blockIdx.x,
-                                                   blockIdx.y, blockIdx.z + bz0);
+  static_assert(!DEFER || (STAGE == 1 && !PRIM_IN), "only the first stage from u defers");
+  flux_body<Pol, SOLVER, NEQ, STAGE, PRIM_IN, LIM, DEFER>(p, src, u, dst, E, s678, sc, kz,
+                                                          blockIdx.x, blockIdx.y, blockIdx.z + bz0);
+}
+
+// The first stage's update of a deferred first stage (DEFER above), once dt
+// is known: up = u - dt/2 * divF from the stored flux differences, through
+// the same Ops::update as the fused stage (a difference minus a zero left
+// flux is the difference itself), so up ends the same bit for bit.
+// block (32, 8); grid (ceil(nx/32), ceil(ny/8), nz)
+template <class Pol, int NEQ>
+__global__ void __launch_bounds__(256)
+k_s1_apply(KParams p, const typename Pol::TU* __restrict__ u, typename Pol::TS* __restrict__ up,
+           const typename Pol::TS* __restrict__ dif, const StepScalars* sc) {
+  using TC = typename Ops<Pol>::TC;
+  if (!sc->active) return;
+  const int ci = blockIdx.x * 32 + threadIdx.x, cj = blockIdx.y * 8 + threadIdx.y;
+  if (ci >= p.nx || cj >= p.ny) return;
+  const TC dtdx = par<TC>(sc->dtd[0][0], sc->dtdf[0][0]);
+  const TC dtdy = par<TC>(sc->dtd[0][1], sc->dtdf[0][1]);
+  const TC dtdz = par<TC>(sc->dtd[0][2], sc->dtdf[0][2]);
+  const bool ct = NEQ >= 8 && p.flux_cd;
+  const long long c = cell_index(p, ci + NG, cj + NG, (int)blockIdx.z + NG);
+#pragma unroll
+  for (int q = 0; q < NEQ; ++q) {
+    if (ct && q >= 5 && q < 8) continue;
+    const TC a = (TC)dif[(3 * q) * p.fs + c], b = (TC)dif[(3 * q + 1) * p.fs + c],
+             h = (TC)dif[(3 * q + 2) * p.fs + c];
+    up[q * p.fs + c] = store_as<typename Pol::TS>(
+        Ops<Pol>::update(Ops<Pol>::ld(u[q * p.fs + c]), dtdx, dtdy, dtdz, TC(0), a, TC(0), b,
+                         TC(0), h));
+  }
 }
 // Products rounded on their own (never fused into a following sum), so the
 // CFL candidate rounds the same way in every kernel that inlines it (the
@@ -1188,12 +1229,13 @@ cfl_body(const KParams& p,
   cfl_block_reduce<TC>(dtp, bad, sc);
 }
 
-// block (32, 8); grid (ceil(nx/32), ceil(ny/8), ceil(nz/kz))
+// block (32, 8); grid (ceil(nx/32), ceil(ny/8), z chunks of kz planes from
+// chunk bz0)
 template <class Pol, int NEQ, bool PRIM_IN>
 __global__ void __launch_bounds__(256)
 k_cfl(KParams p, const typename std::conditional<PRIM_IN, typename Pol::TS, typename Pol::TU>::type* src,
-      StepScalars* sc, int kz, typename Pol::TS* store = nullptr) {
-  cfl_body<Pol, NEQ, PRIM_IN>(p, src, sc, kz, blockIdx.x, blockIdx.y, blockIdx.z, store);
+      StepScalars* sc, int kz, typename Pol::TS* store = nullptr, int bz0 = 0) {
+  cfl_body<Pol, NEQ, PRIM_IN>(p, src, sc, kz, blockIdx.x, blockIdx.y, blockIdx.z + bz0, store);
 }
 
 // get_timestep's scalar tail (src/hydro_core.f90:677-694) and the bookkeeping
@@ -1702,13 +1744,14 @@ __device__ __forceinline__ long long layout_cell(const KParams& p, long long t) 
   return cell_index(p, ax, ay, az);
 }
 
-// block 256; any grid (grid-stride over the cells)
+// block 256; any grid (grid-stride over the cells; [cb, ce) only when ce > 0)
 template <class T>
 __global__ void __launch_bounds__(kLayoutCells)
-k_aos_to_soa(KParams p, const double* __restrict__ aos, T* __restrict__ soa, int neq) {
+k_aos_to_soa(KParams p, const double* __restrict__ aos, T* __restrict__ soa, int neq,
+             long long cb = 0, long long ce = 0) {
   __shared__ double buf[kLayoutCells * kLayoutPad];
-  const long long n = (long long)p.NX * p.NY * p.NZ;
-  for (long long c0 = (long long)blockIdx.x * kLayoutCells; c0 < n;
+  const long long n = ce > 0 ? ce : (long long)p.NX * p.NY * p.NZ;
+  for (long long c0 = cb + (long long)blockIdx.x * kLayoutCells; c0 < n;
        c0 += (long long)gridDim.x * kLayoutCells) {
     const int m = (int)min((long long)kLayoutCells, n - c0);
     for (int i = threadIdx.x; i < m * neq; i += kLayoutCells) {

@@ -107,6 +107,17 @@ struct Ops<PolFP64> {
 };
 
 // ---------------------------------------------------------------------------
+// dt/dx (fr - fl) + dt/dy (gr - gl) + dt/dz (hr - hl) in FP32 with its
+// roundings spelled out (one product, two fused multiply-adds), so that every
+// kernel that inlines it rounds the same way whatever the compiler would
+// contract: the deferred first stage and its update kernel agree bit for bit
+// with the fused stage.
+__device__ __forceinline__ float flux_sum(float dtdx, float dtdy, float dtdz, float fl, float fr,
+                                          float gl, float gr, float hl, float hr) {
+  return __fmaf_rn(dtdz, hr - hl, __fmaf_rn(dtdy, gr - gl, __fmul_rn(dtdx, fr - fl)));
+}
+
+// ---------------------------------------------------------------------------
 // Error-free FP32 transformations (compensated "double-float" arithmetic).
 // The FP32 units are compiled with multiply-add contraction, which could
 // fuse a product into a following sum once these are inlined: every product
@@ -269,8 +280,7 @@ struct Ops<PolMixed> {
   __device__ __forceinline__ static double update(double u, float dtdx, float dtdy, float dtdz,
                                                   float fl, float fr, float gl, float gr,
                                                   float hl, float hr) {
-    const float d = dtdx * (fr - fl) + dtdy * (gr - gl) + dtdz * (hr - hl);
-    return u - f2d(d);
+    return u - f2d(flux_sum(dtdx, dtdy, dtdz, fl, fr, gl, gr, hl, hr));
   }
 
   __device__ __forceinline__ static double ct(double u, float hdta, float a0, float a1,
@@ -366,8 +376,7 @@ struct Ops<PolKahan> {
   __device__ __forceinline__ static float2 update(float2 u, float dtdx, float dtdy, float dtdz,
                                                   float fl, float fr, float gl, float gr,
                                                   float hl, float hr) {
-    const float d = dtdx * (fr - fl) + dtdy * (gr - gl) + dtdz * (hr - hl);
-    return addf(u, -d);
+    return addf(u, -flux_sum(dtdx, dtdy, dtdz, fl, fr, gl, gr, hl, hr));
   }
 
   __device__ __forceinline__ static float2 ct(float2 u, float hdta, float a0, float a1,

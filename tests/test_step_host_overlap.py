@@ -1,10 +1,12 @@
-"""gch_step_host with the download of u behind the second half step: the
-second stage, its CT and the x/y ghost ring run slab by slab of z chunks and
-each finished slab is copied to the host while the next ones compute.  The
-host array must end bit for bit as the serial order leaves it (get_timestep,
-tstep, download), ghost cells included, for every precision, wall type,
-page-locked and pageable host arrays, and boxes whose z extent is not a
-multiple of the chunk depth."""
+"""gch_step_host with its copies overlapped with the step: u goes up slab by
+slab of z chunks while the CFL pass and the first stage's fluxes (deferred:
+their flux differences, the update once dt is known) start on the slabs that
+have landed; the second stage, its CT and the x/y ghost ring run slab by slab
+and each finished slab is copied to the host while the next ones compute.
+The host array must end bit for bit as the serial order leaves it (upload,
+get_timestep, tstep, download), ghost cells included, for every precision,
+wall type, page-locked and pageable host arrays, and boxes whose z extent is
+not a multiple of the chunk depth."""
 import numpy as np
 import pytest
 
@@ -42,7 +44,8 @@ def test_overlapped_step_host_equals_serial(gpu_lib, name, prec, host):
         b.init(u0)
         if a.kz * 3 > p.nz:  # at least three z chunks
             a.kz = b.kz = max(1, p.nz // 4)
-        assert a.step_host_overlaps()
+        # the FP64 step keeps the serial order (bound by its arithmetic)
+        assert a.step_host_overlaps() == (prec != P.FP64)
         h = a.download()
         if host == "pinned":
             h = _pinned(h)
