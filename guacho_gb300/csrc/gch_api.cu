@@ -117,6 +117,14 @@ const double* host_in(gch_domain* d, const double* h, int& st) {
                                 cudaMemcpyHostToDevice, d->stream));
   return d->stage;
 }
+// whether the GPU addresses host array h directly (page-locked, mapped)
+bool host_mapped(const double* h) {
+  cudaPointerAttributes a;
+  const bool m = cudaPointerGetAttributes(&a, h) == cudaSuccess && a.type == cudaMemoryTypeHost &&
+                 a.devicePointer;
+  cudaGetLastError();
+  return m;
+}
 // the device view of a host output array, or the staging buffer (then
 // host_out_finish copies it to the host)
 double* host_out(gch_domain* d, double* h) {
@@ -576,8 +584,12 @@ int gch_step_host(gch_domain_t* d, double* u, int current_iter, int n_iter, doub
                   double tprint, double* dt, int* dump_flag) {
   if (!d || !u || !dt || !dump_flag) return GCH_ERR_PARAM;
   int st = GCH_OK;
-  if (gch::pipe_ok(d)) {
-    // the copies of u in and out overlap the step
+  if (gch::pipe_ok(d) && !host_mapped(u)) {
+    // a pageable array: the copy-engine copies of u in and out overlap the
+    // step.  (A page-locked array keeps the serial order below: the layout
+    // kernels move it over the link themselves, which never stalled, while
+    // copy-engine DMA on this system took 40-540 ms for a step now and then,
+    // with or without the overlap.)
     k_set_ctrl<<<1, 1, 0, d->stream>>>(d->sc, current_iter, n_iter, current_time, tprint, 0.0,
                                        0.0, 1);
     st |= engine(d).step_host(d, u);

@@ -255,7 +255,7 @@ struct Engine {
     return st;
   }
 
-  // ---- gch_step_host with the copies overlapped ----------------------------
+  // ---- gch_step_host with the copies overlapped (pageable host arrays) ------
   // Upload: the host array goes up in slabs of z chunks (copy-engine copies
   // into the staging buffer on the copy stream); each slab is transposed into
   // u as it lands, its CFL candidates are reduced, and the first stage's
@@ -400,7 +400,8 @@ struct Engine {
       ++d->launches;
       gch_mark(d, "k_flux_stage2");
     };
-    // planes [az0, az1) of u (array coordinates) into the staging buffer
+    // planes [az0, az1) of u (array coordinates) into the staging buffer, for
+    // a copy queued below
     auto layout_out = [&](int az0, int az1) {
       cut[np][0] = az0 * plane;
       cut[np][1] = az1 * plane;
@@ -437,7 +438,19 @@ struct Engine {
     }
     finish(plan[ns - 1][0], plan[ns - 1][1]);
     finish(C - 1, 1);
-    ghost<TU>(d, (TU*)d->u, 1);  // the z ghost planes (and the rings again)
+    // the rest of the whole-shell fill: the z ghost planes, and the rings of
+    // the outermost planes
+    {
+      const long long n = 2LL * p.NX * p.NY;
+      const unsigned g = (unsigned)std::min<long long>((n + 255) / 256, 152 * 16);
+      k_ghost_all<TU><<<g, 256, 0, d->stream>>>(p, (TU*)d->u, p.neq, 1, d->sc, 1);
+      const long long nr = 2LL * p.NX + 2LL * (p.NY - 2);
+      const unsigned gr = (unsigned)std::min<long long>((nr + 255) / 256, 152 * 16);
+      k_ghost_ring<TU><<<gr, 256, 0, d->stream>>>(p, (TU*)d->u, p.neq, 1, 0, 1, d->sc);
+      k_ghost_ring<TU><<<gr, 256, 0, d->stream>>>(p, (TU*)d->u, p.neq, 1, p.NZ - 1, p.NZ, d->sc);
+      d->launches += 3;
+      gch_mark(d, "k_ghost");
+    }
     if (d->prim_pre) clear_prim_fresh(d);
     layout_out(0, NG);
     layout_out(NG + p.nz, p.NZ);

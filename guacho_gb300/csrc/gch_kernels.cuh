@@ -1046,12 +1046,13 @@ __device__ __forceinline__ void ghost_all_cell(const KParams& p, T* a, int neq, 
   ghost_fill_at<T>(p, a, neq, L, ax, ay, az);
 }
 
-// block 256; grid-stride over ghost_all_count cells
+// block 256; grid-stride over ghost_all_count cells (with zband_only, the z
+// band alone: the ghost planes of z, which come first in that order)
 template <class T>
 __global__ void __launch_bounds__(256) k_ghost_all(KParams p, T* a, int neq, int layers,
-                                                   const StepScalars* sc) {
+                                                   const StepScalars* sc, int zband_only = 0) {
   if (!sc->active) return;
-  const long long n = ghost_all_count(p, layers);
+  const long long n = zband_only ? 2LL * layers * p.NX * p.NY : ghost_all_count(p, layers);
   for (long long t = blockIdx.x * 256LL + threadIdx.x; t < n; t += (long long)gridDim.x * 256)
     ghost_all_cell<T>(p, a, neq, layers, t);
 }

@@ -254,16 +254,18 @@ int gch_tc_info(gch_domain_t* d, int* nsteps, double* dt_cond);
 /* gch_get_timestep + gch_tstep with the state in HOST memory: uploads u,
  * steps once and downloads u, for callers whose hooks need the host arrays
  * current after every step.  *dt and *dump_flag as gch_get_timestep.
- * Where gch_step_host_overlaps says so, u goes up slab by slab of z while
- * the first half step's fluxes start on the slabs that have landed, and
- * comes back slab by slab while the second half step still computes the
- * slabs above (same bits as the serial order). */
+ * A page-locked u is read and written over the host link by the layout
+ * kernels.  A pageable u goes through copy-engine copies; where
+ * gch_step_host_overlaps says so, it goes up slab by slab of z while the
+ * first half step's fluxes start on the slabs that have landed, and comes
+ * back slab by slab while the second half step still computes the slabs
+ * above (same bits as the serial order). */
 int gch_step_host(gch_domain_t* d, double* u, int current_iter, int n_iter,
                   double current_time, double tprint, double* dt, int* dump_flag);
 
-/* 1 when gch_step_host overlaps its copies with the step: the upload with
- * the CFL pass and the first half step's fluxes, the download with the
- * second half step.  FP32 domains without user spheres, table cooling,
+/* 1 when gch_step_host overlaps its copies of a pageable u with the step:
+ * the upload with the CFL pass and the first half step's fluxes, the
+ * download with the second half step.  FP32 domains without user spheres, table cooling,
  * COOL_H, resistivity, thermal conduction, source terms or passive scalars,
  * with at least three z chunks of the stage kernels (gch_get_kz); 0
  * otherwise (the serial order; always for GCH_FP64, whose step is bound by

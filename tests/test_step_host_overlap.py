@@ -1,11 +1,12 @@
-"""gch_step_host with its copies overlapped with the step: u goes up slab by
-slab of z chunks while the CFL pass and the first stage's fluxes (deferred:
-their flux differences, the update once dt is known) start on the slabs that
-have landed; the second stage, its CT and the x/y ghost ring run slab by slab
-and each finished slab is copied to the host while the next ones compute.
-The host array must end bit for bit as the serial order leaves it (upload,
-get_timestep, tstep, download), ghost cells included, for every precision,
-wall type, page-locked and pageable host arrays, and boxes whose z extent is
+"""gch_step_host with its copies of a pageable host array overlapped with the
+step: u goes up slab by slab of z chunks while the CFL pass and the first
+stage's fluxes (deferred: their flux differences, the update once dt is
+known) start on the slabs that have landed; the second stage, its CT and the
+x/y ghost ring run slab by slab and each finished slab is copied to the host
+while the next ones compute.  Page-locked arrays take the serial order
+(kernel-driven transfers).  Either way the host array must end bit for bit
+as the serial order leaves it (upload, get_timestep, tstep, download), ghost
+cells included, for every precision, wall type, and boxes whose z extent is
 not a multiple of the chunk depth."""
 import numpy as np
 import pytest
