@@ -156,8 +156,9 @@ STAGE2_KAHAN_TRAFFIC_PER_CELL = (1281077760 + 842317056) / 256 ** 3
 # the 262,144 cells; sm__inst_executed_pipe_fp64.avg.pct_of_peak_sustained_active
 # with sm__cycles_elapsed.avg gives the pipe's peak issue rate):
 #   FP64-pipe warp instructions per zone-update of a whole step
-#   k_flux stage 1 44.83 + stage 2 78.03 + k_cfl 4.62 + k_ct 0.91 + 0.90
-FP64_PIPE_WARP_INST_PER_ZONE = 44.83 + 78.03 + 4.62 + 0.91 + 0.90
+#   k_flux stage 1 44.83 + stage 2 78.04 + k_cfl 1.62 (its square roots and
+#   quotients on the integer pipes) + k_ct 0.91 + 0.90
+FP64_PIPE_WARP_INST_PER_ZONE = 44.83 + 78.04 + 1.62 + 0.91 + 0.90
 #   peak: 0.0530 FP64-pipe warp instructions per SM cycle (stage 2: 20,456,302
 #   instructions over 152 SMs x 4,283,477 cycles at 59.27% of peak)
 FP64_PIPE_PEAK_PER_SM_CYCLE = 20456302 / (152 * 4283477.11) / 0.5927
