@@ -630,7 +630,11 @@ def run_ours(args, dist: Dist) -> None:
     sbz = step_bytes_per_zone(headline)
     step_gbs = value / dist.ws * sbz / 1e9
     step_roof = {"bytes_per_zone_update": sbz, "achieved": step_gbs, "peak": pk["hbm_gbs"],
-                 "unit": "GB/s", "frac": step_gbs / pk["hbm_gbs"]}
+                 "unit": "GB/s", "frac": step_gbs / pk["hbm_gbs"],
+                 # the compulsory bytes 2 neq w_u (u read once, written once),
+                 # the bound of a temporally fused single-sweep step
+                 "compulsory_bytes_per_zone_update": 2 * 8 * 8,
+                 "compulsory_frac": value / dist.ws * 128 / 1e9 / pk["hbm_gbs"]}
 
     # ---- batched uneven boxes ----------------------------------------------
     batched = batched_run(args, headline) if args.batch_boxes > 0 else None
