@@ -640,6 +640,12 @@ def run_ours(args, dist: Dist) -> None:
     batched = batched_run(args, headline) if args.batch_boxes > 0 else None
     if batched:
         batched["vs_single_box"] = batched["value"] / (value / dist.ws)
+        # the same boxes with FP64 u (FP32 arithmetic, FP64 pressure recovery)
+        bm = batched_run(args, P.FP32_MIXED)
+        batched["fp32_mixed_fp64u"] = {
+            k: bm[k] for k in ("value", "step_ms_p50", "step_ms_p99", "l1_err_max_over_boxes",
+                               "l1_err_median_over_boxes")}
+        batched["fp32_mixed_fp64u"]["vs_single_box"] = bm["value"] / (mixed_value / dist.ws)
 
     # ---- CPU baseline (rank 0, N=1 only) ------------------------------------
     cpu = None

@@ -105,6 +105,7 @@ int autotune(gch_batch* b) {
   b->tune_ms.clear();
   float best = 0.f;
   int best_kz = std::min(8, nzmax), best_bps = 3;
+  st |= b->gops->prep(b->boxes.data(), n, b->stream);
   for (int kz : {2, 4, 8, 16, 32}) {
     if (kz > nzmax && kz != 2) break;
     for (int bps : {0, 1, 2, 3}) {
@@ -130,7 +131,7 @@ int autotune(gch_batch* b) {
   }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
-  // the probes counted pressure floors of the stage-1 states: clear them
+  // the probes (and the CFL pass before them) counted pressure floors: clear them
   k_batch_clear_info<<<grid_of(n), 128, 0, b->stream>>>(b->sc_list, n);
   st |= cuda_ok(cudaGetLastError());
   b->kz = best_kz;

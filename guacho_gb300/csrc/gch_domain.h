@@ -119,6 +119,9 @@ struct GroupOps {
   // the stage-1 flux kernel alone (writes up and E, leaves u): the
   // autotuner's timing probe
   int (*probe)(gch_domain* const* boxes, int n, int kz, int bps, int* queue, cudaStream_t s);
+  // before the probes: the stored primitives the first stage reads on the
+  // FP32 + FP64-u path (the CFL pass of the current u; leaves u)
+  int (*prep)(gch_domain* const* boxes, int n, cudaStream_t s);
 };
 extern const GroupOps kGroupMixed;
 extern const GroupOps kGroupKahan;

@@ -123,14 +123,15 @@ __global__ void __launch_bounds__(128) k_ghost_grp(const __grid_constant__ Group
                 l / (x.gx * x.gy));
 }
 
-// a1 = u, or primit with table cooling (PRIM_IN)
+// a1 = u, or primit with table cooling (PRIM_IN); a2 = where the primitives
+// recovered from u are stored for the first stage (null: not stored)
 template <class Pol, int NEQ, bool PRIM_IN>
 __global__ void __launch_bounds__(256) k_cfl_grp(const __grid_constant__ GroupArgs g) {
   using TSrc = typename std::conditional<PRIM_IN, typename Pol::TS, typename Pol::TU>::type;
   const GroupBox& x = g.box[group_box(g, blockIdx.x)];
   const int l = blockIdx.x - x.blk0;
   cfl_body<Pol, NEQ, PRIM_IN>(x.p, (const TSrc*)x.a1, x.sc, x.kz, l % x.gx, (l / x.gx) % x.gy,
-                              l / (x.gx * x.gy));
+                              l / (x.gx * x.gy), (typename Pol::TS*)x.a2);
 }
 
 // The user boundary spheres of the boxes that have them: a2 = the array to
@@ -154,12 +155,13 @@ __global__ void __launch_bounds__(256) k_cool_grp(const __grid_constant__ GroupA
 }
 
 // calcprim of the ghost shell after boundaryI: a1 = u, a2 = primit,
-// i0 = blocks per box (grid-stride over the box's shell)
-template <class Pol, int NEQ>
+// i0 = blocks per box (grid-stride over the box's shell).  OWN: the shell
+// of the primitives get_timestep's CFL pass stored (k_prim_shell_own)
+template <class Pol, int NEQ, bool OWN = false>
 __global__ void __launch_bounds__(256) k_calcprim_shell_grp(const __grid_constant__ GroupArgs g) {
   const GroupBox& x = g.box[group_box(g, blockIdx.x)];
-  calcprim_shell_body<Pol, NEQ>(x.p, (const typename Pol::TU*)x.a1, (typename Pol::TS*)x.a2,
-                                x.sc, blockIdx.x - x.blk0, g.i0);
+  calcprim_shell_body<Pol, NEQ, OWN>(x.p, (const typename Pol::TU*)x.a1,
+                                     (typename Pol::TS*)x.a2, x.sc, blockIdx.x - x.blk0, g.i0);
 }
 
 // one thread per box

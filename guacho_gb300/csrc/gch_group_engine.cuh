@@ -101,7 +101,9 @@ struct GroupEngine {
   static int flux(gch_domain* const* boxes, int n, int kz, int bps, int* queue, cudaStream_t s) {
     const KParams& p0 = boxes[0]->kp;
     const int sv = p0.solver, neq = p0.neq, lim = p0.limiter;
-    const bool prim_in = boxes[0]->prim_in;
+    // the first stage reads stored primitives with table cooling and on the
+    // FP32 + FP64-u path (stored by the CFL pass of the same step)
+    const bool prim_in = boxes[0]->prim_in || boxes[0]->prim_pre;
     auto setup = [&](GroupBox& x, gch_domain* d) -> long long {
       const KParams& p = d->kp;
       // stage source: u (or primit) for the first half step, up for the second
@@ -221,14 +223,17 @@ struct GroupEngine {
   }
 
   // get_timestep's CFL pass: from u, or from primit with table cooling (the
-  // reference takes dt from the stored, cooled primitives)
+  // reference takes dt from the stored, cooled primitives).  On the FP32 +
+  // FP64-u path it stores the primitives it recovers from u for the first
+  // stage, and the ghost shell's follow (prim_shell).
   static int cfl(gch_domain* const* boxes, int n, int, cudaStream_t s) {
     const int neq = boxes[0]->kp.neq;
     const bool prim_in = boxes[0]->prim_in;
-    return chunks(
+    int st = chunks(
         boxes, n,
         [&](GroupBox& x, gch_domain* d) {
           x.a1 = prim_in ? d->primit : d->u;
+          x.a2 = d->prim_pre ? d->primit : nullptr;
           return column_setup(x, d->kp);
         },
         [&](GroupArgs& g, unsigned b) {
@@ -238,6 +243,8 @@ struct GroupEngine {
           else if (prim_in) k_cfl_grp<Pol, 5, true><<<b, dim3(32, 8), 0, s>>>(g);
           else k_cfl_grp<Pol, 5, false><<<b, dim3(32, 8), 0, s>>>(g);
         });
+    if (boxes[0]->prim_pre) st |= prim_shell(boxes, n, true, s);
+    return st;
   }
 
   // table cooling of every box (updates u(5) and primit), one block per
@@ -263,6 +270,10 @@ struct GroupEngine {
 
   // primitives of every box's ghost shell after boundaryI (table cooling)
   static int calcprim_shell(gch_domain* const* boxes, int n, cudaStream_t s) {
+    return prim_shell(boxes, n, false, s);
+  }
+  // own: the shell of the primitives the CFL pass stored (FP32 + FP64 u)
+  static int prim_shell(gch_domain* const* boxes, int n, bool own, cudaStream_t s) {
     const int neq = boxes[0]->kp.neq;
     const int per = std::max(4, 152 * 16 / n);
     return chunks(
@@ -275,7 +286,9 @@ struct GroupEngine {
         [&](GroupArgs& g, unsigned b) {
           if (!b) return;
           g.i0 = per;
-          if (neq == 8) k_calcprim_shell_grp<Pol, 8><<<b, 256, 0, s>>>(g);
+          if (own && neq == 8) k_calcprim_shell_grp<Pol, 8, true><<<b, 256, 0, s>>>(g);
+          else if (own) k_calcprim_shell_grp<Pol, 5, true><<<b, 256, 0, s>>>(g);
+          else if (neq == 8) k_calcprim_shell_grp<Pol, 8><<<b, 256, 0, s>>>(g);
           else k_calcprim_shell_grp<Pol, 5><<<b, 256, 0, s>>>(g);
         });
   }
@@ -318,7 +331,11 @@ struct GroupEngine {
     return flux<1>(boxes, n, kz, bps, queue, s);
   }
 
-  static constexpr GroupOps ops() { return GroupOps{&step, &probe}; }
+  static int prep(gch_domain* const* boxes, int n, cudaStream_t s) {
+    return boxes[0]->prim_pre ? cfl(boxes, n, 0, s) : GCH_OK;
+  }
+
+  static constexpr GroupOps ops() { return GroupOps{&step, &probe, &prep}; }
 };
 
 }  // namespace gch
