@@ -843,81 +843,75 @@ ct_body(const KParams& p, const typename Pol::TU* u,
   const TC hx = par<TC>(0.5 * sc->dtd[STAGE - 1][0], sc->hdtdf[STAGE - 1][0]);
   const TC hy = par<TC>(0.5 * sc->dtd[STAGE - 1][1], sc->hdtdf[STAGE - 1][1]);
   const TC hz = par<TC>(0.5 * sc->dtd[STAGE - 1][2], sc->hdtdf[STAGE - 1][2]);
-  const long long sx = 1, sy = p.pitch, sz = (long long)p.pitch * p.NY;
-  const bool inxy = ax > NG && ax < NG + p.nx - 1 && ay > NG && ay < NG + p.ny - 1;
 
-  // E component q at a face neighbour; the ghost layer follows
+  // E at the face neighbours of this column.  The ghost layer follows
   // boundaryI_ef (src/flux_cd_module.f90:45-237): periodic copy, outflow
-  // copy, closed copy with the normal component of the x/y walls negated
-  // and nothing negated on z walls
-  auto e_ghost = [&](int q, int bx, int by, int bz) -> TC {
-    bool fx = false, fy = false, fz = false;
-    const int gx = ghost_src(bx, p.nx, p.bc[0], p.bc[1], fx);
-    const int gy = ghost_src(by, p.ny, p.bc[2], p.bc[3], fy);
-    const int gz = ghost_src(bz, p.nz, p.bc[4], p.bc[5], fz);
-    TC v = (TC)E[q * p.fs + cell_index(p, gx, gy, gz)];
-    if ((fx && q == 0) || (fy && q == 1)) v = -v;
-    return v;
-  };
+  // copy, closed copy with the normal component of the x/y walls negated and
+  // nothing negated on z walls.  The CT reads E1 only at y and z neighbours,
+  // E2 only at x and z neighbours and E3 only in the plane, so a neighbour
+  // beyond a wall is its source cell with no sign change, and every
+  // neighbour is a fixed offset from the cell: the x/y offsets are mapped
+  // once per column, the z ones at the box's bottom and top planes.
+  // 32-bit cell offsets: a padded field is below 2^31 cells (larger boxes are
+  // refused at creation).
+  bool f_;
+  const int pitch = p.pitch, plane = p.pitch * p.NY;
+  const int oxm = ghost_src(ax - 1, p.nx, p.bc[0], p.bc[1], f_) - ax;
+  const int oxp = ghost_src(ax + 1, p.nx, p.bc[0], p.bc[1], f_) - ax;
+  const int oym = (ghost_src(ay - 1, p.ny, p.bc[2], p.bc[3], f_) - ay) * pitch;
+  const int oyp = (ghost_src(ay + 1, p.ny, p.bc[2], p.bc[3], f_) - ay) * pitch;
+  const int ozb = (ghost_src(kb + NG - 1, p.nz, p.bc[4], p.bc[5], f_) - (kb + NG)) * plane;
+  const int ozt = (ghost_src(p.nz + NG, p.nz, p.bc[4], p.bc[5], f_) - (p.nz + NG - 1)) * plane;
+  const long long fs = p.fs;
+  const typename Pol::TS* __restrict__ E1 = E;
+  const typename Pol::TS* __restrict__ E2 = E + fs;
+  const typename Pol::TS* __restrict__ E3 = E + 2 * fs;
+  const typename Pol::TU* U6 = u + 5 * fs;
+  const typename Pol::TU* U7 = u + 6 * fs;
+  const typename Pol::TU* U8 = u + 7 * fs;
+  TD* D6 = dst + 5 * fs;
+  TD* D7 = dst + 6 * fs;
+  TD* D8 = dst + 7 * fs;
+  int c = (int)cell_index(p, ax, ay, kb + NG);
 
   // E1 and E2 of this column at planes k-1 and k: the z neighbours march
   // with the column, so each plane loads only its k+1 values
-  TC e1m = e_ghost(0, ax, ay, kb + NG - 1), e2m = e_ghost(1, ax, ay, kb + NG - 1);
-  TC e1c = e_ghost(0, ax, ay, kb + NG), e2c = e_ghost(1, ax, ay, kb + NG);
-  for (int k = kb; k < ke; ++k) {
-    const int az = k + NG;
-    const long long c = cell_index(p, ax, ay, az);
+  TC e1m = (TC)E1[c + ozb], e2m = (TC)E2[c + ozb];
+  TC e1c = (TC)E1[c], e2c = (TC)E2[c];
+  for (int k = kb; k < ke; ++k, c += plane) {
     if (k + 1 < ke) {  // next plane's B and E into L2 (no registers held)
-      asm volatile("prefetch.global.L2 [%0];" ::"l"(u + 5 * p.fs + c + sz));
-      asm volatile("prefetch.global.L2 [%0];" ::"l"(u + 6 * p.fs + c + sz));
-      asm volatile("prefetch.global.L2 [%0];" ::"l"(u + 7 * p.fs + c + sz));
-      asm volatile("prefetch.global.L2 [%0];" ::"l"(E + 2 * p.fs + c + sz));
+      asm volatile("prefetch.global.L2 [%0];" ::"l"(U6 + c + plane));
+      asm volatile("prefetch.global.L2 [%0];" ::"l"(U7 + c + plane));
+      asm volatile("prefetch.global.L2 [%0];" ::"l"(U8 + c + plane));
+      asm volatile("prefetch.global.L2 [%0];" ::"l"(E3 + c + plane));
       if (k + 2 < p.nz) {
-        asm volatile("prefetch.global.L2 [%0];" ::"l"(E + c + 2 * sz));
-        asm volatile("prefetch.global.L2 [%0];" ::"l"(E + p.fs + c + 2 * sz));
+        asm volatile("prefetch.global.L2 [%0];" ::"l"(E1 + c + 2 * plane));
+        asm volatile("prefetch.global.L2 [%0];" ::"l"(E2 + c + 2 * plane));
       }
     }
-    // the face neighbours of E needed by the three components
-    TC e1p, e2p;
-    if (k + 1 < p.nz) {
-      e1p = (TC)E[c + sz];
-      e2p = (TC)E[p.fs + c + sz];
-    } else {
-      e1p = e_ghost(0, ax, ay, az + 1);
-      e2p = e_ghost(1, ax, ay, az + 1);
-    }
+    const int oz = k + 1 < p.nz ? plane : ozt;  // the plane above, or its source
+    const TC e1p = (TC)E1[c + oz], e2p = (TC)E2[c + oz];
     const TC e2zm = e2m, e2zp = e2p, e1zm = e1m, e1zp = e1p;
     e1m = e1c; e2m = e2c; e1c = e1p; e2c = e2p;
-    TC e3ym, e3yp, e3xm, e3xp, e2xm, e2xp, e1ym, e1yp;
-    if (inxy) {
-      const typename Pol::TS* E1 = E;
-      const typename Pol::TS* E2 = E + p.fs;
-      const typename Pol::TS* E3 = E + 2 * p.fs;
-      e3ym = (TC)E3[c - sy]; e3yp = (TC)E3[c + sy];
-      e3xm = (TC)E3[c - sx]; e3xp = (TC)E3[c + sx];
-      e2xm = (TC)E2[c - sx]; e2xp = (TC)E2[c + sx];
-      e1ym = (TC)E1[c - sy]; e1yp = (TC)E1[c + sy];
-    } else {
-      e3ym = e_ghost(2, ax, ay - 1, az); e3yp = e_ghost(2, ax, ay + 1, az);
-      e3xm = e_ghost(2, ax - 1, ay, az); e3xp = e_ghost(2, ax + 1, ay, az);
-      e2xm = e_ghost(1, ax - 1, ay, az); e2xp = e_ghost(1, ax + 1, ay, az);
-      e1ym = e_ghost(0, ax, ay - 1, az); e1yp = e_ghost(0, ax, ay + 1, az);
-    }
-    const auto u6 = Ops<Pol>::ld(u[5 * p.fs + c]);
-    const auto u7 = Ops<Pol>::ld(u[6 * p.fs + c]);
-    const auto u8 = Ops<Pol>::ld(u[7 * p.fs + c]);
+    const TC e3ym = (TC)E3[c + oym], e3yp = (TC)E3[c + oyp];
+    const TC e3xm = (TC)E3[c + oxm], e3xp = (TC)E3[c + oxp];
+    const TC e2xm = (TC)E2[c + oxm], e2xp = (TC)E2[c + oxp];
+    const TC e1ym = (TC)E1[c + oym], e1yp = (TC)E1[c + oyp];
+    const auto u6 = Ops<Pol>::ld(U6[c]);
+    const auto u7 = Ops<Pol>::ld(U7[c]);
+    const auto u8 = Ops<Pol>::ld(U8[c]);
     // src/flux_cd_module.f90:311-321
     auto b6 = Ops<Pol>::ct(u6, hy, e3ym, e3yp, hz, e2zm, e2zp, true);
     auto b7 = Ops<Pol>::ct(u7, hx, e3xm, e3xp, hz, e1zm, e1zp, false);
     auto b8 = Ops<Pol>::ct(u8, hx, e2xm, e2xp, hy, e1ym, e1yp, true);
     if (p.eight_wave) {
       b6 = add_source<Pol>(b6, dt, dtf, s678[c]);
-      b7 = add_source<Pol>(b7, dt, dtf, s678[p.fs + c]);
-      b8 = add_source<Pol>(b8, dt, dtf, s678[2 * p.fs + c]);
+      b7 = add_source<Pol>(b7, dt, dtf, s678[fs + c]);
+      b8 = add_source<Pol>(b8, dt, dtf, s678[2 * fs + c]);
     }
-    dst[5 * p.fs + c] = store_as<TD>(b6);
-    dst[6 * p.fs + c] = store_as<TD>(b7);
-    dst[7 * p.fs + c] = store_as<TD>(b8);
+    D6[c] = store_as<TD>(b6);
+    D7[c] = store_as<TD>(b7);
+    D8[c] = store_as<TD>(b8);
   }
 }
 
