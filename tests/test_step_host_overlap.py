@@ -23,6 +23,8 @@ CASES = {
     "ot_ragged_walls": lambda: problems.orszag_tang(37, 19, 45, **WALLS),
     "blast_outflow": lambda: problems.blast(24, p_in=1.0),
     "ot_no_flux_cd": lambda: problems.orszag_tang(24, 24, 30, enable_flux_cd=False),
+    # hydro (5 equations, HLLC): the deferred first stage without B
+    "hydro_hllc": lambda: __import__("test_parity_gpu")._hydro_state(24),
 }
 
 
