@@ -36,7 +36,9 @@ struct Engine {
     using TD = typename std::conditional<STAGE == 1, TS, TU>::type;
     using TC = typename Ops<Pol>::TC;
     constexpr size_t smem = FluxLayout<Pol, NEQ, STAGE, PRIM_IN>::kBytes;
-    if constexpr (STAGE == 1 && !PRIM_IN && (NEQ == 5 || NEQ == 8)) {
+    // (the FP32 policies only: the FP64 step keeps the serial order)
+    if constexpr (STAGE == 1 && !PRIM_IN && (NEQ == 5 || NEQ == 8) &&
+                  !std::is_same<Pol, PolFP64>::value) {
       if (d->defer) {  // the flux differences into dif, no update
         static bool attr_d = false;
         if (!attr_d) {
@@ -298,6 +300,8 @@ struct Engine {
     return ns;
   }
   static int step_host(gch_domain* d, double* host) {
+    // the FP64 step keeps the serial order (pipe_ok); no deferred stage there
+    if constexpr (std::is_same<Pol, PolFP64>::value) return GCH_ERR_PARAM;
     const KParams& p = d->kp;
     int st = GCH_OK;
     d->launches = 0;
@@ -368,7 +372,7 @@ struct Engine {
     // the first stage's update, its CT and boundaryII on up
     with_neq(p.neq, [&](auto N) {
       constexpr int n = decltype(N)::value;
-      if constexpr (n == 5 || n == 8)
+      if constexpr ((n == 5 || n == 8) && !std::is_same<Pol, PolFP64>::value)
         k_s1_apply<Pol, n><<<cell_grid(p), cblock, 0, d->stream>>>(p, (const TU*)d->u, (TS*)d->up,
                                                                     (const TS*)d->dif, d->sc);
     });
