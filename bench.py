@@ -692,13 +692,26 @@ def run_ours(args, dist: Dist) -> None:
 
 def run_ncu_case(args) -> None:
     """A short host-driven step sequence (no CUDA graphs) of the benchmark
-    problem for profiler captures: --size, --precision, --steps."""
+    problem for profiler captures: --size, --precision, --steps; with
+    --ncu-batch the batched set of boxes instead (grouped steps)."""
     from guacho_gb300 import build as gbuild
     gbuild.build(verbose=False)
     from guacho_gb300 import params as P
     from guacho_gb300 import problems
     from guacho_gb300.domain import Domain
     prec = {"kahan": P.FP32_KAHAN, "mixed": P.FP32_MIXED, "fp64": P.FP64}[args.precision]
+    if args.ncu_batch:  # the batched set: 3 grouped warm-up steps (tuning), then --steps
+        from guacho_gb300.domain import Batch
+        boxes = problems.batch_boxes(nbox=args.batch_boxes, precision=prec)
+        b = Batch([q for q, _ in boxes])
+        for i, (_, u) in enumerate(boxes):
+            b.upload(i, u)
+        b.advance(3)
+        b.advance(args.steps)
+        print(json.dumps({"ncu_case": args.precision, "boxes": len(boxes), "steps": args.steps,
+                          "zones": sum(q.nx * q.ny * q.nz for q, _ in boxes)}))
+        b.close()
+        return
     p, u0 = problems.turbulence(args.size)
     with Domain(p.replace(precision=prec)) as d:
         d.init(u0)
@@ -800,6 +813,8 @@ def main():
                     help="ncu dram bytes per launch of the dominant kernel, if known")
     ap.add_argument("--ncu-case", action="store_true",
                     help="run a short host-driven step sequence for profiler captures")
+    ap.add_argument("--ncu-batch", action="store_true",
+                    help="with --ncu-case: the batched set (--batch-boxes) instead of one box")
     ap.add_argument("--precision", default="kahan", choices=["kahan", "mixed", "fp64"])
     ap.add_argument("--configs", action="store_true",
                     help="time the other benchmark configurations (one line each)")
