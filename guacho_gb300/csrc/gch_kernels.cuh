@@ -1329,33 +1329,33 @@ __device__ __forceinline__ void cool_body(const KParams& p, typename Pol::TU* u,
   const long long c = cell_index(p, ci + NG, cj + NG, ck + NG);
   if constexpr (!std::is_same<Pol, PolFP64>::value) {
     cool_f32<Pol, NEQ>(p, u, primit, sc, c);
-    return;
-  }
-  double uu[NEQ], pp[NEQ];
+  } else {
+    double uu[NEQ], pp[NEQ];
 #pragma unroll
-  for (int q = 0; q < NEQ; ++q) uu[q] = to_d(u[q * p.fs + c]);
-  unsigned pfl = 0;
-  double T;
-  Ops<PolFP64>::u2prim<NEQ>(p, uu, pp, pfl, &T);
-  if (T > p.tab_Tmin) {
-    const double Eth0 = p.cv * pp[4];
-    double aloss;
-    if (T > 1e8) {
-      aloss = p.tab_tail * sqrt(T);
-    } else {
-      int if1 = (int)(log10(T) * p.tab_inv_dlog) - p.tab_i0;
-      if1 = max(0, min(if1, p.ntab - 2));
-      const double T0 = p.tabT[if1], c0 = p.tabL[if1];
-      const double T1 = p.tabT[if1 + 1], c1 = p.tabL[if1 + 1];
-      aloss = (c1 - c0) * (T - T0) / (T1 - T0) + c0;
+    for (int q = 0; q < NEQ; ++q) uu[q] = to_d(u[q * p.fs + c]);
+    unsigned pfl = 0;
+    double T;
+    Ops<PolFP64>::u2prim<NEQ>(p, uu, pp, pfl, &T);
+    if (T > p.tab_Tmin) {
+      const double Eth0 = p.cv * pp[4];
+      double aloss;
+      if (T > 1e8) {
+        aloss = p.tab_tail * sqrt(T);
+      } else {
+        int if1 = (int)(log10(T) * p.tab_inv_dlog) - p.tab_i0;
+        if1 = max(0, min(if1, p.ntab - 2));
+        const double T0 = p.tabT[if1], c0 = p.tabL[if1];
+        const double T1 = p.tabT[if1 + 1], c1 = p.tabL[if1 + 1];
+        aloss = (c1 - c0) * (T - T0) / (T1 - T0) + c0;
+      }
+      const double dens = pp[0];
+      const double ce = (aloss * (dens * dens)) / (Eth0 * p.Psc);
+      pp[4] = pp[4] * exp(-ce * (sc->dt * p.tsc));
+      u[4 * p.fs + c] = from_d<typename Pol::TU>(uu[4] - Eth0 + p.cv * pp[4]);
     }
-    const double dens = pp[0];
-    const double ce = (aloss * (dens * dens)) / (Eth0 * p.Psc);
-    pp[4] = pp[4] * exp(-ce * (sc->dt * p.tsc));
-    u[4 * p.fs + c] = from_d<typename Pol::TU>(uu[4] - Eth0 + p.cv * pp[4]);
-  }
 #pragma unroll
-  for (int q = 0; q < NEQ; ++q) primit[q * p.fs + c] = (typename Pol::TS)pp[q];
+    for (int q = 0; q < NEQ; ++q) primit[q * p.fs + c] = (typename Pol::TS)pp[q];
+  }
 }
 // block (32, 8); grid (ceil(nx/32), ceil(ny/8), nz)
 template <class Pol, int NEQ>
@@ -1600,14 +1600,14 @@ __global__ void k_visc(KParams p, typename Pol::TU* u, const typename Pol::TU* w
       else
         u[q * p.fs + c] = wc + (double)(eta * lap);
     }
-    return;
-  }
-  for (int q = 0; q < NEQ; ++q) {
-    const double v = val(q, ax, ay, az);
-    u[q * p.fs + c] = from_d<typename Pol::TU>(
-        v + p.eta * (val(q, ax + 1, ay, az) + val(q, ax - 1, ay, az) + val(q, ax, ay + 1, az) +
-                     val(q, ax, ay - 1, az) + val(q, ax, ay, az + 1) + val(q, ax, ay, az - 1) -
-                     6.0 * v));
+  } else {
+    for (int q = 0; q < NEQ; ++q) {
+      const double v = val(q, ax, ay, az);
+      u[q * p.fs + c] = from_d<typename Pol::TU>(
+          v + p.eta * (val(q, ax + 1, ay, az) + val(q, ax - 1, ay, az) + val(q, ax, ay + 1, az) +
+                       val(q, ax, ay - 1, az) + val(q, ax, ay, az + 1) + val(q, ax, ay, az - 1) -
+                       6.0 * v));
+    }
   }
 }
 
