@@ -397,12 +397,21 @@ flux_body(const KParams& p, const typename Src<Pol, NEQ, STAGE, PRIM_IN>::TIn* _
     if (k + 1 < ke) fetch_col(k + 1 + NG + H);
   };
 
+  // Whether a plane starts with a barrier.  The update of the plane before
+  // reads the face fluxes, which the next faces overwrite only after the
+  // barrier that precedes them, and its own cell of P; the staging of the
+  // next plane writes this thread's cell, its column ring and halo cells,
+  // which nothing reads before that barrier.  So without source terms no
+  // thread can overwrite what another still reads, and the barrier is left
+  // out.  With source terms the update reads neighbouring cells of P (the
+  // eight-wave div B), and the TMA rows of stage 2 wait for that update.
+  const bool plane_sync = p.user_src || (NEQ >= 8 && p.eight_wave);
   for (int k = k0; k < ke; ++k) {
     const bool plane = k >= kb;
     const bool zface = k >= kb - 1;
     const bool zwork = STAGE == 1 ? zface : k >= kb - 2;
     const int az = k + NG;
-    if (plane) {
+    if (plane && plane_sync) {
       if constexpr (TMA && STAGE == 2) fence_proxy_async_smem();
       __syncthreads();  // readers of the previous plane are done
       if constexpr (TMA && STAGE == 2)
