@@ -411,84 +411,10 @@ flux_body(const KParams& p, const typename Src<Pol, NEQ, STAGE, PRIM_IN>::TIn* _
     const bool zface = k >= kb - 1;
     const bool zwork = STAGE == 1 ? zface : k >= kb - 2;
     const int az = k + NG;
-    if (plane && plane_sync) {
-      if constexpr (TMA && STAGE == 2) fence_proxy_async_smem();
-      __syncthreads();  // readers of the previous plane are done
-      if constexpr (TMA && STAGE == 2)
-        if (!early2() && k > kb) tma_issue(k);
-    }
-    // 1. the column ring shifts (centre <- p(k), p(k+1) <- p(k+2)) and the
-    //    next plane of the column is formed from the fetched values
-    {
-      if constexpr (ACOL) {
-        cp_async_wait_all();  // this thread's copies
-#pragma unroll
-        for (int q = 0; q < NEQ; ++q) colr[q] = sbc.col[q][ty][tx];
-      }
-      TC nx_[NEQ];
-      S::convert(p, colr, nx_, pfl);
-#pragma unroll
-      for (int q = 0; q < NEQ; ++q) {
-        sP(q, ty + H, tx + H) = sQ[0][q][ty][tx];
-        if (STAGE == 1) {
-          sQ[0][q][ty][tx] = nx_[q];
-        } else {
-          sQ[0][q][ty][tx] = sQ[1][q][ty][tx];
-          sQ[1][q][ty][tx] = nx_[q];
-        }
-      }
-    }
-    if (plane) {
-      //  the halo of plane k
-      if constexpr (TMA) {
-        const unsigned parity = (unsigned)(k - kb) & 1u;  // one phase per plane
-        if (has_halo) {
-          if (mbar_wait(tbar, parity)) halo_from_tma();
-          else *tabort = 1;
-        }
-        fence_proxy_async_smem();  // the raw buffers are read: the next copy may overwrite
-        __syncthreads();
-        if (*tabort) {  // a copy did not arrive: report, drain, leave together
-          if (tid == 0) {
-            atomicOr(&sc->err, GCH_ERR_TIMEOUT);
-            mbar_wait(tbar, parity);
-          }
-          return;
-        }
-        if constexpr (STAGE == 1)
-          if (k + 1 < ke) tma_issue(k + 1);
-      } else {
-        if (has_halo) {
-          TC pr[NEQ];
-          S::load(p, src, gidx(i0 + hx + NG, j0 + hy + NG, az), pr, pfl);
-#pragma unroll
-          for (int q = 0; q < NEQ; ++q) sP(q, hy + H, hx + H) = pr[q];
-        }
-        __syncthreads();
-      }
-    }
-
-    // 2. all faces through one Riemann call site
-    const int nwork = plane ? NT + nfx + nfy : (zwork ? NT : 0);
     const int hslot = (k + 1) & 1;  // face k+1/2
-    for (int w = tid; w < nwork; w += NT) {
-      int kind;  // 0 = z (own column), 1 = x, 2 = y
-      int fx, fy;
-      bool need;
-      if (w < NT) {
-        kind = 0; fx = tx; fy = ty; need = active;
-      } else if (w - NT < nfx) {
-        kind = 1;
-        fx = (w - NT) % (TX + 1);
-        fy = (w - NT) / (TX + 1);
-        need = j0 + fy < p.ny && i0 + fx - 1 < p.nx;
-      } else {
-        kind = 2;
-        fx = (w - NT - nfx) % TX;
-        fy = (w - NT - nfx) / TX;
-        need = i0 + fx < p.nx && j0 + fy - 1 < p.ny;
-      }
-      if (!need) continue;
+    // one face: 0 = the z face k+1/2 of this thread's column (its own
+    // shared-memory cells only), 1 = x face (fx, fy), 2 = y face (fx, fy)
+    auto face = [&](int kind, int fx, int fy) {
       TC l[NEQ], r[NEQ], f[NEQ];
       if (kind == 0) {
         if (STAGE == 1) {
@@ -513,7 +439,7 @@ flux_body(const KParams& p, const typename Src<Pol, NEQ, STAGE, PRIM_IN>::TIn* _
             l[q] = l[q] + al * TC(0.5);
             r[q] = r[q] - ar * TC(0.5);
           }
-          if (!zface) continue;  // slope of p(kb-1) only
+          if (!zface) return;  // slope of p(kb-1) only
         }
       } else if (kind == 1) {
         const int cy = fy + H, cl = fx - 1 + H;
@@ -568,6 +494,93 @@ flux_body(const KParams& p, const typename Src<Pol, NEQ, STAGE, PRIM_IN>::TIn* _
 #pragma unroll
         for (int q = 0; q < NEQ; ++q) sG[perm<1, NEQ>(q)][fy][fx] = f[q];
       }
+    };
+    if (plane && plane_sync) {
+      if constexpr (TMA && STAGE == 2) fence_proxy_async_smem();
+      __syncthreads();  // readers of the previous plane are done
+      if constexpr (TMA && STAGE == 2)
+        if (!early2() && k > kb) tma_issue(k);
+    }
+    // 1. the column ring shifts (centre <- p(k), p(k+1) <- p(k+2)) and the
+    //    next plane of the column is formed from the fetched values
+    {
+      if constexpr (ACOL) {
+        cp_async_wait_all();  // this thread's copies
+#pragma unroll
+        for (int q = 0; q < NEQ; ++q) colr[q] = sbc.col[q][ty][tx];
+      }
+      TC nx_[NEQ];
+      S::convert(p, colr, nx_, pfl);
+#pragma unroll
+      for (int q = 0; q < NEQ; ++q) {
+        sP(q, ty + H, tx + H) = sQ[0][q][ty][tx];
+        if (STAGE == 1) {
+          sQ[0][q][ty][tx] = nx_[q];
+        } else {
+          sQ[0][q][ty][tx] = sQ[1][q][ty][tx];
+          sQ[1][q][ty][tx] = nx_[q];
+        }
+      }
+    }
+    if (plane) {
+      //  the halo of plane k
+      if constexpr (TMA) {
+        const unsigned parity = (unsigned)(k - kb) & 1u;  // one phase per plane
+        if (has_halo) {
+          if (mbar_wait(tbar, parity)) halo_from_tma();
+          else *tabort = 1;
+        } else if (active) {
+          face(0, tx, ty);  // this column's z face while the halo is converted
+        }
+        fence_proxy_async_smem();  // the raw buffers are read: the next copy may overwrite
+        __syncthreads();
+        if (*tabort) {  // a copy did not arrive: report, drain, leave together
+          if (tid == 0) {
+            atomicOr(&sc->err, GCH_ERR_TIMEOUT);
+            mbar_wait(tbar, parity);
+          }
+          return;
+        }
+        if constexpr (STAGE == 1)
+          if (k + 1 < ke) tma_issue(k + 1);
+      } else {
+        if (has_halo) {
+          TC pr[NEQ];
+          S::load(p, src, gidx(i0 + hx + NG, j0 + hy + NG, az), pr, pfl);
+#pragma unroll
+          for (int q = 0; q < NEQ; ++q) sP(q, hy + H, hx + H) = pr[q];
+        } else if (active) {
+          face(0, tx, ty);  // this column's z face while the halo is loaded
+        }
+        __syncthreads();
+      }
+    }
+
+    // 2. all faces through one Riemann call site.  In a plane, the threads
+    //    without a halo cell have already solved their column's z face
+    //    while the halo was converted (below the column shift): the loop takes
+    //    the other NRING z faces and the x and y faces, so a plane needs at
+    //    most three rounds of 256 solves instead of four.
+    const int nzw = plane ? NRING : NT;
+    const int nwork = plane ? NRING + nfx + nfy : (zwork ? NT : 0);
+    for (int w = tid; w < nwork; w += NT) {
+      int kind;  // 0 = z (own column), 1 = x, 2 = y
+      int fx, fy;
+      bool need;
+      if (w < nzw) {
+        kind = 0; fx = tx; fy = ty; need = active;
+      } else if (w - nzw < nfx) {
+        kind = 1;
+        fx = (w - nzw) % (TX + 1);
+        fy = (w - nzw) / (TX + 1);
+        need = j0 + fy < p.ny && i0 + fx - 1 < p.nx;
+      } else {
+        kind = 2;
+        fx = (w - nzw - nfx) % TX;
+        fy = (w - nzw - nfx) / TX;
+        need = i0 + fx < p.nx && j0 + fy - 1 < p.ny;
+      }
+      if (need) face(kind, fx, fy);
     }
     if (!plane) {  // column-private work only: no barrier
       if (NEQ >= 8) bzm = sP(7, ty + H, tx + H);
