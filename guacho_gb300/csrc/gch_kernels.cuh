@@ -405,7 +405,10 @@ flux_body(const KParams& p, const typename Src<Pol, NEQ, STAGE, PRIM_IN>::TIn* _
   // thread can overwrite what another still reads, and the barrier is left
   // out.  With source terms the update reads neighbouring cells of P (the
   // eight-wave div B), and the TMA rows of stage 2 wait for that update.
-  const bool plane_sync = p.user_src || (NEQ >= 8 && p.eight_wave);
+  // (The FP64 kernels, one block per SM and latency-bound, keep the barrier
+  // and the single face call site below: both changes made them slower.)
+  constexpr bool kEarlyZ = sizeof(TC) == 4;
+  const bool plane_sync = !kEarlyZ || p.user_src || (NEQ >= 8 && p.eight_wave);
   for (int k = k0; k < ke; ++k) {
     const bool plane = k >= kb;
     const bool zface = k >= kb - 1;
@@ -529,8 +532,9 @@ flux_body(const KParams& p, const typename Src<Pol, NEQ, STAGE, PRIM_IN>::TIn* _
         if (has_halo) {
           if (mbar_wait(tbar, parity)) halo_from_tma();
           else *tabort = 1;
-        } else if (active) {
-          face(0, tx, ty);  // this column's z face while the halo is converted
+        } else {
+          if constexpr (kEarlyZ)
+            if (active) face(0, tx, ty);  // this column's z face while the halo is converted
         }
         fence_proxy_async_smem();  // the raw buffers are read: the next copy may overwrite
         __syncthreads();
@@ -549,8 +553,9 @@ flux_body(const KParams& p, const typename Src<Pol, NEQ, STAGE, PRIM_IN>::TIn* _
           S::load(p, src, gidx(i0 + hx + NG, j0 + hy + NG, az), pr, pfl);
 #pragma unroll
           for (int q = 0; q < NEQ; ++q) sP(q, hy + H, hx + H) = pr[q];
-        } else if (active) {
-          face(0, tx, ty);  // this column's z face while the halo is loaded
+        } else {
+          if constexpr (kEarlyZ)
+            if (active) face(0, tx, ty);  // this column's z face while the halo is loaded
         }
         __syncthreads();
       }
@@ -561,8 +566,8 @@ flux_body(const KParams& p, const typename Src<Pol, NEQ, STAGE, PRIM_IN>::TIn* _
     //    while the halo was converted (below the column shift): the loop takes
     //    the other NRING z faces and the x and y faces, so a plane needs at
     //    most three rounds of 256 solves instead of four.
-    const int nzw = plane ? NRING : NT;
-    const int nwork = plane ? NRING + nfx + nfy : (zwork ? NT : 0);
+    const int nzw = plane && kEarlyZ ? NRING : NT;
+    const int nwork = plane ? nzw + nfx + nfy : (zwork ? NT : 0);
     for (int w = tid; w < nwork; w += NT) {
       int kind;  // 0 = z (own column), 1 = x, 2 = y
       int fx, fy;
