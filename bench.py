@@ -147,8 +147,8 @@ def peaks() -> dict:
 # algorithmic bytes per cell of the dominant kernel (stage-2 k_flux) and per
 # zone-update of the whole step (two-sweep minimum 3 u + 2 up passes)
 # ncu, 256^3 turbulence, one k_flux<PolKahan,4,8,2,0,2> launch:
-# dram__bytes_read.sum 1281077760 + dram__bytes_write.sum 842317056
-STAGE2_KAHAN_TRAFFIC_PER_CELL = (1281077760 + 842317056) / 256 ** 3
+# dram__bytes_read.sum 1277941760 + dram__bytes_write.sum 838390528
+STAGE2_KAHAN_TRAFFIC_PER_CELL = (1277941760 + 838390528) / 256 ** 3
 
 
 # The plain FP64 path is bound by the FP64 pipe, not by HBM.  ncu on the
