@@ -620,7 +620,7 @@ def run_ours(args, dist: Dist) -> None:
         if traffic is None and headline == P.FP32_KAHAN:
             # dram__bytes_read.sum + dram__bytes_write.sum of one stage-2
             # k_flux launch (FP32 + Kahan, HLLD, van Leer) measured by ncu on
-            # the 256^3 box: 126.59 bytes per cell, scaled by the cell count
+            # the 256^3 box: 126.1 bytes per cell, scaled by the cell count
             traffic = STAGE2_KAHAN_TRAFFIC_PER_CELL * cells
         roof = {"kernel": dom, "bound": "hbm", "achieved": ach, "peak": pk["hbm_gbs"],
                 "unit": "GB/s", "frac": ach / pk["hbm_gbs"], "traffic": traffic,
