@@ -521,6 +521,9 @@ def run_ours(args, dist: Dist) -> None:
     for prec in (P.FP32_KAHAN, P.FP32_MIXED):
         d = Domain(p.replace(precision=prec))
         d.init(u0)
+        # the z-march depth by the library's autotuner (stage-1 probes on
+        # this state; results are the same for every depth)
+        tuned = d.autotune()
         d.advance_timed(W)
         clocks = Clocks()
         dist.barrier()
@@ -534,7 +537,8 @@ def run_ours(args, dist: Dist) -> None:
                 for name, t in d.profile_step():
                     prof_v.setdefault(name, []).append(t)
         variants[prec] = dict(ms=ms_v, clk=clk_v, prof=prof_v,
-                              launches=d.launches_per_step())
+                              launches=d.launches_per_step(), kz=d.kz,
+                              kz_probe_ms={k: round(v, 4) for k, v in tuned.items()})
         d.close()
     ms = variants[headline]["ms"]
     clk = variants[headline]["clk"]
@@ -665,6 +669,13 @@ def run_ours(args, dist: Dist) -> None:
         "dtype": "f32 (u as Kahan-compensated f32 pairs; double-float pressure recovery; f64 dt)",
         "data": "synthetic (seeded turbulence initial state, no dataset)",
         "config": bench_config(n, dist.ws),
+        # the z-march depth each timed FP32 box ran with, chosen by
+        # gch_autotune from these stage-1 probe times (ms per launch)
+        "z_march": {"fp32_kahan": {"kz": variants[P.FP32_KAHAN]["kz"],
+                                   "stage1_probe_ms": variants[P.FP32_KAHAN]["kz_probe_ms"]},
+                    "fp32_mixed_fp64u": {"kz": variants[P.FP32_MIXED]["kz"],
+                                         "stage1_probe_ms":
+                                             variants[P.FP32_MIXED]["kz_probe_ms"]}},
         "fp64_plain": {"value": dist.ws * n ** 3 * k64 / (ms64 * 1e-3),
                        "ms_per_step": ms64 / k64, "steps": k64,
                        "roofline": fp64_pipe_record(n ** 3 * k64 / (ms64 * 1e-3),

@@ -797,7 +797,7 @@ int gch_autotune(gch_domain_t* d, int cap, int* cand_kz, float* cand_ms, int* nc
   st |= cuda_ok(cudaEventCreate(&e1));
   int best_kz = d->kz, n = 0;
   float best = 0.f;
-  for (int kz : {1, 2, 4, 8, 16, 32}) {
+  for (int kz : {1, 2, 4, 8, 12, 16, 20, 24, 32}) {
     if (kz > d->kp.nz || st) break;
     d->kz = kz;
     st |= engine(d).probe(d);  // warm-up

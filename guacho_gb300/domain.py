@@ -198,10 +198,10 @@ class Domain:
     def autotune(self) -> dict:
         """Time the stage-1 kernel for each candidate depth on the current
         state, keep the fastest; returns {kz: ms}."""
-        ck = (C.c_int * 8)()
-        cm = (C.c_float * 8)()
+        ck = (C.c_int * 16)()
+        cm = (C.c_float * 16)()
         n = C.c_int()
-        check("gch_autotune", self._lib.gch_autotune(self._h, 8, ck, cm, C.byref(n)))
+        check("gch_autotune", self._lib.gch_autotune(self._h, 16, ck, cm, C.byref(n)))
         return {int(ck[i]): float(cm[i]) for i in range(n.value)}
 
     def advance_timed(self, steps: int, n_iter: int = 10) -> float:

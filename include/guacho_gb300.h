@@ -294,7 +294,7 @@ int gch_launches_per_step(gch_domain_t* d);
  * depth trades the column warm-up per block against the number of blocks.
  * gch_create picks kz from the box size; gch_autotune times the stage-1
  * flux kernel (it writes only the stage arrays up and E) for kz in
- * {1,2,4,8,16,32} <= nz on the current state, keeps the fastest, and
+ * {1,2,4,8,12,16,20,24,32} <= nz on the current state, keeps the fastest, and
  * reports up to `cap` candidates with their times in ms (outputs may be
  * NULL).  gch_set_kz sets the depth directly (1 <= kz <= nz). */
 int gch_get_kz(gch_domain_t* d);
