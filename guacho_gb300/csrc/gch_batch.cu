@@ -106,7 +106,7 @@ int autotune(gch_batch* b) {
   float best = 0.f;
   int best_kz = std::min(8, nzmax), best_bps = 3;
   st |= b->gops->prep(b->boxes.data(), n, b->stream);
-  for (int kz : {2, 4, 8, 16, 32}) {
+  for (int kz : {2, 4, 8, 12, 16, 20, 24, 32}) {
     if (kz > nzmax && kz != 2) break;
     for (int bps : {0, 1, 2, 3}) {
       st |= b->gops->probe(b->boxes.data(), n, kz, bps, b->queue, b->stream);  // warm-up
