@@ -14,6 +14,7 @@
 //   f2d(x)     exact.  Normal numbers and zero take the fast path;
 //              infinity and NaN map to themselves; subnormal inputs, which
 //              flush-to-zero FP32 arithmetic never produces, become zero.
+//   ge_pos(x, lo)  x >= lo for a positive finite floor lo (below).
 //
 // The fast path of d2f_rn rounds with a single 64-bit add: the 29 mantissa
 // bits that FP32 drops are added to 2^28 - 1 plus the lowest kept bit, so the
@@ -105,6 +106,18 @@ GCH_HD double f2d(float x) {
     return double_of(sign | ((a >> 3) + (896u << 20)), b << 29);
   if (a < 0x00800000u) return double_of(sign, 0u);
   return double_of(sign | 0x7FF00000u | ((a & 0x7FFFFFu) >> 3), b << 29);
+}
+
+// x >= lo for a positive finite lo, false for NaN, on the integer pipes.
+// Non-negative doubles order as their bit patterns (IEEE 754 totalOrder);
+// as unsigned patterns, NaNs with the sign bit clear lie above +infinity and
+// every value with the sign bit set (negatives, -0, negative NaNs) above
+// those.  So x >= lo exactly when bits(x) - bits(lo) wraps to no more than
+// bits(+inf) - bits(lo).  `ge_pos(x, lo) ? x : lo` is then tmax_(x, lo)
+// (x > lo ? x : lo) bit for bit: equal operands have equal bits.
+GCH_HD bool ge_pos(double x, double lo) {
+  const uint64_t l = bits_of(lo);
+  return bits_of(x) - l <= 0x7FF0000000000000ull - l;
 }
 
 }  // namespace gch

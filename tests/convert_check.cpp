@@ -2,7 +2,8 @@
 // FP64 <-> FP32 conversions against the C casts, with the flush rule the
 // header states (results and FP32 inputs below 2^-126 in magnitude become
 // signed zero), and the integer-pipe FP64 division and square root against
-// the IEEE division and square root.
+// the IEEE division and square root, and the integer-pipe floor comparison
+// against the C comparison.
 // Usage: convert_check <n_random>; prints "checked N bad B", exits 1 on a mismatch.
 #include "gch_convert.h"
 #include "gch_ddiv.h"
@@ -54,7 +55,29 @@ int main(int argc, char** argv) {
     const bool ok = std::isnan(want) ? std::isnan(got) : bits_of(got) == bits_of(want);
     if (!ok && bad++ < 8) printf("dsqrt_rn(%a) = %a, want %a\n", a, got, want);
   };
-  convert_cases(n, d2f, f2d, div, sq);
+  // ge_pos against the C comparison, for the floors the FP32 + FP64 u
+  // path uses and the ends of the positive range
+  const double floors[] = {1e-15, 1e-16, 1.0, DBL_MIN, 0x1p-1074, DBL_MAX};
+  auto ge = [&](double x) {
+    for (double lo : floors) {
+      ++checked;
+      if (gch::ge_pos(x, lo) != (x >= lo) && bad++ < 8)
+        printf("ge_pos(%a, %a) = %d, want %d\n", x, lo, (int)gch::ge_pos(x, lo), (int)(x >= lo));
+    }
+  };
+  auto d2f_ge = [&](double x) {
+    d2f(x);
+    ge(x);
+  };
+  auto sq_ge = [&](double a) {
+    sq(a);
+    ge(a);
+  };
+  for (double lo : floors)
+    for (double x : {lo, std::nextafter(lo, 0.0), std::nextafter(lo, INFINITY), -lo, 0.0, -0.0,
+                     (double)INFINITY, -(double)INFINITY, (double)NAN, -(double)NAN})
+      ge(x);
+  convert_cases(n, d2f_ge, f2d, div, sq_ge);
   printf("checked %ld bad %ld\n", checked, bad);
   return bad ? 1 : 0;
 }
