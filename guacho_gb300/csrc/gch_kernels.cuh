@@ -29,8 +29,10 @@ __device__ __forceinline__ void raise_err(int* errp, int bits) {
   if (bits) atomicOr(errp, bits);
 }
 
-// u + dt * s for a source term s: FP64 on the FP64 and FP64-u paths; on the
-// pair path the FP32 product dt*s is added to the pair (no FP64 instruction)
+// u + dt * s for a source term s as a separate accumulation (the FP64 stage
+// update, in the reference's order, and the CT kernels' eight-wave terms):
+// FP64 on the FP64 and FP64-u paths; on the pair path the FP32 product dt*s
+// is added to the pair (no FP64 instruction)
 template <class Pol, class R, class T>
 __device__ __forceinline__ R add_source(R u, double dt, float dtf, T s) {
   if constexpr (std::is_same<Pol, PolKahan>::value) return Ops<PolKahan>::addf(u, dtf * s);
@@ -684,11 +686,23 @@ flux_body(const KParams& p, const typename Src<Pol, NEQ, STAGE, PRIM_IN>::TIn* _
             dst[(3 * q + 2) * p.fs + c] = sH[hn][q][ty][tx] - sH[hp][q][ty][tx];
           }
         } else if (upd(q)) {
-          auto unew = Ops<Pol>::update(Ops<Pol>::ld(uq[q]), dtdx, dtdy, dtdz,
-                                       sF[q][ty][tx], sF[q][ty][tx + 1], sG[q][ty][tx],
-                                       sG[q][ty + 1][tx], sH[hp][q][ty][tx], sH[hn][q][ty][tx]);
-          if (src_terms) unew = add_source<Pol>(unew, dt, dtf, sv[q]);
-          dst[q * p.fs + c] = store_as<TD>(unew);
+          if constexpr (sizeof(TC) == 4) {
+            // FP32 paths: dt s joins the FP32 flux divergence (sv is zero
+            // without source terms).  A second accumulation under
+            // `if (src_terms)` was evaluated for every cell and selected:
+            // 5 FP64 multiply-adds and 4 conversions per cell on the
+            // FP32 + FP64 u path, two-sums on the pair path.
+            dst[q * p.fs + c] = store_as<TD>(Ops<Pol>::update_src(
+                Ops<Pol>::ld(uq[q]), dtdx, dtdy, dtdz, sF[q][ty][tx], sF[q][ty][tx + 1],
+                sG[q][ty][tx], sG[q][ty + 1][tx], sH[hp][q][ty][tx], sH[hn][q][ty][tx], dtf,
+                sv[q]));
+          } else {
+            auto unew = Ops<Pol>::update(Ops<Pol>::ld(uq[q]), dtdx, dtdy, dtdz,
+                                         sF[q][ty][tx], sF[q][ty][tx + 1], sG[q][ty][tx],
+                                         sG[q][ty + 1][tx], sH[hp][q][ty][tx], sH[hn][q][ty][tx]);
+            if (src_terms) unew = add_source<Pol>(unew, dt, dtf, sv[q]);
+            dst[q * p.fs + c] = store_as<TD>(unew);
+          }
         }
       }
       if (ct) {

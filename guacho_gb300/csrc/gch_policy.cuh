@@ -286,6 +286,14 @@ struct Ops<PolMixed> {
                                                   float hl, float hr) {
     return u - f2d(flux_sum(dtdx, dtdy, dtdz, fl, fr, gl, gr, hl, hr));
   }
+  // the same with a source term s: dt s joins the FP32 flux divergence in
+  // one fused multiply-add (s = 0 leaves every bit as update() gives it)
+  __device__ __forceinline__ static double update_src(double u, float dtdx, float dtdy,
+                                                      float dtdz, float fl, float fr, float gl,
+                                                      float gr, float hl, float hr, float dt,
+                                                      float s) {
+    return u - f2d(__fmaf_rn(-dt, s, flux_sum(dtdx, dtdy, dtdz, fl, fr, gl, gr, hl, hr)));
+  }
 
   __device__ __forceinline__ static double ct(double u, float hdta, float a0, float a1,
                                               float hdtb, float b0, float b1, bool first_minus) {
@@ -381,6 +389,13 @@ struct Ops<PolKahan> {
                                                   float fl, float fr, float gl, float gr,
                                                   float hl, float hr) {
     return addf(u, -flux_sum(dtdx, dtdy, dtdz, fl, fr, gl, gr, hl, hr));
+  }
+  // the same with a source term s, as Ops<PolMixed>::update_src
+  __device__ __forceinline__ static float2 update_src(float2 u, float dtdx, float dtdy,
+                                                      float dtdz, float fl, float fr, float gl,
+                                                      float gr, float hl, float hr, float dt,
+                                                      float s) {
+    return addf(u, -__fmaf_rn(-dt, s, flux_sum(dtdx, dtdy, dtdz, fl, fr, gl, gr, hl, hr)));
   }
 
   __device__ __forceinline__ static float2 ct(float2 u, float hdta, float a0, float a1,
