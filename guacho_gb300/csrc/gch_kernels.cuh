@@ -942,17 +942,32 @@ ct_body(const KParams& p, const typename Pol::TU* u,
     const auto u7 = Ops<Pol>::ld(U7[c]);
     const auto u8 = Ops<Pol>::ld(U8[c]);
     // src/flux_cd_module.f90:311-321
-    auto b6 = Ops<Pol>::ct(u6, hy, e3ym, e3yp, hz, e2zm, e2zp, true);
-    auto b7 = Ops<Pol>::ct(u7, hx, e3xm, e3xp, hz, e1zm, e1zp, false);
-    auto b8 = Ops<Pol>::ct(u8, hx, e2xm, e2xp, hy, e1ym, e1yp, true);
-    if (p.eight_wave) {
-      b6 = add_source<Pol>(b6, dt, dtf, s678[c]);
-      b7 = add_source<Pol>(b7, dt, dtf, s678[fs + c]);
-      b8 = add_source<Pol>(b8, dt, dtf, s678[2 * fs + c]);
+    if constexpr (sizeof(TC) == 4) {
+      // FP32 paths: the eight-wave terms join the FP32 differences (zero
+      // without them).  Added after the CT under `if (p.eight_wave)`, the
+      // grouped kernel evaluated them for every cell and selected.
+      TC s6 = TC(0), s7 = TC(0), s8 = TC(0);
+      if (p.eight_wave) {
+        s6 = (TC)s678[c];
+        s7 = (TC)s678[fs + c];
+        s8 = (TC)s678[2 * fs + c];
+      }
+      D6[c] = store_as<TD>(Ops<Pol>::ct_src(u6, hy, e3ym, e3yp, hz, e2zm, e2zp, true, dtf, s6));
+      D7[c] = store_as<TD>(Ops<Pol>::ct_src(u7, hx, e3xm, e3xp, hz, e1zm, e1zp, false, dtf, s7));
+      D8[c] = store_as<TD>(Ops<Pol>::ct_src(u8, hx, e2xm, e2xp, hy, e1ym, e1yp, true, dtf, s8));
+    } else {
+      auto b6 = Ops<Pol>::ct(u6, hy, e3ym, e3yp, hz, e2zm, e2zp, true);
+      auto b7 = Ops<Pol>::ct(u7, hx, e3xm, e3xp, hz, e1zm, e1zp, false);
+      auto b8 = Ops<Pol>::ct(u8, hx, e2xm, e2xp, hy, e1ym, e1yp, true);
+      if (p.eight_wave) {
+        b6 = add_source<Pol>(b6, dt, dtf, s678[c]);
+        b7 = add_source<Pol>(b7, dt, dtf, s678[fs + c]);
+        b8 = add_source<Pol>(b8, dt, dtf, s678[2 * fs + c]);
+      }
+      D6[c] = store_as<TD>(b6);
+      D7[c] = store_as<TD>(b7);
+      D8[c] = store_as<TD>(b8);
     }
-    D6[c] = store_as<TD>(b6);
-    D7[c] = store_as<TD>(b7);
-    D8[c] = store_as<TD>(b8);
   }
 }
 

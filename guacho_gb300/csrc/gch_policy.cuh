@@ -300,6 +300,15 @@ struct Ops<PolMixed> {
     const float d = hdta * (a1 - a0) - hdtb * (b1 - b0);
     return first_minus ? u - f2d(d) : u + f2d(d);
   }
+  // the same with a source term s (Powell's eight-wave terms): dt s joins
+  // the FP32 difference in one fused multiply-add (s = 0 leaves every bit
+  // as ct() gives it: u - (-x) is u + x)
+  __device__ __forceinline__ static double ct_src(double u, float hdta, float a0, float a1,
+                                                  float hdtb, float b0, float b1,
+                                                  bool first_minus, float dt, float s) {
+    const float d = hdta * (a1 - a0) - hdtb * (b1 - b0);
+    return u - f2d(__fmaf_rn(-dt, s, first_minus ? d : -d));
+  }
 };
 
 
@@ -402,6 +411,13 @@ struct Ops<PolKahan> {
                                               float hdtb, float b0, float b1, bool first_minus) {
     const float d = hdta * (a1 - a0) - hdtb * (b1 - b0);
     return addf(u, first_minus ? -d : d);
+  }
+  // the same with a source term s, as Ops<PolMixed>::ct_src
+  __device__ __forceinline__ static float2 ct_src(float2 u, float hdta, float a0, float a1,
+                                                  float hdtb, float b0, float b1,
+                                                  bool first_minus, float dt, float s) {
+    const float d = hdta * (a1 - a0) - hdtb * (b1 - b0);
+    return addf(u, -__fmaf_rn(-dt, s, first_minus ? d : -d));
   }
 };
 
