@@ -92,7 +92,11 @@ GCH_HD float d2f_rn(double x) {
     return float_of(sign | ((uint32_t)(r >> 29) - (896u << 23)));
   }
   if (ahi < kD2fLoHi) return float_of(sign);
-  const bool nan = (b & 0x7FFFFFFFFFFFFFFFull) > 0x7FF0000000000000ull;
+  // |x| >= 2^128: infinity, or NaN when the fraction is not zero.  Tested
+  // on the two 32-bit halves: the same test on the 64-bit pattern was
+  // compiled as an FP64 unordered comparison, an FP64-pipe instruction on
+  // every zero input (which takes this path too).
+  const bool nan = ahi > 0x7FF00000u || (ahi == 0x7FF00000u && (uint32_t)b != 0u);
   return float_of(sign | (nan ? 0x7FC00000u : 0x7F800000u));
 }
 
