@@ -26,8 +26,9 @@
 //
 // The fast path takes normal a and b whose quotient exponent is normal
 // before rounding (a carry out of the largest binade gives infinity, as
-// IEEE 754 does).  Zeros, subnormals, infinities, NaNs and quotients near the
-// ends of the exponent range go to the hardware division.  The same code
+// IEEE 754 does).  A zero over a normal number gives the signed zero
+// directly.  Other zeros, subnormals, infinities, NaNs and quotients near
+// the ends of the exponent range go to the hardware division.  The same code
 // runs on the host (FP32 reciprocal by IEEE division, which rounds like
 // __frcp_rn), so host tests check the digits the device computes.
 #pragma once
@@ -92,6 +93,11 @@ GCH_HD double ddiv_rn(double a, double b) {
                           | ((e << 52) + (M - (1ull << 52)) + up);
     return double_of((uint32_t)(bits >> 32), (uint32_t)bits);
   }
+  // a zero over a normal number: the zero with the quotient's sign (IEEE is
+  // exact here).  Exactly zero fields make these common in the Riemann
+  // solvers (Bz and vz of a 2.5-D problem, static gas where S_M - u = 0).
+  if ((ba << 1) == 0 && (unsigned)(eb - 1) < 2046u)
+    return double_of((uint32_t)((ba ^ bb) >> 32) & 0x80000000u, 0u);
   return a / b;
 }
 
