@@ -1,10 +1,11 @@
-"""Integer-pipe FP64 <-> FP32 conversions used by the FP32 + FP64-u path
-(guacho_gb300/csrc/gch_convert.h), the integer-pipe FP64 division of the
-FP64 Riemann solvers (gch_ddiv.h) and the integer-pipe FP64 square root of
-the FP64 CFL pass (gch_dsqrt.h): bit-identical to the C casts and to the IEEE
-division and square root on random bit patterns, values around the FP32
-range, exact rounding ties, quotients and roots next to a rounding boundary
-and the special values, compiled for the host with g++."""
+"""Integer-pipe FP64 <-> FP32 conversions and floor comparison used by the
+FP32 + FP64-u path (guacho_gb300/csrc/gch_convert.h), the integer-pipe FP64
+division of the FP64 Riemann solvers (gch_ddiv.h) and the integer-pipe FP64
+square root of the FP64 CFL pass (gch_dsqrt.h): bit-identical to the C casts,
+the C comparison and the IEEE division and square root on random bit
+patterns, values around the FP32 range, exact rounding ties, quotients and
+roots next to a rounding boundary and the special values, compiled for the
+host with g++."""
 import shutil
 import subprocess
 from pathlib import Path

@@ -1,9 +1,10 @@
-"""Integer-pipe FP64 <-> FP32 conversions (guacho_gb300/csrc/gch_convert.h),
-the integer-pipe FP64 division (gch_ddiv.h) and square root (gch_dsqrt.h) on
-the device: a kernel runs them on the host check's cases (random bit
-patterns, exact rounding ties and their neighbours, quotients and roots next
-to a rounding boundary, range edges, special values) and compares them
-bitwise with the device's own IEEE division, square root and conversions,
+"""Integer-pipe FP64 <-> FP32 conversions and floor comparison
+(guacho_gb300/csrc/gch_convert.h), the integer-pipe FP64 division (gch_ddiv.h)
+and square root (gch_dsqrt.h) on the device: a kernel runs them on the host
+check's cases (random bit patterns, exact rounding ties and their
+neighbours, quotients and roots next to a rounding boundary, range edges,
+special values) and compares them bitwise with the device's own IEEE
+division, square root, conversions and comparisons,
 under both flag sets the library compiles them with (the FP64 units'
 -fmad=false and the FP32 units' -use_fast_math)."""
 import subprocess
